@@ -1,0 +1,102 @@
+"""Icosahedral and MWSS lat-lon mesh builders (host side, numpy).
+
+The reference loads pickled icosahedral meshes produced by stripy
+(``cmm_s2/tests/precompute_meshes.py:13-17``) and builds the lat-lon
+velocity mesh from the MWSS sample positions
+(``cmm_s2/core/mesh_functions.py:175-194``).  Neither the pickles nor stripy
+are available, so the vertex sets are generated here:
+
+* ``icosahedral_mesh(level)``: the regular icosahedron with its two poles on
+  the z axis, refined ``level`` times by normalised edge-midpoint bisection.
+  Vertex 0 is the north pole and the last vertex is the south pole, which is
+  what ``spherical_triangulation.stencil_pts`` assumes when it patches the
+  tangent frames of the first and last vertices
+  (``cmm_s2/core/mesh_functions.py:137-142``).
+  Triangles are returned in hierarchical order: triangle ``4*f + c`` at level
+  ``j+1`` is child ``c`` of triangle ``f`` at level ``j``.
+* ``mwss_angles(L)``: MWSS colatitudes ``pi*t/L`` (t = 0..L) and longitudes
+  ``2*pi*p/(2L)`` (p = 0..2L-1), the ``pyssht.sample_positions(L, "MWSS")``
+  convention the reference relies on.
+"""
+import numpy as np
+
+
+def _base_icosahedron():
+    z = np.arctan(0.5)
+    pts = [(0.0, 0.0, 1.0)]
+    for k in range(5):
+        lon = 2 * np.pi * k / 5
+        pts.append((np.cos(z) * np.cos(lon), np.cos(z) * np.sin(lon), np.sin(z)))
+    for k in range(5):
+        lon = 2 * np.pi * k / 5 + np.pi / 5
+        pts.append((np.cos(z) * np.cos(lon), np.cos(z) * np.sin(lon), -np.sin(z)))
+    pts.append((0.0, 0.0, -1.0))
+    faces = []
+    for k in range(5):
+        u0, u1 = 1 + k, 1 + (k + 1) % 5
+        l0, l1 = 6 + k, 6 + (k + 1) % 5
+        faces.append((0, u0, u1))
+        faces.append((u0, l0, u1))
+        faces.append((u1, l0, l1))
+        faces.append((l0, 11, l1))
+    return np.array(pts, dtype=np.float64), np.array(faces, dtype=np.int64)
+
+
+def _orient_ccw(verts, faces):
+    a, b, c = verts[faces[:, 0]], verts[faces[:, 1]], verts[faces[:, 2]]
+    d = np.einsum("ij,ij->i", a, np.cross(b, c))
+    flip = d < 0
+    faces = faces.copy()
+    faces[flip, 1], faces[flip, 2] = faces[flip, 2].copy(), faces[flip, 1].copy()
+    return faces
+
+
+def icosahedral_mesh(level):
+    """Return ``(verts (Nv,3) float64, tris (Nt,3) int32)`` for a level-``level``
+    icosahedral refinement; Nv = 10*4**level + 2, Nt = 20*4**level.
+
+    Children of a counter-clockwise face (a, b, c) with normalised edge
+    midpoints mab, mbc, mca are, in order:
+    (a, mab, mca), (mab, b, mbc), (mca, mbc, c), (mbc, mca, mab).
+    """
+    verts, faces = _base_icosahedron()
+    faces = _orient_ccw(verts, faces)
+    for _ in range(level):
+        nv = len(verts)
+        a, b, c = faces[:, 0], faces[:, 1], faces[:, 2]
+        edges = np.concatenate([np.stack([a, b], 1), np.stack([b, c], 1), np.stack([c, a], 1)])
+        key = np.minimum(edges[:, 0], edges[:, 1]) * nv + np.maximum(edges[:, 0], edges[:, 1])
+        ukey, inv = np.unique(key, return_inverse=True)
+        e0, e1 = ukey // nv, ukey % nv
+        mid = verts[e0] + verts[e1]
+        mid /= np.linalg.norm(mid, axis=1)[:, None]
+        mid_id = nv + np.arange(len(ukey))
+        nf = len(faces)
+        mab, mbc, mca = mid_id[inv[:nf]], mid_id[inv[nf:2 * nf]], mid_id[inv[2 * nf:]]
+        children = np.stack([
+            np.stack([a, mab, mca], 1),
+            np.stack([mab, b, mbc], 1),
+            np.stack([mca, mbc, c], 1),
+            np.stack([mbc, mca, mab], 1)], 1)
+        faces = children.reshape(-1, 3)
+        verts = np.concatenate([verts, mid])
+    # move the south pole (base vertex 11) to the end
+    nv = len(verts)
+    order = np.concatenate([np.arange(11), np.arange(12, nv), [11]])
+    remap = np.empty(nv, dtype=np.int64)
+    remap[order] = np.arange(nv)
+    verts = np.ascontiguousarray(verts[order])
+    faces = remap[faces]
+    return verts, faces.astype(np.int32)
+
+
+def mwss_angles(L):
+    """MWSS colatitudes (L+1,) and longitudes (2L,)."""
+    return np.pi * np.arange(L + 1) / L, 2 * np.pi * np.arange(2 * L) / (2 * L)
+
+
+def random_sphere_points(n, seed):
+    """``n`` points uniform on the unit sphere (normalised Gaussians), (n,3)."""
+    rng = np.random.default_rng(seed)
+    x = rng.standard_normal((n, 3))
+    return x / np.linalg.norm(x, axis=1)[:, None]

@@ -1,0 +1,207 @@
+"""Generate the golden fixtures from the reference implementation itself.
+
+Runs only where the reference checkout exists (``REF`` below).  The
+reference's ``cmm_s2.core`` modules are imported unchanged with import shims
+for packages that are absent here:
+
+* ``np.VisibleDeprecationWarning`` (removed in numpy 2) and
+  ``scipy.special.sph_harm`` (removed in scipy 1.18) aliases;
+* empty ``igl``/``numba``/``pathos`` modules (imported, never called);
+* ``stripy.sTriangulation``: returns its input points in input order (the
+  reference reads only ``.points/.x/.y/.z``); for the icosahedral meshes the
+  exact generated points are handed through so both sides see identical
+  vertices;
+* ``pyssht.sample_positions`` / ``elm2ind`` (MWSS positions, l*l+l+m) and,
+  for the one barotropic-vorticity fixture, ``forward``/``inverse`` backed by
+  the oracle's restated MWSS transform (pyssht itself is absent).
+
+Outputs: ``tests/golden/*.npz`` (small; committed).
+Usage: python tests/golden/make_golden.py
+"""
+import os
+import sys
+import types
+
+import numpy as np
+import scipy.special
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+REF = "/root/reference"
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "cmm-s2_gb300"))
+sys.path.insert(0, REF)
+
+from cmm_gpu.meshgen import icosahedral_mesh, random_sphere_points  # noqa: E402
+from cmm_gpu.workloads import submap_stack  # noqa: E402
+from oracle import sht as osht  # noqa: E402
+
+# ----------------------------------------------------------------- shims
+np.VisibleDeprecationWarning = np.exceptions.VisibleDeprecationWarning
+if not hasattr(scipy.special, "sph_harm"):
+    scipy.special.sph_harm = lambda m, l, phi, theta: scipy.special.sph_harm_y(l, m, theta, phi)
+for _name in ["igl", "numba", "pathos", "pathos.multiprocessing"]:
+    sys.modules[_name] = types.ModuleType(_name)
+sys.modules["numba"].njit = lambda *a, **k: (lambda f: f)
+sys.modules["pathos.multiprocessing"].ProcessingPool = object
+
+_EXACT = {"pts": None}
+
+
+class _STri:
+    def __init__(self, lons, lats, refinement_levels=0, permute=False, tree=False):
+        lons = np.asarray(lons, dtype=np.float64)
+        lats = np.asarray(lats, dtype=np.float64)
+        if _EXACT["pts"] is not None and len(_EXACT["pts"]) == len(lons):
+            p = _EXACT["pts"]
+            self.x, self.y, self.z = p[:, 0].copy(), p[:, 1].copy(), p[:, 2].copy()
+        else:
+            self.x = np.cos(lats) * np.cos(lons)
+            self.y = np.cos(lats) * np.sin(lons)
+            self.z = np.sin(lats)
+        self.points = np.stack([self.x, self.y, self.z], 1)
+
+
+_stripy = types.ModuleType("stripy")
+_stripy.sTriangulation = _STri
+sys.modules["stripy"] = _stripy
+_pysh = types.ModuleType("pyssht")
+_pysh.sample_positions = lambda L, Method="MWSS", Grid=False: (np.pi * np.arange(L + 1) / L,
+                                                               2 * np.pi * np.arange(2 * L) / (2 * L))
+_pysh.elm2ind = lambda l, m: l * l + l + m
+_SHT = {}
+
+
+def _sht(L):
+    if L not in _SHT:
+        _SHT[L] = osht.MWSS(L)
+    return _SHT[L]
+
+
+def _forward(f, L, Spin=0, Method="MWSS", Reality=True, backend=None, nthreads=1):
+    return osht.full_from_half(_sht(L).forward(np.real(f)))
+
+
+def _inverse(flm, L, Spin=0, Method="MWSS", Reality=True, backend=None, nthreads=1):
+    return _sht(L).inverse(osht.half_from_full(flm, L))
+
+
+_pysh.forward, _pysh.inverse = _forward, _inverse
+sys.modules["pyssht"] = _pysh
+
+from cmm_s2.core import mesh_functions as rmesh  # noqa: E402
+from cmm_s2.core import spherical_spline as rspl  # noqa: E402
+from cmm_s2.core import evolution_functions as revol  # noqa: E402
+from cmm_s2.core import spherical_harmonic_tools as rsht  # noqa: E402
+from cmm_s2.core import spherical_simulations as rsim  # noqa: E402
+from cmm_s2.core import dynamical_fields as rfields  # noqa: E402
+from cmm_s2.core import utils as rutils  # noqa: E402
+
+
+def ref_mesh(level):
+    verts, _ = icosahedral_mesh(level)
+    _EXACT["pts"] = verts
+    m = rmesh.spherical_triangulation(verts)
+    _EXACT["pts"] = None
+    assert np.array_equal(m.vertices, verts)
+    return m
+
+
+def special_points(verts, tris):
+    """Vertices, edge midpoints, centroids and poles: exact-tie cases."""
+    v = verts[tris[:64]]
+    mids = (v[:, 0] + v[:, 1]) / np.linalg.norm(v[:, 0] + v[:, 1], axis=1)[:, None]
+    cent = v.sum(1) / np.linalg.norm(v.sum(1), axis=1)[:, None]
+    return np.concatenate([verts[:32], mids, cent, [[0, 0, 1.0], [0, 0, -1.0], [1.0, 0, 0]]])
+
+
+def save(name, **arrays):
+    path = os.path.join(HERE, name)
+    np.savez_compressed(path, **arrays)
+    print("wrote", path, sum(a.nbytes for a in map(np.asarray, arrays.values())) // 1024, "KiB raw")
+
+
+def main():
+    # ---- icosahedral meshes, query, PS maps, composite --------------------
+    for level in (3, 4):
+        m = ref_mesh(level)
+        tris = np.asarray(m.simplices)
+        q = np.concatenate([random_sphere_points(3000, seed=10 + level), special_points(m.vertices, tris)])
+        bcc, tri, _ = m.query(q)
+        Hs, Gs, Es = m.ps_split
+        if level != 3:
+            save(f"mesh_l{level}.npz", verts=m.vertices, tris=tris.astype(np.int32), q=q, bcc=bcc,
+                 tri=tri.astype(np.int32))
+            continue
+        save(f"mesh_l{level}.npz", verts=m.vertices, tris=tris.astype(np.int32),
+             H=np.stack([h.T for h in Hs]), G=np.stack(Gs), E=np.stack(Es),
+             tan=np.stack(m.tan_vects), s_pts=m.s_pts, q=q, bcc=bcc, tri=tri.astype(np.int32))
+        jets = submap_stack(m.s_pts, np.stack(m.tan_vects), 3, seed=5)
+        nt = len(tris)
+        mp = rspl.sphere_diffeomorphism(m, jets[0].copy(), np.zeros((3, 19, nt)))
+        img = mp(q)
+        # stencil evaluation: vertex foot points yn and stencil foot points
+        rng = np.random.default_rng(3)
+        rot = np.linalg.qr(rng.standard_normal((3, 3)))[0]
+        rot *= np.sign(np.linalg.det(rot))
+        yn = (m.vertices @ rot.T).T
+        sp = np.einsum("ij,jkn->ikn", rot, m.s_pts)
+        st = mp.stencil_eval(yn.copy(), sp.copy())
+        comp = rspl.composite_sphere_diffeomorphism(m, jets.copy(), np.zeros((3, 3, 19, nt)), [1, 2, 3])
+        for i in range(3):
+            comp.assemble_coefficients(i, jets[i].copy())
+        comp.Nc = 3
+        cimg = comp(q.copy())
+        save("map_l3.npz", jets=jets, coeffs0=mp.coeffs, q=q, img=img, yn=yn, sp=sp, st=st, comp_img=cimg)
+
+        # ---- one CMM update: advect + project (RK4 and Euler), L=8 velocity
+        L = 8
+        mu = rmesh.structure_spherical_triangulation(L)
+        ntu = len(mu.simplices)
+        vals_u = np.zeros((3, 3, 4, len(mu.vertices)))
+        U = rspl.spline_interp_velocity(mu, vals_u, np.zeros((3, 3, 19, ntu)), ts=np.array([0.0, 0.1, 0.2]))
+        Phi, The = np.meshgrid(mu.phi, mu.theta)
+        dinv = osht.inverse_laplacian_diag(L)
+        lp, lmn, lz = osht.ladder_operators(L)
+        for n, t in enumerate([0.0, 0.1, 0.2]):
+            om = rfields.rossby_wave(Phi, The, t=t) + 0.3 * np.sin(The) ** 2 * np.cos(2 * Phi + t)
+            psi = rsht.inv_Laplacian(om, L, dinv)
+            rsht.project_stream(psi, L, lp, lmn, lz, U, n, 0 * psi)
+        U.nVs = 3
+        qv = np.concatenate([random_sphere_points(2000, seed=21), special_points(m.vertices, tris),
+                             np.array(mu.grid_points).reshape(3, -1).T[:40]])
+        bcc_u, tri_u, _ = mu.query(qv)
+        vel = U(0.23, 0.1, qv.T.copy())
+        save("velocity_L8.npz", vals=U.vals, coeffs=U.coeffs, verts=mu.vertices,
+             simplices=np.asarray(mu.simplices), msimplices=mu.msimplices, q=qv, bcc=bcc_u,
+             tri=tri_u, t=0.23, dt=0.1, ts=np.array([0.0, 0.1, 0.2]), vel=vel)
+        map0 = rspl.sphere_diffeomorphism(m, jets[0].copy(), np.zeros((3, 19, nt)))
+        new_rk4 = revol.advect_project_sphere(map0, revol.RK4_proj, 0.05, 0.1, U, identity=False)
+        map1 = rspl.sphere_diffeomorphism(m, jets[1].copy(), np.zeros((3, 19, nt)))
+        U.nVs = 1
+        new_eul = revol.advect_project_sphere(map1, revol.Euler_step_proj, 0.0, 0.1, U, identity=True)
+        U.nVs = 2
+        new_ie = revol.advect_project_sphere(map1, revol.improved_Euler_proj, 0.0, 0.1, U, identity=True)
+        save("advect_l3_L8.npz", jets_prev=jets[0], jets_rk4=new_rk4.vals, jets_euler=new_eul.vals,
+             jets_ieuler=new_ie.vals)
+
+    # ---- coefficient-space operators ----------------------------------------
+    L = 8
+    rng = np.random.default_rng(7)
+    flm = rng.standard_normal(L * L) + 1j * rng.standard_normal(L * L)
+    ca = rsht.coeff_array(flm, L)
+    lp, lmn, lz = osht.ladder_operators(L)
+    am = rsht.angular_momentum(ca, lp, lmn, lz, 0 * ca)
+    save("sht_ops_L8.npz", flm=flm, coeff_array=ca, lm_array=rsht.lm_array(ca, L), ang_x=am[0],
+         ang_y=am[1], ang_z=am[2])
+
+    # ---- a short barotropic run (restated transforms stand in for pyssht) ---
+    m2 = ref_mesh(2)
+    subs = rsim.euler_simulation_sphere_remapping(8, 12, 1.0, m2, rfields.rossby_wave,
+                                                  rot_rate=2 * np.pi, n_maps=5)
+    qe = random_sphere_points(500, seed=99)
+    save("bve_l2_L8.npz", vals=subs.vals[:subs.Nc], Nc=subs.Nc, ns=np.array(subs.ns), q=qe, img=subs(qe.copy()))
+
+
+if __name__ == "__main__":
+    main()

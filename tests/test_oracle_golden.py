@@ -1,0 +1,157 @@
+"""The oracle against the reference's own outputs (tests/golden, made by
+tests/golden/make_golden.py from the unchanged reference code)."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+from oracle import geometry as G
+from oracle import spline as SP
+from oracle import evolution as EV
+from oracle import sht as S
+from oracle.bve import BVEOracle
+
+
+def load(name):
+    return np.load(os.path.join(GOLDEN, name))
+
+
+class TableLocator:
+    """Replays the reference's triangle choices for the fixture queries."""
+
+    def __init__(self, q, tri, fallback):
+        self.map = {tuple(p): t for p, t in zip(np.round(q, 15), tri)}
+        self.fb = fallback
+
+    def locate(self, q):
+        out = self.fb.locate(q)
+        for i, p in enumerate(np.round(q, 15)):
+            t = self.map.get(tuple(p))
+            if t is not None:
+                out[i] = t
+        return out
+
+
+@pytest.mark.parametrize("level", [3, 4])
+def test_cone_locator_matches_qhull(level):
+    d = load(f"mesh_l{level}.npz")
+    verts, tris = d["verts"], d["tris"]
+    loc = G.ConeLocator(verts, tris)
+    tri = loc.locate(d["q"])
+    diff = tri != d["tri"]
+    near = G.edge_distance(verts, tris, d["tri"], d["q"]) <= 1e-14
+    assert not (diff & ~near).any(), np.nonzero(diff & ~near)
+    # every disagreement is a legitimate container of the query
+    assert (G.edge_distance(verts, tris, tri[diff], d["q"][diff]) <= 1e-14).all()
+    bcc, _, _ = G.query(verts, tris, loc, d["q"])
+    same = ~diff
+    np.testing.assert_array_equal(bcc[same], d["bcc"][same])
+
+
+def test_qhull_locator_reproduces_reference_table():
+    d = load("mesh_l3.npz")
+    ql = G.QhullLocator(d["verts"])
+    np.testing.assert_array_equal(ql.tris, d["tris"])
+    np.testing.assert_array_equal(ql.locate(d["q"]), d["tri"])
+
+
+def test_ps_split_and_stencil():
+    d = load("mesh_l3.npz")
+    H, Gs, E = G.ps_split(d["verts"], d["tris"])
+    np.testing.assert_array_equal(H, d["H"])
+    np.testing.assert_array_equal(Gs, d["G"])
+    np.testing.assert_array_equal(E, d["E"])
+    tan, s_pts = G.stencil_points(d["verts"])
+    np.testing.assert_array_equal(tan, d["tan"])
+    np.testing.assert_array_equal(s_pts, d["s_pts"])
+
+
+def test_map_eval_stencil_and_composite():
+    d, m = load("map_l3.npz"), load("mesh_l3.npz")
+    verts, tris = m["verts"], m["tris"]
+    loc = TableLocator(m["q"], m["tri"], G.ConeLocator(verts, tris))
+    mp = SP.MapOracle(verts, tris, loc, d["jets"][0])
+    np.testing.assert_allclose(mp.coeffs, d["coeffs0"], rtol=0, atol=1e-15)
+    with np.errstate(all="ignore"):
+        img = mp(d["q"])
+    # the reference returns NaN at exact centroid ties; the oracle must too
+    np.testing.assert_array_equal(np.isnan(img), np.isnan(d["img"]))
+    ok = np.isfinite(d["img"])
+    np.testing.assert_allclose(img[ok], d["img"][ok], rtol=0, atol=1e-15)
+    st = mp.stencil_eval(d["yn"], d["sp"])
+    np.testing.assert_allclose(st, d["st"], rtol=0, atol=1e-15)
+    comp = SP.CompositeOracle(verts, tris, G.ConeLocator(verts, tris), d["jets"])
+    with np.errstate(all="ignore"):
+        cimg = comp(d["q"])
+    fin = np.isfinite(d["comp_img"]).all(1)
+    np.testing.assert_allclose(cimg[fin], d["comp_img"][fin], rtol=0, atol=1e-13)
+
+
+def test_latlon_mesh_query_and_velocity():
+    d = load("velocity_L8.npz")
+    mu = G.LatLonMesh(8)
+    np.testing.assert_array_equal(mu.vertices, d["verts"])
+    np.testing.assert_array_equal(mu.simplices, d["simplices"])
+    np.testing.assert_array_equal(mu.msimplices, d["msimplices"][..., 3])
+    bcc, tri, _ = mu.query(d["q"])
+    np.testing.assert_array_equal(tri, d["tri"])
+    np.testing.assert_array_equal(bcc, d["bcc"])
+    U = SP.VelocityOracle(mu, d["vals"], d["ts"])
+    for n in range(3):
+        U.init_coeffs(n)
+    np.testing.assert_allclose(U.coeffs, d["coeffs"], rtol=0, atol=1e-13)
+    U.nVs = 3
+    np.testing.assert_allclose(U(float(d["t"]), float(d["dt"]), d["q"].T), d["vel"], rtol=0, atol=1e-13)
+
+
+def test_advect_project():
+    d, m, v = load("advect_l3_L8.npz"), load("mesh_l3.npz"), load("velocity_L8.npz")
+    verts, tris = m["verts"], m["tris"]
+    # the pole foot points land on mesh edges, so replay Qhull's own choices
+    loc = G.QhullLocator(verts)
+    mu = G.LatLonMesh(8)
+    U = SP.VelocityOracle(mu, v["vals"], v["ts"])
+    for n in range(3):
+        U.init_coeffs(n)
+    tan, s_pts = G.stencil_points(verts)
+    U.nVs = 3
+    prev = SP.MapOracle(verts, tris, loc, d["jets_prev"])
+    j = EV.advect_project(prev, EV.rk4_back, 0.05, 0.1, U, verts, s_pts, tan, identity=False)
+    np.testing.assert_allclose(j, d["jets_rk4"], rtol=1e-12, atol=1e-11)
+    U.nVs = 1
+    j = EV.advect_project(None, EV.euler_back, 0.0, 0.1, U, verts, s_pts, tan, identity=True)
+    np.testing.assert_allclose(j, d["jets_euler"], rtol=1e-12, atol=1e-11)
+    U.nVs = 2
+    j = EV.advect_project(None, EV.improved_euler_back, 0.0, 0.1, U, verts, s_pts, tan, identity=True)
+    np.testing.assert_allclose(j, d["jets_ieuler"], rtol=1e-12, atol=1e-11)
+
+
+def test_coefficient_operators():
+    d = load("sht_ops_L8.npz")
+    L = 8
+    ca = S.shifted_from_vec(d["flm"], L)
+    np.testing.assert_array_equal(ca, d["coeff_array"])
+    np.testing.assert_array_equal(S.vec_from_shifted(ca, L), d["lm_array"])
+    lp, lm, lz = S.ladder_operators(L)
+    am = S.angular_momentum(ca, lp, lm, lz)
+    np.testing.assert_allclose(am[0], d["ang_x"], rtol=0, atol=1e-14)
+    np.testing.assert_allclose(am[1], d["ang_y"], rtol=0, atol=1e-14)
+    np.testing.assert_allclose(am[2], d["ang_z"], rtol=0, atol=1e-14)
+
+
+def test_short_barotropic_run():
+    d, = (load("bve_l2_L8.npz"),)
+    from cmm_gpu.meshgen import icosahedral_mesh
+
+    def rossby_wave(phi, theta, t=0):  # cmm_s2/core/dynamical_fields.py:205-210
+        return 30 * np.cos(theta) * np.cos(4 * (phi + 2 * 2 * np.pi * t / 30)) * np.sin(theta) ** 4
+
+    verts, _ = icosahedral_mesh(2)
+    ql = G.QhullLocator(verts)
+    bve = BVEOracle(verts, ql.tris, ql, 8, 12, 1.0, rossby_wave, n_maps=5).run()
+    assert bve.Nc == int(d["Nc"])
+    assert bve.ns == list(d["ns"])
+    np.testing.assert_allclose(bve.stack[:bve.Nc], d["vals"], rtol=0, atol=1e-11)
+    img = bve.composite()(d["q"])
+    np.testing.assert_allclose(img, d["img"], rtol=0, atol=1e-12)
