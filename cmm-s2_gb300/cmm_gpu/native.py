@@ -1,0 +1,155 @@
+"""ctypes binding of libcmmgpu.so (the C ABI declared in include/cmm_gpu.h).
+
+The library is built in-tree by ``__graft_entry__.build()`` into
+``cmm-s2_gb300/lib/libcmmgpu.so``.  There is no fallback: importing this
+module without the library, or calling it without a CUDA device, raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+import torch
+
+_LIB_PATH = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "lib",
+                         "libcmmgpu.so")
+
+if not os.path.exists(_LIB_PATH):
+    raise ImportError(f"libcmmgpu.so not built ({_LIB_PATH}); run __graft_entry__.build()")
+
+lib = ctypes.CDLL(_LIB_PATH)
+
+_p, _i, _i64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64
+_SIGS = {
+    "cmm_last_error": (ctypes.c_char_p, []),
+    "cmm_version": (_i, []),
+    "cmm_mesh_create": (_i, [_p, _i, _p, _i, _i, ctypes.POINTER(_p)]),
+    "cmm_mesh_destroy": (_i, [_p]),
+    "cmm_mesh_check": (_i, [_p, _i, _p, _i, _i, _p]),
+    "cmm_mesh_status": (_i, [_p, _p, ctypes.POINTER(_i), _i]),
+    "cmm_coeff_stride": (_i, [_i]),
+    "cmm_locate": (_i, [_p, _p, _i64, _p, _p, _p]),
+    "cmm_assemble": (_i, [_p, _p, _i, _p, _p]),
+    "cmm_compose": (_i, [_p, ctypes.POINTER(_p), _i, _p, _i64, _p, _p, _p, _p, _p]),
+    "cmm_stencil_eval": (_i, [_p, _p, _p, _p, _i64, _p, _p]),
+}
+for _name, (_res, _args) in _SIGS.items():
+    _f = getattr(lib, _name)
+    _f.restype, _f.argtypes = _res, _args
+
+STATUS = {0: "OK", 1: "ERR_ARG", 2: "ERR_MESH", 3: "ERR_CUDA", 4: "ERR_NONFINITE", 5: "ERR_LOCATE",
+          6: "ERR_TIMEOUT", 7: "ERR_UNSUPPORTED"}
+FLAG_NONFINITE, FLAG_LOCATE = 1, 2
+
+
+class CmmError(RuntimeError):
+    def __init__(self, code, where):
+        msg = lib.cmm_last_error().decode(errors="replace")
+        super().__init__(f"{where}: {STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+def check(code, where):
+    if code != 0:
+        raise CmmError(code, where)
+
+
+def exported_symbols():
+    return sorted(_SIGS)
+
+
+def mesh_check(verts, tris, level):
+    """Host-only hierarchy build; returns the leaf -> row table (no GPU needed)."""
+    verts = np.ascontiguousarray(verts, dtype=np.float64)
+    tris = np.ascontiguousarray(tris, dtype=np.int32)
+    rows = np.empty(len(tris), dtype=np.int32)
+    check(lib.cmm_mesh_check(verts.ctypes.data, len(verts), tris.ctypes.data, len(tris), level,
+                             rows.ctypes.data), "cmm_mesh_check")
+    return rows
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def _stream(device=None):
+    return ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)
+
+
+def _dev(t, dtype=torch.float64):
+    if not (isinstance(t, torch.Tensor) and t.is_cuda):
+        raise TypeError("expected a CUDA tensor")
+    if t.dtype != dtype:
+        raise TypeError(f"expected {dtype}, got {t.dtype}")
+    return t.contiguous()
+
+
+class Mesh:
+    """Device context of an icosahedral mesh (cmm_mesh_create)."""
+
+    def __init__(self, verts, tris, level, device=None):
+        verts = np.ascontiguousarray(verts, dtype=np.float64)
+        tris = np.ascontiguousarray(tris, dtype=np.int32)
+        self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
+        self.nv, self.nt, self.level = len(verts), len(tris), level
+        h = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            check(lib.cmm_mesh_create(verts.ctypes.data, len(verts), tris.ctypes.data, len(tris),
+                                      level, ctypes.byref(h)), "cmm_mesh_create")
+        self.h = h
+        self.stride = lib.cmm_coeff_stride(3)
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h is not None and h.value:
+            lib.cmm_mesh_destroy(h)
+            self.h = None
+
+    # ------------------------------------------------------------------
+    def status(self, clear=True):
+        f = ctypes.c_int()
+        check(lib.cmm_mesh_status(self.h, _stream(self.device), ctypes.byref(f), int(clear)),
+              "cmm_mesh_status")
+        return f.value
+
+    def new_coeffs(self, ncomp=3, batch=()):
+        return torch.zeros((*batch, self.nt, lib.cmm_coeff_stride(ncomp)), dtype=torch.float64,
+                           device=self.device)
+
+    def locate(self, q, want_bcc=True):
+        q = _dev(q)
+        n = q.shape[0]
+        tri = torch.empty(n, dtype=torch.int32, device=q.device)
+        bcc = torch.empty((n, 3), dtype=torch.float64, device=q.device) if want_bcc else None
+        check(lib.cmm_locate(self.h, _ptr(q), n, _ptr(tri), _ptr(bcc), _stream(q.device)), "cmm_locate")
+        return tri, bcc
+
+    def assemble(self, jets, out=None):
+        jets = _dev(jets)
+        ncomp = jets.shape[0] if jets.dim() == 3 else 1
+        if out is None:
+            out = self.new_coeffs(ncomp)
+        check(lib.cmm_assemble(self.h, _ptr(jets), ncomp, _ptr(out), _stream(jets.device)),
+              "cmm_assemble")
+        return out
+
+    def compose(self, coeffs, q, want_tri=False, want_tri_all=False, want_jac=False, out=None):
+        """coeffs: list of coefficient tensors, submap 0 first (applied last)."""
+        q = _dev(q)
+        n = q.shape[0]
+        S = len(coeffs)
+        arr = (ctypes.c_void_p * S)(*[c.data_ptr() for c in coeffs])
+        out = torch.empty((n, 3), dtype=torch.float64, device=q.device) if out is None else out
+        tri = torch.empty(n, dtype=torch.int32, device=q.device) if want_tri else None
+        tri_all = torch.empty((S, n), dtype=torch.int32, device=q.device) if want_tri_all else None
+        jac = torch.empty((n, 3, 3), dtype=torch.float64, device=q.device) if want_jac else None
+        check(lib.cmm_compose(self.h, arr, S, _ptr(q), n, _ptr(out), _ptr(tri), _ptr(tri_all),
+                              _ptr(jac), _stream(q.device)), "cmm_compose")
+        return out, tri, tri_all, jac
+
+    def stencil_eval(self, coeffs, yn, st):
+        yn, st = _dev(yn), _dev(st)
+        nv = yn.shape[1]
+        out = torch.empty_like(st)
+        check(lib.cmm_stencil_eval(self.h, _ptr(coeffs), _ptr(yn), _ptr(st), nv, _ptr(out),
+                                   _stream(yn.device)), "cmm_stencil_eval")
+        return out

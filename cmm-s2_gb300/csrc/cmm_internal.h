@@ -1,0 +1,94 @@
+// Internal declarations shared by the host and device translation units of
+// libcmmgpu.so.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+#include "../../include/cmm_gpu.h"
+
+namespace cmm {
+
+// Per-triangle location record (doubles): rows r1,r2,r3 of the inverse of
+// the vertex matrix [v1 v2 v3] (bcc_i = r_i . q), then |v1+v2+v3|,
+// |v1+v2|, |v2+v3|, |v3+v1|, 3 doubles of padding.
+constexpr int kLocStride = 16;
+// Per-triangle assembly factors (doubles): for each of the 9 gradient
+// ordinates 3..11 (a_x, a_y, a_z, b) with c = a . grad f(v) - b f(v);
+// then the edge-midpoint barycentrics E0[0],E0[1],E1[1],E1[2],E2[0],E2[2]
+// used by ordinates 12..17, the centre barycentrics mid[0..2] (ordinate
+// 18) and 3 doubles of padding.
+constexpr int kAsmStride = 48;
+constexpr int kCoeffStride3 = 64;   // 19 ordinates x 3 components, padded
+constexpr int kCoeffStride1 = 24;   // 19 ordinates, padded
+
+// Device view of an icosahedral mesh.
+struct MeshView {
+  int level, nv, nt;
+  const double* verts;      // (nv,4) x,y,z,0
+  const int4* tri_v;        // (nt) vertex ids of each reference row
+  const double* tri_loc;    // (nt, kLocStride)
+  const double* tri_asm;    // (nt, kAsmStride)
+  const double* root;       // 20 faces x 12: centroid(3), edge normals ab,bc,ca (9)
+  const float* root_f;      // same, FP32
+  const int* root_adj;      // 20 x 3: face across edge ab, bc, ca
+  const double* node_n;     // hierarchy nodes x 9: normals n0,n1,n2 (levels 0..level-1)
+  const float* node_nf;     // same, FP32, unit normals
+  const int* leaf_row;      // (nt) hierarchical leaf -> reference row
+  int* status;              // device status word
+};
+
+// Ordinates of the quadratic patch in each Powell-Sabin sub-triangle,
+// expressed in the sub-triangle's own (V, E, C) corners -- V the triangle
+// vertex with the largest barycentric, E the midpoint of the edge from V to
+// the middle vertex, C the split centre -- in the order
+// V^2, E^2, C^2, 2VE, 2EC, 2VC.  Indexed [argmin][argmax]; built on the
+// host from the reference's ordinate and corner tables.
+struct SplitTables {
+  int ord[3][3][6];
+};
+
+void set_last_error(const std::string& s);
+int cuda_fail(cudaError_t e, const char* what);
+
+struct DeviceBuffer {
+  void* p = nullptr;
+  size_t bytes = 0;
+  ~DeviceBuffer();
+  int alloc(size_t n);
+  int upload(const void* src, size_t n);
+};
+
+}  // namespace cmm
+
+struct cmm_mesh {
+  cmm::MeshView view;
+  cmm::DeviceBuffer verts, tri_v, tri_loc, tri_asm, root, root_f, root_adj, node_n, node_nf, leaf_row,
+      status;
+};
+
+namespace cmm {
+// kernels (locate.cu)
+int launch_locate(const MeshView& m, const double* q, int64_t n, int32_t* tri, double* bcc,
+                  cudaStream_t s);
+int launch_assemble(const MeshView& m, const double* jets, int ncomp, double* coeffs,
+                    cudaStream_t s);
+int launch_compose(const MeshView& m, const double* const* coeffs, int S, const double* q,
+                   int64_t n, double* out, int32_t* tri, int32_t* tri_all, double* jac,
+                   cudaStream_t s);
+int launch_stencil_eval(const MeshView& m, const double* coeffs, const double* yn,
+                        const double* st, int64_t nv, double* out, cudaStream_t s);
+int set_split_tables();
+// Host-side tables of an icosahedral mesh (before upload).
+struct HostMesh {
+  int level = 0, nv = 0, nt = 0;
+  std::vector<double> vpad, loc, asmf, root, node_n;
+  std::vector<float> node_nf;
+  std::vector<int4> tv;
+  std::vector<int> root_adj, leaf_row;
+};
+int build_host(const double* verts, int nv, const int32_t* tris, int nt, int level, HostMesh* hm);
+int upload_mesh(const HostMesh& h, cmm_mesh* m);
+const char* last_error();
+}  // namespace cmm

@@ -54,13 +54,20 @@ def assemble(verts, tris, vals, geom=None):
     return out
 
 
-def split_corners(vs, bcc):
-    """Sub-triangle corners (new_vpoints, cmm_s2/core/spherical_spline.py:668-697)."""
+def split_corners(vs, bcc, tie_fix=False):
+    """Sub-triangle corners (new_vpoints, cmm_s2/core/spherical_spline.py:668-697).
+
+    With tie_fix, a query at the split centre (all bcc equal, where the
+    reference's tables select no sub-triangle and it returns 0/0) uses the
+    sub-triangle (argmin, argmax) = (1, 0) instead."""
     v1, v2, v3 = vs[:, 0], vs[:, 1], vs[:, 2]
     e1, e2, e3 = unit_rows(v1 / 2 + v2 / 2), unit_rows(v2 / 2 + v3 / 2), unit_rows(v3 / 2 + v1 / 2)
     v4 = unit_rows((v1 + v2 + v3) / 3)
     pool = np.stack([v1, v2, v3, v4, e1, e2, e3])          # (7,N,3)
     lo, hi = np.argmin(bcc, axis=1), np.argmax(bcc, axis=1)
+    if tie_fix:
+        tie = lo == hi
+        lo, hi = np.where(tie, 1, lo), np.where(tie, 0, hi)
     js = SPLIT_CORNERS[lo, hi]                               # (N,3)
     n = np.arange(len(bcc))
     return np.stack([pool[js[:, 0], n], pool[js[:, 1], n], pool[js[:, 2], n]], 1), lo, hi
@@ -73,10 +80,10 @@ def _sbb(cf, b):
             + 2 * (b[:, 2] * b[:, 0]) * cf[..., 5, :])
 
 
-def eval_patch(coeffs, tri, bcc_big, vs, pts):
+def eval_patch(coeffs, tri, bcc_big, vs, pts, tie_fix=False):
     """Evaluate un-normalised patches at ``pts`` located in ``tri`` with
     big-triangle bcc ``bcc_big``; coeffs (...,19,Nt).  Returns (...,N)."""
-    vn, lo, hi = split_corners(vs, bcc_big)
+    vn, lo, hi = split_corners(vs, bcc_big, tie_fix)
     ords = SPLIT_ORDINATES[lo, hi]
     b = bary(vn[:, 0], vn[:, 1], vn[:, 2], pts)
     cf = np.stack([coeffs[..., ords[:, k], tri] for k in range(6)], axis=-2)
@@ -86,15 +93,16 @@ def eval_patch(coeffs, tri, bcc_big, vs, pts):
 class MapOracle:
     """sphere_diffeomorphism (cmm_s2/core/spherical_spline.py:155-337)."""
 
-    def __init__(self, verts, tris, locator, vals, geom=None):
+    def __init__(self, verts, tris, locator, vals, geom=None, tie_fix=False):
         self.verts, self.tris, self.loc = verts, tris, locator
+        self.tie_fix = tie_fix
         self.vals = vals
         self.coeffs = assemble(verts, tris, vals, geom)
 
     def __call__(self, q):
         """__call__ (:178-205): normalised image, (3,N)."""
         bcc, tri, vs = query(self.verts, self.tris, self.loc, q)
-        out = eval_patch(self.coeffs, tri, bcc, vs, q)
+        out = eval_patch(self.coeffs, tri, bcc, vs, q, self.tie_fix)
         nrm = np.sqrt(out[0] ** 2 + out[1] ** 2 + out[2] ** 2)
         return (1 / nrm)[None] * out
 
@@ -102,7 +110,7 @@ class MapOracle:
         """stencil_eval (:268-298): locate at q_pts (3,N), evaluate the four
         stencil points st_pts (3,4,N) in that sub-triangle, not normalised."""
         bcc, tri, vs = query(self.verts, self.tris, self.loc, q_pts.T)
-        vn, lo, hi = split_corners(vs, bcc)
+        vn, lo, hi = split_corners(vs, bcc, self.tie_fix)
         ords = SPLIT_ORDINATES[lo, hi]
         cf = np.stack([self.coeffs[:, ords[:, k], tri] for k in range(6)], axis=-2)
         out = np.empty_like(st_pts)
@@ -115,8 +123,9 @@ class MapOracle:
 class CompositeOracle:
     """composite_sphere_diffeomorphism (cmm_s2/core/spherical_spline.py:340-508)."""
 
-    def __init__(self, verts, tris, locator, vals_stack, geom=None):
+    def __init__(self, verts, tris, locator, vals_stack, geom=None, tie_fix=False):
         self.verts, self.tris, self.loc = verts, tris, locator
+        self.tie_fix = tie_fix
         self.geom = geom if geom is not None else ps_split(verts, tris)
         self.vals = vals_stack
         self.coeffs = np.stack([assemble(verts, tris, v, self.geom) for v in vals_stack])
@@ -131,7 +140,7 @@ class CompositeOracle:
         tris, pts = [], []
         for i in reversed(range(n_c)):
             bcc, tri, vs = query(self.verts, self.tris, self.loc, p)
-            out = eval_patch(self.coeffs[i], tri, bcc, vs, p)
+            out = eval_patch(self.coeffs[i], tri, bcc, vs, p, self.tie_fix)
             nrm = np.sqrt(out[0] ** 2 + out[1] ** 2 + out[2] ** 2)
             tris.append(tri)
             pts.append(p)
@@ -142,7 +151,7 @@ class CompositeOracle:
 
 
 # ---------------------------------------------------------------- Jacobians
-def patch_jacobian(coeffs, tri, bcc_big, vs, p):
+def patch_jacobian(coeffs, tri, bcc_big, vs, p, tie_fix=False):
     """Tangent Jacobian of one normalised submap at p (N,3): (N,3,3).
 
     The reference's ``eval_grad`` (cmm_s2/core/spherical_spline.py:208-265)
@@ -151,7 +160,7 @@ def patch_jacobian(coeffs, tri, bcc_big, vs, p):
     (:700-713) and the normalisation derivative (:247-263):
     P(x) = sum_k B_k(gamma(x)) c_k with gamma linear in x,
     J = (I - s s^T) DP (I - p p^T) / |P|, s = P/|P|."""
-    vn, lo, hi = split_corners(vs, bcc_big)
+    vn, lo, hi = split_corners(vs, bcc_big, tie_fix)
     ords = SPLIT_ORDINATES[lo, hi]
     b = bary(vn[:, 0], vn[:, 1], vn[:, 2], p)
     eye = np.eye(3)
@@ -179,7 +188,7 @@ def composite_jacobian(comp, q, n_c=None):
     J = np.broadcast_to(np.eye(3), (len(q), 3, 3)).copy()
     for i in reversed(range(n_c)):
         bcc, tri, vs = query(comp.verts, comp.tris, comp.loc, p)
-        Ji, s = patch_jacobian(comp.coeffs[i], tri, bcc, vs, p)
+        Ji, s = patch_jacobian(comp.coeffs[i], tri, bcc, vs, p, comp.tie_fix)
         J = np.einsum("nab,nbc->nac", Ji, J)
         p = s
     return p, J

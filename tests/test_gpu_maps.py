@@ -1,0 +1,198 @@
+"""GPU parity: point location, assembly, map evaluation, composition,
+stencil evaluation and Jacobians of libcmmgpu.so against the oracle and the
+reference's golden outputs.
+
+Tolerances: triangle ids bit-exact except for queries within 1e-14 of an
+edge of the oracle's triangle (either neighbour contains them; counted);
+FP64 map coordinates within 1e-12 (relative to |X| = 1); barycentrics and
+ordinates within 1e-13; Jacobians within 1e-10 (relative to |J|)."""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import GOLDEN
+from oracle import geometry as OG
+from oracle import spline as OS
+
+pytestmark = pytest.mark.gpu
+EDGE_TOL = 1e-14
+
+
+@pytest.fixture(scope="module")
+def nat():
+    import __graft_entry__
+    __graft_entry__.build()
+    from cmm_gpu import native
+    return native
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def host(t):
+    return t.cpu().numpy()
+
+
+def golden(name):
+    return np.load(os.path.join(GOLDEN, name))
+
+
+def coeff_record_to_ref(rec, nt):
+    """(nt,64) device record -> reference layout (3,19,nt)."""
+    return rec[:, :57].reshape(nt, 19, 3).transpose(2, 1, 0)
+
+
+@pytest.mark.parametrize("level", [3, 4])
+def test_locate_matches_reference_qhull(nat, level):
+    d = golden(f"mesh_l{level}.npz")
+    m = nat.Mesh(d["verts"], d["tris"], level)
+    tri, bcc = m.locate(dev(d["q"]))
+    tri, bcc = host(tri), host(bcc)
+    diff = tri != d["tri"]
+    near = OG.edge_distance(d["verts"], d["tris"], d["tri"], d["q"]) <= EDGE_TOL
+    assert not (diff & ~near).any()
+    # a disagreement is another container of the query
+    assert (OG.edge_distance(d["verts"], d["tris"], tri[diff], d["q"][diff]) <= EDGE_TOL).all()
+    same = ~diff
+    np.testing.assert_allclose(bcc[same], d["bcc"][same], rtol=0, atol=1e-13)
+    assert m.status() == 0
+    print(f"level {level}: {diff.sum()} of {len(tri)} near-edge queries resolved to the neighbour")
+
+
+@pytest.mark.parametrize("level", [5, 7])
+def test_locate_large_levels_against_cone_oracle(nat, level):
+    from cmm_gpu.meshgen import icosahedral_mesh, random_sphere_points
+    verts, tris = icosahedral_mesh(level)
+    q = random_sphere_points(200_000, seed=level)
+    m = nat.Mesh(verts, tris, level)
+    tri, bcc = m.locate(dev(q))
+    tri = host(tri)
+    ref = OG.ConeLocator(verts, tris).locate(q)
+    diff = tri != ref
+    near = OG.edge_distance(verts, tris, ref, q) <= EDGE_TOL
+    assert not (diff & ~near).any()
+    b = host(bcc)
+    assert b.min() > -1e-12
+    assert m.status() == 0
+
+
+def test_assemble_matches_reference(nat):
+    d, g = golden("map_l3.npz"), golden("mesh_l3.npz")
+    m = nat.Mesh(g["verts"], g["tris"], 3)
+    rec = host(m.assemble(dev(d["jets"][0])))
+    np.testing.assert_allclose(coeff_record_to_ref(rec, len(g["tris"])), d["coeffs0"], rtol=0, atol=1e-13)
+
+
+def test_map_eval_and_composite_match_reference(nat):
+    d, g = golden("map_l3.npz"), golden("mesh_l3.npz")
+    m = nat.Mesh(g["verts"], g["tris"], 3)
+    cs = [m.assemble(dev(j)) for j in d["jets"]]
+    out, tri, _, _ = m.compose(cs[:1], dev(d["q"]), want_tri=True)
+    out = host(out)
+    ok = np.isfinite(d["img"]).all(0)
+    assert (~ok).sum() > 0  # the fixture holds split-centre ties
+    np.testing.assert_allclose(out[ok], d["img"].T[ok], rtol=0, atol=1e-12)
+    # at the split centre the reference divides 0/0; the library returns the
+    # (continuous) value of a sub-triangle, equal to the tie-broken oracle
+    orc = OS.MapOracle(g["verts"], g["tris"], OG.ConeLocator(g["verts"], g["tris"]), d["jets"][0],
+                       tie_fix=True)
+    np.testing.assert_allclose(out[~ok], orc(d["q"][~ok]).T, rtol=0, atol=1e-12)
+    cout, _, _, _ = m.compose(cs, dev(d["q"]))
+    cout = host(cout)
+    fin = np.isfinite(d["comp_img"]).all(1)
+    np.testing.assert_allclose(cout[fin], d["comp_img"][fin], rtol=0, atol=1e-12)
+    assert np.isfinite(cout).all()
+    assert m.status() == 0
+
+
+def test_stencil_eval_matches_reference(nat):
+    d, g = golden("map_l3.npz"), golden("mesh_l3.npz")
+    m = nat.Mesh(g["verts"], g["tris"], 3)
+    c = m.assemble(dev(d["jets"][0]))
+    st = host(m.stencil_eval(c, dev(d["yn"]), dev(d["sp"])))
+    np.testing.assert_allclose(st, d["st"], rtol=0, atol=1e-12)
+
+
+def make_stack(level, S, seed):
+    from cmm_gpu.meshgen import icosahedral_mesh
+    from cmm_gpu.workloads import submap_stack
+    verts, tris = icosahedral_mesh(level)
+    tan, s_pts = OG.stencil_points(verts)
+    return verts, tris, submap_stack(s_pts, tan, S, seed=seed)
+
+
+def test_composition_level5_eight_submaps(nat):
+    from cmm_gpu.meshgen import random_sphere_points
+    verts, tris, jets = make_stack(5, 8, seed=11)
+    q = random_sphere_points(20_000, seed=12)
+    m = nat.Mesh(verts, tris, 5)
+    cs = [m.assemble(dev(j)) for j in jets]
+    out, tri, tri_all, _ = m.compose(cs, dev(q), want_tri=True, want_tri_all=True)
+    comp = OS.CompositeOracle(verts, tris, OG.ConeLocator(verts, tris), jets, tie_fix=True)
+    ref, rtri, pts = comp(q, record=True)
+    np.testing.assert_allclose(host(out), ref, rtol=0, atol=1e-12)
+    ta = host(tri_all)[::-1]          # application order: submap S-1 first
+    np.testing.assert_array_equal(host(tri), ta[0])
+    for s in range(8):
+        diff = ta[s] != rtri[s]
+        near = OG.edge_distance(verts, tris, rtri[s], pts[s]) <= 1e-13
+        assert not (diff & ~near).any(), s
+
+
+def test_jacobian_against_oracle_and_differences(nat):
+    from cmm_gpu.meshgen import random_sphere_points
+    verts, tris, jets = make_stack(4, 3, seed=21)
+    q = random_sphere_points(3000, seed=22)
+    m = nat.Mesh(verts, tris, 4)
+    cs = [m.assemble(dev(j)) for j in jets]
+    out, _, _, jac = m.compose(cs, dev(q), want_jac=True)
+    comp = OS.CompositeOracle(verts, tris, OG.ConeLocator(verts, tris), jets, tie_fix=True)
+    X, J = OS.composite_jacobian(comp, q)
+    J_gpu = host(jac)
+    scale = np.abs(J).max(axis=(1, 2))[:, None, None]
+    np.testing.assert_allclose(J_gpu / scale, J / scale, rtol=0, atol=1e-10)
+    # tangent map: J q = 0 and X . J = 0
+    assert np.abs(np.einsum("nij,nj->ni", J_gpu, q)).max() < 1e-12
+    assert np.abs(np.einsum("ni,nij->nj", host(out), J_gpu)).max() < 1e-12
+    # central differences along a tangent direction (away from edges)
+    t = np.cross(q, [0.3, -0.5, 0.8])
+    t /= np.linalg.norm(t, axis=1)[:, None]
+    h = 1e-6
+    qp = q + h * t
+    qm = q - h * t
+    qp /= np.linalg.norm(qp, axis=1)[:, None]
+    qm /= np.linalg.norm(qm, axis=1)[:, None]
+    fp, _, tap, _ = m.compose(cs, dev(qp), want_tri_all=True)
+    fm, _, tam, _ = m.compose(cs, dev(qm), want_tri_all=True)
+    same = (host(tap) == host(tam)).all(0)
+    fd = (host(fp) - host(fm)) / (2 * h)
+    an = np.einsum("nij,nj->ni", J_gpu, t)
+    assert same.mean() > 0.9
+    np.testing.assert_allclose(fd[same], an[same], rtol=0, atol=2e-6 * np.abs(an).max())
+
+
+def test_edge_cases(nat):
+    from cmm_gpu.meshgen import icosahedral_mesh
+    verts, tris = icosahedral_mesh(2)
+    m = nat.Mesh(verts, tris, 2)
+    c = m.new_coeffs()
+    empty = torch.empty((0, 3), dtype=torch.float64, device="cuda")
+    out, tri, _, _ = m.compose([c], empty, want_tri=True)
+    assert out.shape == (0, 3)
+    q = dev(np.array([[np.nan, 0.0, 1.0], [0.0, 0.0, 1.0]]))
+    tri, _ = m.locate(q)
+    assert host(tri)[0] == -1
+    assert m.status(clear=True) & nat.FLAG_NONFINITE
+    assert m.status() == 0
+    with pytest.raises(nat.CmmError) as e:
+        m.compose([c] * 1025, dev(np.zeros((1, 3))))
+    assert e.value.code == 1
+    with pytest.raises(TypeError):
+        m.locate(torch.zeros((3, 3)))
+    # the poles and the 12 base vertices locate without a status flag
+    q = dev(verts[[0, -1] + list(range(1, 11))])
+    tri, bcc = m.locate(q)
+    assert (host(tri) >= 0).all() and m.status() == 0
