@@ -95,6 +95,23 @@ def mwss_angles(L):
     return np.pi * np.arange(L + 1) / L, 2 * np.pi * np.arange(2 * L) / (2 * L)
 
 
+def latlon_mesh_arrays(L):
+    """Arrays of the MWSS lat-lon velocity mesh as the reference builds them
+    (cmm_s2/core/mesh_functions.py:175-194, 332-350): ring colatitudes
+    theta (L+1,), longitudes phi (2L,), ring points grid (3, L+1, 2L) =
+    sphere2cart(phi, theta), and the mesh vertices (2+(L-1)*2L, 3): north
+    pole, interior rings row by row, south pole, converted from
+    (lon, lat = pi/2 - theta) the way stripy does."""
+    theta, phi = mwss_angles(L)
+    Phi, The = np.meshgrid(phi, theta)
+    grid = np.array([np.sin(The) * np.cos(Phi), np.sin(The) * np.sin(Phi), np.cos(The)])
+    XX = np.meshgrid(phi, theta[1:-1])
+    lons = np.concatenate([[0.0], XX[0].reshape(-1), [0.0]])
+    lats = np.concatenate([[np.pi / 2], -XX[1].reshape(-1) + np.pi / 2, [-np.pi / 2]])
+    verts = np.stack([np.cos(lats) * np.cos(lons), np.cos(lats) * np.sin(lons), np.sin(lats)], 1)
+    return theta, phi, grid, verts
+
+
 def random_sphere_points(n, seed):
     """``n`` points uniform on the unit sphere (normalised Gaussians), (n,3)."""
     rng = np.random.default_rng(seed)

@@ -18,7 +18,7 @@ if not os.path.exists(_LIB_PATH):
 
 lib = ctypes.CDLL(_LIB_PATH)
 
-_p, _i, _i64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64
+_p, _i, _i64, _d = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_double
 _SIGS = {
     "cmm_last_error": (ctypes.c_char_p, []),
     "cmm_version": (_i, []),
@@ -31,6 +31,12 @@ _SIGS = {
     "cmm_assemble": (_i, [_p, _p, _i, _p, _p]),
     "cmm_compose": (_i, [_p, ctypes.POINTER(_p), _i, _p, _i64, _p, _p, _p, _p, _p]),
     "cmm_stencil_eval": (_i, [_p, _p, _p, _p, _i64, _p, _p]),
+    "cmm_velmesh_create": (_i, [_i, _p, _p, _p, _p, ctypes.POINTER(_p)]),
+    "cmm_velocity_eval": (_i, [_p, ctypes.POINTER(_p), _i, _d, _d, _d, _p, _i64, _p, _p]),
+    "cmm_integrate": (_i, [_p, ctypes.POINTER(_p), _i, _d, _i, _d, _d, _p, _i64, _p, _p]),
+    "cmm_advect_workspace": (_i64, [_p]),
+    "cmm_advect_project": (_i, [_p, _p, ctypes.POINTER(_p), _i, _d, _i, _d, _d, _p, _p, _p, _d, _p,
+                                _p, _p]),
 }
 for _name, (_res, _args) in _SIGS.items():
     _f = getattr(lib, _name)
@@ -152,4 +158,57 @@ class Mesh:
         out = torch.empty_like(st)
         check(lib.cmm_stencil_eval(self.h, _ptr(coeffs), _ptr(yn), _ptr(st), nv, _ptr(out),
                                    _stream(yn.device)), "cmm_stencil_eval")
+        return out
+
+    def advect_project(self, velmesh, vel_coeffs, ts0, scheme, t, dt, s_pts, tan, prev_coeffs,
+                       eps=1e-5, jets=None, work=None):
+        """One CMM map update; returns (jets (3,4,nv), work)."""
+        s_pts, tan = _dev(s_pts), _dev(tan)
+        if jets is None:
+            jets = torch.empty((3, 4, self.nv), dtype=torch.float64, device=s_pts.device)
+        if work is None:
+            work = torch.empty(lib.cmm_advect_workspace(self.h), dtype=torch.float64,
+                               device=s_pts.device)
+        arr = (ctypes.c_void_p * len(vel_coeffs))(*[c.data_ptr() for c in vel_coeffs])
+        check(lib.cmm_advect_project(self.h, velmesh.h, arr, len(vel_coeffs), ts0, scheme, t, dt,
+                                     _ptr(s_pts), _ptr(tan), _ptr(prev_coeffs), eps, _ptr(jets),
+                                     _ptr(work), _stream(s_pts.device)), "cmm_advect_project")
+        return jets, work
+
+
+EULER, IMPROVED_EULER, RK4 = 0, 1, 2
+
+
+class VelMesh(Mesh):
+    """Device context of the MWSS lat-lon velocity mesh (cmm_velmesh_create)."""
+
+    def __init__(self, L, theta, phi, grid, verts, device=None):  # noqa: super not called
+        theta = np.ascontiguousarray(theta, dtype=np.float64)
+        phi = np.ascontiguousarray(phi, dtype=np.float64)
+        grid = np.ascontiguousarray(np.asarray(grid, dtype=np.float64).reshape(3, -1))
+        verts = np.ascontiguousarray(verts, dtype=np.float64)
+        self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
+        self.L, self.nv, self.level = L, len(verts), -1
+        self.nt = 4 * L * (L - 1)
+        h = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            check(lib.cmm_velmesh_create(L, theta.ctypes.data, phi.ctypes.data, grid.ctypes.data,
+                                         verts.ctypes.data, ctypes.byref(h)), "cmm_velmesh_create")
+        self.h = h
+        self.stride = lib.cmm_coeff_stride(3)
+
+    def velocity(self, vel_coeffs, ts0, t, dt, x):
+        x = _dev(x)
+        out = torch.empty_like(x)
+        arr = (ctypes.c_void_p * len(vel_coeffs))(*[c.data_ptr() for c in vel_coeffs])
+        check(lib.cmm_velocity_eval(self.h, arr, len(vel_coeffs), ts0, t, dt, _ptr(x), x.shape[1],
+                                    _ptr(out), _stream(x.device)), "cmm_velocity_eval")
+        return out
+
+    def integrate(self, vel_coeffs, ts0, scheme, t, dt, x):
+        x = _dev(x)
+        out = torch.empty_like(x)
+        arr = (ctypes.c_void_p * len(vel_coeffs))(*[c.data_ptr() for c in vel_coeffs])
+        check(lib.cmm_integrate(self.h, arr, len(vel_coeffs), ts0, scheme, t, dt, _ptr(x), x.shape[1],
+                                _ptr(out), _stream(x.device)), "cmm_integrate")
         return out

@@ -25,7 +25,7 @@ int cmm_mesh_create(const double* verts, int nv, const int32_t* tris, int nt, in
   *out = nullptr;
   cmm_mesh* m = new (std::nothrow) cmm_mesh();
   if (!m) return arg_error("cmm_mesh_create: out of host memory");
-  int rc = set_split_tables();
+  int rc = CMM_OK;
   HostMesh hm;
   if (!rc) rc = build_host(verts, nv, tris, nt, level, &hm);
   if (!rc) rc = upload_mesh(hm, m);
@@ -74,7 +74,116 @@ int cmm_coeff_stride(int ncomp) {
 int cmm_locate(const cmm_mesh* mesh, const double* q, int64_t n, int32_t* tri, double* bcc,
                void* stream) {
   if (!mesh || n < 0 || (n > 0 && (!q || !tri))) return arg_error("cmm_locate: bad argument");
+  if (mesh->view.kind == kLatLon)
+    return launch_latlon_locate(mesh->view, q, n, tri, bcc, (cudaStream_t)stream);
   return launch_locate(mesh->view, q, n, tri, bcc, (cudaStream_t)stream);
+}
+
+int cmm_velmesh_create(int L, const double* theta, const double* phi, const double* grid,
+                       const double* verts, cmm_mesh** out) {
+  if (!theta || !phi || !grid || !verts || !out) return arg_error("cmm_velmesh_create: null pointer");
+  *out = nullptr;
+  cmm_mesh* m = new (std::nothrow) cmm_mesh();
+  if (!m) return arg_error("cmm_velmesh_create: out of host memory");
+  int rc = build_latlon(L, theta, phi, grid, verts, m);
+  if (rc) {
+    delete m;
+    return rc;
+  }
+  *out = m;
+  return CMM_OK;
+}
+
+namespace {
+int vel_args(const cmm_mesh* vm, const double* const* vc, int nvs, VelPtrs* out, const char* who) {
+  if (!vm || vm->view.kind != kLatLon) {
+    set_last_error(std::string(who) + ": velocity mesh expected");
+    return CMM_ERR_ARG;
+  }
+  if (nvs < 1 || nvs > 3 || !vc) {
+    set_last_error(std::string(who) + ": nvs must be 1..3");
+    return CMM_ERR_ARG;
+  }
+  *out = VelPtrs{};
+  for (int l = 0; l < nvs; ++l) {
+    if (!vc[l]) {
+      set_last_error(std::string(who) + ": null velocity coefficients");
+      return CMM_ERR_ARG;
+    }
+    out->p[l] = vc[l];
+  }
+  return CMM_OK;
+}
+
+int stage_weights(int nvs, double ts0, int scheme, double t, double dt, TimeWeights* tw) {
+  // stage times of each integrator (cmm_s2/core/evolution_functions.py:19-67)
+  double times[4];
+  int nt;
+  if (scheme == CMM_EULER) {
+    times[0] = t;
+    nt = 1;
+  } else if (scheme == CMM_IMPROVED_EULER) {
+    times[0] = t;
+    times[1] = t + dt;
+    nt = 2;
+  } else if (scheme == CMM_RK4) {
+    times[0] = t + dt;
+    times[1] = t + dt / 2;
+    times[2] = t + 0.5 * dt;
+    times[3] = t;
+    nt = 4;
+  } else {
+    return arg_error("unknown integration scheme");
+  }
+  *tw = time_weights(nvs, ts0, dt, times, nt);
+  return CMM_OK;
+}
+}  // namespace
+
+int cmm_velocity_eval(const cmm_mesh* velmesh, const double* const* vel_coeffs, int nvs,
+                      double ts0, double t, double dt, const double* x, int64_t n, double* out,
+                      void* stream) {
+  VelPtrs vc;
+  int rc = vel_args(velmesh, vel_coeffs, nvs, &vc, "cmm_velocity_eval");
+  if (rc) return rc;
+  if (n < 0 || (n > 0 && (!x || !out))) return arg_error("cmm_velocity_eval: bad argument");
+  TimeWeights tw = time_weights(nvs, ts0, dt, &t, 1);
+  return launch_velocity_eval(velmesh->view, vc, nvs, tw, x, n, out, (cudaStream_t)stream);
+}
+
+int cmm_integrate(const cmm_mesh* velmesh, const double* const* vel_coeffs, int nvs, double ts0,
+                  int scheme, double t, double dt, const double* x, int64_t n, double* out,
+                  void* stream) {
+  VelPtrs vc;
+  int rc = vel_args(velmesh, vel_coeffs, nvs, &vc, "cmm_integrate");
+  if (rc) return rc;
+  if (n < 0 || (n > 0 && (!x || !out))) return arg_error("cmm_integrate: bad argument");
+  TimeWeights tw;
+  if ((rc = stage_weights(nvs, ts0, scheme, t, dt, &tw))) return rc;
+  return launch_integrate(velmesh->view, vc, nvs, tw, scheme, dt, x, n, out, (cudaStream_t)stream);
+}
+
+int64_t cmm_advect_workspace(const cmm_mesh* mesh) {
+  return mesh ? 15LL * mesh->view.nv : -1;
+}
+
+int cmm_advect_project(const cmm_mesh* mesh, const cmm_mesh* velmesh,
+                       const double* const* vel_coeffs, int nvs, double ts0, int scheme, double t,
+                       double dt, const double* s_pts, const double* tan,
+                       const double* prev_coeffs, double eps, double* jets, double* work,
+                       void* stream) {
+  if (!mesh || mesh->view.kind != kIcosahedral) return arg_error("cmm_advect_project: map mesh expected");
+  VelPtrs vc;
+  int rc = vel_args(velmesh, vel_coeffs, nvs, &vc, "cmm_advect_project");
+  if (rc) return rc;
+  if (!s_pts || !tan || !jets || !work) return arg_error("cmm_advect_project: null pointer");
+  TimeWeights tw;
+  if ((rc = stage_weights(nvs, ts0, scheme, t, dt, &tw))) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  if ((rc = launch_advect_points(mesh->view, velmesh->view, vc, nvs, tw, scheme, dt, s_pts, work, s)))
+    return rc;
+  const int64_t nv = mesh->view.nv;
+  return launch_project_jets(mesh->view, prev_coeffs, work, work + 3 * nv, tan, eps, jets, s);
 }
 
 int cmm_assemble(const cmm_mesh* mesh, const double* jets, int ncomp, double* coeffs,

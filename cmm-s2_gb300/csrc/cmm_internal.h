@@ -37,17 +37,17 @@ struct MeshView {
   const float* node_nf;     // same, FP32, unit normals
   const int* leaf_row;      // (nt) hierarchical leaf -> reference row
   int* status;              // device status word
+  // MWSS lat-lon velocity mesh (kind == kLatLon)
+  int kind;                 // kIcosahedral or kLatLon
+  int L;                    // band-limit: L+1 rings of 2L points
+  const double* theta;      // (L+1) ring colatitudes
+  const double* phi;        // (2L) longitudes
+  const double* grid;       // ((L+1)*2L, 4) ring points x,y,z,0
+  double dphi, dthe;
 };
 
-// Ordinates of the quadratic patch in each Powell-Sabin sub-triangle,
-// expressed in the sub-triangle's own (V, E, C) corners -- V the triangle
-// vertex with the largest barycentric, E the midpoint of the edge from V to
-// the middle vertex, C the split centre -- in the order
-// V^2, E^2, C^2, 2VE, 2EC, 2VC.  Indexed [argmin][argmax]; built on the
-// host from the reference's ordinate and corner tables.
-struct SplitTables {
-  int ord[3][3][6];
-};
+constexpr int kIcosahedral = 0;
+constexpr int kLatLon = 1;
 
 void set_last_error(const std::string& s);
 int cuda_fail(cudaError_t e, const char* what);
@@ -65,7 +65,7 @@ struct DeviceBuffer {
 struct cmm_mesh {
   cmm::MeshView view;
   cmm::DeviceBuffer verts, tri_v, tri_loc, tri_asm, root, root_f, root_adj, node_n, node_nf, leaf_row,
-      status;
+      status, theta, phi, grid;
 };
 
 namespace cmm {
@@ -79,7 +79,6 @@ int launch_compose(const MeshView& m, const double* const* coeffs, int S, const 
                    cudaStream_t s);
 int launch_stencil_eval(const MeshView& m, const double* coeffs, const double* yn,
                         const double* st, int64_t nv, double* out, cudaStream_t s);
-int set_split_tables();
 // Host-side tables of an icosahedral mesh (before upload).
 struct HostMesh {
   int level = 0, nv = 0, nt = 0;
@@ -91,4 +90,31 @@ struct HostMesh {
 int build_host(const double* verts, int nv, const int32_t* tris, int nt, int level, HostMesh* hm);
 int upload_mesh(const HostMesh& h, cmm_mesh* m);
 const char* last_error();
+
+// lat-lon velocity mesh (velmesh.cpp) and kernels (velocity.cu)
+int build_latlon(int L, const double* theta, const double* phi, const double* grid,
+                 const double* verts, cmm_mesh* m);
+void latlon_triangles(int L, std::vector<int4>& tv);
+
+// Lagrange weights of the velocity time levels for up to 4 evaluation
+// times (one per integrator stage).
+struct TimeWeights {
+  double w[4][3];
+};
+struct VelPtrs {
+  const double* p[3];
+};
+TimeWeights time_weights(int nvs, double ts0, double dt, const double* times, int ntimes);
+int launch_velocity_eval(const MeshView& vm, VelPtrs vc, int nvs, const TimeWeights& tw,
+                         const double* x, int64_t n, double* out, cudaStream_t s);
+int launch_integrate(const MeshView& vm, VelPtrs vc, int nvs, const TimeWeights& tw, int scheme,
+                     double dt, const double* x, int64_t n, double* out, cudaStream_t s);
+int launch_latlon_locate(const MeshView& vm, const double* q, int64_t n, int32_t* tri, double* bcc,
+                         cudaStream_t s);
+int launch_advect_points(const MeshView& mesh, const MeshView& vm, VelPtrs vc, int nvs,
+                         const TimeWeights& tw, int scheme, double dt, const double* s_pts,
+                         double* work, cudaStream_t s);
+int launch_project_jets(const MeshView& mesh, const double* prev_coeffs, const double* yn,
+                        const double* sn, const double* tan, double eps, double* jets,
+                        cudaStream_t s);
 }  // namespace cmm

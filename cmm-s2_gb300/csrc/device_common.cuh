@@ -1,0 +1,192 @@
+// Device helpers shared by the kernel translation units: icosahedral point
+// location, barycentrics, Powell-Sabin sub-triangle selection and the
+// quadratic Bernstein-Bezier patch.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "cmm_internal.h"
+
+namespace cmm {
+namespace dev {
+
+constexpr float kFilter = 1e-6f;
+
+// Ordinates of the quadratic patch of each Powell-Sabin sub-triangle in the
+// sub-triangle's own corners -- V the triangle vertex with the largest
+// barycentric, E the midpoint of the edge from V to the middle vertex, C
+// the split centre -- in the order V^2, E^2, C^2, 2VE, 2EC, 2VC; indexed
+// [argmin][argmax].  Derived from the reference's ordinate and corner
+// tables (cmm_s2/core/spherical_spline.py:660-666) by re-ordering each
+// entry's corners (tests/test_host_abi.py re-derives it).
+__constant__ const int kSplitOrd[3][3][6] = {
+    {{0, 0, 0, 0, 0, 0}, {1, 13, 18, 6, 16, 7}, {2, 13, 18, 11, 16, 10}},
+    {{0, 14, 18, 5, 17, 4}, {0, 0, 0, 0, 0, 0}, {2, 14, 18, 9, 17, 10}},
+    {{0, 12, 18, 3, 15, 4}, {1, 12, 18, 8, 15, 7}, {0, 0, 0, 0, 0, 0}}};
+
+__device__ __forceinline__ float plane_f(const float* nf, float qx, float qy, float qz) {
+  return fmaf(nf[0], qx, fmaf(nf[1], qy, nf[2] * qz));
+}
+
+// FP32-filtered sign test of n.q > 0 (FP64 when |n.q| < kFilter).
+__device__ __forceinline__ bool plane_pos(const float* nf, const double* nd, float qx, float qy,
+                                          float qz, double dx, double dy, double dz) {
+  float t = plane_f(nf, qx, qy, qz);
+  if (fabsf(t) > kFilter) return t > 0.0f;
+  double td = nd[0] * dx + nd[1] * dy + nd[2] * dz;
+  return td > 0.0;
+}
+
+// Reference row of the icosahedral triangle containing q.
+__device__ __forceinline__ int locate_row(const MeshView& m, double x, double y, double z) {
+  const float fx = (float)x, fy = (float)y, fz = (float)z;
+  // root face: nearest face centre (FP32), then exact edge checks with a
+  // bounded walk across a violated edge
+  const float* rf = m.root_f;
+  int f = 0;
+  float best = -4.0f;
+#pragma unroll 4
+  for (int g = 0; g < 20; ++g) {
+    float d = fmaf(rf[12 * g], fx, fmaf(rf[12 * g + 1], fy, rf[12 * g + 2] * fz));
+    if (d > best) {
+      best = d;
+      f = g;
+    }
+  }
+  for (int it = 0; it < 6; ++it) {
+    int e = -1;
+    for (int k = 0; k < 3; ++k) {
+      const float* nf = rf + 12 * f + 3 + 3 * k;
+      float t = plane_f(nf, fx, fy, fz);
+      bool neg;
+      if (fabsf(t) > kFilter) {
+        neg = t < 0.0f;
+      } else {
+        const double* nd = m.root + 12 * f + 3 + 3 * k;
+        neg = (nd[0] * x + nd[1] * y + nd[2] * z) < 0.0;
+      }
+      if (neg) {
+        e = k;
+        break;
+      }
+    }
+    if (e < 0) break;
+    const int g2 = m.root_adj[3 * f + e];
+    if (g2 < 0 || g2 >= 20) break;
+    f = g2;
+  }
+  // descent
+  int64_t off = 0, cnt = 20;
+  for (int j = 0; j < m.level; ++j) {
+    const int64_t node = off + f;
+    const float* nf = m.node_nf + 9 * node;
+    const double* nd = m.node_n + 9 * node;
+    int c;
+    if (plane_pos(nf, nd, fx, fy, fz, x, y, z))
+      c = 0;
+    else if (plane_pos(nf + 3, nd + 3, fx, fy, fz, x, y, z))
+      c = 1;
+    else if (plane_pos(nf + 6, nd + 6, fx, fy, fz, x, y, z))
+      c = 2;
+    else
+      c = 3;
+    off += cnt;
+    cnt *= 4;
+    f = 4 * f + c;
+  }
+  return __ldg(m.leaf_row + f);
+}
+
+struct Bcc {
+  double b0, b1, b2;
+};
+
+__device__ __forceinline__ Bcc bcc_of(const double* L, double x, double y, double z) {
+  return Bcc{L[0] * x + L[1] * y + L[2] * z, L[3] * x + L[4] * y + L[5] * z,
+             L[6] * x + L[7] * y + L[8] * z};
+}
+
+// Powell-Sabin sub-triangle of a big-triangle bcc: lo/hi with numpy's
+// first-occurrence rule (cmm_s2/core/spherical_spline.py:691-697).  When
+// all three are equal (the split centre) the reference's tables select no
+// sub-triangle (it returns 0/0); every sub-triangle is exact there and
+// (lo,hi) = (1,0) is used.
+struct Split {
+  int lo, mid, hi;
+};
+
+__device__ __forceinline__ Split split_of(const Bcc& b) {
+  int lo = 0, hi = 0;
+  double vlo = b.b0, vhi = b.b0;
+  if (b.b1 < vlo) { vlo = b.b1; lo = 1; }
+  if (b.b2 < vlo) { vlo = b.b2; lo = 2; }
+  if (b.b1 > vhi) { vhi = b.b1; hi = 1; }
+  if (b.b2 > vhi) { vhi = b.b2; hi = 2; }
+  if (lo == hi) { lo = 1; hi = 0; }
+  return Split{lo, 3 - lo - hi, hi};
+}
+
+__device__ __forceinline__ double pick(const Bcc& b, int i) {
+  return i == 0 ? b.b0 : (i == 1 ? b.b1 : b.b2);
+}
+
+// Edge-midpoint norm |v_a + v_b| from the location record.
+__device__ __forceinline__ double edge_norm(const double* L, int a, int b) {
+  int s = a + b;  // {0,1}->N12, {1,2}->N23, {0,2}->N31
+  return s == 1 ? L[10] : (s == 3 ? L[11] : L[12]);
+}
+
+struct Gam {
+  double V, E, C;
+};
+
+// Sub-triangle barycentrics from the big-triangle ones (closed form; the
+// sub-triangle's corners are v_hi, (v_hi+v_mid)/|.|, (v1+v2+v3)/|.|).
+__device__ __forceinline__ Gam gamma_of(const double* L, const Bcc& b, const Split& sp) {
+  double bl = pick(b, sp.lo), bm = pick(b, sp.mid), bh = pick(b, sp.hi);
+  return Gam{bh - bm, edge_norm(L, sp.hi, sp.mid) * (bm - bl), L[9] * bl};
+}
+
+template <int NC>
+struct Ords {
+  double c[6][NC];
+};
+
+template <int NC>
+__device__ __forceinline__ void load_ords(const double* rec, const Split& sp, Ords<NC>& o) {
+  const int* id = kSplitOrd[sp.lo][sp.hi];
+#pragma unroll
+  for (int k = 0; k < 6; ++k)
+#pragma unroll
+    for (int c = 0; c < NC; ++c) o.c[k][c] = __ldg(rec + NC * id[k] + c);
+}
+
+template <int NC>
+__device__ __forceinline__ void sbb(const Ords<NC>& o, const Gam& g, double* P) {
+  const double vv = g.V * g.V, ee = g.E * g.E, cc = g.C * g.C;
+  const double ve = 2 * g.V * g.E, ec = 2 * g.E * g.C, vc = 2 * g.V * g.C;
+#pragma unroll
+  for (int c = 0; c < NC; ++c)
+    P[c] = vv * o.c[0][c] + ee * o.c[1][c] + cc * o.c[2][c] + ve * o.c[3][c] + ec * o.c[4][c] +
+           vc * o.c[5][c];
+}
+
+__device__ __forceinline__ void load_loc(const MeshView& m, int t, double* Lr) {
+  const double* L = m.tri_loc + (int64_t)t * kLocStride;
+#pragma unroll
+  for (int k = 0; k < 13; ++k) Lr[k] = __ldg(L + k);
+}
+
+__device__ __forceinline__ void flag(const MeshView& m, int bit) { atomicOr(m.status, bit); }
+
+__device__ __forceinline__ bool finite3(double x, double y, double z) {
+  return isfinite(x) && isfinite(y) && isfinite(z);
+}
+
+inline int grid_for(int64_t n, int block) {
+  int64_t b = (n + block - 1) / block;
+  const int64_t cap = 152LL * 16;
+  return (int)(b < cap ? (b < 1 ? 1 : b) : cap);
+}
+
+}  // namespace dev
+}  // namespace cmm

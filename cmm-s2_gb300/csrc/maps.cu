@@ -22,166 +22,19 @@
 #include <cuda_runtime.h>
 
 #include "cmm_internal.h"
-#include "geom.h"
+#include "device_common.cuh"
 
 namespace cmm {
 
-__constant__ SplitTables c_split;
+using namespace dev;
 
 namespace {
 
-constexpr float kFilter = 1e-6f;
 constexpr int kBlock = 256;
 
 struct SubmapPtrs {
   const double* p[CMM_MAX_SUBMAPS];
 };
-
-// FP32-filtered sign test of n.q; returns the FP64 dot when undecided.
-__device__ __forceinline__ bool plane_pos(const float* nf, const double* nd, float qx, float qy,
-                                          float qz, double dx, double dy, double dz) {
-  float t = fmaf(nf[0], qx, fmaf(nf[1], qy, nf[2] * qz));
-  if (fabsf(t) > kFilter) return t > 0.0f;
-  double td = nd[0] * dx + nd[1] * dy + nd[2] * dz;
-  return td > 0.0;
-}
-
-__device__ __forceinline__ float plane_f(const float* nf, float qx, float qy, float qz) {
-  return fmaf(nf[0], qx, fmaf(nf[1], qy, nf[2] * qz));
-}
-
-// Reference row of the triangle containing q.
-__device__ __forceinline__ int locate_row(const MeshView& m, double x, double y, double z) {
-  const float fx = (float)x, fy = (float)y, fz = (float)z;
-  // root face: nearest face centre (FP32), then exact edge checks with a
-  // bounded walk across the violated edge
-  const float* rf = m.root_f;
-  int f = 0;
-  float best = -4.0f;
-#pragma unroll 4
-  for (int g = 0; g < 20; ++g) {
-    float d = fmaf(rf[12 * g], fx, fmaf(rf[12 * g + 1], fy, rf[12 * g + 2] * fz));
-    if (d > best) {
-      best = d;
-      f = g;
-    }
-  }
-  for (int it = 0; it < 6; ++it) {
-    int e = -1;
-    for (int k = 0; k < 3; ++k) {
-      const float* nf = rf + 12 * f + 3 + 3 * k;
-      float t = plane_f(nf, fx, fy, fz);
-      bool neg;
-      if (fabsf(t) > kFilter) {
-        neg = t < 0.0f;
-      } else {
-        const double* nd = m.root + 12 * f + 3 + 3 * k;
-        neg = (nd[0] * x + nd[1] * y + nd[2] * z) < 0.0;
-      }
-      if (neg) {
-        e = k;
-        break;
-      }
-    }
-    if (e < 0) break;
-    const int g2 = m.root_adj[3 * f + e];
-    if (g2 < 0 || g2 >= 20) break;
-    f = g2;
-  }
-  // descent
-  int64_t off = 0, cnt = 20;
-  for (int j = 0; j < m.level; ++j) {
-    const int64_t node = off + f;
-    const float* nf = m.node_nf + 9 * node;
-    const double* nd = m.node_n + 9 * node;
-    int c;
-    if (plane_pos(nf, nd, fx, fy, fz, x, y, z))
-      c = 0;
-    else if (plane_pos(nf + 3, nd + 3, fx, fy, fz, x, y, z))
-      c = 1;
-    else if (plane_pos(nf + 6, nd + 6, fx, fy, fz, x, y, z))
-      c = 2;
-    else
-      c = 3;
-    off += cnt;
-    cnt *= 4;
-    f = 4 * f + c;
-  }
-  return __ldg(m.leaf_row + f);
-}
-
-struct Bcc {
-  double b0, b1, b2;
-};
-
-__device__ __forceinline__ Bcc bcc_of(const double* L, double x, double y, double z) {
-  return Bcc{L[0] * x + L[1] * y + L[2] * z, L[3] * x + L[4] * y + L[5] * z,
-             L[6] * x + L[7] * y + L[8] * z};
-}
-
-// Powell-Sabin sub-triangle of a big-triangle bcc: lo/hi with numpy's
-// first-occurrence rule; when all three are equal (the split centre) the
-// reference's table has no sub-triangle (it yields 0/0); any sub-triangle
-// is exact there, (lo,hi) = (1,0) is used.
-struct Split {
-  int lo, mid, hi;
-};
-
-__device__ __forceinline__ Split split_of(const Bcc& b) {
-  int lo = 0, hi = 0;
-  double vlo = b.b0, vhi = b.b0;
-  if (b.b1 < vlo) { vlo = b.b1; lo = 1; }
-  if (b.b2 < vlo) { vlo = b.b2; lo = 2; }
-  if (b.b1 > vhi) { vhi = b.b1; hi = 1; }
-  if (b.b2 > vhi) { vhi = b.b2; hi = 2; }
-  if (lo == hi) { lo = 1; hi = 0; }
-  return Split{lo, 3 - lo - hi, hi};
-}
-
-__device__ __forceinline__ double pick(const Bcc& b, int i) {
-  return i == 0 ? b.b0 : (i == 1 ? b.b1 : b.b2);
-}
-
-// Edge-midpoint norm |v_hi + v_mid| from the location record.
-__device__ __forceinline__ double edge_norm(const double* L, int a, int b) {
-  int s = a + b;  // {0,1}->1 N12, {1,2}->3 N23, {0,2}->2 N31
-  return s == 1 ? L[10] : (s == 3 ? L[11] : L[12]);
-}
-
-struct Gam {
-  double V, E, C;
-};
-
-__device__ __forceinline__ Gam gamma_of(const double* L, const Bcc& b, const Split& sp) {
-  double bl = pick(b, sp.lo), bm = pick(b, sp.mid), bh = pick(b, sp.hi);
-  return Gam{bh - bm, edge_norm(L, sp.hi, sp.mid) * (bm - bl), L[9] * bl};
-}
-
-// Six ordinates x ncomp of the sub-triangle, canonical order
-// V^2, E^2, C^2, VE, EC, VC.
-template <int NC>
-struct Ords {
-  double c[6][NC];
-};
-
-template <int NC>
-__device__ __forceinline__ void load_ords(const double* rec, const Split& sp, Ords<NC>& o) {
-  const int* id = c_split.ord[sp.lo][sp.hi];
-#pragma unroll
-  for (int k = 0; k < 6; ++k)
-#pragma unroll
-    for (int c = 0; c < NC; ++c) o.c[k][c] = __ldg(rec + NC * id[k] + c);
-}
-
-template <int NC>
-__device__ __forceinline__ void sbb(const Ords<NC>& o, const Gam& g, double* P) {
-  const double vv = g.V * g.V, ee = g.E * g.E, cc = g.C * g.C;
-  const double ve = 2 * g.V * g.E, ec = 2 * g.E * g.C, vc = 2 * g.V * g.C;
-#pragma unroll
-  for (int c = 0; c < NC; ++c)
-    P[c] = vv * o.c[0][c] + ee * o.c[1][c] + cc * o.c[2][c] + ve * o.c[3][c] + ec * o.c[4][c] +
-           vc * o.c[5][c];
-}
 
 // Tangent image of w under one normalised submap: dS = (dP - s (s.dP)) / |P|.
 __device__ __forceinline__ void push_tangent(const double* L, const Split& sp, const Gam& g,
@@ -203,15 +56,13 @@ __device__ __forceinline__ void push_tangent(const double* L, const Split& sp, c
   for (int c = 0; c < 3; ++c) w[c] = (dP[c] - s[c] * sd) * inv_n;
 }
 
-__device__ __forceinline__ void flag(const MeshView& m, int bit) { atomicOr(m.status, bit); }
-
 __global__ void __launch_bounds__(kBlock) locate_kernel(MeshView m, const double* __restrict__ q,
                                                         int64_t n, int32_t* __restrict__ tri,
                                                         double* __restrict__ bcc) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     double x = q[3 * i], y = q[3 * i + 1], z = q[3 * i + 2];
-    if (!(isfinite(x) && isfinite(y) && isfinite(z))) {
+    if (!finite3(x, y, z)) {
       flag(m, CMM_FLAG_NONFINITE);
       tri[i] = -1;
       if (bcc) bcc[3 * i] = bcc[3 * i + 1] = bcc[3 * i + 2] = nan("");
@@ -229,6 +80,9 @@ __global__ void __launch_bounds__(kBlock) locate_kernel(MeshView m, const double
   }
 }
 
+// One triangle per thread: the 19 ordinates of each component from the
+// jets of its three vertices (assemble_coefficients,
+// cmm_s2/core/spherical_spline.py:300-337) using the per-triangle factors.
 template <int NC>
 __global__ void __launch_bounds__(128) assemble_kernel(MeshView m, const double* __restrict__ jets,
                                                        double* __restrict__ coeffs, int stride) {
@@ -239,7 +93,6 @@ __global__ void __launch_bounds__(128) assemble_kernel(MeshView m, const double*
   const int vid[3] = {tv.x, tv.y, tv.z};
   const double* A = m.tri_asm + (int64_t)t * kAsmStride;
   double* out = coeffs + (int64_t)t * stride;
-  // ordinates 3..11: (corner, factor slot)
   const int corner[9] = {0, 0, 0, 1, 1, 1, 2, 2, 2};
 #pragma unroll
   for (int k = 0; k < NC; ++k) {
@@ -287,7 +140,7 @@ __global__ void __launch_bounds__(kBlock) compose_kernel(MeshView m, SubmapPtrs 
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     double p[3] = {q[3 * i], q[3 * i + 1], q[3 * i + 2]};
-    if (!(isfinite(p[0]) && isfinite(p[1]) && isfinite(p[2]))) {
+    if (!finite3(p[0], p[1], p[2])) {
       flag(m, CMM_FLAG_NONFINITE);
       out[3 * i] = out[3 * i + 1] = out[3 * i + 2] = nan("");
       if (tri) tri[i] = -1;
@@ -314,10 +167,8 @@ __global__ void __launch_bounds__(kBlock) compose_kernel(MeshView m, SubmapPtrs 
       const int t = locate_row(m, p[0], p[1], p[2]);
       if (s == S - 1 && tri) tri[i] = t;
       if (tri_all) tri_all[(int64_t)s * n + i] = t;
-      const double* L = m.tri_loc + (int64_t)t * kLocStride;
       double Lr[13];
-#pragma unroll
-      for (int k = 0; k < 13; ++k) Lr[k] = __ldg(L + k);
+      load_loc(m, t, Lr);
       const Bcc b = bcc_of(Lr, p[0], p[1], p[2]);
       const Split sp = split_of(b);
       const Gam g = gamma_of(Lr, b, sp);
@@ -335,7 +186,7 @@ __global__ void __launch_bounds__(kBlock) compose_kernel(MeshView m, SubmapPtrs 
       p[1] = sN[1];
       p[2] = sN[2];
     }
-    if (!(isfinite(p[0]) && isfinite(p[1]) && isfinite(p[2]))) flag(m, CMM_FLAG_NONFINITE);
+    if (!finite3(p[0], p[1], p[2])) flag(m, CMM_FLAG_NONFINITE);
     out[3 * i] = p[0];
     out[3 * i + 1] = p[1];
     out[3 * i + 2] = p[2];
@@ -355,16 +206,14 @@ __global__ void __launch_bounds__(kBlock) stencil_kernel(MeshView m, const doubl
   const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (v >= nv) return;
   const double x = yn[v], y = yn[nv + v], z = yn[2 * nv + v];
-  if (!(isfinite(x) && isfinite(y) && isfinite(z))) {
+  if (!finite3(x, y, z)) {
     flag(m, CMM_FLAG_NONFINITE);
     for (int k = 0; k < 12; ++k) out[k * nv + v] = nan("");
     return;
   }
   const int t = locate_row(m, x, y, z);
-  const double* L = m.tri_loc + (int64_t)t * kLocStride;
   double Lr[13];
-#pragma unroll
-  for (int k = 0; k < 13; ++k) Lr[k] = __ldg(L + k);
+  load_loc(m, t, Lr);
   const Split sp = split_of(bcc_of(Lr, x, y, z));
   Ords<3> o;
   load_ords<3>(coeffs + (int64_t)t * kCoeffStride3, sp, o);
@@ -380,58 +229,12 @@ __global__ void __launch_bounds__(kBlock) stencil_kernel(MeshView m, const doubl
   }
 }
 
-int grid_for(int64_t n, int block) {
-  int64_t b = (n + block - 1) / block;
-  const int64_t cap = 152LL * 16;
-  return (int)(b < cap ? (b < 1 ? 1 : b) : cap);
-}
-
-}  // namespace
-
-void upload_split_tables_host(SplitTables* t) {
-  // reference tables (cmm_s2/core/spherical_spline.py:660-666)
-  static const int ords[3][3][6] = {{{0, 0, 0, 0, 0, 0}, {18, 1, 13, 7, 6, 16}, {13, 2, 18, 11, 10, 16}},
-                                    {{18, 14, 0, 17, 5, 4}, {0, 0, 0, 0, 0, 0}, {14, 18, 2, 17, 10, 9}},
-                                    {{0, 12, 18, 3, 15, 4}, {1, 18, 12, 7, 15, 8}, {0, 0, 0, 0, 0, 0}}};
-  static const int corners[3][3][3] = {{{0, 0, 0}, {3, 1, 5}, {5, 2, 3}},
-                                       {{3, 6, 0}, {0, 0, 0}, {6, 3, 2}},
-                                       {{0, 4, 3}, {1, 3, 4}, {0, 0, 0}}};
-  for (int lo = 0; lo < 3; ++lo)
-    for (int hi = 0; hi < 3; ++hi) {
-      for (int k = 0; k < 6; ++k) t->ord[lo][hi][k] = 0;
-      if (lo == hi) continue;
-      int pv = -1, pe = -1, pc = -1;
-      for (int p = 0; p < 3; ++p) {
-        int c = corners[lo][hi][p];
-        if (c == hi) pv = p;
-        else if (c == 3) pc = p;
-        else pe = p;
-      }
-      const int* o = ords[lo][hi];
-      auto pair = [&](int a, int b) {
-        int s = a + b;  // {0,1}->o[3], {1,2}->o[4], {0,2}->o[5]
-        return s == 1 ? o[3] : (s == 3 ? o[4] : o[5]);
-      };
-      t->ord[lo][hi][0] = o[pv];
-      t->ord[lo][hi][1] = o[pe];
-      t->ord[lo][hi][2] = o[pc];
-      t->ord[lo][hi][3] = pair(pv, pe);
-      t->ord[lo][hi][4] = pair(pe, pc);
-      t->ord[lo][hi][5] = pair(pv, pc);
-    }
-}
-
-int set_split_tables() {
-  SplitTables t;
-  upload_split_tables_host(&t);
-  cudaError_t e = cudaMemcpyToSymbol(c_split, &t, sizeof(t));
-  return e == cudaSuccess ? CMM_OK : cuda_fail(e, "cudaMemcpyToSymbol(split tables)");
-}
-
-static int check_launch(const char* what) {
+int check_launch(const char* what) {
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? CMM_OK : cuda_fail(e, what);
 }
+
+}  // namespace
 
 int launch_locate(const MeshView& m, const double* q, int64_t n, int32_t* tri, double* bcc,
                   cudaStream_t s) {

@@ -1,0 +1,370 @@
+// Velocity interpolant on the MWSS lat-lon mesh, backward integrators and
+// the CMM map update (sm_103a).
+//
+// Location on the lat-lon mesh restates structure_spherical_triangulation
+// .inds / .containing_simplex_and_bcc_structured
+// (cmm_s2/core/mesh_functions.py:196-282): ring and sector from the angles
+// with numpy's floor-division semantics, the reference's near-row
+// corrections (theta_c <= 0.03 / > 0.85, great-circle side tests with
+// heaviside(0) = 0) and the diagonal side test.  The row tests use the
+// query point itself where the reference re-synthesises it from its angles
+// (equal up to rounding; only exact ties can differ).
+#include <cuda_runtime.h>
+
+#include "cmm_internal.h"
+#include "device_common.cuh"
+#include "geom.h"
+
+namespace cmm {
+
+using namespace dev;
+
+namespace {
+
+constexpr int kBlock = 128;
+constexpr double kTwoPi = 6.283185307179586;
+
+// numpy float floor_divide / remainder for b > 0 (npy_divmod): exact fmod,
+// then the quotient of the exact difference, rounded to the nearest
+// integer below.
+__device__ __forceinline__ double np_floor_divide(double a, double b) {
+  double mod = fmod(a, b);
+  double div = (a - mod) / b;
+  if (mod != 0.0 && (mod < 0.0)) div -= 1.0;
+  if (div == 0.0) return copysign(0.0, a / b);
+  double fl = floor(div);
+  if (div - fl > 0.5) fl += 1.0;
+  return fl;
+}
+
+__device__ __forceinline__ double np_remainder(double a, double b) {
+  double mod = fmod(a, b);
+  if (mod != 0.0) {
+    if (mod < 0.0) mod += b;
+  } else {
+    mod = copysign(0.0, b);
+  }
+  return mod;
+}
+
+__device__ __forceinline__ int py_mod(long long a, int n) {
+  long long r = a % n;
+  return (int)(r < 0 ? r + n : r);
+}
+
+__device__ __forceinline__ D3 gridpt(const MeshView& m, int ring, int p) {
+  const double* g = m.grid + 4 * ((int64_t)ring * 2 * m.L + p);
+  return D3{g[0], g[1], g[2]};
+}
+
+// Triangle (row of the lat-lon table) containing q.
+__device__ __forceinline__ int latlon_locate(const MeshView& m, double x, double y, double z) {
+  const int N = 2 * m.L, M = m.L + 1;
+  double phi = np_remainder(atan2(y, x) + kTwoPi, kTwoPi);
+  const double rho = sqrt(__dadd_rn(__dmul_rn(y, y), __dmul_rn(x, x)));
+  const double theta = atan2(rho, z);
+  const double phiq = np_remainder(phi, kTwoPi);
+  const int phi_l = py_mod((long long)np_floor_divide(phiq - m.phi[0], m.dphi), N);
+  int theta_l = (int)np_floor_divide(theta - m.theta[0], m.dthe);
+  if (theta_l == M - 1) theta_l = M - 2;
+  if (theta_l < 0) theta_l = 0;
+  if (theta_l > M - 2) theta_l = M - 2;
+  const double theta_c = (theta - m.theta[theta_l]) / m.dthe;
+  const int phi_p1 = (phi_l + 1) % N;
+  const D3 q = D3{x, y, z};
+  if (theta_c <= 0.03 && theta_l != 0) {
+    const D3 n = cross(gridpt(m, theta_l, phi_l), gridpt(m, theta_l, phi_p1));
+    if (dot(n, q) > 0.0) theta_l -= 1;
+  } else if (theta_c > 0.85 && theta_l != M - 2) {
+    const D3 n = cross(gridpt(m, theta_l + 1, phi_l), gridpt(m, theta_l + 1, phi_p1));
+    if (-dot(n, q) > 0.0) theta_l += 1;
+  }
+  if (theta_l == 0) return phi_l;
+  if (theta_l == M - 2) return 2 * N * (M - 2) - N + phi_l;
+  const D3 n = cross(gridpt(m, theta_l, phi_l), gridpt(m, theta_l + 1, phi_p1));
+  const int s = (-dot(n, q) > 0.0) ? 1 : 0;
+  return N + 2 * (N * (theta_l - 1) + phi_l) + s;
+}
+
+// Velocity at q: the Powell-Sabin patch of each time level, combined with
+// the stage's Lagrange weights w (spline_interp_velocity.__call__,
+// cmm_s2/core/spherical_spline.py:570-615).
+struct W3 {
+  double a, b, c;
+};
+
+__device__ __forceinline__ W3 stage(const TimeWeights& tw, int s) {
+  return W3{tw.w[s][0], tw.w[s][1], tw.w[s][2]};
+}
+
+__device__ __forceinline__ void velocity_at(const MeshView& m, const VelPtrs& vc, int nvs,
+                                            const W3 w, double x, double y, double z,
+                                            double* V) {
+  const int t = latlon_locate(m, x, y, z);
+  double Lr[13];
+  load_loc(m, t, Lr);
+  const Bcc b = bcc_of(Lr, x, y, z);
+  const Split sp = split_of(b);
+  const Gam g = gamma_of(Lr, b, sp);
+  V[0] = V[1] = V[2] = 0.0;
+#pragma unroll
+  for (int l = 0; l < 3; ++l) {
+    if (l >= nvs) break;
+    const double wl = l == 0 ? w.a : (l == 1 ? w.b : w.c);
+    Ords<3> o;
+    load_ords<3>(vc.p[l] + (int64_t)t * kCoeffStride3, sp, o);
+    double P[3];
+    sbb<3>(o, g, P);
+    V[0] += wl * P[0];
+    V[1] += wl * P[1];
+    V[2] += wl * P[2];
+  }
+}
+
+__device__ __forceinline__ void sphere_proj(double* x) {
+  const double r = 1.0 / sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
+  x[0] *= r;
+  x[1] *= r;
+  x[2] *= r;
+}
+
+// Backward integrators (cmm_s2/core/evolution_functions.py:19-67):
+// scheme 0 Euler_step_proj, 1 improved_Euler_proj, 2 RK4_proj.
+__device__ __forceinline__ void integrate_point(const MeshView& m, const VelPtrs& vc, int nvs,
+                                                const TimeWeights& tw, int scheme, double dt,
+                                                double* x) {
+  double v1[3], v2[3], s[3];
+  velocity_at(m, vc, nvs, stage(tw, 0), x[0], x[1], x[2], v1);
+  if (scheme == 0) {
+    for (int c = 0; c < 3; ++c) x[c] = x[c] - dt * v1[c];
+    sphere_proj(x);
+    return;
+  }
+  if (scheme == 1) {
+    for (int c = 0; c < 3; ++c) s[c] = x[c] - dt * v1[c];
+    sphere_proj(s);
+    velocity_at(m, vc, nvs, stage(tw, 1), s[0], s[1], s[2], v2);
+    for (int c = 0; c < 3; ++c) x[c] = x[c] - (dt / 2) * (v1[c] + v2[c]);
+    sphere_proj(x);
+    return;
+  }
+  double v3[3], v4[3];
+  for (int c = 0; c < 3; ++c) s[c] = x[c] - dt * v1[c] / 2;
+  sphere_proj(s);
+  velocity_at(m, vc, nvs, stage(tw, 1), s[0], s[1], s[2], v2);
+  for (int c = 0; c < 3; ++c) s[c] = x[c] - (dt / 2) * v2[c];
+  sphere_proj(s);
+  velocity_at(m, vc, nvs, stage(tw, 2), s[0], s[1], s[2], v3);
+  for (int c = 0; c < 3; ++c) s[c] = x[c] - dt * v3[c];
+  sphere_proj(s);
+  velocity_at(m, vc, nvs, stage(tw, 3), s[0], s[1], s[2], v4);
+  for (int c = 0; c < 3; ++c) x[c] = x[c] - (dt / 6) * (v1[c] + 2 * v2[c] + 2 * v3[c] + v4[c]);
+  sphere_proj(x);
+}
+
+__global__ void __launch_bounds__(kBlock) latlon_locate_kernel(MeshView m, const double* __restrict__ q,
+                                                               int64_t n, int32_t* __restrict__ tri,
+                                                               double* __restrict__ bcc) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double x = q[3 * i], y = q[3 * i + 1], z = q[3 * i + 2];
+    if (!finite3(x, y, z)) {
+      flag(m, CMM_FLAG_NONFINITE);
+      tri[i] = -1;
+      if (bcc) bcc[3 * i] = bcc[3 * i + 1] = bcc[3 * i + 2] = nan("");
+      continue;
+    }
+    const int t = latlon_locate(m, x, y, z);
+    tri[i] = t;
+    if (bcc) {
+      const Bcc b = bcc_of(m.tri_loc + (int64_t)t * kLocStride, x, y, z);
+      bcc[3 * i] = b.b0;
+      bcc[3 * i + 1] = b.b1;
+      bcc[3 * i + 2] = b.b2;
+    }
+  }
+}
+
+// x, out: (3,n) component-major, as the reference's (3,N) arrays.
+__global__ void __launch_bounds__(kBlock) velocity_kernel(MeshView m, VelPtrs vc, int nvs,
+                                                          TimeWeights tw, const double* __restrict__ x,
+                                                          int64_t n, double* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double px = x[i], py = x[n + i], pz = x[2 * n + i];
+    double V[3] = {nan(""), nan(""), nan("")};
+    if (finite3(px, py, pz))
+      velocity_at(m, vc, nvs, stage(tw, 0), px, py, pz, V);
+    else
+      flag(m, CMM_FLAG_NONFINITE);
+    out[i] = V[0];
+    out[n + i] = V[1];
+    out[2 * n + i] = V[2];
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) integrate_kernel(MeshView m, VelPtrs vc, int nvs,
+                                                           TimeWeights tw, int scheme, double dt,
+                                                           const double* __restrict__ x, int64_t n,
+                                                           double* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double p[3] = {x[i], x[n + i], x[2 * n + i]};
+    if (finite3(p[0], p[1], p[2])) {
+      integrate_point(m, vc, nvs, tw, scheme, dt, p);
+      if (!finite3(p[0], p[1], p[2])) flag(m, CMM_FLAG_NONFINITE);
+    } else {
+      flag(m, CMM_FLAG_NONFINITE);
+    }
+    out[i] = p[0];
+    out[n + i] = p[1];
+    out[2 * n + i] = p[2];
+  }
+}
+
+// Foot points of the mesh vertices and of their stencil points
+// (advect, cmm_s2/core/evolution_functions.py:117-133).  Point i < nv is
+// vertex i, point nv + k*nv + v is stencil point k of vertex v.  work:
+// yn (3,nv) followed by the stencil foot points (3,4,nv).
+__global__ void __launch_bounds__(kBlock) advect_points_kernel(MeshView mesh, MeshView vm, VelPtrs vc,
+                                                               int nvs, TimeWeights tw, int scheme,
+                                                               double dt,
+                                                               const double* __restrict__ s_pts,
+                                                               double* __restrict__ work) {
+  const int64_t nv = mesh.nv, n = 5 * nv;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double p[3];
+    if (i < nv) {
+      p[0] = mesh.verts[4 * i];
+      p[1] = mesh.verts[4 * i + 1];
+      p[2] = mesh.verts[4 * i + 2];
+    } else {
+      const int64_t j = i - nv;  // k*nv + v within the (3, 4nv) stencil array
+      p[0] = s_pts[j];
+      p[1] = s_pts[4 * nv + j];
+      p[2] = s_pts[8 * nv + j];
+    }
+    integrate_point(vm, vc, nvs, tw, scheme, dt, p);
+    if (!finite3(p[0], p[1], p[2])) flag(vm, CMM_FLAG_NONFINITE);
+    if (i < nv) {
+      work[i] = p[0];
+      work[nv + i] = p[1];
+      work[2 * nv + i] = p[2];
+    } else {
+      const int64_t j = i - nv;
+      double* sn = work + 3 * nv;
+      sn[j] = p[0];
+      sn[4 * nv + j] = p[1];
+      sn[8 * nv + j] = p[2];
+    }
+  }
+}
+
+// New jets from the stencil images (spline_proj_sphere,
+// cmm_s2/core/evolution_functions.py:90-113); with a previous map, the
+// images are the previous map evaluated at the stencil foot points in the
+// sub-triangle of the vertex foot point, un-normalised (stencil_eval,
+// cmm_s2/core/spherical_spline.py:268-298).
+__global__ void __launch_bounds__(kBlock) project_jets_kernel(MeshView m, const double* __restrict__ prev,
+                                                              const double* __restrict__ yn,
+                                                              const double* __restrict__ sn,
+                                                              const double* __restrict__ tan,
+                                                              double eps, double* __restrict__ jets) {
+  const int64_t nv = m.nv;
+  const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  double S[4][3];
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) S[k][c] = sn[(c * 4 + k) * nv + v];
+  if (prev) {
+    const double x = yn[v], y = yn[nv + v], z = yn[2 * nv + v];
+    if (!finite3(x, y, z)) {
+      flag(m, CMM_FLAG_NONFINITE);
+      for (int k = 0; k < 12; ++k) jets[k * nv + v] = nan("");
+      return;
+    }
+    const int t = locate_row(m, x, y, z);
+    double Lr[13];
+    load_loc(m, t, Lr);
+    const Split sp = split_of(bcc_of(Lr, x, y, z));
+    Ords<3> o;
+    load_ords<3>(prev + (int64_t)t * kCoeffStride3, sp, o);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const Gam g = gamma_of(Lr, bcc_of(Lr, S[k][0], S[k][1], S[k][2]), sp);
+      double P[3];
+      sbb<3>(o, g, P);
+      S[k][0] = P[0];
+      S[k][1] = P[1];
+      S[k][2] = P[2];
+    }
+  }
+  double mv[3], d1[3], d2[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    mv[c] = (S[0][c] + S[1][c] + S[2][c] + S[3][c]) / 4;
+    d1[c] = (S[1][c] - S[0][c] + S[3][c] - S[2][c]) / (4 * eps);
+    d2[c] = (S[2][c] - S[0][c] + S[3][c] - S[1][c]) / (4 * eps);
+  }
+  const double nm = sqrt(mv[0] * mv[0] + mv[1] * mv[1] + mv[2] * mv[2]);
+  const double* a1 = tan + 3 * v;
+  const double* a2 = tan + 3 * (nv + v);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    jets[(c * 4 + 0) * nv + v] = mv[c] / nm;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) jets[(c * 4 + 1 + k) * nv + v] = d1[k] * a1[c] + d2[k] * a2[c];
+  }
+  if (!finite3(mv[0], mv[1], mv[2])) flag(m, CMM_FLAG_NONFINITE);
+}
+
+int check_launch(const char* what) {
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? CMM_OK : cuda_fail(e, what);
+}
+
+}  // namespace
+
+int launch_latlon_locate(const MeshView& vm, const double* q, int64_t n, int32_t* tri, double* bcc,
+                         cudaStream_t s) {
+  if (n == 0) return CMM_OK;
+  latlon_locate_kernel<<<grid_for(n, kBlock), kBlock, 0, s>>>(vm, q, n, tri, bcc);
+  return check_launch("latlon_locate_kernel");
+}
+
+int launch_velocity_eval(const MeshView& vm, VelPtrs vc, int nvs, const TimeWeights& tw,
+                         const double* x, int64_t n, double* out, cudaStream_t s) {
+  if (n == 0) return CMM_OK;
+  velocity_kernel<<<grid_for(n, kBlock), kBlock, 0, s>>>(vm, vc, nvs, tw, x, n, out);
+  return check_launch("velocity_kernel");
+}
+
+int launch_integrate(const MeshView& vm, VelPtrs vc, int nvs, const TimeWeights& tw, int scheme,
+                     double dt, const double* x, int64_t n, double* out, cudaStream_t s) {
+  if (n == 0) return CMM_OK;
+  integrate_kernel<<<grid_for(n, kBlock), kBlock, 0, s>>>(vm, vc, nvs, tw, scheme, dt, x, n, out);
+  return check_launch("integrate_kernel");
+}
+
+int launch_advect_points(const MeshView& mesh, const MeshView& vm, VelPtrs vc, int nvs,
+                         const TimeWeights& tw, int scheme, double dt, const double* s_pts,
+                         double* work, cudaStream_t s) {
+  const int64_t n = 5LL * mesh.nv;
+  advect_points_kernel<<<grid_for(n, kBlock), kBlock, 0, s>>>(mesh, vm, vc, nvs, tw, scheme, dt,
+                                                               s_pts, work);
+  return check_launch("advect_points_kernel");
+}
+
+int launch_project_jets(const MeshView& mesh, const double* prev_coeffs, const double* yn,
+                        const double* sn, const double* tan, double eps, double* jets,
+                        cudaStream_t s) {
+  const int64_t nv = mesh.nv;
+  project_jets_kernel<<<(int)((nv + kBlock - 1) / kBlock), kBlock, 0, s>>>(mesh, prev_coeffs, yn, sn,
+                                                                           tan, eps, jets);
+  return check_launch("project_jets_kernel");
+}
+
+}  // namespace cmm

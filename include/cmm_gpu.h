@@ -112,6 +112,55 @@ int cmm_compose(const cmm_mesh* mesh, const double* const* coeffs, int S, const 
 int cmm_stencil_eval(const cmm_mesh* mesh, const double* coeffs, const double* yn,
                      const double* st, int64_t nv, double* out, void* stream);
 
+/* ------------------------------------------------------ velocity mesh */
+/* MWSS lat-lon velocity mesh at band-limit L from the caller's HOST arrays:
+ * ring colatitudes theta (L+1), longitudes phi (2L), ring points grid
+ * (3, (L+1)*2L) and mesh vertices verts (2+(L-1)*2L, 3) (north pole, the
+ * interior rings row by row, south pole).  Replaces
+ * structure_spherical_triangulation (cmm_s2/core/mesh_functions.py:175-194,
+ * grid_assemble/full_assembly :352-412).  The handle works with
+ * cmm_locate (structured O(1) query, :196-282) and cmm_assemble. */
+int cmm_velmesh_create(int L, const double* theta, const double* phi, const double* grid,
+                       const double* verts, cmm_mesh** out);
+
+/* Velocity at points x (3,n) at time t from nvs (1..3) time levels of
+ * coefficients (HOST array of nvs device pointers) sampled at ts0,
+ * ts0+dt, ts0+2dt -> out (3,n).  Replaces spline_interp_velocity.__call__
+ * (cmm_s2/core/spherical_spline.py:570-615). */
+int cmm_velocity_eval(const cmm_mesh* velmesh, const double* const* vel_coeffs, int nvs,
+                      double ts0, double t, double dt, const double* x, int64_t n, double* out,
+                      void* stream);
+
+/* Backward foot points of x (3,n) over one step from t+dt to t, projected
+ * onto the sphere after each stage -> out (3,n).  scheme 0: Euler_step_proj,
+ * 1: improved_Euler_proj, 2: RK4_proj
+ * (cmm_s2/core/evolution_functions.py:19-67). */
+#define CMM_EULER 0
+#define CMM_IMPROVED_EULER 1
+#define CMM_RK4 2
+int cmm_integrate(const cmm_mesh* velmesh, const double* const* vel_coeffs, int nvs, double ts0,
+                  int scheme, double t, double dt, const double* x, int64_t n, double* out,
+                  void* stream);
+
+/* Scratch doubles cmm_advect_project needs for a mesh of nv vertices. */
+int64_t cmm_advect_workspace(const cmm_mesh* mesh);
+
+/* One CMM map update (advect_project_sphere,
+ * cmm_s2/core/evolution_functions.py:117-142): integrate the mesh vertices
+ * and the stencil points s_pts (3,4,nv) backward through the velocity,
+ * evaluate the previous map (coefficients prev_coeffs; NULL = identity) at
+ * the stencil foot points in the sub-triangle of each vertex foot point,
+ * and write the new jets (3,4,nv) from the stencil average and centred
+ * differences in the tangent frames tan (2,nv,3) with step eps
+ * (spline_proj_sphere, :90-113).  work: cmm_advect_workspace(mesh) doubles;
+ * on return it holds the vertex foot points (3,nv) followed by the stencil
+ * foot points (3,4,nv). */
+int cmm_advect_project(const cmm_mesh* mesh, const cmm_mesh* velmesh,
+                       const double* const* vel_coeffs, int nvs, double ts0, int scheme, double t,
+                       double dt, const double* s_pts, const double* tan,
+                       const double* prev_coeffs, double eps, double* jets, double* work,
+                       void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,144 @@
+"""GPU parity: lat-lon velocity mesh location, the velocity interpolant, the
+backward integrators and the CMM map update against the reference's golden
+outputs and the oracle.
+
+Tolerances: lat-lon triangle ids bit-exact; velocities within 1e-12
+(relative to max |u|); foot points within 1e-13; new jet values within
+1e-12; jet gradients (centred differences with step 1e-5, which amplify
+rounding by 1e5) within 1e-9."""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import GOLDEN
+from oracle import geometry as OG
+from oracle import spline as OS
+from oracle import evolution as OE
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def nat():
+    import __graft_entry__
+    __graft_entry__.build()
+    from cmm_gpu import native
+    return native
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def host(t):
+    return t.cpu().numpy()
+
+
+def golden(name):
+    return np.load(os.path.join(GOLDEN, name))
+
+
+def velmesh(nat, L):
+    from cmm_gpu.meshgen import latlon_mesh_arrays
+    theta, phi, grid, verts = latlon_mesh_arrays(L)
+    return nat.VelMesh(L, theta, phi, grid, verts), verts
+
+
+def test_latlon_arrays_match_reference():
+    from cmm_gpu.meshgen import latlon_mesh_arrays
+    d = golden("velocity_L8.npz")
+    theta, phi, grid, verts = latlon_mesh_arrays(8)
+    np.testing.assert_array_equal(verts, d["verts"])
+
+
+def test_latlon_locate_matches_reference(nat):
+    d = golden("velocity_L8.npz")
+    vm, verts = velmesh(nat, 8)
+    tri, bcc = vm.locate(dev(d["q"]))
+    np.testing.assert_array_equal(host(tri), d["tri"])
+    np.testing.assert_allclose(host(bcc), d["bcc"], rtol=0, atol=1e-13)
+
+
+@pytest.mark.parametrize("L", [16, 128])
+def test_latlon_locate_random(nat, L):
+    from cmm_gpu.meshgen import random_sphere_points
+    q = random_sphere_points(100_000, seed=L)
+    vm, _ = velmesh(nat, L)
+    tri, _ = vm.locate(dev(q))
+    _, ref, _ = OG.LatLonMesh(L).query(q)
+    np.testing.assert_array_equal(host(tri), ref)
+
+
+def vel_coeffs(nat, vm, vals):
+    return [vm.assemble(dev(vals[n])) for n in range(3)]
+
+
+def test_velocity_matches_reference(nat):
+    d = golden("velocity_L8.npz")
+    vm, _ = velmesh(nat, 8)
+    vc = vel_coeffs(nat, vm, d["vals"])
+    rec = host(vc[1])[:, :57].reshape(-1, 19, 3).transpose(2, 1, 0)
+    np.testing.assert_allclose(rec, d["coeffs"][1], rtol=0, atol=1e-12)
+    u = host(vm.velocity(vc, 0.0, float(d["t"]), float(d["dt"]), dev(d["q"].T)))
+    scale = np.abs(d["vel"]).max()
+    np.testing.assert_allclose(u / scale, d["vel"] / scale, rtol=0, atol=1e-12)
+    for nvs in (1, 2):
+        u = host(vm.velocity(vc[:nvs], 0.0, 0.17, 0.1, dev(d["q"].T)))
+        U = OS.VelocityOracle(OG.LatLonMesh(8), d["vals"], d["ts"])
+        for n in range(3):
+            U.init_coeffs(n)
+        U.nVs = nvs
+        np.testing.assert_allclose(u / scale, U(0.17, 0.1, d["q"].T) / scale, rtol=0, atol=1e-12)
+
+
+@pytest.mark.parametrize("scheme,nvs", [(0, 1), (1, 2), (2, 3)])
+def test_integrators_against_oracle(nat, scheme, nvs):
+    from cmm_gpu.meshgen import random_sphere_points
+    d = golden("velocity_L8.npz")
+    vm, _ = velmesh(nat, 8)
+    vc = vel_coeffs(nat, vm, d["vals"])[:nvs]
+    x = random_sphere_points(5000, seed=scheme).T.copy()
+    out = host(vm.integrate(vc, 0.0, scheme, 0.05, 0.1, dev(x)))
+    U = OS.VelocityOracle(OG.LatLonMesh(8), d["vals"], d["ts"])
+    for n in range(3):
+        U.init_coeffs(n)
+    U.nVs = nvs
+    f = [OE.euler_back, OE.improved_euler_back, OE.rk4_back][scheme]
+    ref = f(0.05, 0.1, x, U)
+    np.testing.assert_allclose(out, ref, rtol=0, atol=1e-13)
+
+
+def test_advect_project_matches_reference(nat):
+    a, m, v = golden("advect_l3_L8.npz"), golden("mesh_l3.npz"), golden("velocity_L8.npz")
+    verts, tris = m["verts"], m["tris"]
+    mesh = nat.Mesh(verts, tris, 3)
+    vm, _ = velmesh(nat, 8)
+    vc = vel_coeffs(nat, vm, v["vals"])
+    tan, s_pts = OG.stencil_points(verts)
+    prev = mesh.assemble(dev(a["jets_prev"]))
+    jets, work = mesh.advect_project(vm, vc, 0.0, nat.RK4, 0.05, 0.1, dev(s_pts), dev(tan), prev)
+    jets, yn = host(jets), host(work)[:3 * len(verts)].reshape(3, -1)
+    # the reference integrates the same points (RK4_proj) -> foot points
+    U = OS.VelocityOracle(OG.LatLonMesh(8), v["vals"], v["ts"])
+    for n in range(3):
+        U.init_coeffs(n)
+    U.nVs = 3
+    yref = OE.rk4_back(0.05, 0.1, verts.T, U)
+    np.testing.assert_allclose(yn, yref, rtol=0, atol=1e-13)
+    # vertices whose foot point lies on a mesh edge may be evaluated in
+    # either neighbouring triangle (the reference's Qhull choice is one)
+    loc = OG.QhullLocator(verts)
+    near = OG.edge_distance(verts, tris, loc.locate(yref.T), yref.T) <= 1e-14
+    ok = ~near
+    ref = a["jets_rk4"]
+    np.testing.assert_allclose(jets[:, 0][:, ok], ref[:, 0][:, ok], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(jets[:, 1:][..., ok], ref[:, 1:][..., ok], rtol=0, atol=1e-9)
+    np.testing.assert_allclose(jets[..., near], ref[..., near], rtol=0, atol=1e-6)
+    for scheme, nvs, key in ((nat.EULER, 1, "jets_euler"), (nat.IMPROVED_EULER, 2, "jets_ieuler")):
+        j, _ = mesh.advect_project(vm, vc[:nvs], 0.0, scheme, 0.0, 0.1, dev(s_pts), dev(tan), None)
+        j = host(j)
+        np.testing.assert_allclose(j[:, 0], a[key][:, 0], rtol=0, atol=1e-12)
+        np.testing.assert_allclose(j[:, 1:], a[key][:, 1:], rtol=0, atol=1e-9)
+    assert mesh.status() == 0 and vm.status() == 0

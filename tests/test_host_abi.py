@@ -34,6 +34,26 @@ def test_exports_every_declared_symbol(native):
     assert native.lib.cmm_version() >= 1
 
 
+def test_split_table_derivation():
+    """The device's (V,E,C) ordinate table is the reference's ordinate/corner
+    tables re-ordered by corner role."""
+    from oracle.spline import SPLIT_ORDINATES, SPLIT_CORNERS
+    src = open(os.path.join(ROOT, "cmm-s2_gb300", "csrc", "device_common.cuh")).read()
+    body = src[src.index("kSplitOrd[3][3][6] = {"):]
+    body = body[body.index("{"):body.index(";")]
+    dev = np.array([int(x) for x in re.findall(r"\d+", body)]).reshape(3, 3, 6)
+    for lo in range(3):
+        for hi in range(3):
+            if lo == hi:
+                continue
+            o, c = SPLIT_ORDINATES[lo, hi], SPLIT_CORNERS[lo, hi]
+            pv, pc = list(c).index(hi), list(c).index(3)
+            pe = 3 - pv - pc
+            pair = {1: o[3], 3: o[4], 2: o[5]}
+            want = [o[pv], o[pe], o[pc], pair[pv + pe], pair[pe + pc], pair[pv + pc]]
+            assert list(dev[lo, hi]) == want, (lo, hi)
+
+
 def test_coeff_stride(native):
     assert native.lib.cmm_coeff_stride(3) == 64
     assert native.lib.cmm_coeff_stride(1) == 24
