@@ -35,6 +35,11 @@ _SIGS = {
     "cmm_velocity_eval": (_i, [_p, ctypes.POINTER(_p), _i, _d, _d, _d, _p, _i64, _p, _p]),
     "cmm_integrate": (_i, [_p, ctypes.POINTER(_p), _i, _d, _i, _d, _d, _p, _i64, _p, _p]),
     "cmm_advect_workspace": (_i64, [_p]),
+    "cmm_sht_create": (_i, [_i, ctypes.POINTER(_p)]),
+    "cmm_sht_destroy": (_i, [_p]),
+    "cmm_sht_forward": (_i, [_p, _p, _p, _p]),
+    "cmm_sht_inverse": (_i, [_p, _p, _i, _p, _p]),
+    "cmm_sht_velocity": (_i, [_p, _p, _p, _p, _p, _p]),
     "cmm_advect_project": (_i, [_p, _p, ctypes.POINTER(_p), _i, _d, _i, _d, _d, _p, _p, _p, _d, _p,
                                 _p, _p]),
 }
@@ -212,3 +217,46 @@ class VelMesh(Mesh):
         check(lib.cmm_integrate(self.h, arr, len(vel_coeffs), ts0, scheme, t, dt, _ptr(x), x.shape[1],
                                 _ptr(out), _stream(x.device)), "cmm_integrate")
         return out
+
+
+class Sht:
+    """MWSS transform plan at band-limit L (cmm_sht_create).
+
+    Coefficients are complex128 tensors (L, L) indexed [m, l] (m <= l)."""
+
+    def __init__(self, L, device=None):
+        self.L = L
+        self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
+        h = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            check(lib.cmm_sht_create(L, ctypes.byref(h)), "cmm_sht_create")
+        self.h = h
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h is not None and h.value:
+            lib.cmm_sht_destroy(h)
+            self.h = None
+
+    def forward(self, samples):
+        samples = _dev(samples)
+        alm = torch.zeros((self.L, self.L), dtype=torch.complex128, device=samples.device)
+        check(lib.cmm_sht_forward(self.h, _ptr(samples), _ptr(alm), _stream(samples.device)),
+              "cmm_sht_forward")
+        return alm
+
+    def inverse(self, alm):
+        alm = _dev(alm, torch.complex128)
+        nf = 1 if alm.dim() == 2 else alm.shape[0]
+        out = torch.empty((nf, self.L + 1, 2 * self.L), dtype=torch.float64, device=alm.device)
+        check(lib.cmm_sht_inverse(self.h, _ptr(alm), nf, _ptr(out), _stream(alm.device)),
+              "cmm_sht_inverse")
+        return out[0] if alm.dim() == 2 else out
+
+    def velocity(self, velmesh, omega, jets=None, psi=None):
+        omega = _dev(omega)
+        if jets is None:
+            jets = torch.empty((3, 4, velmesh.nv), dtype=torch.float64, device=omega.device)
+        check(lib.cmm_sht_velocity(self.h, velmesh.h, _ptr(omega), _ptr(psi), _ptr(jets),
+                                   _stream(omega.device)), "cmm_sht_velocity")
+        return jets

@@ -163,6 +163,33 @@ int cmm_integrate(const cmm_mesh* velmesh, const double* const* vel_coeffs, int 
   return launch_integrate(velmesh->view, vc, nvs, tw, scheme, dt, x, n, out, (cudaStream_t)stream);
 }
 
+int cmm_sht_create(int L, cmm_sht** out) {
+  if (!out) return arg_error("cmm_sht_create: null pointer");
+  *out = nullptr;
+  return sht_create(L, out);
+}
+
+int cmm_sht_destroy(cmm_sht* plan) { return plan ? sht_destroy(plan) : CMM_OK; }
+
+int cmm_sht_forward(cmm_sht* plan, const double* samples, double* alm, void* stream) {
+  if (!plan || !samples || !alm) return arg_error("cmm_sht_forward: null pointer");
+  return sht_forward(plan, samples, (double2*)alm, (cudaStream_t)stream);
+}
+
+int cmm_sht_inverse(cmm_sht* plan, const double* alm, int nf, double* samples, void* stream) {
+  if (!plan || !alm || !samples || (nf != 1 && nf != 12))
+    return arg_error("cmm_sht_inverse: bad argument (nf must be 1 or 12)");
+  return sht_inverse(plan, (const double2*)alm, nf, samples, (cudaStream_t)stream);
+}
+
+int cmm_sht_velocity(cmm_sht* plan, const cmm_mesh* velmesh, const double* omega, double* psi,
+                     double* vel_jets, void* stream) {
+  if (!plan || !velmesh || !omega || !vel_jets) return arg_error("cmm_sht_velocity: null pointer");
+  if (velmesh->view.kind != kLatLon || velmesh->view.L != sht_L(plan))
+    return arg_error("cmm_sht_velocity: velocity mesh of the plan's band-limit expected");
+  return sht_velocity(plan, velmesh, omega, (double2*)psi, vel_jets, (cudaStream_t)stream);
+}
+
 int64_t cmm_advect_workspace(const cmm_mesh* mesh) {
   return mesh ? 15LL * mesh->view.nv : -1;
 }

@@ -117,4 +117,13 @@ int launch_advect_points(const MeshView& mesh, const MeshView& vm, VelPtrs vc, i
 int launch_project_jets(const MeshView& mesh, const double* prev_coeffs, const double* yn,
                         const double* sn, const double* tan, double eps, double* jets,
                         cudaStream_t s);
+
+// spherical-harmonic transforms (sht.cu)
+int sht_create(int L, cmm_sht** out);
+int sht_destroy(cmm_sht* p);
+int sht_L(const cmm_sht* p);
+int sht_forward(cmm_sht* p, const double* samples, double2* out, cudaStream_t s);
+int sht_inverse(cmm_sht* p, const double2* alm, int nf, double* samples, cudaStream_t s);
+int sht_velocity(cmm_sht* p, const cmm_mesh* vm, const double* omega, double2* psi_out,
+                 double* jets, cudaStream_t s);
 }  // namespace cmm

@@ -1,0 +1,573 @@
+// MWSS spherical-harmonic transforms and the vorticity -> velocity-jet
+// pipeline (sm_103a, FP64).
+//
+// Forward (inv_Laplacian, cmm_s2/core/spherical_harmonic_tools.py:14-19):
+//   1. rfft along each of the L+1 rings (cuFFT D2Z), scaled by pi/L;
+//   2. per m, the theta-torus extension F_m(2pi - theta) = (-1)^m F_m(theta)
+//      and its trigonometric interpolant (Nyquist term split evenly) are
+//      resampled on 2L+1 rings theta'_j = pi j / 2L (cuFFT Z2Z 2L forward,
+//      zero padding, Z2Z 4L inverse);
+//   3. Legendre analysis with Clenshaw-Curtis weights in cos(theta), exact
+//      for the degree <= 2L-1 products: f_lm = sum_j w_j F'_m(j) Pbar_lm(j).
+// Inverse (pyssht.inverse in project_stream, :84-91): Legendre synthesis on
+// the L+1 rings, then inverse real FFTs (cuFFT Z2D).
+// Pbar_lm are orthonormal with the Condon-Shortley phase and come from the
+// three-term recurrence in l run on the fly (FP64); rings theta and
+// pi - theta are processed together since Pbar_lm(pi - theta) =
+// (-1)^(l+m) Pbar_lm(theta).
+// Coefficient layout on the device: alm[m][l] complex (double2), m-major,
+// m <= l < L, entries with l < m unused and zero.
+#include <cuda_runtime.h>
+#include <cufft.h>
+
+#include <cmath>
+#include <vector>
+
+#include "cmm_internal.h"
+
+namespace cmm {
+
+namespace {
+
+constexpr int kFields = 12;   // 3 velocity components + 3x3 gradients
+constexpr int kSynthBlock = 64;
+constexpr int kLChunk = 32;
+
+__device__ __forceinline__ double2 cmul(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
+
+// ----------------------------------------------------------------- forward
+// F (L+1, L+1) ring spectra -> torus columns G (2L, L): G[t][m].
+__global__ void torus_kernel(const double2* __restrict__ F, int L, double2* __restrict__ G) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = blockIdx.y;
+  if (m >= L || t >= 2 * L) return;
+  const double s = M_PI / L;
+  double2 v;
+  if (t <= L) {
+    v = F[(int64_t)t * (L + 1) + m];
+  } else {
+    v = F[(int64_t)(2 * L - t) * (L + 1) + m];
+    if (m & 1) v = make_double2(-v.x, -v.y);
+  }
+  G[(int64_t)t * L + m] = cmul(v, s);
+}
+
+// Torus spectrum Gh (2L, L) -> zero-padded H (4L, L), Nyquist split.
+__global__ void pad_kernel(const double2* __restrict__ Gh, int L, double2* __restrict__ H) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = blockIdx.y;  // 0..4L-1
+  if (m >= L || k >= 4 * L) return;
+  const double s = 1.0 / (2 * L);
+  double2 v = make_double2(0.0, 0.0);
+  if (k < L) {
+    v = Gh[(int64_t)k * L + m];
+  } else if (k == L || k == 3 * L) {
+    v = cmul(Gh[(int64_t)L * L + m], 0.5);
+  } else if (k > 3 * L) {
+    v = Gh[(int64_t)(k - 2 * L) * L + m];
+  }
+  H[(int64_t)k * L + m] = cmul(v, s);
+}
+
+// Legendre analysis: one block per m; ring pairs (j, 2L-j) of the fine grid
+// with the quadrature weights folded in.  fine (4L, L): rows 0..2L used.
+__global__ void __launch_bounds__(256) analysis_kernel(const double2* __restrict__ fine, int L,
+                                                       const double* __restrict__ w,
+                                                       const double* __restrict__ ct,
+                                                       const double* __restrict__ pmm,
+                                                       const double* __restrict__ ra,
+                                                       const double* __restrict__ rb,
+                                                       double2* __restrict__ alm) {
+  const int m = blockIdx.x;
+  const int npair = L + 1;  // j = 0..L (j = L is the equator, unpaired)
+  constexpr int R = 8;      // ring pairs per thread (up to 2048 pairs)
+  double2 E[R], O[R];
+  double x[R], p0[R], p1[R];
+  int nr = 0;
+  for (int r = 0; r < R; ++r) {
+    const int j = threadIdx.x + r * blockDim.x;
+    if (j < npair) {
+      const double2 a = fine[(int64_t)j * L + m];
+      double2 e, o;
+      if (j < L) {
+        const double2 b = fine[(int64_t)(2 * L - j) * L + m];
+        e = make_double2(a.x + b.x, a.y + b.y);
+        o = make_double2(a.x - b.x, a.y - b.y);
+      } else {
+        e = a;
+        o = make_double2(0.0, 0.0);
+      }
+      E[r] = cmul(e, w[j]);
+      O[r] = cmul(o, w[j]);
+      x[r] = ct[j];
+      p0[r] = pmm[(int64_t)m * (2 * L + 1) + j];  // Pbar_mm
+      p1[r] = 0.0;
+      nr = r + 1;
+    } else {
+      E[r] = O[r] = make_double2(0.0, 0.0);
+      x[r] = p0[r] = p1[r] = 0.0;
+    }
+  }
+  __shared__ double2 red[kLChunk][8];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int l0 = m; l0 < L; l0 += kLChunk) {
+    double2 acc[kLChunk];
+#pragma unroll
+    for (int q = 0; q < kLChunk; ++q) acc[q] = make_double2(0.0, 0.0);
+#pragma unroll
+    for (int q = 0; q < kLChunk; ++q) {
+      const int l = l0 + q;
+      if (l < L) {
+        const bool even = ((l - m) & 1) == 0;
+        double a = 0.0, b = 0.0;
+        if (l > m) {
+          a = ra[(int64_t)m * L + l];
+          b = rb[(int64_t)m * L + l];
+        }
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          if (r < nr) {
+            double P;
+            if (l == m) {
+              P = p0[r];
+            } else if (l == m + 1) {
+              P = a * x[r] * p0[r];
+              p1[r] = p0[r];
+              p0[r] = P;
+            } else {
+              P = a * (x[r] * p0[r] - b * p1[r]);
+              p1[r] = p0[r];
+              p0[r] = P;
+            }
+            const double2 v = even ? E[r] : O[r];
+            acc[q].x += P * v.x;
+            acc[q].y += P * v.y;
+          }
+        }
+      }
+    }
+    // block reduction of the chunk
+#pragma unroll
+    for (int q = 0; q < kLChunk; ++q) {
+      double vx = acc[q].x, vy = acc[q].y;
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        vx += __shfl_down_sync(0xffffffffu, vx, off);
+        vy += __shfl_down_sync(0xffffffffu, vy, off);
+      }
+      if (lane == 0) red[q][warp] = make_double2(vx, vy);
+    }
+    __syncthreads();
+    if (threadIdx.x < kLChunk) {
+      const int q = threadIdx.x, l = l0 + q;
+      double2 s = make_double2(0.0, 0.0);
+      for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+        s.x += red[q][k].x;
+        s.y += red[q][k].y;
+      }
+      if (l < L) alm[(int64_t)m * L + l] = s;
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------- coefficient operators
+// D_inv (cmm_s2/core/spherical_simulations.py:195-198) applied in place;
+// entries l < m cleared.
+__global__ void dinv_kernel(double2* __restrict__ a, int L) {
+  const int l = blockIdx.x * blockDim.x + threadIdx.x, m = blockIdx.y;
+  if (l >= L) return;
+  const int64_t i = (int64_t)m * L + l;
+  if (l < m || l == 0) {
+    a[i] = make_double2(0.0, 0.0);
+    return;
+  }
+  const double d = -1.0 / ((double)l * (double)(l + 1));
+  a[i] = cmul(a[i], d);
+}
+
+// i(L_x, L_y, L_z) of angular_momentum (spherical_harmonic_tools.py:49-62)
+// on the m >= 0 half of a real field: up = sqrt(l(l+1)-m(m-1)) a_{l,m-1},
+// dn = sqrt(l(l+1)-m(m+1)) a_{l,m+1}, a_{l,-1} = -conj(a_{l,1});
+// iLx a = i (up+dn)/2, iLy a = (up-dn)/2, iLz a = i m a.
+__device__ __forceinline__ void ladder(const double2* __restrict__ a, int L, int l, int m,
+                                       double2* o) {
+  const double ll = (double)l * (double)(l + 1);
+  double2 am1, ap1;
+  if (m == 0) {
+    am1 = (l >= 1) ? a[(int64_t)1 * L + l] : make_double2(0.0, 0.0);
+    am1 = make_double2(-am1.x, am1.y);  // -conj
+  } else {
+    am1 = a[(int64_t)(m - 1) * L + l];
+  }
+  ap1 = (m + 1 <= l) ? a[(int64_t)(m + 1) * L + l] : make_double2(0.0, 0.0);
+  const double cu = sqrt(ll - (double)m * (double)(m - 1));
+  const double cd = sqrt(ll - (double)m * (double)(m + 1));
+  const double2 up = make_double2(cu * am1.x, cu * am1.y);
+  const double2 dn = make_double2(cd * ap1.x, cd * ap1.y);
+  const double2 sx = make_double2((up.x + dn.x) / 2, (up.y + dn.y) / 2);
+  o[0] = make_double2(-sx.y, sx.x);                                   // i * sx
+  o[1] = make_double2((up.x - dn.x) / 2, (up.y - dn.y) / 2);
+  const double2 am = a[(int64_t)m * L + l];
+  o[2] = make_double2(-(double)m * am.y, (double)m * am.x);           // i m a
+}
+
+// fields[f] (f = 0..11): 0..2 = u_i = iL_i psi; 3 + 3i + k = iL_k u_i.
+__global__ void ladder1_kernel(const double2* __restrict__ psi, int L, double2* __restrict__ fields) {
+  const int l = blockIdx.x * blockDim.x + threadIdx.x, m = blockIdx.y;
+  if (l >= L) return;
+  const int64_t fs = (int64_t)L * L, i = (int64_t)m * L + l;
+  if (l < m) {
+    for (int f = 0; f < 3; ++f) fields[f * fs + i] = make_double2(0.0, 0.0);
+    return;
+  }
+  double2 o[3];
+  ladder(psi, L, l, m, o);
+  for (int f = 0; f < 3; ++f) fields[f * fs + i] = o[f];
+}
+
+__global__ void ladder2_kernel(double2* __restrict__ fields, int L) {
+  const int l = blockIdx.x * blockDim.x + threadIdx.x, m = blockIdx.y;
+  if (l >= L) return;
+  const int64_t fs = (int64_t)L * L, i = (int64_t)m * L + l;
+  for (int u = 0; u < 3; ++u) {
+    double2 o[3] = {make_double2(0.0, 0.0), make_double2(0.0, 0.0), make_double2(0.0, 0.0)};
+    if (l >= m) ladder(fields + u * fs, L, l, m, o);
+    for (int k = 0; k < 3; ++k) fields[(3 + 3 * u + k) * fs + i] = o[k];
+  }
+}
+
+// ------------------------------------------------------------- inverse
+// Legendre synthesis of nf fields: block (m, ring-pair tile); each thread
+// one ring pair (t, L-t).  Out: spectra S[f][t][m] (nf, L+1, L+1), m = L
+// column zero (written by the caller's memset).
+template <int NF>
+__global__ void __launch_bounds__(kSynthBlock) synthesis_kernel(const double2* __restrict__ alm, int L,
+                                                                const double* __restrict__ ct,
+                                                                const double* __restrict__ pmm,
+                                                                const double* __restrict__ ra,
+                                                                const double* __restrict__ rb,
+                                                                double2* __restrict__ S) {
+  const int m = blockIdx.x;
+  const int t = blockIdx.y * blockDim.x + threadIdx.x;  // 0..L/2
+  const int npair = L / 2 + 1;
+  const int64_t fs = (int64_t)L * L;
+  __shared__ double2 A[kLChunk][NF];
+  double2 E[NF], O[NF];
+#pragma unroll
+  for (int f = 0; f < NF; ++f) E[f] = O[f] = make_double2(0.0, 0.0);
+  const bool active = t < npair;
+  const double x = active ? ct[t] : 0.0;
+  double p0 = active ? pmm[(int64_t)m * (L + 1) + t] : 0.0, p1 = 0.0;
+  for (int l0 = m; l0 < L; l0 += kLChunk) {
+    __syncthreads();
+    for (int e = threadIdx.x; e < kLChunk * NF; e += blockDim.x) {
+      const int q = e / NF, f = e % NF, l = l0 + q;
+      A[q][f] = (l < L) ? alm[f * fs + (int64_t)m * L + l] : make_double2(0.0, 0.0);
+    }
+    __syncthreads();
+    const int qn = min(kLChunk, L - l0);
+    for (int q = 0; q < qn; ++q) {
+      const int l = l0 + q;
+      double P;
+      if (l == m) {
+        P = p0;
+      } else if (l == m + 1) {
+        P = ra[(int64_t)m * L + l] * x * p0;
+        p1 = p0;
+        p0 = P;
+      } else {
+        P = ra[(int64_t)m * L + l] * (x * p0 - rb[(int64_t)m * L + l] * p1);
+        p1 = p0;
+        p0 = P;
+      }
+      if (((l - m) & 1) == 0) {
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+          E[f].x += P * A[q][f].x;
+          E[f].y += P * A[q][f].y;
+        }
+      } else {
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+          O[f].x += P * A[q][f].x;
+          O[f].y += P * A[q][f].y;
+        }
+      }
+    }
+  }
+  if (!active) return;
+  const int64_t row = L + 1;
+#pragma unroll
+  for (int f = 0; f < NF; ++f) {
+    const int64_t base = (int64_t)f * (L + 1) * row;
+    S[base + (int64_t)t * row + m] = make_double2(E[f].x + O[f].x, E[f].y + O[f].y);
+    if (L - t != t) S[base + (int64_t)(L - t) * row + m] = make_double2(E[f].x - O[f].x, E[f].y - O[f].y);
+  }
+}
+
+// Velocity jets (project_stream, spherical_harmonic_tools.py:81-101) from
+// the 12 synthesised fields on the grid: vals[i][0] = u_i and, with
+// g = (iLx, iLy, iLz) u_i, vals[c][1+i] = (g x X - ((g x X).X/|X|) X)_c;
+// poles from sample 0 of the first and last rings.
+__global__ void jets_kernel(const double* __restrict__ fld, int L, const double* __restrict__ grid,
+                            double* __restrict__ jets) {
+  const int N = 2 * L;
+  const int64_t nv = 2 + (int64_t)(L - 1) * N;
+  const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  int64_t node;  // ring * N + p
+  if (v == 0)
+    node = 0;
+  else if (v == nv - 1)
+    node = (int64_t)L * N;
+  else
+    node = N + (v - 1);
+  const int64_t fs = (int64_t)(L + 1) * N;
+  const double X0 = grid[4 * node], X1 = grid[4 * node + 1], X2 = grid[4 * node + 2];
+  const double nX = sqrt(X0 * X0 + X1 * X1 + X2 * X2);
+  for (int i = 0; i < 3; ++i) {
+    jets[(int64_t)(i * 4) * nv + v] = fld[i * fs + node];
+    const double g0 = fld[(3 + 3 * i) * fs + node], g1 = fld[(4 + 3 * i) * fs + node],
+                 g2 = fld[(5 + 3 * i) * fs + node];
+    const double c0 = g1 * X2 - g2 * X1, c1 = g2 * X0 - g0 * X2, c2 = g0 * X1 - g1 * X0;
+    const double sc = (c0 * X0 + c1 * X1 + c2 * X2) / nX;
+    jets[(int64_t)(0 * 4 + 1 + i) * nv + v] = c0 - sc * X0;
+    jets[(int64_t)(1 * 4 + 1 + i) * nv + v] = c1 - sc * X1;
+    jets[(int64_t)(2 * 4 + 1 + i) * nv + v] = c2 - sc * X2;
+  }
+}
+
+int cufft_fail(cufftResult r, const char* what) {
+  set_last_error(std::string(what) + ": cuFFT error " + std::to_string((int)r));
+  return CMM_ERR_CUDA;
+}
+
+int check_launch(const char* what) {
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? CMM_OK : cuda_fail(e, what);
+}
+
+}  // namespace
+}  // namespace cmm
+
+struct cmm_sht {
+  int L = 0;
+  cufftHandle ring_fwd = 0, torus_fwd = 0, pad_inv = 0, ring_inv = 0;
+  bool have_plans[4] = {false, false, false, false};
+  cmm::DeviceBuffer ct_rings, ct_fine, w_fine, pmm_rings, pmm_fine, ra, rb;
+  cmm::DeviceBuffer spec, torus, pad, alm, fields, synth, samples;
+  ~cmm_sht() {
+    if (have_plans[0]) cufftDestroy(ring_fwd);
+    if (have_plans[1]) cufftDestroy(torus_fwd);
+    if (have_plans[2]) cufftDestroy(pad_inv);
+    if (have_plans[3]) cufftDestroy(ring_inv);
+  }
+};
+
+namespace cmm {
+
+// Sectoral start values Pbar_mm(theta_j) (L, nring) and the recurrence
+// coefficients a_lm = sqrt((4l^2-1)/(l^2-m^2)), b_lm = sqrt(((l-1)^2-m^2)/
+// (4(l-1)^2-1)) (m-major (L, L)); a_{m+1,m} = sqrt(2m+3).
+static void legendre_tables(int L, const std::vector<double>& theta, std::vector<double>& pmm,
+                            std::vector<double>& ct) {
+  const int n = (int)theta.size();
+  pmm.assign((size_t)L * n, 0.0);
+  ct.resize(n);
+  for (int j = 0; j < n; ++j) {
+    const double x = std::cos(theta[j]), s = std::sin(theta[j]);
+    ct[j] = x;
+    double p = std::sqrt(1.0 / (4.0 * M_PI));
+    for (int m = 0; m < L; ++m) {
+      if (m > 0) p = -p * std::sqrt((2.0 * m + 1.0) / (2.0 * m)) * s;
+      pmm[(size_t)m * n + j] = p;
+    }
+  }
+}
+
+int sht_create(int L, cmm_sht** out) {
+  if (L < 2 || L > 4096) {
+    set_last_error("cmm_sht_create: L must be in [2, 4096]");
+    return CMM_ERR_ARG;
+  }
+  cmm_sht* p = new (std::nothrow) cmm_sht();
+  if (!p) {
+    set_last_error("cmm_sht_create: out of host memory");
+    return CMM_ERR_ARG;
+  }
+  p->L = L;
+  std::vector<double> th(L + 1), thf(2 * L + 1), w(2 * L + 1);
+  for (int t = 0; t <= L; ++t) th[t] = M_PI * t / L;
+  for (int j = 0; j <= 2 * L; ++j) thf[j] = M_PI * j / (2 * L);
+  // Clenshaw-Curtis weights on 2L+1 points (M = 2L even)
+  const int M = 2 * L;
+  for (int j = 0; j <= M; ++j) {
+    double s = 1.0;
+    for (int k = 1; k <= M / 2; ++k) {
+      const double b = (k == M / 2) ? 1.0 : 2.0;
+      s -= b / (4.0 * k * k - 1.0) * std::cos(2.0 * M_PI * j * k / M);
+    }
+    w[j] = ((j == 0 || j == M) ? 1.0 : 2.0) / M * s;
+  }
+  std::vector<double> pmm_r, ct_r, pmm_f, ct_f, ra((size_t)L * L, 0.0), rb((size_t)L * L, 0.0);
+  legendre_tables(L, th, pmm_r, ct_r);
+  legendre_tables(L, thf, pmm_f, ct_f);
+  for (int m = 0; m < L; ++m)
+    for (int l = m + 1; l < L; ++l) {
+      const double ld = l, md = m;
+      if (l == m + 1) {
+        ra[(size_t)m * L + l] = std::sqrt(2.0 * md + 3.0);
+      } else {
+        ra[(size_t)m * L + l] = std::sqrt((4.0 * ld * ld - 1.0) / (ld * ld - md * md));
+        rb[(size_t)m * L + l] = std::sqrt(((ld - 1) * (ld - 1) - md * md) / (4.0 * (ld - 1) * (ld - 1) - 1.0));
+      }
+    }
+  int rc;
+  auto fail = [&](int r) {
+    delete p;
+    return r;
+  };
+  // synthesis uses ring pairs t = 0..L/2 only
+  if ((rc = p->ct_rings.upload(ct_r.data(), ct_r.size() * 8))) return fail(rc);
+  if ((rc = p->ct_fine.upload(ct_f.data(), ct_f.size() * 8))) return fail(rc);
+  if ((rc = p->w_fine.upload(w.data(), w.size() * 8))) return fail(rc);
+  if ((rc = p->pmm_rings.upload(pmm_r.data(), pmm_r.size() * 8))) return fail(rc);
+  if ((rc = p->pmm_fine.upload(pmm_f.data(), pmm_f.size() * 8))) return fail(rc);
+  if ((rc = p->ra.upload(ra.data(), ra.size() * 8))) return fail(rc);
+  if ((rc = p->rb.upload(rb.data(), rb.size() * 8))) return fail(rc);
+  const size_t c16 = sizeof(double2);
+  if ((rc = p->spec.alloc((size_t)(L + 1) * (L + 1) * c16))) return fail(rc);
+  if ((rc = p->torus.alloc((size_t)2 * L * L * c16))) return fail(rc);
+  if ((rc = p->pad.alloc((size_t)4 * L * L * c16))) return fail(rc);
+  if ((rc = p->alm.alloc((size_t)L * L * c16))) return fail(rc);
+  if ((rc = p->fields.alloc((size_t)kFields * L * L * c16))) return fail(rc);
+  if ((rc = p->synth.alloc((size_t)kFields * (L + 1) * (L + 1) * c16))) return fail(rc);
+  if ((rc = p->samples.alloc((size_t)kFields * (L + 1) * 2 * L * 8))) return fail(rc);
+  cufftResult r;
+  int n2[1] = {2 * L}, n4[1] = {4 * L};
+  // rings: (L+1) real rows of 2L -> (L+1) x (L+1) complex
+  int inemb[1] = {2 * L}, onemb[1] = {L + 1};
+  r = cufftPlanMany(&p->ring_fwd, 1, n2, inemb, 1, 2 * L, onemb, 1, L + 1, CUFFT_D2Z, L + 1);
+  if (r != CUFFT_SUCCESS) return fail(cufft_fail(r, "cufftPlanMany(ring_fwd)"));
+  p->have_plans[0] = true;
+  // torus: L columns of 2L with stride L
+  int tn[1] = {2 * L};
+  r = cufftPlanMany(&p->torus_fwd, 1, n2, tn, L, 1, tn, L, 1, CUFFT_Z2Z, L);
+  if (r != CUFFT_SUCCESS) return fail(cufft_fail(r, "cufftPlanMany(torus_fwd)"));
+  p->have_plans[1] = true;
+  int pn[1] = {4 * L};
+  r = cufftPlanMany(&p->pad_inv, 1, n4, pn, L, 1, pn, L, 1, CUFFT_Z2Z, L);
+  if (r != CUFFT_SUCCESS) return fail(cufft_fail(r, "cufftPlanMany(pad_inv)"));
+  p->have_plans[2] = true;
+  // inverse rings: kFields*(L+1) rows of L+1 complex -> 2L real
+  int cin[1] = {L + 1}, rout[1] = {2 * L};
+  r = cufftPlanMany(&p->ring_inv, 1, n2, cin, 1, L + 1, rout, 1, 2 * L, CUFFT_Z2D, kFields * (L + 1));
+  if (r != CUFFT_SUCCESS) return fail(cufft_fail(r, "cufftPlanMany(ring_inv)"));
+  p->have_plans[3] = true;
+  *out = p;
+  return CMM_OK;
+}
+
+static int set_streams(cmm_sht* p, cudaStream_t s) {
+  cufftHandle h[4] = {p->ring_fwd, p->torus_fwd, p->pad_inv, p->ring_inv};
+  for (int k = 0; k < 4; ++k) {
+    cufftResult r = cufftSetStream(h[k], s);
+    if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftSetStream");
+  }
+  return CMM_OK;
+}
+
+// samples (L+1, 2L) -> alm (m-major half layout) in p->alm or `out`.
+int sht_forward(cmm_sht* p, const double* samples, double2* out, cudaStream_t s) {
+  const int L = p->L;
+  int rc = set_streams(p, s);
+  if (rc) return rc;
+  cufftResult r = cufftExecD2Z(p->ring_fwd, (cufftDoubleReal*)samples, (cufftDoubleComplex*)p->spec.p);
+  if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExecD2Z");
+  dim3 b(128), g1((L + 127) / 128, 2 * L);
+  torus_kernel<<<g1, b, 0, s>>>((const double2*)p->spec.p, L, (double2*)p->torus.p);
+  if ((rc = check_launch("torus_kernel"))) return rc;
+  r = cufftExecZ2Z(p->torus_fwd, (cufftDoubleComplex*)p->torus.p, (cufftDoubleComplex*)p->torus.p,
+                   CUFFT_FORWARD);
+  if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExecZ2Z(torus)");
+  dim3 g2((L + 127) / 128, 4 * L);
+  pad_kernel<<<g2, b, 0, s>>>((const double2*)p->torus.p, L, (double2*)p->pad.p);
+  if ((rc = check_launch("pad_kernel"))) return rc;
+  r = cufftExecZ2Z(p->pad_inv, (cufftDoubleComplex*)p->pad.p, (cufftDoubleComplex*)p->pad.p, CUFFT_INVERSE);
+  if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExecZ2Z(pad)");
+  if (L + 1 > 8 * 256) {
+    set_last_error("sht_forward: L too large for the analysis kernel");
+    return CMM_ERR_UNSUPPORTED;
+  }
+  analysis_kernel<<<L, 256, 0, s>>>((const double2*)p->pad.p, L, (const double*)p->w_fine.p,
+                                    (const double*)p->ct_fine.p, (const double*)p->pmm_fine.p,
+                                    (const double*)p->ra.p, (const double*)p->rb.p, out);
+  return check_launch("analysis_kernel");
+}
+
+// nf fields (nf, L, L) m-major -> samples (nf, L+1, 2L).
+int sht_inverse(cmm_sht* p, const double2* alm, int nf, double* samples, cudaStream_t s) {
+  const int L = p->L;
+  int rc = set_streams(p, s);
+  if (rc) return rc;
+  double2* S = (double2*)p->synth.p;
+  cudaError_t e = cudaMemsetAsync(S, 0, (size_t)nf * (L + 1) * (L + 1) * sizeof(double2), s);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+  const int npair = L / 2 + 1;
+  dim3 g(L, (npair + kSynthBlock - 1) / kSynthBlock);
+  if (nf == kFields)
+    synthesis_kernel<kFields><<<g, kSynthBlock, 0, s>>>(alm, L, (const double*)p->ct_rings.p,
+                                                        (const double*)p->pmm_rings.p,
+                                                        (const double*)p->ra.p, (const double*)p->rb.p, S);
+  else if (nf == 1)
+    synthesis_kernel<1><<<g, kSynthBlock, 0, s>>>(alm, L, (const double*)p->ct_rings.p,
+                                                  (const double*)p->pmm_rings.p, (const double*)p->ra.p,
+                                                  (const double*)p->rb.p, S);
+  else {
+    set_last_error("sht_inverse: nf must be 1 or 12");
+    return CMM_ERR_ARG;
+  }
+  if ((rc = check_launch("synthesis_kernel"))) return rc;
+  // Z2D over kFields*(L+1) rows; only the first nf*(L+1) rows matter
+  cufftResult r = cufftExecZ2D(p->ring_inv, (cufftDoubleComplex*)S, (cufftDoubleReal*)p->samples.p);
+  if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExecZ2D");
+  if (samples && samples != p->samples.p) {
+    e = cudaMemcpyAsync(samples, p->samples.p, (size_t)nf * (L + 1) * 2 * L * 8, cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync");
+  }
+  return CMM_OK;
+}
+
+int sht_velocity(cmm_sht* p, const cmm_mesh* vm, const double* omega, double2* psi_out,
+                 double* jets, cudaStream_t s) {
+  const int L = p->L;
+  double2* psi = (double2*)p->alm.p;
+  int rc = sht_forward(p, omega, psi, s);
+  if (rc) return rc;
+  dim3 b(128), g((L + 127) / 128, L);
+  dinv_kernel<<<g, b, 0, s>>>(psi, L);
+  if ((rc = check_launch("dinv_kernel"))) return rc;
+  if (psi_out) {
+    cudaError_t e = cudaMemcpyAsync(psi_out, psi, (size_t)L * L * sizeof(double2), cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(psi)");
+  }
+  double2* F = (double2*)p->fields.p;
+  ladder1_kernel<<<g, b, 0, s>>>(psi, L, F);
+  if ((rc = check_launch("ladder1_kernel"))) return rc;
+  ladder2_kernel<<<g, b, 0, s>>>(F, L);
+  if ((rc = check_launch("ladder2_kernel"))) return rc;
+  if ((rc = sht_inverse(p, F, kFields, nullptr, s))) return rc;
+  const int64_t nv = 2 + (int64_t)(L - 1) * 2 * L;
+  jets_kernel<<<(int)((nv + 127) / 128), 128, 0, s>>>((const double*)p->samples.p, L, vm->view.grid, jets);
+  return check_launch("jets_kernel");
+}
+
+int sht_destroy(cmm_sht* p) {
+  delete p;
+  return CMM_OK;
+}
+
+int sht_L(const cmm_sht* p) { return p->L; }
+
+}  // namespace cmm

@@ -6,9 +6,10 @@
 // (cmm_s2/core/mesh_functions.py:196-282): ring and sector from the angles
 // with numpy's floor-division semantics, the reference's near-row
 // corrections (theta_c <= 0.03 / > 0.85, great-circle side tests with
-// heaviside(0) = 0) and the diagonal side test.  The row tests use the
-// query point itself where the reference re-synthesises it from its angles
-// (equal up to rounding; only exact ties can differ).
+// heaviside(0) = 0) and the diagonal side test.  CUDA's atan2/sin/cos are
+// not numpy's, so a query exactly on a ring, meridian or diagonal (a
+// triangle edge or vertex) may resolve to the other triangle that also
+// contains it.
 #include <cuda_runtime.h>
 
 #include "cmm_internal.h"
@@ -72,12 +73,22 @@ __device__ __forceinline__ int latlon_locate(const MeshView& m, double x, double
   const double theta_c = (theta - m.theta[theta_l]) / m.dthe;
   const int phi_p1 = (phi_l + 1) % N;
   const D3 q = D3{x, y, z};
-  if (theta_c <= 0.03 && theta_l != 0) {
-    const D3 n = cross(gridpt(m, theta_l, phi_l), gridpt(m, theta_l, phi_p1));
-    if (dot(n, q) > 0.0) theta_l -= 1;
-  } else if (theta_c > 0.85 && theta_l != M - 2) {
-    const D3 n = cross(gridpt(m, theta_l + 1, phi_l), gridpt(m, theta_l + 1, phi_p1));
-    if (-dot(n, q) > 0.0) theta_l += 1;
+  const bool row_lo = theta_c <= 0.03 && theta_l != 0;
+  const bool row_hi = !row_lo && theta_c > 0.85 && theta_l != M - 2;
+  if (row_lo || row_hi) {
+    // the reference tests the point re-synthesised from its angles,
+    // sphere2cart(phi, theta) (mesh_functions.py:240, 249)
+    double sp, cp, st, cth;
+    sincos(phiq, &sp, &cp);
+    sincos(theta, &st, &cth);
+    const D3 q0 = D3{st * cp, st * sp, cth};
+    if (row_lo) {
+      const D3 n = cross(gridpt(m, theta_l, phi_l), gridpt(m, theta_l, phi_p1));
+      if (dot(n, q0) > 0.0) theta_l -= 1;
+    } else {
+      const D3 n = cross(gridpt(m, theta_l + 1, phi_l), gridpt(m, theta_l + 1, phi_p1));
+      if (-dot(n, q0) > 0.0) theta_l += 1;
+    }
   }
   if (theta_l == 0) return phi_l;
   if (theta_l == M - 2) return 2 * N * (M - 2) - N + phi_l;

@@ -161,6 +161,35 @@ int cmm_advect_project(const cmm_mesh* mesh, const cmm_mesh* velmesh,
                        const double* prev_coeffs, double eps, double* jets, double* work,
                        void* stream);
 
+/* ------------------------------------------- spherical-harmonic transforms */
+/* MWSS transforms at band-limit L (samples on L+1 rings x 2L longitudes,
+ * real fields).  Coefficients use an m-major half layout: alm[m][l]
+ * complex (interleaved re,im doubles), 0 <= m <= l < L, entries with l < m
+ * zero; negative orders follow from a_{l,-m} = (-1)^m conj(a_lm).
+ * The plan owns its FFT plans and scratch buffers. */
+typedef struct cmm_sht cmm_sht;
+int cmm_sht_create(int L, cmm_sht** out);
+int cmm_sht_destroy(cmm_sht* plan);
+
+/* samples (L+1,2L) -> alm (L,L) complex.  Replaces pyssht.forward(...,
+ * Method="MWSS", Reality=True) as called by inv_Laplacian
+ * (cmm_s2/core/spherical_harmonic_tools.py:16). */
+int cmm_sht_forward(cmm_sht* plan, const double* samples, double* alm, void* stream);
+
+/* nf (1 or 12) coefficient fields (nf,L,L) complex -> samples
+ * (nf,L+1,2L).  Replaces pyssht.inverse(..., Method="MWSS", Reality=True)
+ * (cmm_s2/core/spherical_harmonic_tools.py:84,91). */
+int cmm_sht_inverse(cmm_sht* plan, const double* alm, int nf, double* samples, void* stream);
+
+/* Vorticity samples omega (L+1,2L) on the velocity mesh's rings -> velocity
+ * jets (3,4,Nv_u) of the velocity mesh: inv_Laplacian, the angular-momentum
+ * operators and the 12 inverse transforms of project_stream with its
+ * tangent projection and pole handling
+ * (cmm_s2/core/spherical_harmonic_tools.py:14-19, 49-105).  psi (L,L)
+ * complex receives the stream function coefficients when not NULL. */
+int cmm_sht_velocity(cmm_sht* plan, const cmm_mesh* velmesh, const double* omega, double* psi,
+                     double* vel_jets, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

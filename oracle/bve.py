@@ -12,8 +12,12 @@ class BVEOracle:
 
     vorticity: callable (phi, theta) -> omega0 on arrays of angles."""
 
-    def __init__(self, verts, tris, locator, L, Nt, T, vorticity, rot_rate=2 * np.pi, n_maps=10):
+    def __init__(self, verts, tris, locator, L, Nt, T, vorticity, rot_rate=2 * np.pi, n_maps=10,
+                 closed=False, tie_fix=False):
+        """closed/tie_fix: evaluation options of MapOracle (see
+        oracle.spline.split_bary_closed and split_corners)."""
         self.verts, self.tris, self.loc = verts, tris, locator
+        self.closed, self.tie_fix = closed, tie_fix
         self.L, self.Nt, self.T = L, Nt, T
         self.vort, self.rot = vorticity, rot_rate
         ns = [i for i in range(1, Nt) if i % n_maps == 0]
@@ -40,7 +44,7 @@ class BVEOracle:
 
     # ------------------------------------------------------------------
     def _map(self, jets):
-        return MapOracle(self.verts, self.tris, self.loc, jets, self.geom)
+        return MapOracle(self.verts, self.tris, self.loc, jets, self.geom, self.tie_fix, self.closed)
 
     def _vorticity_at(self, X):
         """omega at the back-traced grid points X (3,Q) (:269-272)."""
@@ -64,7 +68,8 @@ class BVEOracle:
         return advect_project(prev, integ, t, self.dt, self.U, self.verts, self.s_pts, self.tan, identity)
 
     def composite(self):
-        return CompositeOracle(self.verts, self.tris, self.loc, self.stack[:self.Nc], self.geom)
+        return CompositeOracle(self.verts, self.tris, self.loc, self.stack[:self.Nc], self.geom,
+                               self.tie_fix, self.closed)
 
     def sample_grid(self, jets):
         """submaps(curr_map(sample_pts)) (:268), (3,Q)."""

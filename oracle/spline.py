@@ -80,12 +80,55 @@ def _sbb(cf, b):
             + 2 * (b[:, 2] * b[:, 0]) * cf[..., 5, :])
 
 
-def eval_patch(coeffs, tri, bcc_big, vs, pts, tie_fix=False):
+def inverse_rows(vs):
+    """Rows of the inverse vertex matrix of each triangle, (N,3,3):
+    bcc = R q with R = [v2 x v3, v3 x v1, v1 x v2] / det(v1,v2,v3)."""
+    v1, v2, v3 = vs[:, 0], vs[:, 1], vs[:, 2]
+    from .geometry import det_cols
+    d = det_cols(v1, v2, v3)
+    return np.stack([np.cross(v2, v3), np.cross(v3, v1), np.cross(v1, v2)], 1) / d[:, None, None]
+
+
+def split_bary_closed(vs, R, pts, lo, hi):
+    """Sub-triangle barycentrics of pts in closed form, (N,3) in the corner
+    order of SPLIT_CORNERS[lo, hi].
+
+    The reference's new_vpoints + bary_coords (cmm_s2/core/spherical_spline.py:
+    668-689, cmm_s2/core/utils.py:58-67) compute them from four determinants
+    per point.  The sub-triangle's corners are v_hi, e = (v_hi+v_mid)/|.| and
+    c = (v1+v2+v3)/|.|, so the same linear map is
+        g_V = b_hi - b_mid,  g_E = |v_hi+v_mid| (b_mid - b_lo),  g_C = |v1+v2+v3| b_lo
+    with b = R pts the big-triangle barycentrics.  This evaluation shares its
+    rounding between nearby points (the finite-difference jets of
+    cmm_s2/core/evolution_functions.py:102-103 then do not amplify it)."""
+    n = np.arange(len(pts))
+    b = np.einsum("nij,nj->ni", R, pts)
+    mid = 3 - lo - hi
+    v = [vs[:, 0], vs[:, 1], vs[:, 2]]
+    N4 = np.linalg.norm(vs[:, 0] + vs[:, 1] + vs[:, 2], axis=1)
+    Ne = np.linalg.norm(np.stack(v)[hi, n] + np.stack(v)[mid, n], axis=1)
+    gV, gE, gC = b[n, hi] - b[n, mid], Ne * (b[n, mid] - b[n, lo]), N4 * b[n, lo]
+    corn = SPLIT_CORNERS[lo, hi]
+    out = np.empty((len(pts), 3))
+    for p in range(3):
+        c = corn[:, p]
+        out[:, p] = np.where(c == hi, gV, np.where(c == 3, gC, gE))
+    return out
+
+
+def eval_patch(coeffs, tri, bcc_big, vs, pts, tie_fix=False, closed=False):
     """Evaluate un-normalised patches at ``pts`` located in ``tri`` with
-    big-triangle bcc ``bcc_big``; coeffs (...,19,Nt).  Returns (...,N)."""
+    big-triangle bcc ``bcc_big``; coeffs (...,19,Nt).  Returns (...,N).
+    closed=True uses split_bary_closed for the sub-triangle barycentrics."""
+    if closed:
+        R = inverse_rows(vs)
+        bcc_big = np.einsum("nij,nj->ni", R, pts)
     vn, lo, hi = split_corners(vs, bcc_big, tie_fix)
     ords = SPLIT_ORDINATES[lo, hi]
-    b = bary(vn[:, 0], vn[:, 1], vn[:, 2], pts)
+    if closed:
+        b = split_bary_closed(vs, R, pts, lo, hi)
+    else:
+        b = bary(vn[:, 0], vn[:, 1], vn[:, 2], pts)
     cf = np.stack([coeffs[..., ords[:, k], tri] for k in range(6)], axis=-2)
     return _sbb(cf, b)
 
@@ -93,29 +136,38 @@ def eval_patch(coeffs, tri, bcc_big, vs, pts, tie_fix=False):
 class MapOracle:
     """sphere_diffeomorphism (cmm_s2/core/spherical_spline.py:155-337)."""
 
-    def __init__(self, verts, tris, locator, vals, geom=None, tie_fix=False):
+    def __init__(self, verts, tris, locator, vals, geom=None, tie_fix=False, closed=False):
         self.verts, self.tris, self.loc = verts, tris, locator
-        self.tie_fix = tie_fix
+        self.tie_fix, self.closed = tie_fix, closed
         self.vals = vals
         self.coeffs = assemble(verts, tris, vals, geom)
 
     def __call__(self, q):
         """__call__ (:178-205): normalised image, (3,N)."""
         bcc, tri, vs = query(self.verts, self.tris, self.loc, q)
-        out = eval_patch(self.coeffs, tri, bcc, vs, q, self.tie_fix)
+        out = eval_patch(self.coeffs, tri, bcc, vs, q, self.tie_fix, self.closed)
         nrm = np.sqrt(out[0] ** 2 + out[1] ** 2 + out[2] ** 2)
         return (1 / nrm)[None] * out
 
-    def stencil_eval(self, q_pts, st_pts):
+    def stencil_eval(self, q_pts, st_pts, closed=None):
         """stencil_eval (:268-298): locate at q_pts (3,N), evaluate the four
-        stencil points st_pts (3,4,N) in that sub-triangle, not normalised."""
+        stencil points st_pts (3,4,N) in that sub-triangle, not normalised.
+        closed=True evaluates the sub-triangle barycentrics with
+        split_bary_closed (same linear map, shared rounding)."""
+        closed = self.closed if closed is None else closed
         bcc, tri, vs = query(self.verts, self.tris, self.loc, q_pts.T)
+        if closed:
+            R = inverse_rows(vs)
+            bcc = np.einsum("nij,nj->ni", R, q_pts.T)
         vn, lo, hi = split_corners(vs, bcc, self.tie_fix)
         ords = SPLIT_ORDINATES[lo, hi]
         cf = np.stack([self.coeffs[:, ords[:, k], tri] for k in range(6)], axis=-2)
         out = np.empty_like(st_pts)
         for i in range(4):
-            b = bary(vn[:, 0], vn[:, 1], vn[:, 2], st_pts[:, i, :].T)
+            if closed:
+                b = split_bary_closed(vs, R, st_pts[:, i, :].T, lo, hi)
+            else:
+                b = bary(vn[:, 0], vn[:, 1], vn[:, 2], st_pts[:, i, :].T)
             out[:, i, :] = _sbb(cf, b)
         return out
 
@@ -123,9 +175,9 @@ class MapOracle:
 class CompositeOracle:
     """composite_sphere_diffeomorphism (cmm_s2/core/spherical_spline.py:340-508)."""
 
-    def __init__(self, verts, tris, locator, vals_stack, geom=None, tie_fix=False):
+    def __init__(self, verts, tris, locator, vals_stack, geom=None, tie_fix=False, closed=False):
         self.verts, self.tris, self.loc = verts, tris, locator
-        self.tie_fix = tie_fix
+        self.tie_fix, self.closed = tie_fix, closed
         self.geom = geom if geom is not None else ps_split(verts, tris)
         self.vals = vals_stack
         self.coeffs = np.stack([assemble(verts, tris, v, self.geom) for v in vals_stack])
@@ -140,7 +192,7 @@ class CompositeOracle:
         tris, pts = [], []
         for i in reversed(range(n_c)):
             bcc, tri, vs = query(self.verts, self.tris, self.loc, p)
-            out = eval_patch(self.coeffs[i], tri, bcc, vs, p, self.tie_fix)
+            out = eval_patch(self.coeffs[i], tri, bcc, vs, p, self.tie_fix, self.closed)
             nrm = np.sqrt(out[0] ** 2 + out[1] ** 2 + out[2] ** 2)
             tris.append(tri)
             pts.append(p)

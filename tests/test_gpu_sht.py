@@ -1,0 +1,119 @@
+"""GPU parity: MWSS transforms and the vorticity -> velocity-jet pipeline
+against the oracle's restated transform and the reference's closed forms.
+
+Tolerances: coefficients and samples within 1e-12 relative to their
+largest magnitude; velocity jets within 1e-12 relative (values) and 1e-11
+relative (gradients, which carry an extra factor ~L)."""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import GOLDEN
+from oracle import sht as S
+from oracle import geometry as OG
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def nat():
+    import __graft_entry__
+    __graft_entry__.build()
+    from cmm_gpu import native
+    return native
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def mhalf(a_lm):
+    """oracle (L,L) [l,m] -> device layout [m,l]."""
+    return np.ascontiguousarray(a_lm.T)
+
+
+@pytest.mark.parametrize("L", [8, 32, 128])
+def test_forward_matches_oracle_on_generic_samples(nat, L):
+    rng = np.random.default_rng(L)
+    f = rng.standard_normal((L + 1, 2 * L))
+    f[0] = f[0, 0]   # the poles are single points
+    f[-1] = f[-1, 0]
+    ref = S.MWSS(L).forward(f)
+    got = nat.Sht(L).forward(dev(f)).cpu().numpy()
+    scale = np.abs(ref).max()
+    np.testing.assert_allclose(got / scale, mhalf(ref) / scale, rtol=0, atol=1e-12)
+
+
+@pytest.mark.parametrize("L", [8, 64])
+def test_inverse_matches_oracle(nat, L):
+    rng = np.random.default_rng(L + 1)
+    a = np.tril(rng.standard_normal((L, L)) + 1j * rng.standard_normal((L, L)))
+    a[:, 0] = a[:, 0].real
+    ref = S.MWSS(L).inverse(a)
+    sht = nat.Sht(L)
+    got = sht.inverse(dev(mhalf(a))).cpu().numpy()
+    scale = np.abs(ref).max()
+    np.testing.assert_allclose(got / scale, ref / scale, rtol=0, atol=1e-12)
+    many = np.stack([mhalf(a * (k + 1)) for k in range(12)])
+    got12 = sht.inverse(dev(many)).cpu().numpy()
+    for k in range(12):
+        np.testing.assert_allclose(got12[k] / scale, (k + 1) * ref / scale, rtol=0, atol=1e-12)
+
+
+def grid(L):
+    from cmm_gpu.meshgen import latlon_mesh_arrays
+    theta, phi, g, verts = latlon_mesh_arrays(L)
+    Phi, The = np.meshgrid(phi, theta)
+    return theta, phi, g, verts, Phi, The
+
+
+def test_velocity_jets_match_reference_fixture(nat):
+    """The fixture's velocity levels came from the reference's project_stream
+    (with the restated transform standing in for pyssht)."""
+    d = np.load(os.path.join(GOLDEN, "velocity_L8.npz"))
+    L = 8
+    theta, phi, g, verts, Phi, The = grid(L)
+    vm = nat.VelMesh(L, theta, phi, g, verts)
+    sht = nat.Sht(L)
+    for n, t in enumerate([0.0, 0.1, 0.2]):
+        om = (30 * np.cos(The) * np.cos(4 * (Phi + 2 * 2 * np.pi * t / 30)) * np.sin(The) ** 4
+              + 0.3 * np.sin(The) ** 2 * np.cos(2 * Phi + t))
+        jets = sht.velocity(vm, dev(om)).cpu().numpy()
+        ref = d["vals"][n]
+        s = np.abs(ref).max(axis=(1, 2), keepdims=True)
+        np.testing.assert_allclose(jets[:, :1] / s, ref[:, :1] / s, rtol=0, atol=1e-12)
+        np.testing.assert_allclose(jets[:, 1:] / s, ref[:, 1:] / s, rtol=0, atol=1e-11)
+
+
+@pytest.mark.parametrize("L", [64, 256])
+def test_rossby_haurwitz_velocity_closed_form(nat, L):
+    """cmm_s2/tests/test_spherical_harmonic_tools.py:48-61 closed forms."""
+    theta, phi, g, verts, Phi, The = grid(L)
+    vm = nat.VelMesh(L, theta, phi, g, verts)
+    om = 30 * np.cos(The) * np.cos(4 * Phi) * np.sin(The) ** 4
+    jets = nat.Sht(L).velocity(vm, dev(om)).cpu().numpy()
+    x, y, z = [c.reshape(-1) for c in g]
+    psi_x = -32 * z * x ** 3 + 16 * z * (1 - z ** 2) * x
+    psi_z = -(1 - z ** 2) ** 2 + 4 * z ** 2 * (1 - z ** 2) + 8 * x ** 2 * (1 - 3 * z ** 2) - 8 * x ** 4
+    vel = np.array([y * psi_z, z * psi_x - x * psi_z, -y * psi_x]).reshape(3, L + 1, 2 * L)
+    ref = np.concatenate([vel[:, 0, :1], vel[:, 1:-1].reshape(3, -1), vel[:, -1, :1]], 1)
+    assert np.abs(jets[:, 0] - ref).max() < 1e-12
+
+
+def test_velocity_generic_against_oracle(nat):
+    L = 48
+    theta, phi, g, verts, Phi, The = grid(L)
+    rng = np.random.default_rng(5)
+    om = np.exp(-((np.cos(The) - 0.3) ** 2) / 0.05) * np.cos(3 * Phi) + 0.1 * rng.standard_normal(Phi.shape)
+    om[0] = om[0, 0]
+    om[-1] = om[-1, 0]
+    vm = nat.VelMesh(L, theta, phi, g, verts)
+    jets = nat.Sht(L).velocity(vm, dev(om)).cpu().numpy()
+    sht = S.MWSS(L)
+    lp, lm, lz = S.ladder_operators(L)
+    psi = S.inv_laplacian(om, sht, S.inverse_laplacian_diag(L))
+    ref = S.velocity_jets(psi, sht, g, lp, lm, lz)
+    s = np.abs(ref).max(axis=(1, 2), keepdims=True)
+    np.testing.assert_allclose(jets / s, ref / s, rtol=0, atol=1e-11)

@@ -54,11 +54,21 @@ def test_latlon_arrays_match_reference():
 
 
 def test_latlon_locate_matches_reference(nat):
+    """Bit-exact triangle ids, except queries lying on a triangle edge or
+    vertex (ring points, meridians), which may resolve to another triangle
+    that contains them."""
     d = golden("velocity_L8.npz")
     vm, verts = velmesh(nat, 8)
     tri, bcc = vm.locate(dev(d["q"]))
-    np.testing.assert_array_equal(host(tri), d["tri"])
-    np.testing.assert_allclose(host(bcc), d["bcc"], rtol=0, atol=1e-13)
+    tri, bcc = host(tri), host(bcc)
+    mu = OG.LatLonMesh(8)
+    diff = tri != d["tri"]
+    on_edge = OG.edge_distance(mu.vertices, mu.simplices, d["tri"], d["q"]) <= 1e-14
+    assert not (diff & ~on_edge).any(), np.nonzero(diff & ~on_edge)
+    assert (bcc[diff].min(axis=1) >= -1e-13).all()
+    same = ~diff
+    np.testing.assert_allclose(bcc[same], d["bcc"][same], rtol=0, atol=1e-13)
+    print(f"{diff.sum()} of {len(tri)} edge/vertex queries resolved to another container")
 
 
 @pytest.mark.parametrize("L", [16, 128])
@@ -132,9 +142,23 @@ def test_advect_project_matches_reference(nat):
     loc = OG.QhullLocator(verts)
     near = OG.edge_distance(verts, tris, loc.locate(yref.T), yref.T) <= 1e-14
     ok = ~near
+    # (1) against the oracle evaluated in closed form (the same linear maps
+    #     with the per-triangle inverse vertex matrix the kernels use)
+    prev_o = OS.MapOracle(verts, tris, loc, a["jets_prev"], closed=True)
+    sn = OE.rk4_back(0.05, 0.1, s_pts.reshape(3, -1), U).reshape(s_pts.shape)
+    jo = OE.jets_from_stencil(prev_o.stencil_eval(yref, sn), tan)
+    np.testing.assert_allclose(jets[:, 0][:, ok], jo[:, 0][:, ok], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(jets[:, 1:][..., ok], jo[:, 1:][..., ok], rtol=0, atol=1e-10)
+    # (2) against the reference: values within 1e-12; gradients within the
+    #     reference's own rounding noise (its four per-point determinant
+    #     evaluations round independently and the 1/(4 eps) difference
+    #     amplifies that by 2.5e4: the closed-form oracle differs from the
+    #     reference by up to ~9e-9 here)
     ref = a["jets_rk4"]
+    noise = np.abs(jo[:, 1:][..., ok] - ref[:, 1:][..., ok]).max()
+    assert noise < 2e-8
     np.testing.assert_allclose(jets[:, 0][:, ok], ref[:, 0][:, ok], rtol=0, atol=1e-12)
-    np.testing.assert_allclose(jets[:, 1:][..., ok], ref[:, 1:][..., ok], rtol=0, atol=1e-9)
+    np.testing.assert_allclose(jets[:, 1:][..., ok], ref[:, 1:][..., ok], rtol=0, atol=2 * noise + 1e-10)
     np.testing.assert_allclose(jets[..., near], ref[..., near], rtol=0, atol=1e-6)
     for scheme, nvs, key in ((nat.EULER, 1, "jets_euler"), (nat.IMPROVED_EULER, 2, "jets_ieuler")):
         j, _ = mesh.advect_project(vm, vc[:nvs], 0.0, scheme, 0.0, 0.1, dev(s_pts), dev(tan), None)
