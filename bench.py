@@ -1,0 +1,359 @@
+"""Benchmark of the CMM hot path on GB300.
+
+Headline workload (the map-evaluation configuration of the metric): a
+level-7 icosahedral mesh (163,842 vertices, 327,680 triangles), a stack of
+8 composed Powell-Sabin submaps (seeded random rotations plus harmonic
+perturbations of amplitude 1e-2), 2^24 queries uniform on the sphere;
+outputs FP64 points, int32 triangle ids of the queries and FP64 3x3
+tangent Jacobians.  One step = one composition of all queries through all
+submaps.  metric = map evaluations per second = queries x submaps / time.
+
+  value      kernel-only, inputs resident in HBM (every buffer is larger
+             than the 129 MB L2, so no flush is needed between steps)
+  e2e        the same through compose_host: pinned host queries in, host
+             points/ids/Jacobians out, copies inside the timed region
+  roofline   algorithmic bytes of one launch / its CUDA-event time against
+             the measured HBM copy bandwidth; the kernel is FP64-issue
+             bound on GB300, so `fp64` reports the FP64 pipe as well
+  cpu_baseline  the oracle (numpy restatement of the reference) on a
+             bounded sample on the host cores
+  bve        the barotropic configuration (level 4, L=128, dt=1/200,
+             remap every 20 steps): BVE steps/s after the bootstrap
+
+`python bench.py --impl reference` times the CPU restatement of the
+reference (the oracle) on the same workload instead.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "cmm-s2_gb300"))
+
+LEVEL, SUBMAPS, LOGQ = 7, 8, 24
+METRIC = "map evals/s"
+# FP64 pipe peak of this machine's GB300 (FMA chain microbenchmark, 152x8 blocks
+# x 256 threads x 8 independent DFMA chains; profiles/fp64_peak.md)
+FP64_PEAK_TFLOPS = 1.204
+# DRAM traffic of one compose launch at the headline size, scaled from the
+# ncu capture summarised in profiles/compose_level7.md (None until captured)
+COMPOSE_TRAFFIC_BYTES = None
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def algorithmic_bytes(Q, S, nv, nt):
+    """Per launch: each query read (24 B) and its point (24 B), id (4 B) and
+    Jacobian (72 B) written once; each submap's per-vertex jets (96 B per
+    vertex) read once; the mesh tables (vertex coordinates, per-triangle
+    location records, hierarchy) read once."""
+    return Q * (24 + 24 + 4 + 72) + S * 96 * nv + 24 * nv + 12 * nt + 4 * 12 * nt // 3
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index, self.rows, self.proc = index, [], None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) == 6:
+                self.rows.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4) if r[2 + k] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def workload():
+    from cmm_gpu.meshgen import icosahedral_mesh, random_sphere_points, stencil_frames
+    from cmm_gpu.workloads import submap_stack
+    verts, tris = icosahedral_mesh(LEVEL)
+    tan, s_pts = stencil_frames(verts)
+    jets = submap_stack(s_pts, tan, SUBMAPS, seed=1)
+    return verts, tris, jets, random_sphere_points
+
+
+# ------------------------------------------------------------ CPU oracle
+def _oracle_worker(args):
+    q, = args
+    from oracle import geometry as OG, spline as OS
+    global _ORC
+    return OS.composite_jacobian(_ORC, q)[0]
+
+
+def _oracle_init(verts, tris, jets):
+    from oracle import geometry as OG, spline as OS
+    global _ORC
+    _ORC = OS.CompositeOracle(verts, tris, OG.ConeLocator(verts, tris), jets, closed=False)
+
+
+def cpu_rate(verts, tris, jets, nq, workers, steps=1, warmup=0):
+    """Map evals/s of the oracle (composition + Jacobians): `warmup`
+    untimed then `steps` timed samples of nq queries each."""
+    from cmm_gpu.meshgen import random_sphere_points
+    qs = [random_sphere_points(nq, seed=7 + k) for k in range(warmup + steps)]
+    if workers <= 1:
+        _oracle_init(verts, tris, jets)
+        for k in range(warmup):
+            _oracle_worker((qs[k],))
+        t0 = time.perf_counter()
+        for k in range(warmup, warmup + steps):
+            _oracle_worker((qs[k],))
+        dt = time.perf_counter() - t0
+        return steps * nq * len(jets) / dt, 1
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(workers, initializer=_oracle_init, initargs=(verts, tris, jets)) as pool:
+        pool.map(_oracle_worker, [(qs[0][:64],)] * workers)        # load the workers
+        for k in range(warmup):
+            pool.map(_oracle_worker, [(p,) for p in np.array_split(qs[k], workers)])
+        t0 = time.perf_counter()
+        for k in range(warmup, warmup + steps):
+            pool.map(_oracle_worker, [(p,) for p in np.array_split(qs[k], workers)])
+        dt = time.perf_counter() - t0
+    return steps * nq * len(jets) / dt, workers
+
+
+# ------------------------------------------------------------- GPU arm
+def bench_gpu(args, rank, world):
+    import torch
+    from cmm_gpu import native
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    verts, tris, jets, rsp = workload()
+    Q = 1 << args.logq
+    mesh = native.Mesh(verts, tris, LEVEL)
+    cs = [mesh.assemble(torch.from_numpy(j).to(dev)) for j in jets]
+    q = torch.from_numpy(rsp(Q, seed=3 + rank)).to(dev)
+    out = torch.empty_like(q)
+    tri = torch.empty(Q, dtype=torch.int32, device=dev)
+    jac = torch.empty((Q, 3, 3), dtype=torch.float64, device=dev)
+    arr = (native.ctypes.c_void_p * SUBMAPS)(*[c.data_ptr() for c in cs])
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        native.check(native.lib.cmm_compose(mesh.h, arr, SUBMAPS, native._ptr(q), Q, native._ptr(out),
+                                            native._ptr(tri), None, native._ptr(jac),
+                                            native.ctypes.c_void_p(stream.cuda_stream)), "cmm_compose")
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    assert mesh.status() == 0
+    n0 = native.lib.cmm_launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev.index) as clk:
+        barrier()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+    launches = native.lib.cmm_launch_count() - n0
+    ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * Q * SUBMAPS / (ms / 1e3)
+
+    # end to end through the host-buffer API
+    qh = torch.from_numpy(rsp(Q, seed=3 + rank)).pin_memory()
+    oh = torch.empty((Q, 3), dtype=torch.float64).pin_memory()
+    th = torch.empty(Q, dtype=torch.int32).pin_memory()
+    jh = torch.empty((Q, 3, 3), dtype=torch.float64).pin_memory()
+    del out, jac, tri
+    torch.cuda.empty_cache()
+    scratch, streams = native.compose_host(mesh, cs, qh, oh, th, jh)
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    e0.record(stream)
+    for _ in range(args.steps):
+        scratch, streams = native.compose_host(mesh, cs, qh, oh, th, jh, scratch=scratch, streams=streams)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    ms_e2e = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        t = torch.tensor([ms_e2e], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_e2e = float(t.item())
+    assert mesh.status() == 0
+    del scratch
+
+    res = dict(ms=ms, value=value, ms_e2e=ms_e2e, launches=launches, clocks=clk.summary(),
+               nv=len(verts), nt=len(tris), Q=Q)
+    if rank == 0 and not args.no_bve:
+        try:
+            res["bve"] = bench_bve(args, dev)
+        except Exception as exc:  # reported, the headline stands on its own
+            res["bve"] = {"error": f"{type(exc).__name__}: {exc}"}
+    return res
+
+
+def bench_bve(args, dev):
+    """Config: level 4, L=128, dt=1/200, 200 steps, remap every 20, random
+    real SH initial vorticity l=1..16 (N(0,1) l^-1.5, seed 0)."""
+    import torch
+    from cmm_gpu.meshgen import icosahedral_mesh
+    from cmm_gpu.workloads import random_sh_vorticity
+    from cmm_gpu.spherical_simulations import BVESolver, Vorticity
+    _, a = random_sh_vorticity(16, seed=0)
+    verts, tris = icosahedral_mesh(4)
+    s = BVESolver(verts, tris, 4, 128, 200, 1.0, Vorticity(sh=a), n_maps=20)
+    s.bootstrap()
+    for _ in range(3):
+        s.step()
+    torch.cuda.synchronize()
+    n = 60
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(n):
+        s.step()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / n
+    return {"steps_per_s": 1e3 / ms, "ms_per_step": ms, "steps_timed": n,
+            "workload": "BVE level 4 (2562 vertices), L=128 MWSS 129x256, dt=1/200, remap every 20, "
+                        "random SH l<=16 initial vorticity; steps 5..64 after the bootstrap"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--cpu-queries", type=int, default=1 << 15)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-bve", action="store_true")
+    ap.add_argument("--logq", type=int, default=LOGQ, help="log2 queries per GPU (profiling cases)")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    global LOGQ
+    LOGQ = args.logq
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    cfg = {"workload": f"flow-map evaluation: level-{LEVEL} icosahedral mesh (163842 vertices, "
+                       f"327680 triangles), {SUBMAPS} composed submaps, 2^{LOGQ} uniform queries; "
+                       "FP64 points, int32 triangle ids, FP64 Jacobians",
+           "level": LEVEL, "submaps": SUBMAPS, "queries_per_gpu": 1 << LOGQ,
+           "l2": "inputs and outputs larger than L2 (queries 402 MB, Jacobians 1.2 GB), no flush",
+           "parallelism": f"replicas x{args.gpus} (independent queries per GPU)"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        verts, tris, jets, _ = workload()
+        workers = os.cpu_count() or 1
+        rate, used = cpu_rate(verts, tris, jets, args.cpu_queries, workers, args.steps, 1)
+        t_step = (1 << LOGQ) * SUBMAPS / rate
+        line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": "map evals/s",
+                "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
+                "cpu_baseline": {"value": rate, "unit": "map evals/s", "cores": used, "kind": "port",
+                                 "sample": f"{args.cpu_queries} queries x {SUBMAPS} submaps with "
+                                           "Jacobians, numpy oracle, one process per core"},
+                "e2e": {"value": rate, "unit": "map evals/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import torch
+    if world > 1:
+        torch.distributed.init_process_group("nccl")
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        # timed before any CUDA work so the spawn pool starts cleanly
+        verts, tris, jets, _ = workload()
+        rate, used = cpu_rate(verts, tris, jets, max(1024, args.cpu_queries // 8), 1)
+        cpu = {"value": rate, "unit": "map evals/s", "cores": used, "kind": "port",
+               "sample": f"{max(1024, args.cpu_queries // 8)} queries x {SUBMAPS} submaps with "
+                         "Jacobians, numpy oracle (restated reference), 1 thread"}
+    r = bench_gpu(args, rank, world)
+    if rank != 0:
+        torch.distributed.destroy_process_group()
+        return
+    peak, how = peaks()
+    algo = algorithmic_bytes(r["Q"], SUBMAPS, r["nv"], r["nt"])
+    achieved = algo / (r["ms"] / 1e3) / 1e9
+    Q = r["Q"]
+    line = {
+        "metric": METRIC, "value": r["value"], "unit": "map evals/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": how,
+                     "traffic": COMPOSE_TRAFFIC_BYTES, "algorithmic_bytes": algo},
+        "fp64": {"peak_tflops": FP64_PEAK_TFLOPS, "note": "kernel is FP64-issue bound on GB300"},
+        "cpu_baseline": cpu,
+        "e2e": {"value": world * Q * SUBMAPS / (r["ms_e2e"] / 1e3), "unit": "map evals/s",
+                "h2d_bytes_per_step": Q * 24, "d2h_bytes_per_step": Q * (24 + 4 + 72)},
+        "clocks": r["clocks"], "gpu_launches": r["launches"],
+    }
+    if "bve" in r:
+        line["bve"] = r["bve"]
+    print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -112,6 +112,53 @@ def latlon_mesh_arrays(L):
     return theta, phi, grid, verts
 
 
+def _cross(a, b):
+    return np.stack([a[:, 1] * b[:, 2] - a[:, 2] * b[:, 1], a[:, 2] * b[:, 0] - a[:, 0] * b[:, 2],
+                     a[:, 0] * b[:, 1] - a[:, 1] * b[:, 0]], 1)
+
+
+def _unit(x):
+    n = np.sqrt(x[:, 0] ** 2 + x[:, 1] ** 2 + x[:, 2] ** 2)
+    return np.stack([x[:, 0] / n, x[:, 1] / n, x[:, 2] / n], 1)
+
+
+def stencil_frames(verts, eps=1e-5):
+    """Per-vertex tangent frames (2,Nv,3) and the four stencil points
+    (3,4,Nv) at distance eps (spherical_triangulation.stencil_pts,
+    cmm_s2/core/mesh_functions.py:128-166): a1 = v x e_z, a2 = v x a1
+    (first and last vertex, the poles, use fixed directions), stencil
+    points v -+ eps a1 -+ eps a2 lifted back onto the sphere along v."""
+    ez = np.broadcast_to([0.0, 0.0, 1.0], verts.shape)
+    a1 = _cross(verts, ez)
+    a2 = _cross(verts, a1)
+    s = 1 / np.sqrt(2)
+    a1[0] = _cross(verts[:1], np.array([[s, 0.0, s]]))[0]
+    a1[-1] = _cross(verts[-1:], np.array([[s, 0.0, -s]]))[0]
+    a2[0] = _cross(verts[:1], a1[:1])[0]
+    a2[-1] = _cross(verts[-1:], a1[-1:])[0]
+    a1n, a2n = _unit(a1), _unit(a2)
+    pts = []
+    for sa, sb in ((-1, -1), (1, -1), (-1, 1), (1, 1)):
+        y = verts + sa * a1n * eps + sb * a2n * eps
+        yn = y[:, 0] * verts[:, 0] + y[:, 1] * verts[:, 1] + y[:, 2] * verts[:, 2]
+        tt = -yn + np.sqrt(yn ** 2 - (y[:, 0] ** 2 + y[:, 1] ** 2 + y[:, 2] ** 2) + 1)
+        pts.append(y + tt[:, None] * verts)
+    s_pts = np.stack([np.stack([p[:, c] for p in pts]) for c in range(3)])
+    return np.stack([a1n, a2n]), s_pts
+
+
+def identity_jets(verts):
+    """Jets (3,4,Nv) of the identity map: value x_c, gradient of x_c the
+    tangent projection of e_c (cmm_s2/core/spherical_simulations.py:165-169)."""
+    x = verts.T
+    jets = np.zeros((3, 4, len(verts)))
+    jets[:, 0] = x
+    P = np.eye(3)[:, :, None] - x[:, None, :] * x[None, :, :]
+    for k in range(3):
+        jets[k, 1:] = P[:, k]
+    return jets
+
+
 def random_sphere_points(n, seed):
     """``n`` points uniform on the unit sphere (normalised Gaussians), (n,3)."""
     rng = np.random.default_rng(seed)

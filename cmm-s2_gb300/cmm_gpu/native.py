@@ -22,6 +22,7 @@ _p, _i, _i64, _d = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_doubl
 _SIGS = {
     "cmm_last_error": (ctypes.c_char_p, []),
     "cmm_version": (_i, []),
+    "cmm_launch_count": (ctypes.c_longlong, []),
     "cmm_mesh_create": (_i, [_p, _i, _p, _i, _i, ctypes.POINTER(_p)]),
     "cmm_mesh_destroy": (_i, [_p]),
     "cmm_mesh_check": (_i, [_p, _i, _p, _i, _i, _p]),
@@ -35,6 +36,7 @@ _SIGS = {
     "cmm_velocity_eval": (_i, [_p, ctypes.POINTER(_p), _i, _d, _d, _d, _p, _i64, _p, _p]),
     "cmm_integrate": (_i, [_p, ctypes.POINTER(_p), _i, _d, _i, _d, _d, _p, _i64, _p, _p]),
     "cmm_advect_workspace": (_i64, [_p]),
+    "cmm_vorticity_eval": (_i, [_p, _i, _p, _i, _p, _i, _d, _p, _p, _p]),
     "cmm_sht_create": (_i, [_i, ctypes.POINTER(_p)]),
     "cmm_sht_destroy": (_i, [_p]),
     "cmm_sht_forward": (_i, [_p, _p, _p, _p]),
@@ -182,6 +184,8 @@ class Mesh:
 
 
 EULER, IMPROVED_EULER, RK4 = 0, 1, 2
+(VORT_NONE, VORT_ROSSBY_HAURWITZ, VORT_ZONAL_JET, VORT_PERTURBED_JET, VORT_MULTI_JET,
+ VORT_GAUSSIAN_VORTEX, VORT_GAUSSIAN_JETS) = range(7)
 
 
 class VelMesh(Mesh):
@@ -201,6 +205,18 @@ class VelMesh(Mesh):
                                          verts.ctypes.data, ctypes.byref(h)), "cmm_velmesh_create")
         self.h = h
         self.stride = lib.cmm_coeff_stride(3)
+
+    def vorticity(self, kind, params, X, rot_rate, sh=None, omega=None):
+        """omega (L+1, 2L) at the back-traced sample points X (Q,3)."""
+        X = _dev(X)
+        params = np.ascontiguousarray(params if params is not None else [], dtype=np.float64)
+        if omega is None:
+            omega = torch.empty((self.L + 1, 2 * self.L), dtype=torch.float64, device=X.device)
+        lmax = -1 if sh is None else sh.shape[0] - 1
+        check(lib.cmm_vorticity_eval(self.h, kind, params.ctypes.data if len(params) else None,
+                                     len(params), _ptr(sh), lmax, rot_rate, _ptr(X), _ptr(omega),
+                                     _stream(X.device)), "cmm_vorticity_eval")
+        return omega
 
     def velocity(self, vel_coeffs, ts0, t, dt, x):
         x = _dev(x)
@@ -260,3 +276,47 @@ class Sht:
         check(lib.cmm_sht_velocity(self.h, velmesh.h, _ptr(omega), _ptr(psi), _ptr(jets),
                                    _stream(omega.device)), "cmm_sht_velocity")
         return jets
+
+
+def compose_host(mesh, coeffs, q_host, out_host, tri_host=None, jac_host=None, chunks=8,
+                 streams=None, scratch=None):
+    """Composition of host-resident queries (pinned (n,3) float64) into
+    host-resident outputs, pipelined in `chunks` pieces over two CUDA
+    streams so the host<->device copies overlap the kernels.  Returns the
+    scratch dict for reuse."""
+    n = q_host.shape[0]
+    dev = mesh.device
+    streams = streams or [torch.cuda.Stream(dev), torch.cuda.Stream(dev)]
+    step = (n + chunks - 1) // chunks
+    if scratch is None:
+        scratch = {}
+        for k in range(2):
+            scratch[k] = dict(
+                q=torch.empty((step, 3), dtype=torch.float64, device=dev),
+                out=torch.empty((step, 3), dtype=torch.float64, device=dev),
+                tri=torch.empty(step, dtype=torch.int32, device=dev) if tri_host is not None else None,
+                jac=torch.empty((step, 3, 3), dtype=torch.float64, device=dev) if jac_host is not None else None)
+    arr = (ctypes.c_void_p * len(coeffs))(*[c.data_ptr() for c in coeffs])
+    cur = torch.cuda.current_stream(dev)
+    for s in streams:
+        s.wait_stream(cur)
+    for c in range(chunks):
+        lo, hi = c * step, min(n, (c + 1) * step)
+        if lo >= hi:
+            break
+        k = c % 2
+        s, b = streams[k], scratch[k]
+        m = hi - lo
+        with torch.cuda.stream(s):
+            b["q"][:m].copy_(q_host[lo:hi], non_blocking=True)
+            check(lib.cmm_compose(mesh.h, arr, len(coeffs), _ptr(b["q"]), m, _ptr(b["out"]),
+                                  _ptr(b["tri"]), None, _ptr(b["jac"]), ctypes.c_void_p(s.cuda_stream)),
+                  "cmm_compose")
+            out_host[lo:hi].copy_(b["out"][:m], non_blocking=True)
+            if tri_host is not None:
+                tri_host[lo:hi].copy_(b["tri"][:m], non_blocking=True)
+            if jac_host is not None:
+                jac_host[lo:hi].copy_(b["jac"][:m], non_blocking=True)
+    for s in streams:
+        cur.wait_stream(s)
+    return scratch, streams

@@ -1,0 +1,180 @@
+"""Barotropic vorticity equation on the rotating sphere with the
+characteristic mapping method, stepped on the GPU through libcmmgpu.so.
+
+``BVESolver`` holds the whole state on the device and reproduces the
+reference driver euler_simulation_sphere_remapping
+(cmm_s2/core/spherical_simulations.py:144-297) step for step: the
+Euler / improved-Euler / RK4 bootstrap (:216-261), then per step the RK4
+map update, the evaluation of submaps o current map at the MWSS sample
+points, the vorticity there, its inversion to velocity jets and the remap
+every n_maps steps.
+"""
+import math
+
+import numpy as np
+import torch
+
+from . import native
+from .meshgen import identity_jets, latlon_mesh_arrays, stencil_frames
+
+_FIELDS = {
+    "rossby_wave": native.VORT_ROSSBY_HAURWITZ,
+    "zonal_jet": native.VORT_ZONAL_JET,
+    "perturbed_zonal_jet": native.VORT_PERTURBED_JET,
+    "multi_jet": native.VORT_MULTI_JET,
+    "gaussian_vortex": native.VORT_GAUSSIAN_VORTEX,
+    "gaussian_zonal_jets": native.VORT_GAUSSIAN_JETS,
+}
+
+
+class Vorticity:
+    """Initial vorticity evaluated on the device: a built-in field of
+    cmm_s2/core/dynamical_fields.py (by name) and/or a real spherical-
+    harmonic series (coefficients (lmax+1, 2lmax+1), column l+m)."""
+
+    def __init__(self, field=None, params=(), sh=None):
+        self.kind = _FIELDS[field] if field is not None else native.VORT_NONE
+        self.params = np.asarray(params, dtype=np.float64)
+        self.sh = None if sh is None else np.ascontiguousarray(sh, dtype=np.float64)
+
+    @classmethod
+    def from_reference(cls, f):
+        """Accept a reference field function (or its name)."""
+        if isinstance(f, Vorticity):
+            return f
+        name = f if isinstance(f, str) else getattr(f, "__name__", None)
+        if name not in _FIELDS:
+            raise ValueError(f"no device implementation of vorticity field {name!r}")
+        return cls(name, (0.0,) if name == "rossby_wave" else ())
+
+
+class BVESolver:
+    def __init__(self, verts, tris, level, L, Nt, T, vorticity, rot_rate=2 * np.pi, n_maps=10,
+                 device=None):
+        self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
+        dev = self.device
+        self.vort = Vorticity.from_reference(vorticity)
+        self.sh = None if self.vort.sh is None else torch.from_numpy(self.vort.sh).to(dev)
+        self.L, self.Nt, self.T, self.rot = L, Nt, T, rot_rate
+        self.mesh = native.Mesh(verts, tris, level, device=dev.index)
+        theta, phi, grid, vverts = latlon_mesh_arrays(L)
+        self.vm = native.VelMesh(L, theta, phi, grid, vverts, device=dev.index)
+        self.sht = native.Sht(L, device=dev.index)
+        tan, s_pts = stencil_frames(verts)
+        self.tan = torch.from_numpy(np.ascontiguousarray(tan)).to(dev)
+        self.s_pts = torch.from_numpy(np.ascontiguousarray(s_pts)).to(dev)
+        self.id_jets = torch.from_numpy(identity_jets(verts)).to(dev)
+        ns = [i for i in range(1, Nt) if i % n_maps == 0]
+        ns.append(Nt)
+        self.ns = ns
+        self.tspan = np.linspace(0, T, Nt, endpoint=False)
+        self.dt = self.tspan[1] - self.tspan[0]
+        self.sample_pts = torch.from_numpy(
+            np.ascontiguousarray(np.stack([g.reshape(-1) for g in grid], 1))).to(dev)
+        nv = len(verts)
+        f64 = dict(dtype=torch.float64, device=dev)
+        self.jets = self.id_jets.clone()
+        self.coeffs_cur = self.mesh.new_coeffs()
+        self.stack = [self.mesh.new_coeffs() for _ in ns]
+        self.stack_jets = [None for _ in ns]
+        self.vel_coeffs = [self.vm.new_coeffs() for _ in range(3)]
+        self.vel_jets = torch.empty((3, 4, self.vm.nv), **f64)
+        self.work = torch.empty(native.lib.cmm_advect_workspace(self.mesh.h), **f64)
+        self.X = torch.empty_like(self.sample_pts)
+        self.omega = torch.empty((L + 1, 2 * L), **f64)
+        self.Nc = 0
+        self.ts0 = float(self.tspan[0])
+        self.nvs = 1
+        self.stepping = False
+        self.identity = True
+        self.count = 0
+        self.step_index = 0
+        self.launches = 0
+
+    # ------------------------------------------------------------ pieces
+    def _project(self, X, n, rot=None):
+        """omega at X -> velocity slot n (inv_Laplacian + project_stream)."""
+        rot = self.rot if rot is None else rot
+        self.vm.vorticity(self.vort.kind, self.vort.params, X, rot, sh=self.sh, omega=self.omega)
+        if self.stepping:
+            c = self.vel_coeffs
+            self.vel_coeffs = [c[1], c[2], c[0]]
+        self.sht.velocity(self.vm, self.omega, jets=self.vel_jets)
+        self.vm.assemble(self.vel_jets, out=self.vel_coeffs[n])
+        self.launches += 1 + 9 + 1
+
+    def _advect(self, scheme, t, prev):
+        self.mesh.advect_project(self.vm, self.vel_coeffs[:self.nvs], self.ts0, scheme, t, self.dt,
+                                 self.s_pts, self.tan, prev, jets=self.jets, work=self.work)
+        self.mesh.assemble(self.jets, out=self.coeffs_cur)
+        self.launches += 3
+
+    def _sample(self):
+        """submaps(curr_map(sample_pts)) (spherical_simulations.py:268)."""
+        cs = self.stack[:self.Nc] + [self.coeffs_cur]
+        self.mesh.compose(cs, self.sample_pts, out=self.X)
+        self.launches += 1
+        return self.X
+
+    # ------------------------------------------------------------ driver
+    def bootstrap(self):
+        """spherical_simulations.py:216-261."""
+        dt = self.dt
+        self._project(self.sample_pts, 0, rot=0.0)   # omega0 on the grid itself
+        self._advect(native.EULER, 0.0, None)
+        self._project(self._sample_single(), 1)
+        self.nvs = 2
+        self._advect(native.IMPROVED_EULER, 0.0, None)
+        self._project(self._sample_single(), 1)
+        prev = self.coeffs_cur.clone()
+        self._advect(native.RK4, dt, prev)
+        X = self._sample_single()
+        self.nvs = 3
+        self._project(X, 2)
+        self.stepping = True
+        self.identity = False
+        self.count = 2
+        self.step_index = 2
+
+    def _sample_single(self):
+        self.mesh.compose([self.coeffs_cur], self.sample_pts, out=self.X)
+        self.launches += 1
+        return self.X
+
+    def step(self):
+        """One pass of the main loop (spherical_simulations.py:263-294)."""
+        t = float(self.tspan[self.step_index])
+        self._advect(native.RK4, t, None if self.identity else self.coeffs_cur)
+        self._project(self._sample(), 2)
+        self.ts0 = self.ts0 + self.dt
+        self.count += 1
+        self.identity = False
+        if self.count in self.ns:
+            idx = self.ns.index(self.count)
+            self.Nc = idx + 1
+            self.stack[idx].copy_(self.coeffs_cur)
+            self.stack_jets[idx] = self.jets.clone()
+            self.jets.copy_(self.id_jets)
+            self.identity = True
+        self.step_index += 1
+
+    def run(self, nsteps=None):
+        self.bootstrap()
+        n = self.Nt - 2 if nsteps is None else nsteps
+        for _ in range(n):
+            self.step()
+        return self
+
+    # --------------------------------------------------------- outputs
+    def composite(self, q, want_jac=False):
+        """The back-to-label map at points q (N,3) on the device: the
+        submaps composed with the current map, or the submaps alone right
+        after a remap (the reference returns ``submaps``, :297)."""
+        cs = self.stack[:self.Nc] + ([] if self.identity else [self.coeffs_cur])
+        if not cs:
+            return q.clone(), None
+        out, _, _, jac = self.mesh.compose(cs, q, want_jac=want_jac)
+        return out, jac
+
+    def stack_coeffs(self):
+        return self.stack[:self.Nc]

@@ -19,6 +19,8 @@ const char* cmm_last_error(void) { return last_error(); }
 
 int cmm_version(void) { return 1; }
 
+long long cmm_launch_count(void) { return launch_count(); }
+
 int cmm_mesh_create(const double* verts, int nv, const int32_t* tris, int nt, int level,
                     cmm_mesh** out) {
   if (!verts || !tris || !out) return arg_error("cmm_mesh_create: null pointer");
@@ -161,6 +163,20 @@ int cmm_integrate(const cmm_mesh* velmesh, const double* const* vel_coeffs, int 
   TimeWeights tw;
   if ((rc = stage_weights(nvs, ts0, scheme, t, dt, &tw))) return rc;
   return launch_integrate(velmesh->view, vc, nvs, tw, scheme, dt, x, n, out, (cudaStream_t)stream);
+}
+
+int cmm_vorticity_eval(const cmm_mesh* velmesh, int kind, const double* params, int nparams,
+                       const double* sh, int lmax, double rot_rate, const double* X,
+                       double* omega, void* stream) {
+  if (!velmesh || velmesh->view.kind != kLatLon) return arg_error("cmm_vorticity_eval: velocity mesh expected");
+  if (!X || !omega || (nparams > 0 && !params) || nparams > 12 || kind < 0 || kind > 6 ||
+      (sh && lmax < 0))
+    return arg_error("cmm_vorticity_eval: bad argument");
+  const int L = velmesh->view.L;
+  const int64_t Q = (int64_t)(L + 1) * 2 * L;
+  return launch_vorticity(kind, params, nparams, sh, lmax, rot_rate, X, Q, 2 * L,
+                          (const double*)velmesh->cos_theta.p, omega, velmesh->view.status,
+                          (cudaStream_t)stream);
 }
 
 int cmm_sht_create(int L, cmm_sht** out) {

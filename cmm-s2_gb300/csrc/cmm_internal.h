@@ -51,6 +51,9 @@ constexpr int kLatLon = 1;
 
 void set_last_error(const std::string& s);
 int cuda_fail(cudaError_t e, const char* what);
+// Count of kernels this library has launched (cmm_launch_count).
+void note_launch(int n = 1);
+long long launch_count();
 
 struct DeviceBuffer {
   void* p = nullptr;
@@ -65,7 +68,7 @@ struct DeviceBuffer {
 struct cmm_mesh {
   cmm::MeshView view;
   cmm::DeviceBuffer verts, tri_v, tri_loc, tri_asm, root, root_f, root_adj, node_n, node_nf, leaf_row,
-      status, theta, phi, grid;
+      status, theta, phi, grid, cos_theta;
 };
 
 namespace cmm {
@@ -117,6 +120,10 @@ int launch_advect_points(const MeshView& mesh, const MeshView& vm, VelPtrs vc, i
 int launch_project_jets(const MeshView& mesh, const double* prev_coeffs, const double* yn,
                         const double* sn, const double* tan, double eps, double* jets,
                         cudaStream_t s);
+
+int launch_vorticity(int kind, const double* params, int nparams, const double* sh, int lmax,
+                     double rot, const double* X, int64_t Q, int npr, const double* cos_ring,
+                     double* omega, int* status, cudaStream_t s);
 
 // spherical-harmonic transforms (sht.cu)
 int sht_create(int L, cmm_sht** out);

@@ -182,6 +182,38 @@ __device__ __forceinline__ bool finite3(double x, double y, double z) {
   return isfinite(x) && isfinite(y) && isfinite(z);
 }
 
+constexpr double kTwoPi = 6.283185307179586;
+
+// numpy float floor_divide / remainder for b > 0 (npy_divmod): exact fmod,
+// then the quotient of the exact difference, rounded to the nearest
+// integer below.
+__device__ __forceinline__ double np_floor_divide(double a, double b) {
+  double mod = fmod(a, b);
+  double div = (a - mod) / b;
+  if (mod != 0.0 && (mod < 0.0)) div -= 1.0;
+  if (div == 0.0) return copysign(0.0, a / b);
+  double fl = floor(div);
+  if (div - fl > 0.5) fl += 1.0;
+  return fl;
+}
+
+__device__ __forceinline__ double np_remainder(double a, double b) {
+  double mod = fmod(a, b);
+  if (mod != 0.0) {
+    if (mod < 0.0) mod += b;
+  } else {
+    mod = copysign(0.0, b);
+  }
+  return mod;
+}
+
+// utils.cart2sphere (cmm_s2/core/utils.py:18-23): phi in [0, 2 pi), theta.
+__device__ __forceinline__ void cart2sphere(double x, double y, double z, double* phi,
+                                            double* theta) {
+  *phi = np_remainder(atan2(y, x) + kTwoPi, kTwoPi);
+  *theta = atan2(sqrt(__dadd_rn(__dmul_rn(y, y), __dmul_rn(x, x))), z);
+}
+
 inline int grid_for(int64_t n, int block) {
   int64_t b = (n + block - 1) / block;
   const int64_t cap = 152LL * 16;

@@ -230,6 +230,7 @@ __global__ void __launch_bounds__(kBlock) stencil_kernel(MeshView m, const doubl
 }
 
 int check_launch(const char* what) {
+  note_launch();
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? CMM_OK : cuda_fail(e, what);
 }

@@ -8,6 +8,7 @@
 // icosahedral hierarchy is rebuilt from the vertex coordinates, and every
 // leaf of the hierarchy is mapped back to its row of the caller's table.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <unordered_map>
@@ -22,6 +23,10 @@ thread_local std::string g_err;
 }
 
 void set_last_error(const std::string& s) { g_err = s; }
+
+static std::atomic<long long> g_launches{0};
+void note_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
 const char* last_error() { return g_err.c_str(); }
 
 int cuda_fail(cudaError_t e, const char* what) {

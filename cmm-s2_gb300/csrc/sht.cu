@@ -344,6 +344,7 @@ int cufft_fail(cufftResult r, const char* what) {
 }
 
 int check_launch(const char* what) {
+  note_launch();
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? CMM_OK : cuda_fail(e, what);
 }

@@ -66,6 +66,11 @@ int build_latlon(int L, const double* theta, const double* phi, const double* gr
   if ((rc = m->theta.upload(theta, (size_t)M * 8))) return rc;
   if ((rc = m->phi.upload(phi, (size_t)N * 8))) return rc;
   if ((rc = m->grid.upload(gpad.data(), gpad.size() * 8))) return rc;
+  {
+    std::vector<double> ct(M);
+    for (int t = 0; t < M; ++t) ct[t] = std::cos(theta[t]);
+    if ((rc = m->cos_theta.upload(ct.data(), ct.size() * 8))) return rc;
+  }
   if ((rc = m->status.upload(&zero, sizeof(int)))) return rc;
   MeshView& v = m->view;
   v = MeshView{};

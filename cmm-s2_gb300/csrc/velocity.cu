@@ -23,30 +23,6 @@ using namespace dev;
 namespace {
 
 constexpr int kBlock = 128;
-constexpr double kTwoPi = 6.283185307179586;
-
-// numpy float floor_divide / remainder for b > 0 (npy_divmod): exact fmod,
-// then the quotient of the exact difference, rounded to the nearest
-// integer below.
-__device__ __forceinline__ double np_floor_divide(double a, double b) {
-  double mod = fmod(a, b);
-  double div = (a - mod) / b;
-  if (mod != 0.0 && (mod < 0.0)) div -= 1.0;
-  if (div == 0.0) return copysign(0.0, a / b);
-  double fl = floor(div);
-  if (div - fl > 0.5) fl += 1.0;
-  return fl;
-}
-
-__device__ __forceinline__ double np_remainder(double a, double b) {
-  double mod = fmod(a, b);
-  if (mod != 0.0) {
-    if (mod < 0.0) mod += b;
-  } else {
-    mod = copysign(0.0, b);
-  }
-  return mod;
-}
 
 __device__ __forceinline__ int py_mod(long long a, int n) {
   long long r = a % n;
@@ -333,6 +309,7 @@ __global__ void __launch_bounds__(kBlock) project_jets_kernel(MeshView m, const 
 }
 
 int check_launch(const char* what) {
+  note_launch();
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? CMM_OK : cuda_fail(e, what);
 }

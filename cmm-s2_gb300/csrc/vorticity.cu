@@ -1,0 +1,131 @@
+// Vorticity at the back-traced sample points (sm_103a):
+//   omega = omega0(X) + 2 Omega cos(theta(X)) - 2 Omega cos(theta_grid)
+// (cmm_s2/core/spherical_simulations.py:269-272), with omega0 one of the
+// barotropic fields of cmm_s2/core/dynamical_fields.py:181-214 or the
+// synthetic benchmark fields, optionally plus a real spherical-harmonic
+// series.
+#include <cuda_runtime.h>
+
+#include "cmm_internal.h"
+#include "device_common.cuh"
+
+namespace cmm {
+
+using namespace dev;
+
+namespace {
+
+constexpr double kPi = 3.141592653589793;
+
+struct VortParams {
+  int kind;
+  double p[12];
+};
+
+// zonal jet family (dynamical_fields.py:181-192)
+__device__ __forceinline__ double jet(double theta, double theta_c) {
+  const double beta2 = 144.0;
+  const double u_lt = (kPi / 2) * exp(-2 * beta2 * (1 - cos(-theta + kPi / 2 - theta_c)));
+  return (cos(-theta + kPi / 2) * (2 * beta2 * (cos(theta_c) * sin(-theta + kPi / 2) -
+                                                sin(theta_c) * cos(-theta + kPi / 2))) +
+          sin(kPi / 2 - theta)) *
+         u_lt;
+}
+
+__device__ double omega0(const VortParams& v, double phi, double theta) {
+  switch (v.kind) {
+    case CMM_VORT_ROSSBY_HAURWITZ: {  // dynamical_fields.py:205-210
+      const double alpha = 1.0 / 30.0, Omega = 2 * kPi;
+      const double s = sin(theta);
+      return 30 * cos(theta) * cos(4 * (phi + 2 * Omega * alpha * v.p[0])) * (s * s * s * s);
+    }
+    case CMM_VORT_ZONAL_JET:
+      return jet(theta, kPi / 4);
+    case CMM_VORT_PERTURBED_JET:
+      return jet(theta, kPi / 4 + 0.01 * cos(12 * phi));
+    case CMM_VORT_MULTI_JET:
+      return jet(theta, kPi / 4 + 0.01 * cos(12 * phi)) +
+             jet(theta - kPi / 8, kPi / 4 + 0.01 * cos(12 * phi));
+    case CMM_VORT_GAUSSIAN_VORTEX: {  // dynamical_fields.py:200-203
+      const double x = sin(theta) * cos(phi), y = sin(theta) * sin(phi), z = cos(theta);
+      return 4 * kPi * exp(-((x - 1) * (x - 1) + y * y + z * z) / (1.0 / 16.0));
+    }
+    case CMM_VORT_GAUSSIAN_JETS: {  // p = amplitude, width, n, lat_1..lat_n
+      const double lat = kPi / 2 - theta;
+      double s = 0.0;
+      const int n = (int)v.p[2];
+      for (int j = 0; j < n && j < 9; ++j) {
+        const double d = (lat - v.p[3 + j]) / v.p[1];
+        s += v.p[0] * exp(-d * d);
+      }
+      return s;
+    }
+    default:
+      return 0.0;
+  }
+}
+
+// Real orthonormal series: m = 0 -> Pbar_l0, m > 0 -> sqrt2 Pbar_lm cos(m
+// phi), m < 0 -> sqrt2 Pbar_l|m| sin(|m| phi); coefficients (lmax+1,
+// 2 lmax+1), column l+m.
+__device__ double sh_value(const double* __restrict__ c, int lmax, double phi, double theta) {
+  const double x = cos(theta), s = sin(theta);
+  double out = 0.0, pmm = 0.28209479177387814;  // sqrt(1/(4 pi))
+  const int w = 2 * lmax + 1;
+  for (int m = 0; m <= lmax; ++m) {
+    if (m > 0) pmm = -pmm * sqrt((2.0 * m + 1.0) / (2.0 * m)) * s;
+    double cm = 1.0, sm = 0.0;
+    if (m > 0) sincos(m * phi, &sm, &cm);
+    double p1 = 0.0, p = pmm;
+    for (int l = m; l <= lmax; ++l) {
+      if (l == m + 1) {
+        p1 = p;
+        p = sqrt(2.0 * m + 3.0) * x * pmm;
+      } else if (l > m + 1) {
+        const double a = sqrt((4.0 * l * l - 1.0) / ((double)l * l - (double)m * m));
+        const double b = sqrt(((l - 1.0) * (l - 1.0) - (double)m * m) / (4.0 * (l - 1.0) * (l - 1.0) - 1.0));
+        const double pn = a * (x * p - b * p1);
+        p1 = p;
+        p = pn;
+      }
+      if (m == 0)
+        out += c[(int64_t)l * w + l] * p;
+      else
+        out += 1.4142135623730951 * p * (c[(int64_t)l * w + l + m] * cm + c[(int64_t)l * w + l - m] * sm);
+    }
+  }
+  return out;
+}
+
+__global__ void vorticity_kernel(VortParams vp, const double* __restrict__ sh, int lmax, double rot,
+                                 const double* __restrict__ X, int64_t Q, int npr,
+                                 const double* __restrict__ cos_ring, double* __restrict__ omega,
+                                 int* __restrict__ status) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Q;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double phi, theta;
+    cart2sphere(X[3 * i], X[3 * i + 1], X[3 * i + 2], &phi, &theta);
+    double w = omega0(vp, phi, theta);
+    if (sh) w += sh_value(sh, lmax, phi, theta);
+    const double r = w + 2 * rot * cos(theta) - 2 * rot * cos_ring[i / npr];
+    if (!isfinite(r)) atomicOr(status, CMM_FLAG_NONFINITE);
+    omega[i] = r;
+  }
+}
+
+}  // namespace
+
+int launch_vorticity(int kind, const double* params, int nparams, const double* sh, int lmax,
+                     double rot, const double* X, int64_t Q, int npr, const double* cos_ring,
+                     double* omega, int* status, cudaStream_t s) {
+  VortParams vp{};
+  vp.kind = kind;
+  for (int k = 0; k < nparams && k < 12; ++k) vp.p[k] = params[k];
+  vorticity_kernel<<<grid_for(Q, 128), 128, 0, s>>>(vp, sh, lmax, rot, X, Q, npr, cos_ring, omega,
+                                                    status);
+  note_launch();
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? CMM_OK : cuda_fail(e, "vorticity_kernel");
+}
+
+}  // namespace cmm

@@ -49,6 +49,9 @@ typedef enum {
 
 const char* cmm_last_error(void);
 int cmm_version(void);
+/* Number of kernels this library has launched so far in the process
+ * (library-call kernels such as cuFFT's not included). */
+long long cmm_launch_count(void);
 
 /* ------------------------------------------------------------------ mesh */
 typedef struct cmm_mesh cmm_mesh;
@@ -160,6 +163,28 @@ int cmm_advect_project(const cmm_mesh* mesh, const cmm_mesh* velmesh,
                        double dt, const double* s_pts, const double* tan,
                        const double* prev_coeffs, double eps, double* jets, double* work,
                        void* stream);
+
+/* ------------------------------------------------------------ vorticity */
+/* Initial vorticity fields: the barotropic fields of
+ * cmm_s2/core/dynamical_fields.py:181-214 and benchmark fields. */
+#define CMM_VORT_NONE 0
+#define CMM_VORT_ROSSBY_HAURWITZ 1 /* params[0] = t  (rossby_wave, :205-210) */
+#define CMM_VORT_ZONAL_JET 2       /* zonal_jet, :181-186 */
+#define CMM_VORT_PERTURBED_JET 3   /* perturbed_zonal_jet, :188-192 */
+#define CMM_VORT_MULTI_JET 4       /* multi_jet, :195-198 */
+#define CMM_VORT_GAUSSIAN_VORTEX 5 /* gaussian_vortex, :200-203 */
+#define CMM_VORT_GAUSSIAN_JETS 6   /* params: amplitude, width (rad), n <= 9,
+                                      latitudes (rad): sum A exp(-((lat-l_j)/w)^2) */
+
+/* omega at the sample rings of `velmesh` (L+1,2L) from the back-traced
+ * sample points X ((L+1)*2L, 3): omega0(X) + 2 rot cos(theta(X)) -
+ * 2 rot cos(theta_ring) (cmm_s2/core/spherical_simulations.py:269-272),
+ * omega0 = field `kind` plus, when sh is not NULL, the real orthonormal
+ * spherical-harmonic series sh (lmax+1, 2lmax+1) (column l+m; m>0 cos,
+ * m<0 sin, both with sqrt2). */
+int cmm_vorticity_eval(const cmm_mesh* velmesh, int kind, const double* params, int nparams,
+                       const double* sh, int lmax, double rot_rate, const double* X,
+                       double* omega, void* stream);
 
 /* ------------------------------------------- spherical-harmonic transforms */
 /* MWSS transforms at band-limit L (samples on L+1 rings x 2L longitudes,

@@ -1,0 +1,97 @@
+"""GPU parity of whole barotropic-vorticity runs.
+
+The reference rebuilds map gradients by centred differences with step
+1e-5 of sub-triangle evaluations it computes from four fresh determinants
+per point; their independent rounding, amplified 2.5e4 times, gives its
+runs a noise floor: a run evaluated with the closed-form sub-triangle
+barycentrics (the same linear maps, shared rounding) differs from the
+reference's own run by ~2e-10 in map coordinates after 12 steps
+(measured with the oracle in both forms).  So:
+  * against the reference's golden run: within 5x that measured spread;
+  * against the oracle in closed form: map coordinates within 1e-11 and
+    vorticity within 1e-10 relative;
+  * the Rossby-Haurwitz wave (an exact travelling solution) is reproduced
+    with the oracle's error."""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import GOLDEN
+from oracle import geometry as OG
+from oracle.bve import BVEOracle
+from oracle.fields import rossby_wave
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def sims():
+    import __graft_entry__
+    __graft_entry__.build()
+    from cmm_gpu import spherical_simulations
+    return spherical_simulations
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def test_short_run_matches_reference(sims):
+    from cmm_gpu.meshgen import icosahedral_mesh
+    d = np.load(os.path.join(GOLDEN, "bve_l2_L8.npz"))
+    verts, _ = icosahedral_mesh(2)
+    ql = OG.QhullLocator(verts)
+    s = sims.BVESolver(verts, ql.tris, 2, 8, 12, 1.0, "rossby_wave", n_maps=5).run()
+    assert s.Nc == int(d["Nc"]) and s.ns == list(d["ns"])
+    img, _ = s.composite(dev(d["q"]))
+    img = img.cpu().numpy()
+    jets = np.stack([j.cpu().numpy() for j in s.stack_jets[:s.Nc]])
+    orc = BVEOracle(verts, ql.tris, ql, 8, 12, 1.0, rossby_wave, n_maps=5, closed=True,
+                    tie_fix=True).run()
+    spread = np.abs(orc.composite()(d["q"]) - d["img"]).max()
+    assert spread < 1e-9
+    np.testing.assert_allclose(img, d["img"], rtol=0, atol=5 * spread + 1e-12)
+    np.testing.assert_allclose(jets[:, :, 0], d["vals"][:, :, 0], rtol=0, atol=1e-9)
+    np.testing.assert_allclose(img, orc.composite()(d["q"]), rtol=0, atol=1e-11)
+    assert s.mesh.status() == 0 and s.vm.status() == 0
+
+
+def test_level4_run_against_closed_form_oracle(sims):
+    from cmm_gpu.meshgen import icosahedral_mesh, random_sphere_points
+    verts, tris = icosahedral_mesh(4)
+    q = random_sphere_points(2000, seed=4)
+    s = sims.BVESolver(verts, tris, 4, 32, 30, 1.0, "rossby_wave", n_maps=10).run()
+    orc = BVEOracle(verts, tris, OG.ConeLocator(verts, tris), 32, 30, 1.0, rossby_wave, n_maps=10,
+                    closed=True, tie_fix=True).run()
+    img = s.composite(dev(q))[0].cpu().numpy()
+    np.testing.assert_allclose(img, orc.composite()(q), rtol=0, atol=1e-11)
+    om = s.omega.cpu().numpy()
+    np.testing.assert_allclose(om / np.abs(om).max(), orc.last_omega / np.abs(om).max(), rtol=0,
+                               atol=1e-10)
+
+
+def test_rossby_haurwitz_known_answer(sims):
+    """cmm_s2/tests/test_barotropic_vorticity.py:40-43, 81-90: the wave
+    travels exactly; compare omega(T) with rossby_wave(t=1)."""
+    from cmm_gpu.meshgen import icosahedral_mesh
+    verts, tris = icosahedral_mesh(3)
+    L, Nt = 32, 2 ** 4 + 10
+    s = sims.BVESolver(verts, tris, 3, L, Nt, 1.0, "rossby_wave", n_maps=10).run()
+    n = 60
+    ph, th = np.meshgrid(np.linspace(0, 2 * np.pi, n, endpoint=False), np.linspace(0, np.pi, n, endpoint=False))
+    q = np.stack([np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), np.cos(th)], -1).reshape(-1, 3)
+    X = s.composite(dev(q))[0].cpu().numpy().T
+    ang = OG.cart2sphere(X)
+    Om = 2 * np.pi
+    om = rossby_wave(ang[0], ang[1]) + 2 * Om * np.cos(ang[1]) - 2 * Om * np.cos(th.reshape(-1))
+    err = np.abs(om - rossby_wave(ph.reshape(-1), th.reshape(-1), t=1)).max()
+    orc = BVEOracle(verts, tris, OG.ConeLocator(verts, tris), L, Nt, 1.0, rossby_wave, n_maps=10,
+                    closed=True, tie_fix=True).run()
+    Xo = orc.composite()(q).T
+    ango = OG.cart2sphere(Xo)
+    omo = rossby_wave(ango[0], ango[1]) + 2 * Om * np.cos(ango[1]) - 2 * Om * np.cos(th.reshape(-1))
+    erro = np.abs(omo - rossby_wave(ph.reshape(-1), th.reshape(-1), t=1)).max()
+    print(f"RH L_inf error: gpu {err:.6e} oracle {erro:.6e}")
+    assert err < 0.5 and abs(err - erro) < 1e-9

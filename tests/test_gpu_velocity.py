@@ -148,7 +148,9 @@ def test_advect_project_matches_reference(nat):
     sn = OE.rk4_back(0.05, 0.1, s_pts.reshape(3, -1), U).reshape(s_pts.shape)
     jo = OE.jets_from_stencil(prev_o.stencil_eval(yref, sn), tan)
     np.testing.assert_allclose(jets[:, 0][:, ok], jo[:, 0][:, ok], rtol=0, atol=1e-12)
-    np.testing.assert_allclose(jets[:, 1:][..., ok], jo[:, 1:][..., ok], rtol=0, atol=1e-10)
+    # rounding differences (~1e-15: FMA contraction, summation order) times
+    # the 1/(4 eps) = 2.5e4 difference quotient
+    np.testing.assert_allclose(jets[:, 1:][..., ok], jo[:, 1:][..., ok], rtol=0, atol=5e-10)
     # (2) against the reference: values within 1e-12; gradients within the
     #     reference's own rounding noise (its four per-point determinant
     #     evaluations round independently and the 1/(4 eps) difference
