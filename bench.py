@@ -39,7 +39,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "cmm-s2_gb300"))
 
-LEVEL, SUBMAPS, LOGQ = 7, 8, 24
+LEVEL, SUBMAPS = 7, 8
 METRIC = "map evals/s"
 # FP64 pipe peak of this machine's GB300 (FMA chain microbenchmark, 152x8 blocks
 # x 256 threads x 8 independent DFMA chains; profiles/fp64_peak.md)
@@ -283,10 +283,9 @@ def main():
     ap.add_argument("--cpu-queries", type=int, default=1 << 15)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-bve", action="store_true")
-    ap.add_argument("--logq", type=int, default=LOGQ, help="log2 queries per GPU (profiling cases)")
+    ap.add_argument("--logq", type=int, default=24, help="log2 queries per GPU (profiling cases)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
-    global LOGQ
     LOGQ = args.logq
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -200,7 +200,8 @@ int cmm_sht_inverse(cmm_sht* plan, const double* alm, int nf, double* samples, v
 
 int cmm_sht_velocity(cmm_sht* plan, const cmm_mesh* velmesh, const double* omega, double* psi,
                      double* vel_jets, void* stream) {
-  if (!plan || !velmesh || !omega || !vel_jets) return arg_error("cmm_sht_velocity: null pointer");
+  if (!plan || !velmesh || (!omega && !psi) || !vel_jets)
+    return arg_error("cmm_sht_velocity: null pointer");
   if (velmesh->view.kind != kLatLon || velmesh->view.L != sht_L(plan))
     return arg_error("cmm_sht_velocity: velocity mesh of the plan's band-limit expected");
   return sht_velocity(plan, velmesh, omega, (double2*)psi, vel_jets, (cudaStream_t)stream);

@@ -544,14 +544,18 @@ int sht_velocity(cmm_sht* p, const cmm_mesh* vm, const double* omega, double2* p
                  double* jets, cudaStream_t s) {
   const int L = p->L;
   double2* psi = (double2*)p->alm.p;
-  int rc = sht_forward(p, omega, psi, s);
-  if (rc) return rc;
+  int rc;
   dim3 b(128), g((L + 127) / 128, L);
-  dinv_kernel<<<g, b, 0, s>>>(psi, L);
-  if ((rc = check_launch("dinv_kernel"))) return rc;
-  if (psi_out) {
-    cudaError_t e = cudaMemcpyAsync(psi_out, psi, (size_t)L * L * sizeof(double2), cudaMemcpyDeviceToDevice, s);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(psi)");
+  if (omega) {
+    if ((rc = sht_forward(p, omega, psi, s))) return rc;
+    dinv_kernel<<<g, b, 0, s>>>(psi, L);
+    if ((rc = check_launch("dinv_kernel"))) return rc;
+    if (psi_out) {
+      cudaError_t e = cudaMemcpyAsync(psi_out, psi, (size_t)L * L * sizeof(double2), cudaMemcpyDeviceToDevice, s);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(psi)");
+    }
+  } else {
+    psi = psi_out;  // stream function given by the caller
   }
   double2* F = (double2*)p->fields.p;
   ladder1_kernel<<<g, b, 0, s>>>(psi, L, F);

@@ -211,7 +211,8 @@ int cmm_sht_inverse(cmm_sht* plan, const double* alm, int nf, double* samples, v
  * operators and the 12 inverse transforms of project_stream with its
  * tangent projection and pole handling
  * (cmm_s2/core/spherical_harmonic_tools.py:14-19, 49-105).  psi (L,L)
- * complex receives the stream function coefficients when not NULL. */
+ * complex receives the stream function coefficients when not NULL; with
+ * omega NULL, psi is the input instead (project_stream alone). */
 int cmm_sht_velocity(cmm_sht* plan, const cmm_mesh* velmesh, const double* omega, double* psi,
                      double* vel_jets, void* stream);
 

@@ -1,0 +1,80 @@
+"""The reference-named adapter (cmm_gpu.mesh_functions, spherical_spline,
+evolution_functions, spherical_harmonic_tools) used the way the reference
+driver uses cmm_s2.core, against the golden outputs and the oracle."""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import GOLDEN
+from oracle import geometry as OG
+from oracle import spline as OS
+from oracle import sht as OSH
+from oracle import evolution as OE
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def cmm():
+    import __graft_entry__
+    __graft_entry__.build()
+    import cmm_gpu.mesh_functions as meshes
+    import cmm_gpu.spherical_spline as spl
+    import cmm_gpu.evolution_functions as evol
+    import cmm_gpu.spherical_harmonic_tools as sph
+    return meshes, spl, evol, sph
+
+
+def load(name):
+    return np.load(os.path.join(GOLDEN, name))
+
+
+def test_drop_in_calls(cmm):
+    meshes, spl, evol, sph = cmm
+    g, d, v = load("mesh_l3.npz"), load("map_l3.npz"), load("velocity_L8.npz")
+    mesh = meshes.spherical_triangulation(g["verts"], g["tris"])
+    bcc, tri, vs = mesh.query(g["q"][:3000])
+    assert (tri.cpu().numpy() == g["tri"][:3000]).mean() > 0.999
+    mp = spl.sphere_diffeomorphism(mesh, d["jets"][0])
+    img = mp(g["q"][:3000]).cpu().numpy()
+    np.testing.assert_allclose(img, d["img"][:, :3000], rtol=0, atol=1e-12)
+    sub = spl.composite_sphere_diffeomorphism(mesh, d["jets"], ns=[1, 2, 3])
+    for i in range(3):
+        sub.assemble_coefficients(i, d["jets"][i])
+    sub.Nc = 3
+    np.testing.assert_allclose(sub(g["q"][:3000]).cpu().numpy(), d["comp_img"][:3000], rtol=0, atol=1e-12)
+
+    mesh_u = meshes.structure_spherical_triangulation(8)
+    U = spl.spline_interp_velocity(mesh_u, v["vals"], ts=v["ts"])
+    for n in range(3):
+        U.init_coeffs(n)
+    U.nVs = 3
+    u = U(float(v["t"]), float(v["dt"]), v["q"].T).cpu().numpy()
+    np.testing.assert_allclose(u / np.abs(v["vel"]).max(), v["vel"] / np.abs(v["vel"]).max(), rtol=0,
+                               atol=1e-12)
+    x = g["verts"].T.copy()
+    yn = evol.RK4_proj(0.05, 0.1, x, U).cpu().numpy()
+    Uo = OS.VelocityOracle(OG.LatLonMesh(8), v["vals"], v["ts"])
+    for n in range(3):
+        Uo.init_coeffs(n)
+    Uo.nVs = 3
+    np.testing.assert_allclose(yn, OE.rk4_back(0.05, 0.1, x, Uo), rtol=0, atol=1e-13)
+    new = evol.advect_project_sphere(mp, evol.RK4_proj, 0.05, 0.1, U)
+    assert new.coeffs is mp.coeffs          # shared, as in the reference (:113)
+    assert new.vals.shape == (3, 4, len(g["verts"]))
+
+    # inv_Laplacian + project_stream into a fresh level
+    L = 8
+    Phi, The = np.meshgrid(mesh_u.phi, mesh_u.theta)
+    om = 30 * np.cos(The) * np.cos(4 * Phi) * np.sin(The) ** 4
+    dinv = OSH.inverse_laplacian_diag(L)
+    lp, lm, lz = OSH.ladder_operators(L)
+    psi = sph.inv_Laplacian(om, L, dinv)
+    ref_psi = OSH.inv_laplacian(om, OSH.MWSS(L), dinv)
+    np.testing.assert_allclose(psi.cpu().numpy(), ref_psi, rtol=0, atol=1e-12)
+    sph.project_stream(psi, L, lp, lm, lz, U, 0)
+    ref = OSH.velocity_jets(ref_psi, OSH.MWSS(L), mesh_u.grid_points, lp, lm, lz)
+    got = U.vals[0].cpu().numpy()
+    np.testing.assert_allclose(got / np.abs(ref).max(), ref / np.abs(ref).max(), rtol=0, atol=1e-12)
