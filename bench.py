@@ -41,12 +41,13 @@ sys.path.insert(0, os.path.join(ROOT, "cmm-s2_gb300"))
 
 LEVEL, SUBMAPS = 7, 8
 METRIC = "map evals/s"
-# FP64 pipe peak of this machine's GB300 (FMA chain microbenchmark, 152x8 blocks
-# x 256 threads x 8 independent DFMA chains; profiles/fp64_peak.md)
-FP64_PEAK_TFLOPS = 1.204
-# DRAM traffic of one compose launch at the headline size, scaled from the
-# ncu capture summarised in profiles/compose_level7.md (None until captured)
-COMPOSE_TRAFFIC_BYTES = None
+# DRAM bytes (read + write) of one compose launch per query, from the ncu
+# capture of 2^22 queries summarised in profiles/compose_level7.md
+# (18.348 GB + 0.420 GB); the gathers scale with the number of queries.
+COMPOSE_TRAFFIC_PER_QUERY = (18.348423e9 + 0.420334e9) / (1 << 22)
+# FP64 instructions per map evaluation (query x submap) with Jacobians,
+# from the same capture (FP64 pipe 88.6 % busy for 9.599 ms).
+FP64_INSTR_PER_EVAL = 152
 
 
 def peaks():
@@ -79,7 +80,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -189,6 +190,18 @@ def bench_gpu(args, rank, world):
         if world > 1:
             torch.distributed.barrier()
 
+    # FP64 issue rate of this GPU (8 independent FMA chains per thread)
+    sink = torch.empty(152 * 8 * 256, dtype=torch.float64, device=dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    native.lib.cmm_fp64_probe(152 * 8, 100, native._ptr(sink), native.ctypes.c_void_p(stream.cuda_stream))
+    e0.record(stream)
+    native.check(native.lib.cmm_fp64_probe(152 * 8, 20000, native._ptr(sink),
+                                           native.ctypes.c_void_p(stream.cuda_stream)), "cmm_fp64_probe")
+    e1.record(stream)
+    torch.cuda.synchronize()
+    fp64_fma_per_s = 152 * 8 * 256 * 8 * 20000 / (e0.elapsed_time(e1) / 1e3)
+    del sink
+
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -238,7 +251,7 @@ def bench_gpu(args, rank, world):
     del scratch
 
     res = dict(ms=ms, value=value, ms_e2e=ms_e2e, launches=launches, clocks=clk.summary(),
-               nv=len(verts), nt=len(tris), Q=Q)
+               nv=len(verts), nt=len(tris), Q=Q, fp64_fma_per_s=fp64_fma_per_s)
     if rank == 0 and not args.no_bve:
         try:
             res["bve"] = bench_bve(args, dev)
@@ -340,8 +353,13 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": how,
-                     "traffic": COMPOSE_TRAFFIC_BYTES, "algorithmic_bytes": algo},
-        "fp64": {"peak_tflops": FP64_PEAK_TFLOPS, "note": "kernel is FP64-issue bound on GB300"},
+                     "traffic": COMPOSE_TRAFFIC_PER_QUERY * Q, "algorithmic_bytes": algo},
+        "fp64": {"bound": "fp64 pipe (binding on GB300)",
+                 "instr_per_eval": FP64_INSTR_PER_EVAL,
+                 "achieved_tinstr_s": FP64_INSTR_PER_EVAL * r["value"] / world / 1e12,
+                 "peak_tinstr_s": r["fp64_fma_per_s"] / 1e12,
+                 "frac": FP64_INSTR_PER_EVAL * r["value"] / world / r["fp64_fma_per_s"],
+                 "peak_kind": "measured (FMA-chain probe in this run)"},
         "cpu_baseline": cpu,
         "e2e": {"value": world * Q * SUBMAPS / (r["ms_e2e"] / 1e3), "unit": "map evals/s",
                 "h2d_bytes_per_step": Q * 24, "d2h_bytes_per_step": Q * (24 + 4 + 72)},

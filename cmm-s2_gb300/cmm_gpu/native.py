@@ -23,6 +23,7 @@ _SIGS = {
     "cmm_last_error": (ctypes.c_char_p, []),
     "cmm_version": (_i, []),
     "cmm_launch_count": (ctypes.c_longlong, []),
+    "cmm_fp64_probe": (_i, [_i, _i, _p, _p]),
     "cmm_mesh_create": (_i, [_p, _i, _p, _i, _i, ctypes.POINTER(_p)]),
     "cmm_mesh_destroy": (_i, [_p]),
     "cmm_mesh_check": (_i, [_p, _i, _p, _i, _i, _p]),

@@ -21,6 +21,11 @@ int cmm_version(void) { return 1; }
 
 long long cmm_launch_count(void) { return launch_count(); }
 
+int cmm_fp64_probe(int blocks, int iters, double* sink, void* stream) {
+  if (blocks < 1 || iters < 1 || !sink) return arg_error("cmm_fp64_probe: bad argument");
+  return launch_fp64_probe(blocks, iters, sink, (cudaStream_t)stream);
+}
+
 int cmm_mesh_create(const double* verts, int nv, const int32_t* tris, int nt, int level,
                     cmm_mesh** out) {
   if (!verts || !tris || !out) return arg_error("cmm_mesh_create: null pointer");

@@ -125,6 +125,8 @@ int launch_vorticity(int kind, const double* params, int nparams, const double* 
                      double rot, const double* X, int64_t Q, int npr, const double* cos_ring,
                      double* omega, int* status, cudaStream_t s);
 
+int launch_fp64_probe(int blocks, int iters, double* sink, cudaStream_t s);
+
 // spherical-harmonic transforms (sht.cu)
 int sht_create(int L, cmm_sht** out);
 int sht_destroy(cmm_sht* p);

@@ -52,6 +52,11 @@ int cmm_version(void);
 /* Number of kernels this library has launched so far in the process
  * (library-call kernels such as cuFFT's not included). */
 long long cmm_launch_count(void);
+/* FP64 issue-rate calibration (no counterpart in the reference): `blocks`
+ * blocks of 256 threads each run 8 independent chains of `iters` FP64 FMAs
+ * (16 * iters flops per thread); sink receives blocks*256 doubles.  Time it
+ * on `stream` to obtain the FP64 peak of the GPU. */
+int cmm_fp64_probe(int blocks, int iters, double* sink, void* stream);
 
 /* ------------------------------------------------------------------ mesh */
 typedef struct cmm_mesh cmm_mesh;
