@@ -45,6 +45,8 @@ _SIGS = {
     "cmm_sht_velocity": (_i, [_p, _p, _p, _p, _p, _p]),
     "cmm_advect_project": (_i, [_p, _p, ctypes.POINTER(_p), _i, _d, _i, _d, _d, _p, _p, _p, _d, _p,
                                 _p, _p]),
+    "cmm_advect_project_noalloc": (_i, [_p, _p, ctypes.POINTER(_p), _i, _d, _i, _d, _d, _p, _p, _p,
+                                        _d, _p, _p]),
 }
 for _name, (_res, _args) in _SIGS.items():
     _f = getattr(lib, _name)

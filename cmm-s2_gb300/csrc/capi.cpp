@@ -184,6 +184,22 @@ int cmm_vorticity_eval(const cmm_mesh* velmesh, int kind, const double* params, 
                           (cudaStream_t)stream);
 }
 
+int cmm_advect_project_noalloc(const cmm_mesh* mesh, const cmm_mesh* velmesh,
+                               const double* const* vel_coeffs, int nvs, double ts0, int scheme,
+                               double t, double dt, const double* s_pts, const double* tan,
+                               const double* prev_coeffs, double eps, double* jets, void* stream) {
+  if (!mesh || mesh->view.kind != kIcosahedral)
+    return arg_error("cmm_advect_project_noalloc: map mesh expected");
+  VelPtrs vc;
+  int rc = vel_args(velmesh, vel_coeffs, nvs, &vc, "cmm_advect_project_noalloc");
+  if (rc) return rc;
+  if (!s_pts || !tan || !jets) return arg_error("cmm_advect_project_noalloc: null pointer");
+  TimeWeights tw;
+  if ((rc = stage_weights(nvs, ts0, scheme, t, dt, &tw))) return rc;
+  return advect_project_noalloc(mesh->view, velmesh->view, vc, nvs, tw, scheme, dt, s_pts, tan,
+                                prev_coeffs, eps, jets, (cudaStream_t)stream);
+}
+
 int cmm_sht_create(int L, cmm_sht** out) {
   if (!out) return arg_error("cmm_sht_create: null pointer");
   *out = nullptr;

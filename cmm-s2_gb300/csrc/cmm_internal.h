@@ -121,6 +121,14 @@ int launch_project_jets(const MeshView& mesh, const double* prev_coeffs, const d
                         const double* sn, const double* tan, double eps, double* jets,
                         cudaStream_t s);
 
+// Allocation-free variant of the map update (velocity.cu): foot-point
+// scratch in a fixed device array sized for kNoAllocMaxVerts vertices.
+constexpr int kNoAllocMaxVerts = 10242;
+int advect_project_noalloc(const MeshView& mesh, const MeshView& vm, VelPtrs vc, int nvs,
+                           const TimeWeights& tw, int scheme, double dt, const double* s_pts,
+                           const double* tan, const double* prev_coeffs, double eps,
+                           double* jets, cudaStream_t s);
+
 int launch_vorticity(int kind, const double* params, int nparams, const double* sh, int lmax,
                      double rot, const double* X, int64_t Q, int npr, const double* cos_ring,
                      double* omega, int* status, cudaStream_t s);

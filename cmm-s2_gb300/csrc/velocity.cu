@@ -12,6 +12,9 @@
 // contains it.
 #include <cuda_runtime.h>
 
+#include <mutex>
+#include <string>
+
 #include "cmm_internal.h"
 #include "device_common.cuh"
 #include "geom.h"
@@ -344,6 +347,58 @@ int launch_advect_points(const MeshView& mesh, const MeshView& vm, VelPtrs vc, i
   advect_points_kernel<<<grid_for(n, kBlock), kBlock, 0, s>>>(mesh, vm, vc, nvs, tw, scheme, dt,
                                                                s_pts, work);
   return check_launch("advect_points_kernel");
+}
+
+// ---------------------------------------------- allocation-free map update
+// Foot-point scratch of advect_project_noalloc: a fixed array in device
+// memory that exists on every GPU this library is loaded on, for meshes of
+// up to kNoAllocMaxVerts vertices (icosahedral level 5).  Host code must not
+// use the name g_advect_scratch as a pointer; the device address of each
+// GPU's copy is looked up once per device with cudaGetSymbolAddress.
+static __device__ __align__(256) double g_advect_scratch[15 * kNoAllocMaxVerts];
+
+namespace {
+constexpr int kMaxDevices = 64;
+double* g_scratch_addr[kMaxDevices] = {};
+std::mutex g_scratch_mu;
+}  // namespace
+
+static int noalloc_scratch(double** out) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  if (dev < 0 || dev >= kMaxDevices) {
+    set_last_error("advect_project_noalloc: device ordinal out of range");
+    return CMM_ERR_UNSUPPORTED;
+  }
+  std::lock_guard<std::mutex> lock(g_scratch_mu);
+  if (!g_scratch_addr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_advect_scratch);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_advect_scratch)");
+    g_scratch_addr[dev] = (double*)p;
+  }
+  *out = g_scratch_addr[dev];
+  return CMM_OK;
+}
+
+int advect_project_noalloc(const MeshView& mesh, const MeshView& vm, VelPtrs vc, int nvs,
+                           const TimeWeights& tw, int scheme, double dt, const double* s_pts,
+                           const double* tan, const double* prev_coeffs, double eps,
+                           double* jets, cudaStream_t s) {
+  if (mesh.nv > kNoAllocMaxVerts) {
+    set_last_error("cmm_advect_project_noalloc: mesh has more than " +
+                   std::to_string(kNoAllocMaxVerts) +
+                   " vertices (icosahedral level 5); use cmm_advect_project with a workspace");
+    return CMM_ERR_ARG;
+  }
+  double* work = nullptr;
+  int rc = noalloc_scratch(&work);
+  if (rc) return rc;
+  // every scratch entry is written by advect_points_kernel before
+  // project_jets_kernel reads it, so nothing needs clearing
+  if ((rc = launch_advect_points(mesh, vm, vc, nvs, tw, scheme, dt, s_pts, work, s))) return rc;
+  return launch_project_jets(mesh, prev_coeffs, work, work + 3 * (int64_t)mesh.nv, tan, eps, jets, s);
 }
 
 int launch_project_jets(const MeshView& mesh, const double* prev_coeffs, const double* yn,

@@ -169,6 +169,29 @@ int cmm_advect_project(const cmm_mesh* mesh, const cmm_mesh* velmesh,
                        const double* prev_coeffs, double eps, double* jets, double* work,
                        void* stream);
 
+/* The same map update as cmm_advect_project, for callers that cannot
+ * allocate device memory -- for instance an application that has handed
+ * all of the GPU's memory to its own pool, or a solver loop that must not
+ * call cudaMalloc/cudaFree, which can synchronise the whole device.  It
+ * allocates nothing: its foot-point scratch (15 doubles per vertex) is a
+ * fixed array compiled into the library, present on every GPU that loads
+ * it until the process exits.  No counterpart in the reference.
+ *  - Meshes of at most 10242 vertices (icosahedral level 5); larger ones
+ *    are rejected with CMM_ERR_ARG (use cmm_advect_project with a
+ *    workspace).
+ *  - The first call on each device looks up that device's copy of the
+ *    scratch array (cudaGetSymbolAddress) with the device current; make
+ *    that first call before any stream capture.
+ *  - All calls on a device share the one array and it keeps the last
+ *    call's contents (every entry is rewritten before it is read, so
+ *    nothing needs clearing): calls that overlap on the GPU, on different
+ *    streams or from different threads, race and must be serialised by
+ *    the caller. */
+int cmm_advect_project_noalloc(const cmm_mesh* mesh, const cmm_mesh* velmesh,
+                               const double* const* vel_coeffs, int nvs, double ts0, int scheme,
+                               double t, double dt, const double* s_pts, const double* tan,
+                               const double* prev_coeffs, double eps, double* jets, void* stream);
+
 /* ------------------------------------------------------------ vorticity */
 /* Initial vorticity fields: the barotropic fields of
  * cmm_s2/core/dynamical_fields.py:181-214 and benchmark fields. */
