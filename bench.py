@@ -257,6 +257,13 @@ def bench_gpu(args, rank, world):
             res["bve"] = bench_bve(args, dev)
         except Exception as exc:  # reported, the headline stands on its own
             res["bve"] = {"error": f"{type(exc).__name__}: {exc}"}
+        if not args.no_bve3:
+            del q, mesh, cs
+            torch.cuda.empty_cache()
+            try:
+                res["bve_l7_L1024"] = bench_bve3(args, dev)
+            except Exception as exc:
+                res["bve_l7_L1024"] = {"error": f"{type(exc).__name__}: {exc}"}
     return res
 
 
@@ -287,6 +294,39 @@ def bench_bve(args, dev):
                         "random SH l<=16 initial vorticity; steps 5..64 after the bootstrap"}
 
 
+def bench_bve3(args, dev, steps=8):
+    """Config: level-7 mesh, L=1024 MWSS (1025 x 2048), 1000-step run with
+    remap every 10 (first steps timed); initial vorticity 4 zonal Gaussian
+    jets (width 0.1 rad at latitudes +-0.5, +-1.1 rad, amplitude 10) plus a
+    seeded l <= 64 perturbation with a k^-3 energy spectrum at 1 % of the
+    jets' amplitude (rms 0.1), evaluated through its scalar spline."""
+    import torch
+    from cmm_gpu.meshgen import icosahedral_mesh
+    from cmm_gpu.workloads import spectral_perturbation
+    from cmm_gpu.spherical_simulations import BVESolver, Vorticity
+    pert = spectral_perturbation(64, seed=3, slope=-2.0, rms=0.1)
+    vort = Vorticity("gaussian_zonal_jets", (10.0, 0.1, 4, 0.5, -0.5, 1.1, -1.1), spline_sh=pert)
+    verts, tris = icosahedral_mesh(7)
+    t0 = time.perf_counter()
+    s = BVESolver(verts, tris, 7, 1024, 1000, 1.0, vort, n_maps=10)
+    s.bootstrap()
+    s.step()
+    torch.cuda.synchronize()
+    setup = time.perf_counter() - t0
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        s.step()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    ok = s.mesh.status() == 0 and s.vm.status() == 0
+    return {"steps_per_s": 1e3 / ms, "ms_per_step": ms, "steps_timed": steps, "form": "fp64",
+            "setup_s": setup, "status_ok": ok,
+            "workload": "BVE level 7 (163842 vertices), L=1024 MWSS 1025x2048, remap every 10, "
+                        "4 Gaussian zonal jets + 1% k^-3 l<=64 perturbation (spline); steps 4..11"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -296,6 +336,7 @@ def main():
     ap.add_argument("--cpu-queries", type=int, default=1 << 15)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-bve", action="store_true")
+    ap.add_argument("--no-bve3", action="store_true", help="skip the level-7 / L=1024 BVE run")
     ap.add_argument("--logq", type=int, default=24, help="log2 queries per GPU (profiling cases)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -365,8 +406,9 @@ def main():
                 "h2d_bytes_per_step": Q * 24, "d2h_bytes_per_step": Q * (24 + 4 + 72)},
         "clocks": r["clocks"], "gpu_launches": r["launches"],
     }
-    if "bve" in r:
-        line["bve"] = r["bve"]
+    for key in ("bve", "bve_l7_L1024"):
+        if key in r:
+            line[key] = r[key]
     print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()

@@ -37,7 +37,8 @@ _SIGS = {
     "cmm_velocity_eval": (_i, [_p, ctypes.POINTER(_p), _i, _d, _d, _d, _p, _i64, _p, _p]),
     "cmm_integrate": (_i, [_p, ctypes.POINTER(_p), _i, _d, _i, _d, _d, _p, _i64, _p, _p]),
     "cmm_advect_workspace": (_i64, [_p]),
-    "cmm_vorticity_eval": (_i, [_p, _i, _p, _i, _p, _i, _d, _p, _p, _p]),
+    "cmm_vorticity_eval": (_i, [_p, _i, _p, _i, _p, _i, _p, _d, _p, _p, _p]),
+    "cmm_sht_scalar_jets": (_i, [_p, _p, _p, _p, _p]),
     "cmm_sht_create": (_i, [_i, ctypes.POINTER(_p)]),
     "cmm_sht_destroy": (_i, [_p]),
     "cmm_sht_forward": (_i, [_p, _p, _p, _p]),
@@ -209,7 +210,7 @@ class VelMesh(Mesh):
         self.h = h
         self.stride = lib.cmm_coeff_stride(3)
 
-    def vorticity(self, kind, params, X, rot_rate, sh=None, omega=None):
+    def vorticity(self, kind, params, X, rot_rate, sh=None, omega=None, spline=None):
         """omega (L+1, 2L) at the back-traced sample points X (Q,3)."""
         X = _dev(X)
         params = np.ascontiguousarray(params if params is not None else [], dtype=np.float64)
@@ -217,8 +218,8 @@ class VelMesh(Mesh):
             omega = torch.empty((self.L + 1, 2 * self.L), dtype=torch.float64, device=X.device)
         lmax = -1 if sh is None else sh.shape[0] - 1
         check(lib.cmm_vorticity_eval(self.h, kind, params.ctypes.data if len(params) else None,
-                                     len(params), _ptr(sh), lmax, rot_rate, _ptr(X), _ptr(omega),
-                                     _stream(X.device)), "cmm_vorticity_eval")
+                                     len(params), _ptr(sh), lmax, _ptr(spline), rot_rate, _ptr(X),
+                                     _ptr(omega), _stream(X.device)), "cmm_vorticity_eval")
         return omega
 
     def velocity(self, vel_coeffs, ts0, t, dt, x):
@@ -271,6 +272,15 @@ class Sht:
         check(lib.cmm_sht_inverse(self.h, _ptr(alm), nf, _ptr(out), _stream(alm.device)),
               "cmm_sht_inverse")
         return out[0] if alm.dim() == 2 else out
+
+    def scalar_jets(self, velmesh, alm, jets=None):
+        """Scalar jets (4, Nv_u) of the field with coefficients alm [m,l]."""
+        alm = _dev(alm, torch.complex128)
+        if jets is None:
+            jets = torch.empty((4, velmesh.nv), dtype=torch.float64, device=alm.device)
+        check(lib.cmm_sht_scalar_jets(self.h, velmesh.h, _ptr(alm), _ptr(jets), _stream(alm.device)),
+              "cmm_sht_scalar_jets")
+        return jets
 
     def velocity(self, velmesh, omega, jets=None, psi=None):
         omega = _dev(omega)

@@ -29,13 +29,18 @@ _FIELDS = {
 
 class Vorticity:
     """Initial vorticity evaluated on the device: a built-in field of
-    cmm_s2/core/dynamical_fields.py (by name) and/or a real spherical-
-    harmonic series (coefficients (lmax+1, 2lmax+1), column l+m)."""
+    cmm_s2/core/dynamical_fields.py (by name), plus optionally a real
+    spherical-harmonic series (coefficients (lmax+1, 2lmax+1), column l+m)
+    evaluated either pointwise (`sh`) or through its scalar Powell-Sabin
+    spline on the velocity mesh (`spline_sh`, the reference's
+    project_onto_S12 route, cmm_s2/core/spherical_harmonic_tools.py:108-142;
+    ~150 operations per point instead of O(lmax^2))."""
 
-    def __init__(self, field=None, params=(), sh=None):
+    def __init__(self, field=None, params=(), sh=None, spline_sh=None):
         self.kind = _FIELDS[field] if field is not None else native.VORT_NONE
         self.params = np.asarray(params, dtype=np.float64)
         self.sh = None if sh is None else np.ascontiguousarray(sh, dtype=np.float64)
+        self.spline_sh = None if spline_sh is None else np.ascontiguousarray(spline_sh, dtype=np.float64)
 
     @classmethod
     def from_reference(cls, f):
@@ -82,6 +87,11 @@ class BVESolver:
         self.work = torch.empty(native.lib.cmm_advect_workspace(self.mesh.h), **f64)
         self.X = torch.empty_like(self.sample_pts)
         self.omega = torch.empty((L + 1, 2 * L), **f64)
+        self.spline = None
+        if self.vort.spline_sh is not None:
+            from .workloads import real_to_complex_sh
+            alm = torch.from_numpy(real_to_complex_sh(self.vort.spline_sh, L)).to(dev)
+            self.spline = self.vm.assemble(self.sht.scalar_jets(self.vm, alm))
         self.Nc = 0
         self.ts0 = float(self.tspan[0])
         self.nvs = 1
@@ -95,7 +105,8 @@ class BVESolver:
     def _project(self, X, n, rot=None):
         """omega at X -> velocity slot n (inv_Laplacian + project_stream)."""
         rot = self.rot if rot is None else rot
-        self.vm.vorticity(self.vort.kind, self.vort.params, X, rot, sh=self.sh, omega=self.omega)
+        self.vm.vorticity(self.vort.kind, self.vort.params, X, rot, sh=self.sh, omega=self.omega,
+                          spline=self.spline)
         if self.stepping:
             c = self.vel_coeffs
             self.vel_coeffs = [c[1], c[2], c[0]]

@@ -61,6 +61,33 @@ def submap_stack(s_pts, tan, n_submaps, seed, amp=1e-2):
     return np.stack(out)
 
 
+def real_to_complex_sh(a, L):
+    """Real orthonormal coefficients a (lmax+1, 2lmax+1) (column l+m; m>0 ->
+    sqrt2 Pbar cos(m phi), m<0 -> sqrt2 Pbar sin(|m| phi)) -> complex
+    coefficients of the transforms, m-major half layout (L, L) [m, l]:
+    c_l0 = a_l0, c_lm = (a_{l,m} - i a_{l,-m}) / sqrt2."""
+    lmax = a.shape[0] - 1
+    out = np.zeros((L, L), dtype=np.complex128)
+    for l in range(min(lmax + 1, L)):
+        out[0, l] = a[l, l]
+        for m in range(1, l + 1):
+            out[m, l] = (a[l, l + m] - 1j * a[l, l - m]) / np.sqrt(2)
+    return out
+
+
+def spectral_perturbation(lmax, seed, slope=-2.0, rms=None):
+    """Real SH coefficients a_lm ~ N(0,1) l^slope for 1 <= l <= lmax
+    (slope -2 gives an energy spectrum sum_m a_lm^2 ~ l^-3), scaled to the
+    given root-mean-square over the sphere when rms is set."""
+    rng = np.random.default_rng(seed)
+    a = np.zeros((lmax + 1, 2 * lmax + 1))
+    for l in range(1, lmax + 1):
+        a[l, :2 * l + 1] = rng.standard_normal(2 * l + 1) * float(l) ** slope
+    if rms is not None:
+        a *= rms / np.sqrt(np.sum(a ** 2) / (4 * np.pi))
+    return a
+
+
 def random_sh_vorticity(L_max, seed, slope=-1.5):
     """omega0(phi, theta) = sum_{l=1..L_max} sum_m a_lm Y^real_lm, a_lm ~ N(0,1) l^slope.
 

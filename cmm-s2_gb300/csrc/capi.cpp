@@ -171,17 +171,24 @@ int cmm_integrate(const cmm_mesh* velmesh, const double* const* vel_coeffs, int 
 }
 
 int cmm_vorticity_eval(const cmm_mesh* velmesh, int kind, const double* params, int nparams,
-                       const double* sh, int lmax, double rot_rate, const double* X,
-                       double* omega, void* stream) {
+                       const double* sh, int lmax, const double* spline, double rot_rate,
+                       const double* X, double* omega, void* stream) {
   if (!velmesh || velmesh->view.kind != kLatLon) return arg_error("cmm_vorticity_eval: velocity mesh expected");
   if (!X || !omega || (nparams > 0 && !params) || nparams > 12 || kind < 0 || kind > 6 ||
       (sh && lmax < 0))
     return arg_error("cmm_vorticity_eval: bad argument");
   const int L = velmesh->view.L;
   const int64_t Q = (int64_t)(L + 1) * 2 * L;
-  return launch_vorticity(kind, params, nparams, sh, lmax, rot_rate, X, Q, 2 * L,
-                          (const double*)velmesh->cos_theta.p, omega, velmesh->view.status,
-                          (cudaStream_t)stream);
+  return launch_vorticity(kind, params, nparams, sh, lmax, velmesh->view, spline, rot_rate, X, Q,
+                          2 * L, (const double*)velmesh->cos_theta.p, omega, (cudaStream_t)stream);
+}
+
+int cmm_sht_scalar_jets(cmm_sht* plan, const cmm_mesh* velmesh, const double* alm, double* jets,
+                        void* stream) {
+  if (!plan || !velmesh || !alm || !jets) return arg_error("cmm_sht_scalar_jets: null pointer");
+  if (velmesh->view.kind != kLatLon || velmesh->view.L != sht_L(plan))
+    return arg_error("cmm_sht_scalar_jets: velocity mesh of the plan's band-limit expected");
+  return sht_scalar_jets(plan, velmesh, (const double2*)alm, jets, (cudaStream_t)stream);
 }
 
 int cmm_advect_project_noalloc(const cmm_mesh* mesh, const cmm_mesh* velmesh,

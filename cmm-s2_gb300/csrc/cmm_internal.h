@@ -130,8 +130,8 @@ int advect_project_noalloc(const MeshView& mesh, const MeshView& vm, VelPtrs vc,
                            double* jets, cudaStream_t s);
 
 int launch_vorticity(int kind, const double* params, int nparams, const double* sh, int lmax,
-                     double rot, const double* X, int64_t Q, int npr, const double* cos_ring,
-                     double* omega, int* status, cudaStream_t s);
+                     const MeshView& vm, const double* spline, double rot, const double* X,
+                     int64_t Q, int npr, const double* cos_ring, double* omega, cudaStream_t s);
 
 int launch_fp64_probe(int blocks, int iters, double* sink, cudaStream_t s);
 
@@ -143,4 +143,5 @@ int sht_forward(cmm_sht* p, const double* samples, double2* out, cudaStream_t s)
 int sht_inverse(cmm_sht* p, const double2* alm, int nf, double* samples, cudaStream_t s);
 int sht_velocity(cmm_sht* p, const cmm_mesh* vm, const double* omega, double2* psi_out,
                  double* jets, cudaStream_t s);
+int sht_scalar_jets(cmm_sht* p, const cmm_mesh* vm, const double2* alm, double* jets, cudaStream_t s);
 }  // namespace cmm

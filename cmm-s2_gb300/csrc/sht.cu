@@ -237,6 +237,39 @@ __global__ void ladder2_kernel(double2* __restrict__ fields, int L) {
   }
 }
 
+// fields 0..3 = a, iLx a, iLy a, iLz a (project_onto_S12,
+// spherical_harmonic_tools.py:121-123).
+__global__ void scalar_fields_kernel(const double2* __restrict__ a, int L, double2* __restrict__ fields) {
+  const int l = blockIdx.x * blockDim.x + threadIdx.x, m = blockIdx.y;
+  if (l >= L) return;
+  const int64_t fs = (int64_t)L * L, i = (int64_t)m * L + l;
+  double2 o[3] = {make_double2(0.0, 0.0), make_double2(0.0, 0.0), make_double2(0.0, 0.0)};
+  if (l >= m) ladder(a, L, l, m, o);
+  fields[i] = (l >= m) ? a[i] : make_double2(0.0, 0.0);
+  for (int k = 0; k < 3; ++k) fields[(1 + k) * fs + i] = o[k];
+}
+
+// Scalar jets (4, Nv_u): value, then the tangent gradient
+// g x X - ((g x X).X/|X|) X with g = (iLx, iLy, iLz) f (:125-138).
+__global__ void scalar_jets_kernel(const double* __restrict__ fld, int L, const double* __restrict__ grid,
+                                   double* __restrict__ jets) {
+  const int N = 2 * L;
+  const int64_t nv = 2 + (int64_t)(L - 1) * N;
+  const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  const int64_t node = v == 0 ? 0 : (v == nv - 1 ? (int64_t)L * N : N + (v - 1));
+  const int64_t fs = (int64_t)(L + 1) * N;
+  const double X0 = grid[4 * node], X1 = grid[4 * node + 1], X2 = grid[4 * node + 2];
+  const double nX = sqrt(X0 * X0 + X1 * X1 + X2 * X2);
+  const double g0 = fld[fs + node], g1 = fld[2 * fs + node], g2 = fld[3 * fs + node];
+  const double c0 = g1 * X2 - g2 * X1, c1 = g2 * X0 - g0 * X2, c2 = g0 * X1 - g1 * X0;
+  const double sc = (c0 * X0 + c1 * X1 + c2 * X2) / nX;
+  jets[v] = fld[node];
+  jets[nv + v] = c0 - sc * X0;
+  jets[2 * nv + v] = c1 - sc * X1;
+  jets[3 * nv + v] = c2 - sc * X2;
+}
+
 // ------------------------------------------------------------- inverse
 // Legendre synthesis of nf fields: block (m, ring-pair tile); each thread
 // one ring pair (t, L-t).  Out: spectra S[f][t][m] (nf, L+1, L+1), m = L
@@ -513,7 +546,8 @@ int sht_inverse(cmm_sht* p, const double2* alm, int nf, double* samples, cudaStr
   int rc = set_streams(p, s);
   if (rc) return rc;
   double2* S = (double2*)p->synth.p;
-  cudaError_t e = cudaMemsetAsync(S, 0, (size_t)nf * (L + 1) * (L + 1) * sizeof(double2), s);
+  // all kFields spectra: the batched Z2D below transforms every row
+  cudaError_t e = cudaMemsetAsync(S, 0, (size_t)kFields * (L + 1) * (L + 1) * sizeof(double2), s);
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
   const int npair = L / 2 + 1;
   dim3 g(L, (npair + kSynthBlock - 1) / kSynthBlock);
@@ -525,8 +559,12 @@ int sht_inverse(cmm_sht* p, const double2* alm, int nf, double* samples, cudaStr
     synthesis_kernel<1><<<g, kSynthBlock, 0, s>>>(alm, L, (const double*)p->ct_rings.p,
                                                   (const double*)p->pmm_rings.p, (const double*)p->ra.p,
                                                   (const double*)p->rb.p, S);
+  else if (nf == 4)
+    synthesis_kernel<4><<<g, kSynthBlock, 0, s>>>(alm, L, (const double*)p->ct_rings.p,
+                                                  (const double*)p->pmm_rings.p, (const double*)p->ra.p,
+                                                  (const double*)p->rb.p, S);
   else {
-    set_last_error("sht_inverse: nf must be 1 or 12");
+    set_last_error("sht_inverse: nf must be 1, 4 or 12");
     return CMM_ERR_ARG;
   }
   if ((rc = check_launch("synthesis_kernel"))) return rc;
@@ -566,6 +604,20 @@ int sht_velocity(cmm_sht* p, const cmm_mesh* vm, const double* omega, double2* p
   const int64_t nv = 2 + (int64_t)(L - 1) * 2 * L;
   jets_kernel<<<(int)((nv + 127) / 128), 128, 0, s>>>((const double*)p->samples.p, L, vm->view.grid, jets);
   return check_launch("jets_kernel");
+}
+
+int sht_scalar_jets(cmm_sht* p, const cmm_mesh* vm, const double2* alm, double* jets, cudaStream_t s) {
+  const int L = p->L;
+  double2* F = (double2*)p->fields.p;
+  dim3 b(128), g((L + 127) / 128, L);
+  scalar_fields_kernel<<<g, b, 0, s>>>(alm, L, F);
+  int rc = check_launch("scalar_fields_kernel");
+  if (rc) return rc;
+  if ((rc = sht_inverse(p, F, 4, nullptr, s))) return rc;
+  const int64_t nv = 2 + (int64_t)(L - 1) * 2 * L;
+  scalar_jets_kernel<<<(int)((nv + 127) / 128), 128, 0, s>>>((const double*)p->samples.p, L,
+                                                             vm->view.grid, jets);
+  return check_launch("scalar_jets_kernel");
 }
 
 int sht_destroy(cmm_sht* p) {

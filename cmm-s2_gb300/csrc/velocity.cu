@@ -27,55 +27,6 @@ namespace {
 
 constexpr int kBlock = 128;
 
-__device__ __forceinline__ int py_mod(long long a, int n) {
-  long long r = a % n;
-  return (int)(r < 0 ? r + n : r);
-}
-
-__device__ __forceinline__ D3 gridpt(const MeshView& m, int ring, int p) {
-  const double* g = m.grid + 4 * ((int64_t)ring * 2 * m.L + p);
-  return D3{g[0], g[1], g[2]};
-}
-
-// Triangle (row of the lat-lon table) containing q.
-__device__ __forceinline__ int latlon_locate(const MeshView& m, double x, double y, double z) {
-  const int N = 2 * m.L, M = m.L + 1;
-  double phi = np_remainder(atan2(y, x) + kTwoPi, kTwoPi);
-  const double rho = sqrt(__dadd_rn(__dmul_rn(y, y), __dmul_rn(x, x)));
-  const double theta = atan2(rho, z);
-  const double phiq = np_remainder(phi, kTwoPi);
-  const int phi_l = py_mod((long long)np_floor_divide(phiq - m.phi[0], m.dphi), N);
-  int theta_l = (int)np_floor_divide(theta - m.theta[0], m.dthe);
-  if (theta_l == M - 1) theta_l = M - 2;
-  if (theta_l < 0) theta_l = 0;
-  if (theta_l > M - 2) theta_l = M - 2;
-  const double theta_c = (theta - m.theta[theta_l]) / m.dthe;
-  const int phi_p1 = (phi_l + 1) % N;
-  const D3 q = D3{x, y, z};
-  const bool row_lo = theta_c <= 0.03 && theta_l != 0;
-  const bool row_hi = !row_lo && theta_c > 0.85 && theta_l != M - 2;
-  if (row_lo || row_hi) {
-    // the reference tests the point re-synthesised from its angles,
-    // sphere2cart(phi, theta) (mesh_functions.py:240, 249)
-    double sp, cp, st, cth;
-    sincos(phiq, &sp, &cp);
-    sincos(theta, &st, &cth);
-    const D3 q0 = D3{st * cp, st * sp, cth};
-    if (row_lo) {
-      const D3 n = cross(gridpt(m, theta_l, phi_l), gridpt(m, theta_l, phi_p1));
-      if (dot(n, q0) > 0.0) theta_l -= 1;
-    } else {
-      const D3 n = cross(gridpt(m, theta_l + 1, phi_l), gridpt(m, theta_l + 1, phi_p1));
-      if (-dot(n, q0) > 0.0) theta_l += 1;
-    }
-  }
-  if (theta_l == 0) return phi_l;
-  if (theta_l == M - 2) return 2 * N * (M - 2) - N + phi_l;
-  const D3 n = cross(gridpt(m, theta_l, phi_l), gridpt(m, theta_l + 1, phi_p1));
-  const int s = (-dot(n, q) > 0.0) ? 1 : 0;
-  return N + 2 * (N * (theta_l - 1) + phi_l) + s;
-}
-
 // Velocity at q: the Powell-Sabin patch of each time level, combined with
 // the stage's Lagrange weights w (spline_interp_velocity.__call__,
 // cmm_s2/core/spherical_spline.py:570-615).

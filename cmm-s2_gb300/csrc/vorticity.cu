@@ -97,18 +97,20 @@ __device__ double sh_value(const double* __restrict__ c, int lmax, double phi, d
   return out;
 }
 
-__global__ void vorticity_kernel(VortParams vp, const double* __restrict__ sh, int lmax, double rot,
+__global__ void vorticity_kernel(VortParams vp, const double* __restrict__ sh, int lmax,
+                                 MeshView vm, const double* __restrict__ spline, double rot,
                                  const double* __restrict__ X, int64_t Q, int npr,
-                                 const double* __restrict__ cos_ring, double* __restrict__ omega,
-                                 int* __restrict__ status) {
+                                 const double* __restrict__ cos_ring, double* __restrict__ omega) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Q;
        i += (int64_t)gridDim.x * blockDim.x) {
+    const double x = X[3 * i], y = X[3 * i + 1], z = X[3 * i + 2];
     double phi, theta;
-    cart2sphere(X[3 * i], X[3 * i + 1], X[3 * i + 2], &phi, &theta);
+    cart2sphere(x, y, z, &phi, &theta);
     double w = omega0(vp, phi, theta);
     if (sh) w += sh_value(sh, lmax, phi, theta);
+    if (spline) w += latlon_scalar(vm, spline, x, y, z);
     const double r = w + 2 * rot * cos(theta) - 2 * rot * cos_ring[i / npr];
-    if (!isfinite(r)) atomicOr(status, CMM_FLAG_NONFINITE);
+    if (!isfinite(r)) atomicOr(vm.status, CMM_FLAG_NONFINITE);
     omega[i] = r;
   }
 }
@@ -116,13 +118,13 @@ __global__ void vorticity_kernel(VortParams vp, const double* __restrict__ sh, i
 }  // namespace
 
 int launch_vorticity(int kind, const double* params, int nparams, const double* sh, int lmax,
-                     double rot, const double* X, int64_t Q, int npr, const double* cos_ring,
-                     double* omega, int* status, cudaStream_t s) {
+                     const MeshView& vm, const double* spline, double rot, const double* X,
+                     int64_t Q, int npr, const double* cos_ring, double* omega, cudaStream_t s) {
   VortParams vp{};
   vp.kind = kind;
   for (int k = 0; k < nparams && k < 12; ++k) vp.p[k] = params[k];
-  vorticity_kernel<<<grid_for(Q, 128), 128, 0, s>>>(vp, sh, lmax, rot, X, Q, npr, cos_ring, omega,
-                                                    status);
+  vorticity_kernel<<<grid_for(Q, 128), 128, 0, s>>>(vp, sh, lmax, vm, spline, rot, X, Q, npr,
+                                                    cos_ring, omega);
   note_launch();
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? CMM_OK : cuda_fail(e, "vorticity_kernel");

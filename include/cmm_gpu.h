@@ -209,10 +209,14 @@ int cmm_advect_project_noalloc(const cmm_mesh* mesh, const cmm_mesh* velmesh,
  * 2 rot cos(theta_ring) (cmm_s2/core/spherical_simulations.py:269-272),
  * omega0 = field `kind` plus, when sh is not NULL, the real orthonormal
  * spherical-harmonic series sh (lmax+1, 2lmax+1) (column l+m; m>0 cos,
- * m<0 sin, both with sqrt2). */
+ * m<0 sin, both with sqrt2), plus, when spline is not NULL, the scalar
+ * Powell-Sabin spline with ncomp=1 coefficients `spline` on `velmesh`
+ * (the spherical_spline a caller builds with cmm_sht_scalar_jets +
+ * cmm_assemble, as project_onto_S12 does,
+ * cmm_s2/core/spherical_harmonic_tools.py:108-142). */
 int cmm_vorticity_eval(const cmm_mesh* velmesh, int kind, const double* params, int nparams,
-                       const double* sh, int lmax, double rot_rate, const double* X,
-                       double* omega, void* stream);
+                       const double* sh, int lmax, const double* spline, double rot_rate,
+                       const double* X, double* omega, void* stream);
 
 /* ------------------------------------------- spherical-harmonic transforms */
 /* MWSS transforms at band-limit L (samples on L+1 rings x 2L longitudes,
@@ -243,6 +247,14 @@ int cmm_sht_inverse(cmm_sht* plan, const double* alm, int nf, double* samples, v
  * omega NULL, psi is the input instead (project_stream alone). */
 int cmm_sht_velocity(cmm_sht* plan, const cmm_mesh* velmesh, const double* omega, double* psi,
                      double* vel_jets, void* stream);
+
+/* Scalar jets (4, Nv_u) on the velocity mesh's vertices of the real field
+ * with coefficients alm (L,L) complex: value, then the tangent gradient
+ * from the angular-momentum operators (project_onto_S12,
+ * cmm_s2/core/spherical_harmonic_tools.py:108-142).  With cmm_assemble
+ * (ncomp = 1) this builds the scalar spherical_spline of the field. */
+int cmm_sht_scalar_jets(cmm_sht* plan, const cmm_mesh* velmesh, const double* alm, double* jets,
+                        void* stream);
 
 #ifdef __cplusplus
 }

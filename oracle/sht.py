@@ -201,6 +201,34 @@ def velocity_jets(psi_shifted, sht, grid_points, lp, lm, lz):
     return vals
 
 
+def scalar_jets(alm_half, sht, grid_points, lp, lm, lz):
+    """project_onto_S12 (cmm_s2/core/spherical_harmonic_tools.py:108-142):
+    jets (4,Nv_u) of the field with coefficients alm_half (L,L) [l,m>=0]:
+    value from the inverse transform, gradient from the angular-momentum
+    operators, g x X tangent-projected, poles from sample 0."""
+    L = sht.L
+    nv = 2 + (L - 1) * 2 * L
+    vals = np.zeros((4, nv))
+    X = grid_points
+    c = shifted_from_vec(full_from_half(alm_half), L)
+
+    def synth(ci):
+        return sht.inverse(half_from_full(vec_from_shifted(ci, L), L))
+
+    def put(dst, field):
+        dst[1:-1] = field[1:-1].reshape((L - 1) * 2 * L)
+        dst[-1] = field[-1, 0]
+        dst[0] = field[0, 0]
+
+    G = [synth(gk) for gk in angular_momentum(c, lp, lm, lz)]
+    cr = [G[1] * X[2] - G[2] * X[1], G[2] * X[0] - G[0] * X[2], G[0] * X[1] - G[1] * X[0]]
+    sc = (cr[0] * X[0] + cr[1] * X[1] + cr[2] * X[2]) / np.sqrt(X[0] ** 2 + X[1] ** 2 + X[2] ** 2)
+    for k in range(3):
+        put(vals[1 + k], cr[k] - sc * X[k])
+    put(vals[0], synth(c))
+    return vals
+
+
 def inv_laplacian(samples, sht, dinv):
     """inv_Laplacian (cmm_s2/core/spherical_harmonic_tools.py:14-19): shifted layout."""
     L = sht.L

@@ -54,6 +54,33 @@ def assemble(verts, tris, vals, geom=None):
     return out
 
 
+def assemble_scalar(verts, tris, vals, geom=None):
+    """spherical_spline.assemble_coefficients (cmm_s2/core/spherical_spline.py:
+    115-152): vals (4,Nv) = value, gradient -> coeffs (19,Nt)."""
+    H, G, E = geom if geom is not None else ps_split(verts, tris)
+    tv = vals[:, tris]                 # (4,Nt,3)
+    out = np.zeros((19, len(tris)))
+    out[0], out[1], out[2] = tv[0, :, 0], tv[0, :, 1], tv[0, :, 2]
+
+    def grad_ord(h, g, gi, corner):
+        dot = h[:, 0] * tv[1, :, corner] + h[:, 1] * tv[2, :, corner] + h[:, 2] * tv[3, :, corner]
+        return (1 / g[:, gi]) * (dot / 2 - g[:, 0] * tv[0, :, corner])
+
+    spec = [(3, 0, 1, 0), (4, 6, 1, 0), (5, 4, 2, 0), (6, 2, 1, 1), (7, 7, 1, 1), (8, 1, 2, 1),
+            (9, 5, 1, 2), (10, 8, 1, 2), (11, 3, 2, 2)]
+    for o, k, gi, corner in spec:
+        out[o] = grad_ord(H[k], G[k], gi, corner)
+    e1, e2, e3, mid = E[0], E[1], E[2], G[9]
+    out[12] = e1[:, 0] * out[3] + e1[:, 1] * out[8]
+    out[13] = e2[:, 1] * out[6] + e2[:, 2] * out[11]
+    out[14] = e3[:, 2] * out[9] + e3[:, 0] * out[5]
+    out[15] = e1[:, 0] * out[4] + e1[:, 1] * out[7]
+    out[16] = e2[:, 1] * out[7] + e2[:, 2] * out[10]
+    out[17] = e3[:, 0] * out[4] + e3[:, 2] * out[10]
+    out[18] = mid[:, 0] * out[4] + mid[:, 1] * out[7] + mid[:, 2] * out[10]
+    return out
+
+
 def split_corners(vs, bcc, tie_fix=False):
     """Sub-triangle corners (new_vpoints, cmm_s2/core/spherical_spline.py:668-697).
 

@@ -195,6 +195,21 @@ def main():
     save("sht_ops_L8.npz", flm=flm, coeff_array=ca, lm_array=rsht.lm_array(ca, L), ang_x=am[0],
          ang_y=am[1], ang_z=am[2])
 
+    # ---- scalar spline of a spherical-harmonic field (project_onto_S12) -----
+    L = 8
+    mu = rmesh.structure_spherical_triangulation(L)
+    alms = np.zeros((L, 2 * L + 1), dtype=complex)
+    rng = np.random.default_rng(11)
+    half = np.tril(rng.standard_normal((L, L)) + 1j * rng.standard_normal((L, L)))
+    half[:, 0] = half[:, 0].real
+    alms[:] = osht.shifted_from_vec(osht.full_from_half(half), L)
+    sp = rsht.project_onto_S12(alms, L, mu)
+    ph = np.linspace(0.1, 6.2, 23)
+    th = np.linspace(0.05, 3.1, 19)
+    PH, TH = np.meshgrid(ph, th)
+    save("scalar_L8.npz", alm_half=half, vals=sp.vals, coeffs=sp.coeffs, phi=PH, theta=TH,
+         value=sp(PH.copy(), TH.copy()))
+
     # ---- a short barotropic run (restated transforms stand in for pyssht) ---
     m2 = ref_mesh(2)
     subs = rsim.euler_simulation_sphere_remapping(8, 12, 1.0, m2, rfields.rossby_wave,

@@ -117,3 +117,27 @@ def test_velocity_generic_against_oracle(nat):
     ref = S.velocity_jets(psi, sht, g, lp, lm, lz)
     s = np.abs(ref).max(axis=(1, 2), keepdims=True)
     np.testing.assert_allclose(jets / s, ref / s, rtol=0, atol=1e-11)
+
+
+def test_scalar_spline_route_matches_reference(nat):
+    """cmm_sht_scalar_jets + cmm_assemble(ncomp=1) + the spline term of
+    cmm_vorticity_eval against the reference's project_onto_S12 fixture."""
+    from oracle import spline as OSP
+    d = np.load(os.path.join(GOLDEN, "scalar_L8.npz"))
+    L = 8
+    theta, phi, g, verts, Phi, The = grid(L)
+    vm = nat.VelMesh(L, theta, phi, g, verts)
+    sht = nat.Sht(L)
+    jets = sht.scalar_jets(vm, dev(mhalf(d["alm_half"]))).cpu().numpy()
+    np.testing.assert_allclose(jets, d["vals"], rtol=0, atol=1e-12)
+    co = vm.assemble(dev(jets))
+    rec = co.cpu().numpy()[:, :19].T
+    np.testing.assert_allclose(rec, d["coeffs"], rtol=0, atol=1e-12)
+    rng = np.random.default_rng(3)
+    X = rng.standard_normal(((L + 1) * 2 * L, 3))
+    X /= np.linalg.norm(X, axis=1)[:, None]
+    om = vm.vorticity(nat.VORT_NONE, [], dev(X), 0.0, spline=co).cpu().numpy().reshape(-1)
+    mu = OG.LatLonMesh(L)
+    bcc, tri, vs = mu.query(X)
+    ref = OSP.eval_patch(d["coeffs"], tri, bcc, vs, X)
+    np.testing.assert_allclose(om, ref, rtol=0, atol=1e-12)

@@ -155,3 +155,22 @@ def test_short_barotropic_run():
     np.testing.assert_allclose(bve.stack[:bve.Nc], d["vals"], rtol=0, atol=1e-11)
     img = bve.composite()(d["q"])
     np.testing.assert_allclose(img, d["img"], rtol=0, atol=1e-12)
+
+
+def test_project_onto_s12_scalar_spline():
+    """project_onto_S12 + spherical_spline (cmm_s2/core/spherical_harmonic_tools.py:108-142,
+    cmm_s2/core/spherical_spline.py:19-152) with the restated transform."""
+    d = load("scalar_L8.npz")
+    L = 8
+    mu = G.LatLonMesh(L)
+    sht = S.MWSS(L)
+    lp, lm, lz = S.ladder_operators(L)
+    vals = S.scalar_jets(d["alm_half"], sht, mu.grid_points, lp, lm, lz)
+    np.testing.assert_allclose(vals, d["vals"], rtol=0, atol=1e-12)
+    co = SP.assemble_scalar(mu.vertices, mu.simplices, vals)
+    np.testing.assert_allclose(co, d["coeffs"], rtol=0, atol=1e-12)
+    ph, th = d["phi"].reshape(-1), d["theta"].reshape(-1)
+    q = np.stack([np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), np.cos(th)], 1)
+    bcc, tri, vs = mu.query(q)
+    val = SP.eval_patch(co, tri, bcc, vs, q)
+    np.testing.assert_allclose(val, d["value"].reshape(-1), rtol=0, atol=1e-12)
