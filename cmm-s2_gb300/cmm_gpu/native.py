@@ -40,6 +40,8 @@ _SIGS = {
     "cmm_vorticity_eval": (_i, [_p, _i, _p, _i, _p, _i, _p, _d, _p, _p, _p]),
     "cmm_sht_scalar_jets": (_i, [_p, _p, _p, _p, _p]),
     "cmm_sht_create": (_i, [_i, ctypes.POINTER(_p)]),
+    "cmm_sht_set_precision": (_i, [_p, _i]),
+    "cmm_sht_status": (_i, [_p, _p, ctypes.POINTER(_i), _i]),
     "cmm_sht_destroy": (_i, [_p]),
     "cmm_sht_forward": (_i, [_p, _p, _p, _p]),
     "cmm_sht_inverse": (_i, [_p, _p, _i, _p, _p]),
@@ -257,6 +259,19 @@ class Sht:
         if h is not None and h.value:
             lib.cmm_sht_destroy(h)
             self.h = None
+
+    FP64, SPLIT_BF16 = 0, 1
+
+    def set_precision(self, mode):
+        with torch.cuda.device(self.device):
+            check(lib.cmm_sht_set_precision(self.h, mode), "cmm_sht_set_precision")
+        return self
+
+    def status(self, clear=True):
+        f = ctypes.c_int()
+        check(lib.cmm_sht_status(self.h, _stream(self.device), ctypes.byref(f), int(clear)),
+              "cmm_sht_status")
+        return f.value
 
     def forward(self, samples):
         samples = _dev(samples)

@@ -55,7 +55,7 @@ class Vorticity:
 
 class BVESolver:
     def __init__(self, verts, tris, level, L, Nt, T, vorticity, rot_rate=2 * np.pi, n_maps=10,
-                 device=None):
+                 device=None, precision="fp64"):
         self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
         dev = self.device
         self.vort = Vorticity.from_reference(vorticity)
@@ -65,6 +65,10 @@ class BVESolver:
         theta, phi, grid, vverts = latlon_mesh_arrays(L)
         self.vm = native.VelMesh(L, theta, phi, grid, vverts, device=dev.index)
         self.sht = native.Sht(L, device=dev.index)
+        if precision == "split_bf16":
+            self.sht.set_precision(native.Sht.SPLIT_BF16)
+        elif precision != "fp64":
+            raise ValueError("precision must be 'fp64' or 'split_bf16'")
         tan, s_pts = stencil_frames(verts)
         self.tan = torch.from_numpy(np.ascontiguousarray(tan)).to(dev)
         self.s_pts = torch.from_numpy(np.ascontiguousarray(s_pts)).to(dev)

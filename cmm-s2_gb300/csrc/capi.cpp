@@ -215,6 +215,16 @@ int cmm_sht_create(int L, cmm_sht** out) {
 
 int cmm_sht_destroy(cmm_sht* plan) { return plan ? sht_destroy(plan) : CMM_OK; }
 
+int cmm_sht_set_precision(cmm_sht* plan, int mode) {
+  if (!plan) return arg_error("cmm_sht_set_precision: null pointer");
+  return sht_set_precision(plan, mode);
+}
+
+int cmm_sht_status(cmm_sht* plan, void* stream, int* flags, int clear) {
+  if (!plan || !flags) return arg_error("cmm_sht_status: null pointer");
+  return sht_status(plan, (cudaStream_t)stream, flags, clear);
+}
+
 int cmm_sht_forward(cmm_sht* plan, const double* samples, double* alm, void* stream) {
   if (!plan || !samples || !alm) return arg_error("cmm_sht_forward: null pointer");
   return sht_forward(plan, samples, (double2*)alm, (cudaStream_t)stream);

@@ -144,4 +144,14 @@ int sht_inverse(cmm_sht* p, const double2* alm, int nf, double* samples, cudaStr
 int sht_velocity(cmm_sht* p, const cmm_mesh* vm, const double* omega, double2* psi_out,
                  double* jets, cudaStream_t s);
 int sht_scalar_jets(cmm_sht* p, const cmm_mesh* vm, const double2* alm, double* jets, cudaStream_t s);
+int sht_set_precision(cmm_sht* p, int mode);
+int sht_status(cmm_sht* p, cudaStream_t s, int* flags, int clear);
+
+// split-BF16 tensor-core Legendre synthesis (sht_tc.cu)
+struct TcPlan;
+int tc_plan_create(int L, const double* ct_rings, const double* pmm_rings, const double* ra,
+                   const double* rb, TcPlan** out);
+void tc_plan_destroy(TcPlan* p);
+size_t tc_plan_bytes(const TcPlan* p);
+int tc_synthesis(TcPlan* p, const double2* fields, double2* S, int* status, cudaStream_t s);
 }  // namespace cmm

@@ -387,15 +387,18 @@ int check_launch(const char* what) {
 
 struct cmm_sht {
   int L = 0;
+  int precision = CMM_SHT_FP64;
   cufftHandle ring_fwd = 0, torus_fwd = 0, pad_inv = 0, ring_inv = 0;
   bool have_plans[4] = {false, false, false, false};
   cmm::DeviceBuffer ct_rings, ct_fine, w_fine, pmm_rings, pmm_fine, ra, rb;
-  cmm::DeviceBuffer spec, torus, pad, alm, fields, synth, samples;
+  cmm::DeviceBuffer spec, torus, pad, alm, fields, synth, samples, status;
+  cmm::TcPlan* tc = nullptr;
   ~cmm_sht() {
     if (have_plans[0]) cufftDestroy(ring_fwd);
     if (have_plans[1]) cufftDestroy(torus_fwd);
     if (have_plans[2]) cufftDestroy(pad_inv);
     if (have_plans[3]) cufftDestroy(ring_inv);
+    if (tc) cmm::tc_plan_destroy(tc);
   }
 };
 
@@ -478,6 +481,10 @@ int sht_create(int L, cmm_sht** out) {
   if ((rc = p->fields.alloc((size_t)kFields * L * L * c16))) return fail(rc);
   if ((rc = p->synth.alloc((size_t)kFields * (L + 1) * (L + 1) * c16))) return fail(rc);
   if ((rc = p->samples.alloc((size_t)kFields * (L + 1) * 2 * L * 8))) return fail(rc);
+  {
+    const int zero = 0;
+    if ((rc = p->status.upload(&zero, sizeof(int)))) return fail(rc);
+  }
   cufftResult r;
   int n2[1] = {2 * L}, n4[1] = {4 * L};
   // rings: (L+1) real rows of 2L -> (L+1) x (L+1) complex
@@ -551,7 +558,9 @@ int sht_inverse(cmm_sht* p, const double2* alm, int nf, double* samples, cudaStr
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
   const int npair = L / 2 + 1;
   dim3 g(L, (npair + kSynthBlock - 1) / kSynthBlock);
-  if (nf == kFields)
+  if (nf == kFields && p->precision == CMM_SHT_SPLIT_BF16) {
+    if ((rc = tc_synthesis(p->tc, alm, S, (int*)p->status.p, s))) return rc;
+  } else if (nf == kFields)
     synthesis_kernel<kFields><<<g, kSynthBlock, 0, s>>>(alm, L, (const double*)p->ct_rings.p,
                                                         (const double*)p->pmm_rings.p,
                                                         (const double*)p->ra.p, (const double*)p->rb.p, S);
@@ -567,7 +576,8 @@ int sht_inverse(cmm_sht* p, const double2* alm, int nf, double* samples, cudaStr
     set_last_error("sht_inverse: nf must be 1, 4 or 12");
     return CMM_ERR_ARG;
   }
-  if ((rc = check_launch("synthesis_kernel"))) return rc;
+  if (!(nf == kFields && p->precision == CMM_SHT_SPLIT_BF16) && (rc = check_launch("synthesis_kernel")))
+    return rc;
   // Z2D over kFields*(L+1) rows; only the first nf*(L+1) rows matter
   cufftResult r = cufftExecZ2D(p->ring_inv, (cufftDoubleComplex*)S, (cufftDoubleReal*)p->samples.p);
   if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExecZ2D");
@@ -618,6 +628,35 @@ int sht_scalar_jets(cmm_sht* p, const cmm_mesh* vm, const double2* alm, double* 
   scalar_jets_kernel<<<(int)((nv + 127) / 128), 128, 0, s>>>((const double*)p->samples.p, L,
                                                              vm->view.grid, jets);
   return check_launch("scalar_jets_kernel");
+}
+
+int sht_set_precision(cmm_sht* p, int mode) {
+  if (mode != CMM_SHT_FP64 && mode != CMM_SHT_SPLIT_BF16) {
+    set_last_error("cmm_sht_set_precision: unknown mode");
+    return CMM_ERR_ARG;
+  }
+  if (mode == CMM_SHT_SPLIT_BF16 && !p->tc) {
+    int rc = tc_plan_create(p->L, (const double*)p->ct_rings.p, (const double*)p->pmm_rings.p,
+                            (const double*)p->ra.p, (const double*)p->rb.p, &p->tc);
+    if (rc) return rc;
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return cuda_fail(e, "cmm_sht_set_precision");
+  }
+  p->precision = mode;
+  return CMM_OK;
+}
+
+int sht_status(cmm_sht* p, cudaStream_t s, int* flags, int clear) {
+  int h = 0;
+  cudaError_t e = cudaMemcpyAsync(&h, p->status.p, sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(e, "cmm_sht_status");
+  *flags = h;
+  if (clear) {
+    e = cudaMemsetAsync(p->status.p, 0, sizeof(int), s);
+    if (e != cudaSuccess) return cuda_fail(e, "cmm_sht_status(clear)");
+  }
+  return CMM_OK;
 }
 
 int sht_destroy(cmm_sht* p) {

@@ -1,0 +1,405 @@
+// Split-BF16 Legendre synthesis on the 5th-generation tensor cores
+// (tcgen05, sm_103a).
+//
+// For each order m the inverse transform's Legendre stage is a product
+//   S_even/odd[t][n] = sum_{l: l-m even/odd} Pbar_lm(theta_t) A[l][n]
+// over ring pairs t (theta_t and pi - theta_t share |Pbar|; the parity of
+// l-m gives the sign), with 24 real columns n (12 complex fields).  Each
+// operand is split into two bf16 values, x = hi + lo (hi = bf16(x),
+// lo = bf16(x - hi)), and the product is taken as three tensor-core
+// products hi*hi + hi*lo + lo*hi accumulated in FP32 in tensor memory; the
+// FP32 partial sums of every 64-l chunk are drained into FP64 registers
+// (compensated accumulation across chunks).
+//
+// Data movement: the Pbar tables (per m, ring block of 128 pairs, l chunk)
+// are built once per plan directly in the shared-memory image the MMA
+// reads (K-major, no swizzle, 8x8 core matrices of 128 bytes), so a chunk
+// is one bulk asynchronous copy (cp.async.bulk) into shared memory.  One
+// elected thread issues tcgen05.mma (M=128 ring pairs, N=32 columns,
+// K=16) into two accumulators of 32 TMEM columns (even / odd l); all four
+// warps read them back with tcgen05.ld.  Every wait on an mbarrier is
+// bounded; on a timeout the kernel records CMM_FLAG_TIMEOUT, drains its own
+// operations (bounded), releases its tensor memory and returns.
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+
+#include <vector>
+
+#include "cmm_internal.h"
+
+namespace cmm {
+
+namespace {
+
+constexpr int kM = 128;                  // ring pairs per CTA (MMA M)
+constexpr int kN = 32;                   // real columns per MMA (24 used)
+constexpr int kNUsed = 24;
+constexpr int kKc = 64;                  // l values per parity per chunk
+constexpr int kPTile = kM * kKc * 2;     // bytes of one bf16 P tile = 16 KiB
+constexpr int kATile = kN * kKc * 2;     // 4 KiB
+constexpr int kPRecord = 4 * kPTile;     // E_hi, E_lo, O_hi, O_lo
+constexpr int kARecord = 4 * kATile;
+constexpr int kThreads = 128;
+constexpr uint32_t kTmemCols = 64;       // 2 accumulators x 32 columns
+constexpr long long kSpinLimit = 1LL << 26;
+
+// Byte offset of element (row, k) in a K-major no-swizzle tile image with
+// 8x8 core matrices: core (row/8, k/8) at (row/8 * (K/8) + k/8) * 128,
+// rows of 16 bytes inside.  Row-group stride (SBO) = (K/8) * 128 = 1024,
+// k-group stride (LBO) = 128.
+__host__ __device__ __forceinline__ int tile_offset(int row, int k) {
+  return ((row >> 3) * (kKc >> 3) + (k >> 3)) * 128 + (row & 7) * 16 + (k & 7) * 2;
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait; false on timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  for (long long i = 0; i < kSpinLimit; ++i)
+    if (mbar_test(bar, parity)) return true;
+  return false;
+}
+
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// Shared-memory matrix descriptor: start, leading (k-group) and stride
+// (row-group) byte offsets, descriptor version 1, no swizzle.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)((128u >> 4) & 0x3FFFu) << 16;    // LBO: next core matrix along K
+  d |= (uint64_t)((1024u >> 4) & 0x3FFFu) << 32;   // SBO: next 8-row group
+  d |= (uint64_t)1 << 46;
+  return d;
+}
+
+// Instruction descriptor of kind::f16: D f32, A and B bf16, both K-major,
+// N = 32, M = 128.
+__device__ __forceinline__ uint32_t mma_idesc() {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kN >> 3) << 17) | ((uint32_t)(kM >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                   smem_u32(bar))
+               : "memory");
+}
+
+// 32 lanes x 32 consecutive 32-bit columns -> this thread's 32 values.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]),
+        "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]),
+        "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr)
+      : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+struct TcGeometry {
+  int L, npair, nrb;
+  const int* cbase;   // (L+1) prefix sums of chunks per m
+};
+
+__device__ __forceinline__ int nchunks(int L, int m) {
+  const int kmax = (L - m + 1) / 2;   // number of l with l - m even
+  return (kmax + kKc - 1) / kKc;
+}
+
+// ---------------------------------------------------------------- tables
+// One thread per (m, ring pair t): Pbar_lm(theta_t) for l = m..L-1 by the
+// three-term recurrence in FP64, split into bf16 hi/lo, written into the
+// tile images of record (m, chunk, ring block).
+__global__ void build_ptab_kernel(TcGeometry g, const double* __restrict__ ct,
+                                  const double* __restrict__ pmm, const double* __restrict__ ra,
+                                  const double* __restrict__ rb, unsigned char* __restrict__ tab) {
+  const int m = blockIdx.y;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int L = g.L;
+  if (t >= g.nrb * kM) return;
+  const int blk = t / kM, row = t % kM;
+  const bool real_row = t < g.npair;
+  const double x = real_row ? ct[t] : 0.0;
+  double p0 = real_row ? pmm[(int64_t)m * (L + 1) + t] : 0.0, p1 = 0.0;
+  // the table is zeroed at creation: padding rows and l >= L stay zero
+  for (int l = m; l < L && real_row; ++l) {
+    double P;
+    if (l == m) {
+      P = p0;
+    } else if (l == m + 1) {
+      P = ra[(int64_t)m * L + l] * x * p0;
+      p1 = p0;
+      p0 = P;
+    } else {
+      P = ra[(int64_t)m * L + l] * (x * p0 - rb[(int64_t)m * L + l] * p1);
+      p1 = p0;
+      p0 = P;
+    }
+    const int par = (l - m) & 1, j = (l - m) >> 1, c = j / kKc, k = j % kKc;
+    unsigned char* rec = tab + ((int64_t)(g.cbase[m] + c) * g.nrb + blk) * kPRecord;
+    const int off = tile_offset(row, k);
+    const __nv_bfloat16 h = __double2bfloat16(P);
+    const __nv_bfloat16 r = __double2bfloat16(P - (double)__bfloat162float(h));
+    *(__nv_bfloat16*)(rec + (2 * par) * kPTile + off) = h;
+    *(__nv_bfloat16*)(rec + (2 * par + 1) * kPTile + off) = r;
+  }
+}
+
+// Per step: the 12 coefficient fields (12, L, L) [f][m][l] complex -> A tile
+// images per (m, chunk): column n = 2f + (0 re, 1 im), n >= 24 zero.
+__global__ void build_atab_kernel(TcGeometry g, const double2* __restrict__ fields,
+                                  unsigned char* __restrict__ atab) {
+  const int m = blockIdx.y;
+  const int L = g.L;
+  const int nch = nchunks(L, m);
+  const int per_chunk = 2 * kN * kKc;   // (par, n, k)
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nch * per_chunk; e += gridDim.x * blockDim.x) {
+    const int c = e / per_chunk, r = e % per_chunk;
+    const int par = r / (kN * kKc), n = (r / kKc) % kN, k = r % kKc;
+    const int l = m + par + 2 * (c * kKc + k);
+    double v = 0.0;
+    if (n < kNUsed && l < L) {
+      const double2 a = fields[(int64_t)(n >> 1) * L * L + (int64_t)m * L + l];
+      v = (n & 1) ? a.y : a.x;
+    }
+    const __nv_bfloat16 h = __double2bfloat16(v);
+    const __nv_bfloat16 lo = __double2bfloat16(v - (double)__bfloat162float(h));
+    unsigned char* rec = atab + (int64_t)(g.cbase[m] + c) * kARecord;
+    const int off = tile_offset(n, k);
+    *(__nv_bfloat16*)(rec + (2 * par) * kATile + off) = h;
+    *(__nv_bfloat16*)(rec + (2 * par + 1) * kATile + off) = lo;
+  }
+}
+
+// ------------------------------------------------------------ synthesis
+// Block (ring block, m); 128 threads.  Writes spectra S[f][t][m] for the
+// ring pair (t, L-t) of each row.
+__global__ void __launch_bounds__(kThreads) synth_tc_kernel(TcGeometry g,
+                                                            const unsigned char* __restrict__ ptab,
+                                                            const unsigned char* __restrict__ atab,
+                                                            double2* __restrict__ S,
+                                                            int* __restrict__ status) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  unsigned char* sP = smem;                    // kPRecord bytes
+  unsigned char* sA = smem + kPRecord;         // kARecord bytes
+  __shared__ __align__(8) uint64_t load_bar, mma_bar;
+  __shared__ uint32_t tmem_base_s;
+  __shared__ int abort_s;
+  const int blk = blockIdx.x, m = blockIdx.y, L = g.L;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  if (tid == 0) {
+    mbar_init(&load_bar, 1);
+    mbar_init(&mma_bar, 1);
+    abort_s = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&tmem_base_s)),
+                 "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_base_s;
+  const uint32_t idesc = mma_idesc();
+  double accE[kNUsed], accO[kNUsed];
+#pragma unroll
+  for (int n = 0; n < kNUsed; ++n) accE[n] = accO[n] = 0.0;
+  const int nch = nchunks(L, m);
+  uint32_t ph_load = 0, ph_mma = 0;
+  for (int c = 0; c < nch; ++c) {
+    if (tid == 0) {
+      const unsigned char* srcP = ptab + ((int64_t)(g.cbase[m] + c) * g.nrb + blk) * kPRecord;
+      const unsigned char* srcA = atab + (int64_t)(g.cbase[m] + c) * kARecord;
+      mbar_expect_tx(&load_bar, kPRecord + kARecord);
+      for (int q = 0; q < 4; ++q) bulk_g2s(sP + q * kPTile, srcP + q * kPTile, kPTile, &load_bar);
+      bulk_g2s(sA, srcA, kARecord, &load_bar);
+      if (!mbar_wait(&load_bar, ph_load)) abort_s = 1;
+      if (!abort_s) {
+        tc_fence_after();
+        const uint32_t p0 = smem_u32(sP), a0 = smem_u32(sA);
+        for (int ks = 0; ks < kKc / 16; ++ks)
+          for (int par = 0; par < 2; ++par) {
+            const uint64_t ph = smem_desc(p0 + (2 * par) * kPTile + ks * 256);
+            const uint64_t pl = smem_desc(p0 + (2 * par + 1) * kPTile + ks * 256);
+            const uint64_t ah = smem_desc(a0 + (2 * par) * kATile + ks * 256);
+            const uint64_t al = smem_desc(a0 + (2 * par + 1) * kATile + ks * 256);
+            const uint32_t d = tmem + par * kN;
+            mma_bf16(d, ph, ah, idesc, ks > 0 ? 1u : 0u);
+            mma_bf16(d, ph, al, idesc, 1u);
+            mma_bf16(d, pl, ah, idesc, 1u);
+          }
+        mma_commit(&mma_bar);
+        if (!mbar_wait(&mma_bar, ph_mma)) abort_s = 1;
+      }
+    }
+    ph_load ^= 1u;
+    ph_mma ^= 1u;
+    __syncthreads();
+    if (abort_s) break;
+    tc_fence_after();
+    float vE[32], vO[32];
+    const uint32_t lane_base = (uint32_t)(32 * warp) << 16;
+    tmem_ld32(tmem + lane_base, vE);
+    tmem_ld32(tmem + lane_base + kN, vO);
+#pragma unroll
+    for (int n = 0; n < kNUsed; ++n) {
+      accE[n] += (double)vE[n];
+      accO[n] += (double)vO[n];
+    }
+    tc_fence_before();
+    __syncthreads();
+  }
+  if (abort_s) {
+    if (tid == 0) atomicOr(status, CMM_FLAG_TIMEOUT);
+  } else {
+    const int row = tid;   // TMEM lane = thread index
+    const int t = blk * kM + row;
+    if (t < g.npair) {
+      const int64_t row_len = L + 1;
+      for (int f = 0; f < kNUsed / 2; ++f) {
+        const int64_t base = (int64_t)f * (L + 1) * row_len;
+        S[base + (int64_t)t * row_len + m] =
+            make_double2(accE[2 * f] + accO[2 * f], accE[2 * f + 1] + accO[2 * f + 1]);
+        if (L - t != t)
+          S[base + (int64_t)(L - t) * row_len + m] =
+              make_double2(accE[2 * f] - accO[2 * f], accE[2 * f + 1] - accO[2 * f + 1]);
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols)
+                 : "memory");
+}
+
+int check(const char* what) {
+  note_launch();
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? CMM_OK : cuda_fail(e, what);
+}
+
+}  // namespace
+
+// Host side --------------------------------------------------------------
+struct TcPlan {
+  int L = 0, npair = 0, nrb = 0, total_chunks = 0;
+  DeviceBuffer cbase, ptab, atab;
+};
+
+static int tc_chunks(int L, int m) {
+  const int kmax = (L - m + 1) / 2;
+  return (kmax + kKc - 1) / kKc;
+}
+
+int tc_plan_create(int L, const double* ct_rings, const double* pmm_rings, const double* ra,
+                   const double* rb, TcPlan** out) {
+  TcPlan* p = new (std::nothrow) TcPlan();
+  if (!p) {
+    set_last_error("tc plan: out of host memory");
+    return CMM_ERR_ARG;
+  }
+  p->L = L;
+  p->npair = L / 2 + 1;
+  p->nrb = (p->npair + kM - 1) / kM;
+  std::vector<int> cb(L + 1, 0);
+  for (int m = 0; m < L; ++m) cb[m + 1] = cb[m] + tc_chunks(L, m);
+  p->total_chunks = cb[L];
+  int rc;
+  if ((rc = p->cbase.upload(cb.data(), cb.size() * sizeof(int))) ||
+      (rc = p->ptab.alloc((size_t)p->total_chunks * p->nrb * kPRecord)) ||
+      (rc = p->atab.alloc((size_t)p->total_chunks * kARecord))) {
+    delete p;
+    return rc;
+  }
+  cudaMemset(p->ptab.p, 0, p->ptab.bytes);
+  TcGeometry g{L, p->npair, p->nrb, (const int*)p->cbase.p};
+  dim3 grid((p->nrb * kM + 127) / 128, L);
+  build_ptab_kernel<<<grid, 128>>>(g, ct_rings, pmm_rings, ra, rb, (unsigned char*)p->ptab.p);
+  if ((rc = check("build_ptab_kernel"))) {
+    delete p;
+    return rc;
+  }
+  cudaError_t e = cudaFuncSetAttribute(synth_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       kPRecord + kARecord);
+  if (e != cudaSuccess) {
+    delete p;
+    return cuda_fail(e, "cudaFuncSetAttribute(synth_tc_kernel)");
+  }
+  *out = p;
+  return CMM_OK;
+}
+
+void tc_plan_destroy(TcPlan* p) { delete p; }
+
+size_t tc_plan_bytes(const TcPlan* p) { return p->ptab.bytes + p->atab.bytes; }
+
+int tc_synthesis(TcPlan* p, const double2* fields, double2* S, int* status, cudaStream_t s) {
+  TcGeometry g{p->L, p->npair, p->nrb, (const int*)p->cbase.p};
+  build_atab_kernel<<<dim3(16, p->L), 256, 0, s>>>(g, fields, (unsigned char*)p->atab.p);
+  int rc = check("build_atab_kernel");
+  if (rc) return rc;
+  synth_tc_kernel<<<dim3(p->nrb, p->L), kThreads, kPRecord + kARecord, s>>>(
+      g, (const unsigned char*)p->ptab.p, (const unsigned char*)p->atab.p, S, status);
+  return check("synth_tc_kernel");
+}
+
+}  // namespace cmm

@@ -46,6 +46,7 @@ typedef enum {
 /* Bits of the device status word. */
 #define CMM_FLAG_NONFINITE 1
 #define CMM_FLAG_LOCATE 2
+#define CMM_FLAG_TIMEOUT 4   /* a bounded wait inside a kernel ran out */
 
 const char* cmm_last_error(void);
 int cmm_version(void);
@@ -227,6 +228,20 @@ int cmm_vorticity_eval(const cmm_mesh* velmesh, int kind, const double* params, 
 typedef struct cmm_sht cmm_sht;
 int cmm_sht_create(int L, cmm_sht** out);
 int cmm_sht_destroy(cmm_sht* plan);
+
+/* Arithmetic of the 12-field Legendre synthesis of cmm_sht_velocity /
+ * cmm_sht_inverse: CMM_SHT_FP64 (default; FP64 recurrence and sums) or
+ * CMM_SHT_SPLIT_BF16: each factor split into bf16 hi + lo, products
+ * hi*hi + hi*lo + lo*hi on the tensor cores (tcgen05) accumulated in FP32
+ * per 64-degree chunk and in FP64 across chunks; Pbar tables (about
+ * 1.5 GB at L = 1024) are built when the mode is first selected.  The
+ * pyssht calls this replaces work in FP64. */
+#define CMM_SHT_FP64 0
+#define CMM_SHT_SPLIT_BF16 1
+int cmm_sht_set_precision(cmm_sht* plan, int mode);
+/* Read (and with clear != 0, reset) the plan's device status word
+ * (CMM_FLAG_TIMEOUT); synchronises `stream`. */
+int cmm_sht_status(cmm_sht* plan, void* stream, int* flags, int clear);
 
 /* samples (L+1,2L) -> alm (L,L) complex.  Replaces pyssht.forward(...,
  * Method="MWSS", Reality=True) as called by inv_Laplacian

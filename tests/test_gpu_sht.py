@@ -141,3 +141,38 @@ def test_scalar_spline_route_matches_reference(nat):
     bcc, tri, vs = mu.query(X)
     ref = OSP.eval_patch(d["coeffs"], tri, bcc, vs, X)
     np.testing.assert_allclose(om, ref, rtol=0, atol=1e-12)
+
+
+@pytest.mark.parametrize("L", [32, 128, 256])
+def test_split_bf16_synthesis_against_fp64(nat, L):
+    """The 12-field synthesis on the tensor cores (three bf16 products,
+    FP32 per 64-degree chunk, FP64 across chunks) against the FP64 path.
+    Stated error: max |split - fp64| <= 1e-4 of max |fp64| per field (each
+    split factor carries ~2^-17 relative error)."""
+    rng = np.random.default_rng(L)
+    a = np.zeros((12, L, L), dtype=complex)
+    for f in range(12):
+        c = np.tril(rng.standard_normal((L, L)) + 1j * rng.standard_normal((L, L)))
+        c[:, 0] = c[:, 0].real
+        a[f] = mhalf(c / (1 + np.arange(L))[:, None])
+    ref = nat.Sht(L).inverse(dev(a)).cpu().numpy()
+    tc = nat.Sht(L).set_precision(nat.Sht.SPLIT_BF16)
+    got = tc.inverse(dev(a)).cpu().numpy()
+    assert tc.status() == 0
+    err = np.abs(got - ref).max(axis=(1, 2)) / np.abs(ref).max(axis=(1, 2))
+    print(f"L={L}: split-BF16 synthesis relative error per field max {err.max():.3e}")
+    assert err.max() < 1e-4
+    assert err.max() > 1e-9   # the tensor-core path really ran (not FP64)
+
+
+def test_split_bf16_velocity_jets(nat):
+    L = 128
+    theta, phi, g, verts, Phi, The = grid(L)
+    vm = nat.VelMesh(L, theta, phi, g, verts)
+    om = 30 * np.cos(The) * np.cos(4 * Phi) * np.sin(The) ** 4 + np.exp(-((np.cos(The) - 0.5) / 0.1) ** 2)
+    ref = nat.Sht(L).velocity(vm, dev(om)).cpu().numpy()
+    tc = nat.Sht(L).set_precision(nat.Sht.SPLIT_BF16)
+    got = tc.velocity(vm, dev(om)).cpu().numpy()
+    err = np.abs(got - ref).max() / np.abs(ref).max()
+    print(f"split-BF16 velocity jets relative error {err:.3e}")
+    assert err < 1e-4
