@@ -255,15 +255,16 @@ def bench_gpu(args, rank, world):
     if rank == 0 and not args.no_bve:
         try:
             res["bve"] = bench_bve(args, dev)
+            res["rh_error"] = bench_rh_error(dev)
         except Exception as exc:  # reported, the headline stands on its own
             res["bve"] = {"error": f"{type(exc).__name__}: {exc}"}
-        if not args.no_bve3:
-            del q, mesh, cs
-            torch.cuda.empty_cache()
-            try:
-                res["bve_l7_L1024"] = bench_bve3(args, dev)
-            except Exception as exc:
-                res["bve_l7_L1024"] = {"error": f"{type(exc).__name__}: {exc}"}
+    if rank == 0 and not args.no_bve3:
+        del q, mesh, cs
+        torch.cuda.empty_cache()
+        try:
+            res["bve_l7_L1024"] = bench_bve3(args, dev)
+        except Exception as exc:
+            res["bve_l7_L1024"] = {"error": f"{type(exc).__name__}: {exc}"}
     return res
 
 
@@ -307,24 +308,60 @@ def bench_bve3(args, dev, steps=8):
     pert = spectral_perturbation(64, seed=3, slope=-2.0, rms=0.1)
     vort = Vorticity("gaussian_zonal_jets", (10.0, 0.1, 4, 0.5, -0.5, 1.1, -1.1), spline_sh=pert)
     verts, tris = icosahedral_mesh(7)
-    t0 = time.perf_counter()
-    s = BVESolver(verts, tris, 7, 1024, 1000, 1.0, vort, n_maps=10)
-    s.bootstrap()
-    s.step()
-    torch.cuda.synchronize()
-    setup = time.perf_counter() - t0
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(steps):
+    out = {"workload": "BVE level 7 (163842 vertices), L=1024 MWSS 1025x2048, remap every 10, "
+                       "4 Gaussian zonal jets + 1% k^-3 l<=64 perturbation (spline); steps 4..11"}
+    omegas = {}
+    for form in ("fp64", "split_bf16"):
+        t0 = time.perf_counter()
+        s = BVESolver(verts, tris, 7, 1024, 1000, 1.0, vort, n_maps=10, precision=form)
+        s.bootstrap()
         s.step()
-    e1.record()
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / steps
-    ok = s.mesh.status() == 0 and s.vm.status() == 0
-    return {"steps_per_s": 1e3 / ms, "ms_per_step": ms, "steps_timed": steps, "form": "fp64",
-            "setup_s": setup, "status_ok": ok,
-            "workload": "BVE level 7 (163842 vertices), L=1024 MWSS 1025x2048, remap every 10, "
-                        "4 Gaussian zonal jets + 1% k^-3 l<=64 perturbation (spline); steps 4..11"}
+        torch.cuda.synchronize()
+        setup = time.perf_counter() - t0
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            s.step()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        ok = s.mesh.status() == 0 and s.vm.status() == 0 and s.sht.status() == 0
+        out[form] = {"steps_per_s": 1e3 / ms, "ms_per_step": ms, "steps_timed": steps,
+                     "setup_s": setup, "status_ok": ok}
+        omegas[form] = s.omega.clone()
+        del s
+        torch.cuda.empty_cache()
+    d = (omegas["split_bf16"] - omegas["fp64"]).abs().max().item()
+    out["split_vs_fp64_omega_rel"] = d / omegas["fp64"].abs().max().item()
+    out["speedup_split_over_fp64"] = out["split_bf16"]["steps_per_s"] / out["fp64"]["steps_per_s"]
+    return out
+
+
+def bench_rh_error(dev):
+    """Rossby-Haurwitz wave (exact travelling solution, T=1): L_inf vorticity
+    error of the FP64 and split-BF16 forms (level 4, L=64, 42 steps)."""
+    import torch
+    from cmm_gpu.meshgen import icosahedral_mesh
+    from cmm_gpu.spherical_simulations import BVESolver
+    verts, tris = icosahedral_mesh(4)
+    n = 96
+    ph, th = np.meshgrid(np.linspace(0, 2 * np.pi, n, endpoint=False),
+                         np.linspace(0, np.pi, n, endpoint=False))
+    q = np.stack([np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), np.cos(th)], -1).reshape(-1, 3)
+    Om, res = 2 * np.pi, {}
+
+    def rh(phi, theta, t=0.0):
+        return 30 * np.cos(theta) * np.cos(4 * (phi + 2 * Om * t / 30)) * np.sin(theta) ** 4
+
+    for form in ("fp64", "split_bf16"):
+        s = BVESolver(verts, tris, 4, 64, 42, 1.0, "rossby_wave", n_maps=10, precision=form).run()
+        X = s.composite(torch.from_numpy(q).to(dev))[0].cpu().numpy()
+        pX = (np.arctan2(X[:, 1], X[:, 0]) + 2 * np.pi) % (2 * np.pi)
+        tX = np.arctan2(np.sqrt(X[:, 0] ** 2 + X[:, 1] ** 2), X[:, 2])
+        om = rh(pX, tX) + 2 * Om * np.cos(tX) - 2 * Om * np.cos(th.reshape(-1))
+        res[form] = float(np.abs(om - rh(ph.reshape(-1), th.reshape(-1), 1.0)).max())
+    res["ratio_split_over_fp64"] = res["split_bf16"] / res["fp64"]
+    return res
 
 
 def main():
@@ -406,7 +443,7 @@ def main():
                 "h2d_bytes_per_step": Q * 24, "d2h_bytes_per_step": Q * (24 + 4 + 72)},
         "clocks": r["clocks"], "gpu_launches": r["launches"],
     }
-    for key in ("bve", "bve_l7_L1024"):
+    for key in ("bve", "rh_error", "bve_l7_L1024"):
         if key in r:
             line[key] = r[key]
     print(json.dumps(line))

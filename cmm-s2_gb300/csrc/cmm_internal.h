@@ -149,9 +149,11 @@ int sht_status(cmm_sht* p, cudaStream_t s, int* flags, int clear);
 
 // split-BF16 tensor-core Legendre synthesis (sht_tc.cu)
 struct TcPlan;
-int tc_plan_create(int L, const double* ct_rings, const double* pmm_rings, const double* ra,
-                   const double* rb, TcPlan** out);
+int tc_plan_create(int L, const double* ct_rings, const double* pmm_rings, const double* ct_fine,
+                   const double* pmm_fine, const double* ra, const double* rb, TcPlan** out);
 void tc_plan_destroy(TcPlan* p);
 size_t tc_plan_bytes(const TcPlan* p);
 int tc_synthesis(TcPlan* p, const double2* fields, double2* S, int* status, cudaStream_t s);
+int tc_analysis(TcPlan* p, const double2* fine, const double* w, double2* alm, int* status,
+                cudaStream_t s);
 }  // namespace cmm

@@ -14,7 +14,9 @@
 // Pbar_lm are orthonormal with the Condon-Shortley phase and come from the
 // three-term recurrence in l run on the fly (FP64); rings theta and
 // pi - theta are processed together since Pbar_lm(pi - theta) =
-// (-1)^(l+m) Pbar_lm(theta).
+// (-1)^(l+m) Pbar_lm(theta).  In CMM_SHT_SPLIT_BF16 mode both Legendre
+// contractions (forward analysis, 12-field synthesis) run instead on the
+// tensor cores from precomputed split-bf16 tables (sht_tc.cu).
 // Coefficient layout on the device: alm[m][l] complex (double2), m-major,
 // m <= l < L, entries with l < m unused and zero.
 #include <cuda_runtime.h>
@@ -537,6 +539,9 @@ int sht_forward(cmm_sht* p, const double* samples, double2* out, cudaStream_t s)
   if ((rc = check_launch("pad_kernel"))) return rc;
   r = cufftExecZ2Z(p->pad_inv, (cufftDoubleComplex*)p->pad.p, (cufftDoubleComplex*)p->pad.p, CUFFT_INVERSE);
   if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExecZ2Z(pad)");
+  if (p->precision == CMM_SHT_SPLIT_BF16)
+    return tc_analysis(p->tc, (const double2*)p->pad.p, (const double*)p->w_fine.p, out,
+                       (int*)p->status.p, s);
   if (L + 1 > 8 * 256) {
     set_last_error("sht_forward: L too large for the analysis kernel");
     return CMM_ERR_UNSUPPORTED;
@@ -637,6 +642,7 @@ int sht_set_precision(cmm_sht* p, int mode) {
   }
   if (mode == CMM_SHT_SPLIT_BF16 && !p->tc) {
     int rc = tc_plan_create(p->L, (const double*)p->ct_rings.p, (const double*)p->pmm_rings.p,
+                            (const double*)p->ct_fine.p, (const double*)p->pmm_fine.p,
                             (const double*)p->ra.p, (const double*)p->rb.p, &p->tc);
     if (rc) return rc;
     cudaError_t e = cudaDeviceSynchronize();

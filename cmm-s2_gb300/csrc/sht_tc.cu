@@ -19,7 +19,13 @@
 // K=16) into two accumulators of 32 TMEM columns (even / odd l); all four
 // warps read them back with tcgen05.ld.  Every wait on an mbarrier is
 // bounded; on a timeout the kernel records CMM_FLAG_TIMEOUT, drains its own
-// operations (bounded), releases its tensor memory and returns.
+// operations (a second bounded wait), releases its tensor memory and
+// returns.
+//
+// The forward analysis f_lm = sum_j w_j Pbar_lm(theta'_j) F'_m(j) is the
+// same contraction transposed: M = 128 degrees, N = 16 (re, im), K = 64
+// fine ring pairs per chunk, with the quadrature weights and the ring-pair
+// parity folding applied to the data tiles.
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 
@@ -271,7 +277,10 @@ __global__ void __launch_bounds__(kThreads) synth_tc_kernel(TcGeometry g,
       mbar_expect_tx(&load_bar, kPRecord + kARecord);
       for (int q = 0; q < 4; ++q) bulk_g2s(sP + q * kPTile, srcP + q * kPTile, kPTile, &load_bar);
       bulk_g2s(sA, srcA, kARecord, &load_bar);
-      if (!mbar_wait(&load_bar, ph_load)) abort_s = 1;
+      if (!mbar_wait(&load_bar, ph_load)) {
+        abort_s = 1;
+        mbar_wait(&load_bar, ph_load);   // bounded drain of the copies in flight
+      }
       if (!abort_s) {
         tc_fence_after();
         const uint32_t p0 = smem_u32(sP), a0 = smem_u32(sA);
@@ -287,7 +296,10 @@ __global__ void __launch_bounds__(kThreads) synth_tc_kernel(TcGeometry g,
             mma_bf16(d, pl, ah, idesc, 1u);
           }
         mma_commit(&mma_bar);
-        if (!mbar_wait(&mma_bar, ph_mma)) abort_s = 1;
+        if (!mbar_wait(&mma_bar, ph_mma)) {
+          abort_s = 1;
+          mbar_wait(&mma_bar, ph_mma);   // bounded drain of the MMAs in flight
+        }
       }
     }
     ph_load ^= 1u;
@@ -331,6 +343,210 @@ __global__ void __launch_bounds__(kThreads) synth_tc_kernel(TcGeometry g,
                  : "memory");
 }
 
+// -------------------------------------------------------------- analysis
+// f_lm = sum_j Pbar_lm(theta'_j) X_par(l)[j] over the L+1 ring pairs j of
+// the 2L+1 fine rings, X_even = w_j (F_j + F_{2L-j}), X_odd = w_j (F_j -
+// F_{2L-j}) (ring L unpaired).  MMA rows are degrees l (128 per block, one
+// parity per accumulator), columns the real and imaginary parts (N = 16,
+// 2 used), K = 64 ring pairs per chunk.
+constexpr int kNA = 16;
+constexpr int kXTile = kNA * kKc * 2;        // 2 KiB
+constexpr int kXRecord = 4 * kXTile;         // E_hi, E_lo, O_hi, O_lo
+constexpr uint32_t kTmemColsA = 32;
+
+struct TcFwdGeometry {
+  int L, nck;           // ring-pair chunks of 64
+  const int* lbase;     // (L+1) prefix sums of 128-degree blocks per m
+};
+
+__device__ __forceinline__ int nlblocks(int L, int m) {
+  const int kmax = (L - m + 1) / 2;
+  return (kmax + kM - 1) / kM;
+}
+
+__device__ __forceinline__ uint32_t mma_idesc_n16() {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kNA >> 3) << 17) | ((uint32_t)(kM >> 4) << 24);
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// One thread per (m, fine ring pair j): Pbar_lm(theta'_j), l = m..L-1.
+__global__ void build_ftab_kernel(TcFwdGeometry g, const double* __restrict__ ct,
+                                  const double* __restrict__ pmm, const double* __restrict__ ra,
+                                  const double* __restrict__ rb, unsigned char* __restrict__ tab) {
+  const int m = blockIdx.y;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int L = g.L;
+  if (j > L) return;   // pairs j = 0..L
+  const double x = ct[j];
+  double p0 = pmm[(int64_t)m * (2 * L + 1) + j], p1 = 0.0;
+  const int c = j / kKc, k = j % kKc;
+  for (int l = m; l < L; ++l) {
+    double P;
+    if (l == m) {
+      P = p0;
+    } else if (l == m + 1) {
+      P = ra[(int64_t)m * L + l] * x * p0;
+      p1 = p0;
+      p0 = P;
+    } else {
+      P = ra[(int64_t)m * L + l] * (x * p0 - rb[(int64_t)m * L + l] * p1);
+      p1 = p0;
+      p0 = P;
+    }
+    const int par = (l - m) & 1, i = (l - m) >> 1, lb = i / kM, row = i % kM;
+    unsigned char* rec = tab + ((int64_t)(g.lbase[m] + lb) * g.nck + c) * kPRecord;
+    const int off = tile_offset(row, k);
+    const __nv_bfloat16 h = __double2bfloat16(P);
+    const __nv_bfloat16 r = __double2bfloat16(P - (double)__bfloat162float(h));
+    *(__nv_bfloat16*)(rec + (2 * par) * kPTile + off) = h;
+    *(__nv_bfloat16*)(rec + (2 * par + 1) * kPTile + off) = r;
+  }
+}
+
+// Per transform: weighted, parity-folded fine-ring data -> X tile images
+// per (m, ring chunk).  fine: (4L, L) complex [j][m], rows 0..2L used.
+__global__ void build_xtab_kernel(TcFwdGeometry g, const double2* __restrict__ fine,
+                                  const double* __restrict__ w, unsigned char* __restrict__ xtab) {
+  const int m = blockIdx.y;
+  const int L = g.L;
+  const int total = g.nck * 2 * kNA * kKc;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+    const int c = e / (2 * kNA * kKc), r = e % (2 * kNA * kKc);
+    const int par = r / (kNA * kKc), n = (r / kKc) % kNA, k = r % kKc;
+    const int j = c * kKc + k;
+    double v = 0.0;
+    if (n < 2 && j <= L) {
+      const double2 a = fine[(int64_t)j * L + m];
+      double2 s;
+      if (j < L) {
+        const double2 b = fine[(int64_t)(2 * L - j) * L + m];
+        s = par == 0 ? make_double2(a.x + b.x, a.y + b.y) : make_double2(a.x - b.x, a.y - b.y);
+      } else {
+        s = par == 0 ? a : make_double2(0.0, 0.0);
+      }
+      v = w[j] * (n == 0 ? s.x : s.y);
+    }
+    const __nv_bfloat16 h = __double2bfloat16(v);
+    const __nv_bfloat16 lo = __double2bfloat16(v - (double)__bfloat162float(h));
+    unsigned char* rec = xtab + ((int64_t)m * g.nck + c) * kXRecord;
+    const int off = tile_offset(n, k);
+    *(__nv_bfloat16*)(rec + (2 * par) * kXTile + off) = h;
+    *(__nv_bfloat16*)(rec + (2 * par + 1) * kXTile + off) = lo;
+  }
+}
+
+// Block (degree block, m); 128 threads; writes alm[m][l].
+__global__ void __launch_bounds__(kThreads) analysis_tc_kernel(TcFwdGeometry g,
+                                                               const unsigned char* __restrict__ ptab,
+                                                               const unsigned char* __restrict__ xtab,
+                                                               double2* __restrict__ alm,
+                                                               int* __restrict__ status) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  unsigned char* sP = smem;                 // kPRecord
+  unsigned char* sX = smem + kPRecord;      // kXRecord
+  __shared__ __align__(8) uint64_t load_bar, mma_bar;
+  __shared__ uint32_t tmem_base_s;
+  __shared__ int abort_s;
+  const int lb = blockIdx.x, m = blockIdx.y, L = g.L;
+  if (lb >= nlblocks(L, m)) return;   // uniform for the block
+  const int tid = threadIdx.x, warp = tid >> 5;
+  if (tid == 0) {
+    mbar_init(&load_bar, 1);
+    mbar_init(&mma_bar, 1);
+    abort_s = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&tmem_base_s)),
+                 "r"(kTmemColsA)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_base_s;
+  const uint32_t idesc = mma_idesc_n16();
+  double aE0 = 0.0, aE1 = 0.0, aO0 = 0.0, aO1 = 0.0;
+  uint32_t ph_load = 0, ph_mma = 0;
+  for (int c = 0; c < g.nck; ++c) {
+    if (tid == 0) {
+      const unsigned char* srcP = ptab + ((int64_t)(g.lbase[m] + lb) * g.nck + c) * kPRecord;
+      const unsigned char* srcX = xtab + ((int64_t)m * g.nck + c) * kXRecord;
+      mbar_expect_tx(&load_bar, kPRecord + kXRecord);
+      for (int q = 0; q < 4; ++q) bulk_g2s(sP + q * kPTile, srcP + q * kPTile, kPTile, &load_bar);
+      bulk_g2s(sX, srcX, kXRecord, &load_bar);
+      if (!mbar_wait(&load_bar, ph_load)) {
+        abort_s = 1;
+        mbar_wait(&load_bar, ph_load);   // bounded drain of the copies in flight
+      }
+      if (!abort_s) {
+        tc_fence_after();
+        const uint32_t p0 = smem_u32(sP), x0 = smem_u32(sX);
+        for (int ks = 0; ks < kKc / 16; ++ks)
+          for (int par = 0; par < 2; ++par) {
+            const uint64_t ph = smem_desc(p0 + (2 * par) * kPTile + ks * 256);
+            const uint64_t pl = smem_desc(p0 + (2 * par + 1) * kPTile + ks * 256);
+            const uint64_t xh = smem_desc(x0 + (2 * par) * kXTile + ks * 256);
+            const uint64_t xl = smem_desc(x0 + (2 * par + 1) * kXTile + ks * 256);
+            const uint32_t d = tmem + par * kNA;
+            mma_bf16(d, ph, xh, idesc, ks > 0 ? 1u : 0u);
+            mma_bf16(d, ph, xl, idesc, 1u);
+            mma_bf16(d, pl, xh, idesc, 1u);
+          }
+        mma_commit(&mma_bar);
+        if (!mbar_wait(&mma_bar, ph_mma)) {
+          abort_s = 1;
+          mbar_wait(&mma_bar, ph_mma);   // bounded drain of the MMAs in flight
+        }
+      }
+    }
+    ph_load ^= 1u;
+    ph_mma ^= 1u;
+    __syncthreads();
+    if (abort_s) break;
+    tc_fence_after();
+    float vE[16], vO[16];
+    const uint32_t lane_base = (uint32_t)(32 * warp) << 16;
+    tmem_ld16(tmem + lane_base, vE);
+    tmem_ld16(tmem + lane_base + kNA, vO);
+    aE0 += (double)vE[0];
+    aE1 += (double)vE[1];
+    aO0 += (double)vO[0];
+    aO1 += (double)vO[1];
+    tc_fence_before();
+    __syncthreads();
+  }
+  if (abort_s) {
+    if (tid == 0) atomicOr(status, CMM_FLAG_TIMEOUT);
+  } else {
+    const int i = lb * kM + tid;
+    const int lE = m + 2 * i, lO = m + 1 + 2 * i;
+    if (lE < L) alm[(int64_t)m * L + lE] = make_double2(aE0, aE1);
+    if (lO < L) alm[(int64_t)m * L + lO] = make_double2(aO0, aO1);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemColsA)
+                 : "memory");
+}
+
 int check(const char* what) {
   note_launch();
   cudaError_t e = cudaGetLastError();
@@ -343,6 +559,9 @@ int check(const char* what) {
 struct TcPlan {
   int L = 0, npair = 0, nrb = 0, total_chunks = 0;
   DeviceBuffer cbase, ptab, atab;
+  // analysis: degree blocks of 128 per m (prefix sums), ring-pair chunks
+  int nck = 0, total_lblocks = 0;
+  DeviceBuffer lbase, ftab, xtab;
 };
 
 static int tc_chunks(int L, int m) {
@@ -350,8 +569,8 @@ static int tc_chunks(int L, int m) {
   return (kmax + kKc - 1) / kKc;
 }
 
-int tc_plan_create(int L, const double* ct_rings, const double* pmm_rings, const double* ra,
-                   const double* rb, TcPlan** out) {
+int tc_plan_create(int L, const double* ct_rings, const double* pmm_rings, const double* ct_fine,
+                   const double* pmm_fine, const double* ra, const double* rb, TcPlan** out) {
   TcPlan* p = new (std::nothrow) TcPlan();
   if (!p) {
     set_last_error("tc plan: out of host memory");
@@ -384,13 +603,40 @@ int tc_plan_create(int L, const double* ct_rings, const double* pmm_rings, const
     delete p;
     return cuda_fail(e, "cudaFuncSetAttribute(synth_tc_kernel)");
   }
+  // analysis tables over the L+1 fine ring pairs
+  p->nck = (L + 1 + kKc - 1) / kKc;
+  std::vector<int> lb(L + 1, 0);
+  for (int m = 0; m < L; ++m) lb[m + 1] = lb[m] + ((L - m + 1) / 2 + kM - 1) / kM;
+  p->total_lblocks = lb[L];
+  if ((rc = p->lbase.upload(lb.data(), lb.size() * sizeof(int))) ||
+      (rc = p->ftab.alloc((size_t)p->total_lblocks * p->nck * kPRecord)) ||
+      (rc = p->xtab.alloc((size_t)L * p->nck * kXRecord))) {
+    delete p;
+    return rc;
+  }
+  cudaMemset(p->ftab.p, 0, p->ftab.bytes);
+  TcFwdGeometry gf{L, p->nck, (const int*)p->lbase.p};
+  build_ftab_kernel<<<dim3((L + 1 + 127) / 128, L), 128>>>(gf, ct_fine, pmm_fine, ra, rb,
+                                                            (unsigned char*)p->ftab.p);
+  if ((rc = check("build_ftab_kernel"))) {
+    delete p;
+    return rc;
+  }
+  e = cudaFuncSetAttribute(analysis_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           kPRecord + kXRecord);
+  if (e != cudaSuccess) {
+    delete p;
+    return cuda_fail(e, "cudaFuncSetAttribute(analysis_tc_kernel)");
+  }
   *out = p;
   return CMM_OK;
 }
 
 void tc_plan_destroy(TcPlan* p) { delete p; }
 
-size_t tc_plan_bytes(const TcPlan* p) { return p->ptab.bytes + p->atab.bytes; }
+size_t tc_plan_bytes(const TcPlan* p) {
+  return p->ptab.bytes + p->atab.bytes + p->ftab.bytes + p->xtab.bytes;
+}
 
 int tc_synthesis(TcPlan* p, const double2* fields, double2* S, int* status, cudaStream_t s) {
   TcGeometry g{p->L, p->npair, p->nrb, (const int*)p->cbase.p};
@@ -400,6 +646,21 @@ int tc_synthesis(TcPlan* p, const double2* fields, double2* S, int* status, cuda
   synth_tc_kernel<<<dim3(p->nrb, p->L), kThreads, kPRecord + kARecord, s>>>(
       g, (const unsigned char*)p->ptab.p, (const unsigned char*)p->atab.p, S, status);
   return check("synth_tc_kernel");
+}
+
+// fine (4L, L) complex after the padded inverse transform, rows 0..2L;
+// w the 2L+1 Clenshaw-Curtis weights -> alm[m][l], l >= m.
+int tc_analysis(TcPlan* p, const double2* fine, const double* w, double2* alm, int* status,
+                cudaStream_t s) {
+  const int L = p->L;
+  TcFwdGeometry g{L, p->nck, (const int*)p->lbase.p};
+  build_xtab_kernel<<<dim3(8, L), 256, 0, s>>>(g, fine, w, (unsigned char*)p->xtab.p);
+  int rc = check("build_xtab_kernel");
+  if (rc) return rc;
+  const int maxlb = ((L + 1) / 2 + kM - 1) / kM;
+  analysis_tc_kernel<<<dim3(maxlb, L), kThreads, kPRecord + kXRecord, s>>>(
+      g, (const unsigned char*)p->ftab.p, (const unsigned char*)p->xtab.p, alm, status);
+  return check("analysis_tc_kernel");
 }
 
 }  // namespace cmm

@@ -165,6 +165,27 @@ def test_split_bf16_synthesis_against_fp64(nat, L):
     assert err.max() > 1e-9   # the tensor-core path really ran (not FP64)
 
 
+@pytest.mark.parametrize("L", [33, 128, 256])
+def test_split_bf16_analysis_against_fp64(nat, L):
+    """The forward Legendre analysis on the tensor cores (M = 128 degrees,
+    K = 64 fine ring pairs per chunk, weights folded into the data tiles)
+    against the FP64 path on generic samples.  Stated error:
+    max |split - fp64| <= 1e-4 of max |fp64|."""
+    rng = np.random.default_rng(1000 + L)
+    f = rng.standard_normal((L + 1, 2 * L))
+    f[0] = f[0, 0]
+    f[-1] = f[-1, 0]
+    ref = nat.Sht(L).forward(dev(f)).cpu().numpy()
+    tc = nat.Sht(L).set_precision(nat.Sht.SPLIT_BF16)
+    got = tc.forward(dev(f)).cpu().numpy()
+    assert tc.status() == 0
+    low = np.tril(np.ones((L, L), dtype=bool)).T   # [m, l] entries with l >= m
+    err = np.abs(got - ref)[low].max() / np.abs(ref[low]).max()
+    print(f"L={L}: split-BF16 analysis relative error {err:.3e}")
+    assert err < 1e-4
+    assert err > 1e-9
+
+
 def test_split_bf16_velocity_jets(nat):
     L = 128
     theta, phi, g, verts, Phi, The = grid(L)
