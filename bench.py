@@ -258,9 +258,15 @@ def bench_gpu(args, rank, world):
             res["rh_error"] = bench_rh_error(dev)
         except Exception as exc:  # reported, the headline stands on its own
             res["bve"] = {"error": f"{type(exc).__name__}: {exc}"}
-    if rank == 0 and not args.no_bve3:
+    if rank == 0 and not (args.no_bve3 and args.no_kernels):
         del q, mesh, cs
         torch.cuda.empty_cache()
+    if rank == 0 and not args.no_kernels:
+        try:
+            res["kernels"] = bench_kernels(dev)
+        except Exception as exc:
+            res["kernels"] = {"error": f"{type(exc).__name__}: {exc}"}
+    if rank == 0 and not args.no_bve3:
         try:
             res["bve_l7_L1024"] = bench_bve3(args, dev)
         except Exception as exc:
@@ -364,6 +370,97 @@ def bench_rh_error(dev):
     return res
 
 
+def bench_kernels(dev, level=7, L=1024, reps=5, stack=8, warm=True, nvtx=False):
+    """Per-stage times of one BVE step at (level, L) with the Gaussian-jet
+    initial condition, each stage timed alone with CUDA events (average of
+    `reps` after one warm-up) and set against its algorithmic bytes (or
+    Legendre FLOPs):
+      locate        2^22 uniform queries: 24 B in, 4 B id + 24 B bcc out;
+      compose_grid  the MWSS sample points through `stack` submaps (no
+                    Jacobian): 48 B per point + 96 B per vertex per submap;
+      assemble_map  jets -> coefficient records: 96 B per vertex + 384 B
+                    factors + 512 B record per triangle;
+      assemble_vel  the same on the velocity mesh;
+      advect_rk4    5 Nv points x (24 in + 24 out) + 96 B per vertex jets
+                    + min(288 B per velocity vertex, 20 Nv x 3 x 288 B);
+      vorticity     32 B per sample point + 32 B per velocity vertex
+                    (scalar spline jets);
+      sht_forward / sht_velocity: Legendre FLOPs 2 (L+1)^2 L (forward,
+                    2 real columns) and 24 (L/2+1) L (L+1) (12 inverse
+                    fields), FFTs and small kernels included in the time."""
+    import torch
+    from cmm_gpu import native
+    from cmm_gpu.meshgen import icosahedral_mesh, random_sphere_points
+    from cmm_gpu.workloads import spectral_perturbation
+    from cmm_gpu.spherical_simulations import BVESolver, Vorticity
+    peak, how = peaks()
+    pert = spectral_perturbation(64, seed=3, slope=-2.0, rms=0.1)
+    vort = Vorticity("gaussian_zonal_jets", (10.0, 0.1, 4, 0.5, -0.5, 1.1, -1.1), spline_sh=pert)
+    verts, tris = icosahedral_mesh(level)
+    nv, nt = len(verts), len(tris)
+    nvu, ntu, Qg = 2 + (L - 1) * 2 * L, 4 * L * (L - 1), (L + 1) * 2 * L
+    out = {"level": level, "L": L, "reps": reps, "stack": stack, "peak_gbs": peak, "peak_kind": how}
+    stream = torch.cuda.current_stream(dev)
+
+    def timed(fn):
+        if warm:
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        if nvtx:   # the profiler captures the timed launches only
+            torch.cuda.nvtx.range_push("timed")
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        if nvtx:
+            torch.cuda.nvtx.range_pop()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    def put(name, ms, nbytes=None, flops=None):
+        d = {"ms": ms}
+        if nbytes is not None:
+            d.update(bytes=nbytes, gbs=nbytes / ms / 1e6, frac_hbm=nbytes / ms / 1e6 / peak)
+        if flops is not None:
+            d.update(flops=flops, tflops=flops / ms / 1e9)
+        out[name] = d
+
+    for form in ("fp64", "split_bf16"):
+        s = BVESolver(verts, tris, level, L, 1000, 1.0, vort, n_maps=10, precision=form)
+        s.bootstrap()
+        s.step()
+        torch.cuda.synchronize()
+        f_fwd = 2.0 * (L + 1) ** 2 * L
+        f_inv = 24.0 * (L // 2 + 1) * L * (L + 1)
+        put(f"sht_forward_{form}", timed(lambda: s.sht.forward(s.omega)), flops=f_fwd)
+        put(f"sht_velocity_{form}", timed(lambda: s.sht.velocity(s.vm, s.omega, jets=s.vel_jets)),
+            flops=f_fwd + f_inv)
+        if form == "split_bf16":
+            break
+        q = torch.from_numpy(random_sphere_points(1 << 22, seed=5)).to(dev)
+        put("locate", timed(lambda: s.mesh.locate(q)), nbytes=(1 << 22) * 52)
+        del q
+        cs = [s.coeffs_cur] * stack
+        put("compose_grid", timed(lambda: s.mesh.compose(cs, s.sample_pts, out=s.X)),
+            nbytes=Qg * 48 + stack * 96 * nv)
+        put("assemble_map", timed(lambda: s.mesh.assemble(s.jets, out=s.stack[0])),
+            nbytes=nv * 96 + nt * (384 + 512))
+        put("assemble_vel", timed(lambda: s.vm.assemble(s.vel_jets, out=s.vel_coeffs[0])),
+            nbytes=nvu * 96 + ntu * (384 + 512))
+        prev, jt = s.coeffs_cur.clone(), torch.empty_like(s.jets)
+        put("advect_rk4", timed(lambda: s.mesh.advect_project(
+            s.vm, s.vel_coeffs, s.ts0, native.RK4, 0.0, s.dt, s.s_pts, s.tan, prev, jets=jt,
+            work=s.work)),
+            nbytes=5 * nv * 48 + 96 * nv + min(288 * nvu, 20 * nv * 3 * 288))
+        put("vorticity", timed(lambda: s.vm.vorticity(s.vort.kind, s.vort.params, s.X, s.rot,
+                                                      omega=s.omega, spline=s.spline)),
+            nbytes=Qg * 32 + 32 * nvu)
+        del s, cs, prev, jt
+        torch.cuda.empty_cache()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -375,6 +472,13 @@ def main():
     ap.add_argument("--no-bve", action="store_true")
     ap.add_argument("--no-bve3", action="store_true", help="skip the level-7 / L=1024 BVE run")
     ap.add_argument("--logq", type=int, default=24, help="log2 queries per GPU (profiling cases)")
+    ap.add_argument("--no-kernels", action="store_true", help="skip the per-stage timings")
+    ap.add_argument("--kernels-only", action="store_true",
+                    help="print only the per-stage timings of one BVE step (profiling runs)")
+    ap.add_argument("--kernels-level", type=int, default=7)
+    ap.add_argument("--kernels-L", type=int, default=1024)
+    ap.add_argument("--kernels-profile", action="store_true",
+                    help="one untimed-warm-up-free launch per stage inside an NVTX range 'timed'")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     LOGQ = args.logq
@@ -407,6 +511,13 @@ def main():
         return
 
     import torch
+    if args.kernels_only:
+        dev = torch.device("cuda", 0)
+        torch.cuda.set_device(dev)
+        prof = args.kernels_profile
+        print(json.dumps({"kernels": bench_kernels(dev, args.kernels_level, args.kernels_L,
+                                                   reps=1 if prof else 5, warm=not prof, nvtx=prof)}))
+        return
     if world > 1:
         torch.distributed.init_process_group("nccl")
     cpu = None
@@ -443,7 +554,7 @@ def main():
                 "h2d_bytes_per_step": Q * 24, "d2h_bytes_per_step": Q * (24 + 4 + 72)},
         "clocks": r["clocks"], "gpu_launches": r["launches"],
     }
-    for key in ("bve", "rh_error", "bve_l7_L1024"):
+    for key in ("bve", "rh_error", "bve_l7_L1024", "kernels"):
         if key in r:
             line[key] = r[key]
     print(json.dumps(line))

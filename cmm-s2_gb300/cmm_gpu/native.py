@@ -42,6 +42,7 @@ _SIGS = {
     "cmm_sht_create": (_i, [_i, ctypes.POINTER(_p)]),
     "cmm_sht_set_precision": (_i, [_p, _i]),
     "cmm_sht_status": (_i, [_p, _p, ctypes.POINTER(_i), _i]),
+    "cmm_sht_power": (_i, [_p, _p, _p, _p]),
     "cmm_sht_destroy": (_i, [_p]),
     "cmm_sht_forward": (_i, [_p, _p, _p, _p]),
     "cmm_sht_inverse": (_i, [_p, _p, _i, _p, _p]),
@@ -287,6 +288,13 @@ class Sht:
         check(lib.cmm_sht_inverse(self.h, _ptr(alm), nf, _ptr(out), _stream(alm.device)),
               "cmm_sht_inverse")
         return out[0] if alm.dim() == 2 else out
+
+    def power(self, alm):
+        """Angular power per degree, sum over m = -l..l of |a_lm|^2 (L,)."""
+        alm = _dev(alm, torch.complex128)
+        out = torch.empty(self.L, dtype=torch.float64, device=alm.device)
+        check(lib.cmm_sht_power(self.h, _ptr(alm), _ptr(out), _stream(alm.device)), "cmm_sht_power")
+        return out
 
     def scalar_jets(self, velmesh, alm, jets=None):
         """Scalar jets (4, Nv_u) of the field with coefficients alm [m,l]."""

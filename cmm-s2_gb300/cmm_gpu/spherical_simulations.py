@@ -66,8 +66,11 @@ class BVESolver:
         self.vm = native.VelMesh(L, theta, phi, grid, vverts, device=dev.index)
         self.sht = native.Sht(L, device=dev.index)
         if precision == "split_bf16":
+            self.precision_mode = native.Sht.SPLIT_BF16
             self.sht.set_precision(native.Sht.SPLIT_BF16)
-        elif precision != "fp64":
+        elif precision == "fp64":
+            self.precision_mode = native.Sht.FP64
+        else:
             raise ValueError("precision must be 'fp64' or 'split_bf16'")
         tan, s_pts = stencil_frames(verts)
         self.tan = torch.from_numpy(np.ascontiguousarray(tan)).to(dev)
@@ -96,6 +99,8 @@ class BVESolver:
             from .workloads import real_to_complex_sh
             alm = torch.from_numpy(real_to_complex_sh(self.vort.spline_sh, L)).to(dev)
             self.spline = self.vm.assemble(self.sht.scalar_jets(self.vm, alm))
+        self.cos_grid = self.sample_pts[:, 2].reshape(L + 1, 2 * L)
+        self.diag0 = None
         self.Nc = 0
         self.ts0 = float(self.tspan[0])
         self.nvs = 1
@@ -136,6 +141,7 @@ class BVESolver:
         """spherical_simulations.py:216-261."""
         dt = self.dt
         self._project(self.sample_pts, 0, rot=0.0)   # omega0 on the grid itself
+        self.diag0 = self.invariants()
         self._advect(native.EULER, 0.0, None)
         self._project(self._sample_single(), 1)
         self.nvs = 2
@@ -179,6 +185,64 @@ class BVESolver:
         for _ in range(n):
             self.step()
         return self
+
+    # ----------------------------------------------------- diagnostics
+    def invariants(self):
+        """Enstrophy and energy of the absolute vorticity omega + 2 Omega
+        cos(theta) on the MWSS grid, from its FP64 transform
+        (figures/data_gen_convergence.py:58-62, 90-95):
+        enstrophy = sum_lm |w_lm|^2, energy = 0.5 (p_0 + sum_l p_l / (l(l+1)))
+        with p_l = sum_m |w_lm|^2 (energy_spectrum,
+        core/spherical_harmonic_tools.py:157-163)."""
+        mode = self.precision_mode
+        if mode != native.Sht.FP64:
+            self.sht.set_precision(native.Sht.FP64)
+        try:
+            alm = self.sht.forward(self.omega + 2.0 * self.rot * self.cos_grid)
+            p = self.sht.power(alm)
+        finally:
+            if mode != native.Sht.FP64:
+                self.sht.set_precision(mode)
+        ell = torch.arange(1, self.L, dtype=torch.float64, device=p.device)
+        return {"enstrophy": float(p.sum()),
+                "energy": float(0.5 * (p[0] + (p[1:] / (ell * (ell + 1))).sum()))}
+
+    def diagnostics(self, omega_true=None, jacobian=True):
+        """Accuracy and conservation of the current state on the MWSS grid:
+        enstrophy / energy and their drift relative to t = 0; with
+        omega_true (exact relative vorticity on the grid, (L+1, 2L)) the
+        L_inf and L2 errors relative to max |omega_true| and its RMS
+        (data_gen_convergence.py:84-86); with `jacobian`, the largest
+        deviation of the back-to-label map's tangent Jacobian determinant
+        from 1 over the sample points (the map is area preserving)."""
+        d = self.invariants()
+        if self.diag0 is not None:
+            d["enstrophy_drift"] = abs(d["enstrophy"] - self.diag0["enstrophy"]) / self.diag0["enstrophy"]
+            d["energy_drift"] = abs(d["energy"] - self.diag0["energy"]) / self.diag0["energy"]
+        if omega_true is not None:
+            ot = torch.as_tensor(omega_true, dtype=torch.float64, device=self.device)
+            err = (self.omega - ot).abs()
+            d["linf_rel"] = float(err.max() / ot.abs().max())
+            d["l2_rel"] = float(err.pow(2).mean().sqrt() / ot.pow(2).mean().sqrt())
+        if jacobian:
+            x = self.sample_pts
+            X, J = self.composite(x, want_jac=True)
+            if J is None:
+                d["jac_det_dev"] = 0.0
+            else:
+                a = torch.zeros_like(x)
+                a[:, 0] = 1.0
+                a[x[:, 0].abs() > 0.9, 0] = 0.0
+                a[x[:, 0].abs() > 0.9, 1] = 1.0
+                t1 = torch.linalg.cross(a, x)
+                t1 = t1 / t1.norm(dim=1, keepdim=True)
+                t2 = torch.linalg.cross(x, t1)
+                j1 = torch.einsum("nij,nj->ni", J, t1)
+                j2 = torch.einsum("nij,nj->ni", J, t2)
+                n = X / X.norm(dim=1, keepdim=True)
+                det = (n * torch.linalg.cross(j1, j2)).sum(1)
+                d["jac_det_dev"] = float((det - 1.0).abs().max())
+        return d
 
     # --------------------------------------------------------- outputs
     def composite(self, q, want_jac=False):

@@ -220,6 +220,11 @@ int cmm_sht_set_precision(cmm_sht* plan, int mode) {
   return sht_set_precision(plan, mode);
 }
 
+int cmm_sht_power(cmm_sht* plan, const double* alm, double* power, void* stream) {
+  if (!plan || !alm || !power) return arg_error("cmm_sht_power: null pointer");
+  return sht_power(plan, (const double2*)alm, power, (cudaStream_t)stream);
+}
+
 int cmm_sht_status(cmm_sht* plan, void* stream, int* flags, int clear) {
   if (!plan || !flags) return arg_error("cmm_sht_status: null pointer");
   return sht_status(plan, (cudaStream_t)stream, flags, clear);

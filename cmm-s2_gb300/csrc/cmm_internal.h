@@ -20,6 +20,9 @@ constexpr int kLocStride = 16;
 // used by ordinates 12..17, the centre barycentrics mid[0..2] (ordinate
 // 18) and 3 doubles of padding.
 constexpr int kAsmStride = 48;
+// On the device the 45 used factors are stored factor-major,
+// tri_asm[j * nt + t], so that a warp's loads of one factor coalesce.
+constexpr int kAsmFactors = 45;
 constexpr int kCoeffStride3 = 64;   // 19 ordinates x 3 components, padded
 constexpr int kCoeffStride1 = 24;   // 19 ordinates, padded
 
@@ -29,7 +32,7 @@ struct MeshView {
   const double* verts;      // (nv,4) x,y,z,0
   const int4* tri_v;        // (nt) vertex ids of each reference row
   const double* tri_loc;    // (nt, kLocStride)
-  const double* tri_asm;    // (nt, kAsmStride)
+  const double* tri_asm;    // (kAsmFactors, nt), factor-major
   const double* root;       // 20 faces x 12: centroid(3), edge normals ab,bc,ca (9)
   const float* root_f;      // same, FP32
   const int* root_adj;      // 20 x 3: face across edge ab, bc, ca
@@ -144,16 +147,20 @@ int sht_inverse(cmm_sht* p, const double2* alm, int nf, double* samples, cudaStr
 int sht_velocity(cmm_sht* p, const cmm_mesh* vm, const double* omega, double2* psi_out,
                  double* jets, cudaStream_t s);
 int sht_scalar_jets(cmm_sht* p, const cmm_mesh* vm, const double2* alm, double* jets, cudaStream_t s);
+int sht_power(cmm_sht* p, const double2* alm, double* power, cudaStream_t s);
 int sht_set_precision(cmm_sht* p, int mode);
 int sht_status(cmm_sht* p, cudaStream_t s, int* flags, int clear);
 
 // split-BF16 tensor-core Legendre synthesis (sht_tc.cu)
+// Upload per-triangle factors (nt, kAsmStride) factor-major (kAsmFactors, nt).
+int upload_asm_factors(DeviceBuffer& dst, const std::vector<double>& asmf, int nt);
+
 struct TcPlan;
 int tc_plan_create(int L, const double* ct_rings, const double* pmm_rings, const double* ct_fine,
                    const double* pmm_fine, const double* ra, const double* rb, TcPlan** out);
 void tc_plan_destroy(TcPlan* p);
 size_t tc_plan_bytes(const TcPlan* p);
-int tc_synthesis(TcPlan* p, const double2* fields, double2* S, int* status, cudaStream_t s);
-int tc_analysis(TcPlan* p, const double2* fine, const double* w, double2* alm, int* status,
+int tc_synthesis(TcPlan* p, const double2* fields, float2* S, int* status, cudaStream_t s);
+int tc_analysis(TcPlan* p, const float2* fine, const double* w, double2* alm, int* status,
                 cudaStream_t s);
 }  // namespace cmm

@@ -231,7 +231,7 @@ __device__ __forceinline__ D3 gridpt(const MeshView& m, int ring, int p) {
 // near-row corrections and the diagonal side test
 // (structure_spherical_triangulation.inds / containing_simplex_and_bcc_structured,
 // cmm_s2/core/mesh_functions.py:201-282).
-__device__ __forceinline__ int latlon_locate(const MeshView& m, double x, double y, double z) {
+static __device__ __noinline__ int latlon_locate_exact(const MeshView& m, double x, double y, double z) {
   const int N = 2 * m.L, M = m.L + 1;
   double phi = np_remainder(atan2(y, x) + kTwoPi, kTwoPi);
   const double rho = sqrt(__dadd_rn(__dmul_rn(y, y), __dmul_rn(x, x)));
@@ -261,6 +261,50 @@ __device__ __forceinline__ int latlon_locate(const MeshView& m, double x, double
       const D3 n = cross(gridpt(m, theta_l + 1, phi_l), gridpt(m, theta_l + 1, phi_p1));
       if (-dot(n, q0) > 0.0) theta_l += 1;
     }
+  }
+  if (theta_l == 0) return phi_l;
+  if (theta_l == M - 2) return 2 * N * (M - 2) - N + phi_l;
+  const D3 n = cross(gridpt(m, theta_l, phi_l), gridpt(m, theta_l + 1, phi_p1));
+  const int s = (-dot(n, q) > 0.0) ? 1 : 0;
+  return N + 2 * (N * (theta_l - 1) + phi_l) + s;
+}
+
+// The same location with the angles taken in FP32 (FP64 atan2/fmod cost
+// ~100 FP64 instructions on a part whose FP64 rate is 1/58 of FP32): the
+// cell indices and the row-correction thresholds are read off the FP32
+// angles when every fractional part is farther than the FP32 error bound
+// (2e-6 rad, scaled to cell units) from a decision boundary; the sign tests
+// then run in FP64 against q and are trusted when |n.q| > 1e-13 (the
+// re-synthesised point q0 of the reference differs from q by ~1e-16).
+// Otherwise the exact FP64 path decides, so both give the same triangle.
+__device__ __forceinline__ int latlon_locate(const MeshView& m, double x, double y, double z) {
+  const int N = 2 * m.L, M = m.L + 1;
+  const float xf = (float)x, yf = (float)y, zf = (float)z;
+  float phif = atan2f(yf, xf);
+  if (phif < 0.f) phif += 6.28318530717958647692f;
+  const float thef = atan2f(sqrtf(xf * xf + yf * yf), zf);
+  const float u = (phif - (float)m.phi[0]) / (float)m.dphi;
+  const float v = (thef - (float)m.theta[0]) / (float)m.dthe;
+  const float du = 2e-6f / (float)m.dphi, dv = 2e-6f / (float)m.dthe;
+  const float uf = floorf(u), vf = floorf(v);
+  const float fu = u - uf, fv = v - vf;
+  const int phi_l = (int)uf;
+  int theta_l = (int)vf;
+  if (!(fu > du && fu < 1.f - du && fv > dv && fv < 1.f - dv && fabsf(fv - 0.03f) > dv &&
+        fabsf(fv - 0.85f) > dv && phi_l >= 0 && phi_l < N && theta_l >= 0 && theta_l <= M - 2))
+    return latlon_locate_exact(m, x, y, z);
+  const int phi_p1 = (phi_l + 1) % N;
+  const D3 q = D3{x, y, z};
+  const bool row_lo = fv <= 0.03f && theta_l != 0;
+  const bool row_hi = !row_lo && fv > 0.85f && theta_l != M - 2;
+  if (row_lo) {
+    const double d = dot(cross(gridpt(m, theta_l, phi_l), gridpt(m, theta_l, phi_p1)), q);
+    if (fabs(d) <= 1e-13) return latlon_locate_exact(m, x, y, z);
+    if (d > 0.0) theta_l -= 1;
+  } else if (row_hi) {
+    const double d = -dot(cross(gridpt(m, theta_l + 1, phi_l), gridpt(m, theta_l + 1, phi_p1)), q);
+    if (fabs(d) <= 1e-13) return latlon_locate_exact(m, x, y, z);
+    if (d > 0.0) theta_l += 1;
   }
   if (theta_l == 0) return phi_l;
   if (theta_l == M - 2) return 2 * N * (M - 2) - N + phi_l;

@@ -82,52 +82,73 @@ __global__ void __launch_bounds__(kBlock) locate_kernel(MeshView m, const double
 
 // One triangle per thread: the 19 ordinates of each component from the
 // jets of its three vertices (assemble_coefficients,
-// cmm_s2/core/spherical_spline.py:300-337) using the per-triangle factors.
+// cmm_s2/core/spherical_spline.py:300-337) using the per-triangle factors
+// (factor-major, coalesced loads).  The block's records are staged in
+// shared memory (rows padded to stride+1 doubles against bank conflicts)
+// and written out as one contiguous, coalesced range, record padding
+// included (zeros).
+constexpr int kAsmTri = 64;   // triangles (threads) per block
+
 template <int NC>
-__global__ void __launch_bounds__(128) assemble_kernel(MeshView m, const double* __restrict__ jets,
-                                                       double* __restrict__ coeffs, int stride) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= m.nt) return;
-  const int nv = m.nv;
-  const int4 tv = m.tri_v[t];
-  const int vid[3] = {tv.x, tv.y, tv.z};
-  const double* A = m.tri_asm + (int64_t)t * kAsmStride;
-  double* out = coeffs + (int64_t)t * stride;
-  const int corner[9] = {0, 0, 0, 1, 1, 1, 2, 2, 2};
+__global__ void __launch_bounds__(kAsmTri) assemble_kernel(MeshView m, const double* __restrict__ jets,
+                                                           double* __restrict__ coeffs) {
+  constexpr int kStride = NC == 3 ? kCoeffStride3 : kCoeffStride1;
+  constexpr int kRow = kStride + 1;
+  __shared__ double rec[kAsmTri * kRow];
+  const int t0 = blockIdx.x * kAsmTri;
+  const int nblk = min(kAsmTri, m.nt - t0);
+  const int tl = threadIdx.x, t = t0 + tl;
+  double* out = rec + tl * kRow;
+  if (tl < nblk) {
+    const int nv = m.nv, nt = m.nt;
+    const int4 tv = m.tri_v[t];
+    const int vid[3] = {tv.x, tv.y, tv.z};
+    const double* A = m.tri_asm + t;   // factor j at A[j * nt]
+    const int corner[9] = {0, 0, 0, 1, 1, 1, 2, 2, 2};
 #pragma unroll
-  for (int k = 0; k < NC; ++k) {
-    double f[3], c[19];
+    for (int k = 0; k < NC; ++k) {
+      double f[3], c[19];
 #pragma unroll
-    for (int v = 0; v < 3; ++v) f[v] = __ldg(jets + (int64_t)(k * 4) * nv + vid[v]);
-    c[0] = f[0];
-    c[1] = f[1];
-    c[2] = f[2];
+      for (int v = 0; v < 3; ++v) f[v] = __ldg(jets + (int64_t)(k * 4) * nv + vid[v]);
+      c[0] = f[0];
+      c[1] = f[1];
+      c[2] = f[2];
 #pragma unroll
-    for (int o = 0; o < 9; ++o) {
-      const int v = vid[corner[o]];
-      double gx, gy, gz;
-      if (NC == 3) {  // d_j f_k = jets[j][1+k]
-        gx = __ldg(jets + (int64_t)(0 * 4 + 1 + k) * nv + v);
-        gy = __ldg(jets + (int64_t)(1 * 4 + 1 + k) * nv + v);
-        gz = __ldg(jets + (int64_t)(2 * 4 + 1 + k) * nv + v);
-      } else {  // scalar: d_j f = jets[1+j]
-        gx = __ldg(jets + (int64_t)1 * nv + v);
-        gy = __ldg(jets + (int64_t)2 * nv + v);
-        gz = __ldg(jets + (int64_t)3 * nv + v);
+      for (int o = 0; o < 9; ++o) {
+        const int v = vid[corner[o]];
+        double gx, gy, gz;
+        if (NC == 3) {  // d_j f_k = jets[j][1+k]
+          gx = __ldg(jets + (int64_t)(0 * 4 + 1 + k) * nv + v);
+          gy = __ldg(jets + (int64_t)(1 * 4 + 1 + k) * nv + v);
+          gz = __ldg(jets + (int64_t)(2 * 4 + 1 + k) * nv + v);
+        } else {  // scalar: d_j f = jets[1+j]
+          gx = __ldg(jets + (int64_t)1 * nv + v);
+          gy = __ldg(jets + (int64_t)2 * nv + v);
+          gz = __ldg(jets + (int64_t)3 * nv + v);
+        }
+        const double a0 = __ldg(A + (int64_t)(4 * o) * nt), a1 = __ldg(A + (int64_t)(4 * o + 1) * nt),
+                     a2 = __ldg(A + (int64_t)(4 * o + 2) * nt), a3 = __ldg(A + (int64_t)(4 * o + 3) * nt);
+        c[3 + o] = a0 * gx + a1 * gy + a2 * gz - a3 * f[corner[o]];
       }
-      const double* a = A + 4 * o;
-      c[3 + o] = a[0] * gx + a[1] * gy + a[2] * gz - a[3] * f[corner[o]];
-    }
-    c[12] = A[36] * c[3] + A[37] * c[8];
-    c[13] = A[38] * c[6] + A[39] * c[11];
-    c[14] = A[41] * c[9] + A[40] * c[5];
-    c[15] = A[36] * c[4] + A[37] * c[7];
-    c[16] = A[38] * c[7] + A[39] * c[10];
-    c[17] = A[40] * c[4] + A[41] * c[10];
-    c[18] = A[42] * c[4] + A[43] * c[7] + A[44] * c[10];
+      double e[9];
 #pragma unroll
-    for (int o = 0; o < 19; ++o) out[NC * o + k] = c[o];
+      for (int j = 0; j < 9; ++j) e[j] = __ldg(A + (int64_t)(36 + j) * nt);
+      c[12] = e[0] * c[3] + e[1] * c[8];
+      c[13] = e[2] * c[6] + e[3] * c[11];
+      c[14] = e[5] * c[9] + e[4] * c[5];
+      c[15] = e[0] * c[4] + e[1] * c[7];
+      c[16] = e[2] * c[7] + e[3] * c[10];
+      c[17] = e[4] * c[4] + e[5] * c[10];
+      c[18] = e[6] * c[4] + e[7] * c[7] + e[8] * c[10];
+#pragma unroll
+      for (int o = 0; o < 19; ++o) out[NC * o + k] = c[o];
+    }
+#pragma unroll
+    for (int j = 19 * NC; j < kStride; ++j) out[j] = 0.0;
   }
+  __syncthreads();
+  double* dst = coeffs + (int64_t)t0 * kStride;
+  for (int i = tl; i < nblk * kStride; i += kAsmTri) dst[i] = rec[(i / kStride) * kRow + i % kStride];
 }
 
 template <bool JAC>
@@ -246,11 +267,11 @@ int launch_locate(const MeshView& m, const double* q, int64_t n, int32_t* tri, d
 
 int launch_assemble(const MeshView& m, const double* jets, int ncomp, double* coeffs,
                     cudaStream_t s) {
-  const int blocks = (m.nt + 127) / 128;
+  const int blocks = (m.nt + kAsmTri - 1) / kAsmTri;
   if (ncomp == 3)
-    assemble_kernel<3><<<blocks, 128, 0, s>>>(m, jets, coeffs, kCoeffStride3);
+    assemble_kernel<3><<<blocks, kAsmTri, 0, s>>>(m, jets, coeffs);
   else
-    assemble_kernel<1><<<blocks, 128, 0, s>>>(m, jets, coeffs, kCoeffStride1);
+    assemble_kernel<1><<<blocks, kAsmTri, 0, s>>>(m, jets, coeffs);
   return check_launch("assemble_kernel");
 }
 

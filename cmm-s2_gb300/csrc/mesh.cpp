@@ -290,13 +290,20 @@ int build_host(const double* verts, int nv, const int32_t* tris, int nt, int lev
   return CMM_OK;
 }
 
+int upload_asm_factors(DeviceBuffer& dst, const std::vector<double>& asmf, int nt) {
+  std::vector<double> soa((size_t)kAsmFactors * nt);
+  for (int t = 0; t < nt; ++t)
+    for (int j = 0; j < kAsmFactors; ++j) soa[(size_t)j * nt + t] = asmf[(size_t)t * kAsmStride + j];
+  return dst.upload(soa.data(), soa.size() * 8);
+}
+
 int upload_mesh(const HostMesh& h, cmm_mesh* m) {
   const int level = h.level, nv = h.nv, nt = h.nt;
   int rc;
   if ((rc = m->verts.upload(h.vpad.data(), h.vpad.size() * 8))) return rc;
   if ((rc = m->tri_v.upload(h.tv.data(), h.tv.size() * sizeof(int4)))) return rc;
   if ((rc = m->tri_loc.upload(h.loc.data(), h.loc.size() * 8))) return rc;
-  if ((rc = m->tri_asm.upload(h.asmf.data(), h.asmf.size() * 8))) return rc;
+  if ((rc = upload_asm_factors(m->tri_asm, h.asmf, nt))) return rc;
   if ((rc = m->root.upload(h.root.data(), h.root.size() * 8))) return rc;
   {
     std::vector<float> rf(h.root.begin(), h.root.end());

@@ -36,31 +36,42 @@ constexpr int kSynthBlock = 64;
 constexpr int kLChunk = 32;
 
 __device__ __forceinline__ double2 cmul(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
+__device__ __forceinline__ float2 cmul(float2 a, double s) {
+  return make_float2(a.x * (float)s, a.y * (float)s);
+}
 
 // ----------------------------------------------------------------- forward
+// C = double2 (FP64 form) or float2 (ring FFTs of the split-BF16 form).
 // F (L+1, L+1) ring spectra -> torus columns G (2L, L): G[t][m].
-__global__ void torus_kernel(const double2* __restrict__ F, int L, double2* __restrict__ G) {
+template <typename C>
+__global__ void torus_kernel(const C* __restrict__ F, int L, C* __restrict__ G) {
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
   const int t = blockIdx.y;
   if (m >= L || t >= 2 * L) return;
   const double s = M_PI / L;
-  double2 v;
+  C v;
   if (t <= L) {
     v = F[(int64_t)t * (L + 1) + m];
   } else {
     v = F[(int64_t)(2 * L - t) * (L + 1) + m];
-    if (m & 1) v = make_double2(-v.x, -v.y);
+    if (m & 1) {
+      v.x = -v.x;
+      v.y = -v.y;
+    }
   }
   G[(int64_t)t * L + m] = cmul(v, s);
 }
 
 // Torus spectrum Gh (2L, L) -> zero-padded H (4L, L), Nyquist split.
-__global__ void pad_kernel(const double2* __restrict__ Gh, int L, double2* __restrict__ H) {
+template <typename C>
+__global__ void pad_kernel(const C* __restrict__ Gh, int L, C* __restrict__ H) {
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
   const int k = blockIdx.y;  // 0..4L-1
   if (m >= L || k >= 4 * L) return;
   const double s = 1.0 / (2 * L);
-  double2 v = make_double2(0.0, 0.0);
+  C v;
+  v.x = 0;
+  v.y = 0;
   if (k < L) {
     v = Gh[(int64_t)k * L + m];
   } else if (k == L || k == 3 * L) {
@@ -69,6 +80,24 @@ __global__ void pad_kernel(const double2* __restrict__ Gh, int L, double2* __res
     v = Gh[(int64_t)(k - 2 * L) * L + m];
   }
   H[(int64_t)k * L + m] = cmul(v, s);
+}
+
+// Zero the m = L column of nrows spectra rows of length L+1 (an
+// out-of-place C2R transform may overwrite its input).
+__global__ void zero_nyquist_kernel(float2* __restrict__ S, int L, int nrows) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < nrows) S[(int64_t)r * (L + 1) + L] = make_float2(0.f, 0.f);
+}
+
+// FP64 samples -> FP32 (input of the split form's ring FFT).
+__global__ void to_float_kernel(const double* __restrict__ a, int64_t n, float* __restrict__ b) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (float)a[i];
+}
+
+__global__ void to_double_kernel(const float* __restrict__ a, int64_t n, double* __restrict__ b) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (double)a[i];
 }
 
 // Legendre analysis: one block per m; ring pairs (j, 2L-j) of the fine grid
@@ -239,6 +268,27 @@ __global__ void ladder2_kernel(double2* __restrict__ fields, int L) {
   }
 }
 
+// power[l] = sum over all orders -l..l of |a_lm|^2 = |a_l0|^2 + 2 sum_{m>0}
+// |a_lm|^2 (real field); one block per degree.  The summand of
+// energy_spectrum (cmm_s2/core/spherical_harmonic_tools.py:157-163).
+__global__ void power_kernel(const double2* __restrict__ a, int L, double* __restrict__ power) {
+  const int l = blockIdx.x;
+  double s = 0.0;
+  for (int m = threadIdx.x; m <= l; m += blockDim.x) {
+    const double2 v = a[(int64_t)m * L + l];
+    s += (m == 0 ? 1.0 : 2.0) * (v.x * v.x + v.y * v.y);
+  }
+  __shared__ double red[8];
+  for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+    power[l] = t;
+  }
+}
+
 // fields 0..3 = a, iLx a, iLy a, iLz a (project_onto_S12,
 // spherical_harmonic_tools.py:121-123).
 __global__ void scalar_fields_kernel(const double2* __restrict__ a, int L, double2* __restrict__ fields) {
@@ -345,7 +395,8 @@ __global__ void __launch_bounds__(kSynthBlock) synthesis_kernel(const double2* _
 // the 12 synthesised fields on the grid: vals[i][0] = u_i and, with
 // g = (iLx, iLy, iLz) u_i, vals[c][1+i] = (g x X - ((g x X).X/|X|) X)_c;
 // poles from sample 0 of the first and last rings.
-__global__ void jets_kernel(const double* __restrict__ fld, int L, const double* __restrict__ grid,
+template <typename R>
+__global__ void jets_kernel(const R* __restrict__ fld, int L, const double* __restrict__ grid,
                             double* __restrict__ jets) {
   const int N = 2 * L;
   const int64_t nv = 2 + (int64_t)(L - 1) * N;
@@ -362,9 +413,9 @@ __global__ void jets_kernel(const double* __restrict__ fld, int L, const double*
   const double X0 = grid[4 * node], X1 = grid[4 * node + 1], X2 = grid[4 * node + 2];
   const double nX = sqrt(X0 * X0 + X1 * X1 + X2 * X2);
   for (int i = 0; i < 3; ++i) {
-    jets[(int64_t)(i * 4) * nv + v] = fld[i * fs + node];
-    const double g0 = fld[(3 + 3 * i) * fs + node], g1 = fld[(4 + 3 * i) * fs + node],
-                 g2 = fld[(5 + 3 * i) * fs + node];
+    jets[(int64_t)(i * 4) * nv + v] = (double)fld[i * fs + node];
+    const double g0 = (double)fld[(3 + 3 * i) * fs + node], g1 = (double)fld[(4 + 3 * i) * fs + node],
+                 g2 = (double)fld[(5 + 3 * i) * fs + node];
     const double c0 = g1 * X2 - g2 * X1, c1 = g2 * X0 - g0 * X2, c2 = g0 * X1 - g1 * X0;
     const double sc = (c0 * X0 + c1 * X1 + c2 * X2) / nX;
     jets[(int64_t)(0 * 4 + 1 + i) * nv + v] = c0 - sc * X0;
@@ -395,11 +446,19 @@ struct cmm_sht {
   cmm::DeviceBuffer ct_rings, ct_fine, w_fine, pmm_rings, pmm_fine, ra, rb;
   cmm::DeviceBuffer spec, torus, pad, alm, fields, synth, samples, status;
   cmm::TcPlan* tc = nullptr;
+  // split-BF16 form: FP32 ring FFTs and buffers, made with the tc plan
+  cufftHandle f_ring_fwd = 0, f_torus_fwd = 0, f_pad_inv = 0, f_ring_inv = 0;
+  bool have_fplans[4] = {false, false, false, false};
+  cmm::DeviceBuffer f_in, f_spec, f_torus, f_pad, f_synth, f_samples;
   ~cmm_sht() {
     if (have_plans[0]) cufftDestroy(ring_fwd);
     if (have_plans[1]) cufftDestroy(torus_fwd);
     if (have_plans[2]) cufftDestroy(pad_inv);
     if (have_plans[3]) cufftDestroy(ring_inv);
+    if (have_fplans[0]) cufftDestroy(f_ring_fwd);
+    if (have_fplans[1]) cufftDestroy(f_torus_fwd);
+    if (have_fplans[2]) cufftDestroy(f_pad_inv);
+    if (have_fplans[3]) cufftDestroy(f_ring_inv);
     if (tc) cmm::tc_plan_destroy(tc);
   }
 };
@@ -513,11 +572,43 @@ int sht_create(int L, cmm_sht** out) {
 }
 
 static int set_streams(cmm_sht* p, cudaStream_t s) {
-  cufftHandle h[4] = {p->ring_fwd, p->torus_fwd, p->pad_inv, p->ring_inv};
-  for (int k = 0; k < 4; ++k) {
+  cufftHandle h[8] = {p->ring_fwd, p->torus_fwd, p->pad_inv, p->ring_inv,
+                      p->f_ring_fwd, p->f_torus_fwd, p->f_pad_inv, p->f_ring_inv};
+  for (int k = 0; k < 8; ++k) {
+    if (k >= 4 && !p->have_fplans[k - 4]) continue;
     cufftResult r = cufftSetStream(h[k], s);
     if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftSetStream");
   }
+  return CMM_OK;
+}
+
+// FP32 FFT plans and buffers of the split-BF16 form (same shapes as the
+// FP64 plans of sht_create).
+static int make_float_plans(cmm_sht* p) {
+  const int L = p->L;
+  int rc;
+  if ((rc = p->f_in.alloc((size_t)(L + 1) * 2 * L * sizeof(float))) ||
+      (rc = p->f_spec.alloc((size_t)(L + 1) * (L + 1) * sizeof(float2))) ||
+      (rc = p->f_torus.alloc((size_t)2 * L * L * sizeof(float2))) ||
+      (rc = p->f_pad.alloc((size_t)4 * L * L * sizeof(float2))) ||
+      (rc = p->f_synth.alloc((size_t)kFields * (L + 1) * (L + 1) * sizeof(float2))) ||
+      (rc = p->f_samples.alloc((size_t)kFields * (L + 1) * 2 * L * sizeof(float))))
+    return rc;
+  int n2[1] = {2 * L}, n4[1] = {4 * L};
+  int inemb[1] = {2 * L}, onemb[1] = {L + 1}, tn[1] = {2 * L}, pn[1] = {4 * L};
+  int cin[1] = {L + 1}, rout[1] = {2 * L};
+  cufftResult r = cufftPlanMany(&p->f_ring_fwd, 1, n2, inemb, 1, 2 * L, onemb, 1, L + 1, CUFFT_R2C, L + 1);
+  if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftPlanMany(f_ring_fwd)");
+  p->have_fplans[0] = true;
+  r = cufftPlanMany(&p->f_torus_fwd, 1, n2, tn, L, 1, tn, L, 1, CUFFT_C2C, L);
+  if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftPlanMany(f_torus_fwd)");
+  p->have_fplans[1] = true;
+  r = cufftPlanMany(&p->f_pad_inv, 1, n4, pn, L, 1, pn, L, 1, CUFFT_C2C, L);
+  if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftPlanMany(f_pad_inv)");
+  p->have_fplans[2] = true;
+  r = cufftPlanMany(&p->f_ring_inv, 1, n2, cin, 1, L + 1, rout, 1, 2 * L, CUFFT_C2R, kFields * (L + 1));
+  if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftPlanMany(f_ring_inv)");
+  p->have_fplans[3] = true;
   return CMM_OK;
 }
 
@@ -526,22 +617,36 @@ int sht_forward(cmm_sht* p, const double* samples, double2* out, cudaStream_t s)
   const int L = p->L;
   int rc = set_streams(p, s);
   if (rc) return rc;
+  dim3 b(128), g1((L + 127) / 128, 2 * L), g2((L + 127) / 128, 4 * L);
+  if (p->precision == CMM_SHT_SPLIT_BF16) {
+    // ring FFTs in FP32, Legendre analysis on the tensor cores
+    const int64_t ns = (int64_t)(L + 1) * 2 * L;
+    to_float_kernel<<<(int)((ns + 255) / 256), 256, 0, s>>>(samples, ns, (float*)p->f_in.p);
+    if ((rc = check_launch("to_float_kernel"))) return rc;
+    cufftResult r = cufftExecR2C(p->f_ring_fwd, (cufftReal*)p->f_in.p, (cufftComplex*)p->f_spec.p);
+    if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExecR2C");
+    torus_kernel<float2><<<g1, b, 0, s>>>((const float2*)p->f_spec.p, L, (float2*)p->f_torus.p);
+    if ((rc = check_launch("torus_kernel"))) return rc;
+    r = cufftExecC2C(p->f_torus_fwd, (cufftComplex*)p->f_torus.p, (cufftComplex*)p->f_torus.p, CUFFT_FORWARD);
+    if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExecC2C(torus)");
+    pad_kernel<float2><<<g2, b, 0, s>>>((const float2*)p->f_torus.p, L, (float2*)p->f_pad.p);
+    if ((rc = check_launch("pad_kernel"))) return rc;
+    r = cufftExecC2C(p->f_pad_inv, (cufftComplex*)p->f_pad.p, (cufftComplex*)p->f_pad.p, CUFFT_INVERSE);
+    if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExecC2C(pad)");
+    return tc_analysis(p->tc, (const float2*)p->f_pad.p, (const double*)p->w_fine.p, out,
+                       (int*)p->status.p, s);
+  }
   cufftResult r = cufftExecD2Z(p->ring_fwd, (cufftDoubleReal*)samples, (cufftDoubleComplex*)p->spec.p);
   if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExecD2Z");
-  dim3 b(128), g1((L + 127) / 128, 2 * L);
-  torus_kernel<<<g1, b, 0, s>>>((const double2*)p->spec.p, L, (double2*)p->torus.p);
+  torus_kernel<double2><<<g1, b, 0, s>>>((const double2*)p->spec.p, L, (double2*)p->torus.p);
   if ((rc = check_launch("torus_kernel"))) return rc;
   r = cufftExecZ2Z(p->torus_fwd, (cufftDoubleComplex*)p->torus.p, (cufftDoubleComplex*)p->torus.p,
                    CUFFT_FORWARD);
   if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExecZ2Z(torus)");
-  dim3 g2((L + 127) / 128, 4 * L);
-  pad_kernel<<<g2, b, 0, s>>>((const double2*)p->torus.p, L, (double2*)p->pad.p);
+  pad_kernel<double2><<<g2, b, 0, s>>>((const double2*)p->torus.p, L, (double2*)p->pad.p);
   if ((rc = check_launch("pad_kernel"))) return rc;
   r = cufftExecZ2Z(p->pad_inv, (cufftDoubleComplex*)p->pad.p, (cufftDoubleComplex*)p->pad.p, CUFFT_INVERSE);
   if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExecZ2Z(pad)");
-  if (p->precision == CMM_SHT_SPLIT_BF16)
-    return tc_analysis(p->tc, (const double2*)p->pad.p, (const double*)p->w_fine.p, out,
-                       (int*)p->status.p, s);
   if (L + 1 > 8 * 256) {
     set_last_error("sht_forward: L too large for the analysis kernel");
     return CMM_ERR_UNSUPPORTED;
@@ -557,15 +662,28 @@ int sht_inverse(cmm_sht* p, const double2* alm, int nf, double* samples, cudaStr
   const int L = p->L;
   int rc = set_streams(p, s);
   if (rc) return rc;
+  if (nf == kFields && p->precision == CMM_SHT_SPLIT_BF16) {
+    // tensor-core synthesis into FP32 spectra, FP32 ring FFTs
+    const int nrows = kFields * (L + 1);
+    zero_nyquist_kernel<<<(nrows + 255) / 256, 256, 0, s>>>((float2*)p->f_synth.p, L, nrows);
+    if ((rc = check_launch("zero_nyquist_kernel"))) return rc;
+    if ((rc = tc_synthesis(p->tc, alm, (float2*)p->f_synth.p, (int*)p->status.p, s))) return rc;
+    cufftResult r = cufftExecC2R(p->f_ring_inv, (cufftComplex*)p->f_synth.p, (cufftReal*)p->f_samples.p);
+    if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExecC2R");
+    if (samples) {
+      const int64_t ns = (int64_t)nf * (L + 1) * 2 * L;
+      to_double_kernel<<<(int)((ns + 255) / 256), 256, 0, s>>>((const float*)p->f_samples.p, ns, samples);
+      return check_launch("to_double_kernel");
+    }
+    return CMM_OK;
+  }
   double2* S = (double2*)p->synth.p;
   // all kFields spectra: the batched Z2D below transforms every row
   cudaError_t e = cudaMemsetAsync(S, 0, (size_t)kFields * (L + 1) * (L + 1) * sizeof(double2), s);
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
   const int npair = L / 2 + 1;
   dim3 g(L, (npair + kSynthBlock - 1) / kSynthBlock);
-  if (nf == kFields && p->precision == CMM_SHT_SPLIT_BF16) {
-    if ((rc = tc_synthesis(p->tc, alm, S, (int*)p->status.p, s))) return rc;
-  } else if (nf == kFields)
+  if (nf == kFields)
     synthesis_kernel<kFields><<<g, kSynthBlock, 0, s>>>(alm, L, (const double*)p->ct_rings.p,
                                                         (const double*)p->pmm_rings.p,
                                                         (const double*)p->ra.p, (const double*)p->rb.p, S);
@@ -581,8 +699,7 @@ int sht_inverse(cmm_sht* p, const double2* alm, int nf, double* samples, cudaStr
     set_last_error("sht_inverse: nf must be 1, 4 or 12");
     return CMM_ERR_ARG;
   }
-  if (!(nf == kFields && p->precision == CMM_SHT_SPLIT_BF16) && (rc = check_launch("synthesis_kernel")))
-    return rc;
+  if ((rc = check_launch("synthesis_kernel"))) return rc;
   // Z2D over kFields*(L+1) rows; only the first nf*(L+1) rows matter
   cufftResult r = cufftExecZ2D(p->ring_inv, (cufftDoubleComplex*)S, (cufftDoubleReal*)p->samples.p);
   if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExecZ2D");
@@ -617,8 +734,18 @@ int sht_velocity(cmm_sht* p, const cmm_mesh* vm, const double* omega, double2* p
   if ((rc = check_launch("ladder2_kernel"))) return rc;
   if ((rc = sht_inverse(p, F, kFields, nullptr, s))) return rc;
   const int64_t nv = 2 + (int64_t)(L - 1) * 2 * L;
-  jets_kernel<<<(int)((nv + 127) / 128), 128, 0, s>>>((const double*)p->samples.p, L, vm->view.grid, jets);
+  if (p->precision == CMM_SHT_SPLIT_BF16)
+    jets_kernel<float><<<(int)((nv + 127) / 128), 128, 0, s>>>((const float*)p->f_samples.p, L,
+                                                                vm->view.grid, jets);
+  else
+    jets_kernel<double><<<(int)((nv + 127) / 128), 128, 0, s>>>((const double*)p->samples.p, L,
+                                                                 vm->view.grid, jets);
   return check_launch("jets_kernel");
+}
+
+int sht_power(cmm_sht* p, const double2* alm, double* power, cudaStream_t s) {
+  power_kernel<<<p->L, 256, 0, s>>>(alm, p->L, power);
+  return check_launch("power_kernel");
 }
 
 int sht_scalar_jets(cmm_sht* p, const cmm_mesh* vm, const double2* alm, double* jets, cudaStream_t s) {
@@ -645,6 +772,7 @@ int sht_set_precision(cmm_sht* p, int mode) {
                             (const double*)p->ct_fine.p, (const double*)p->pmm_fine.p,
                             (const double*)p->ra.p, (const double*)p->rb.p, &p->tc);
     if (rc) return rc;
+    if ((rc = make_float_plans(p))) return rc;
     cudaError_t e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return cuda_fail(e, "cmm_sht_set_precision");
   }

@@ -8,8 +8,9 @@
 // operand is split into two bf16 values, x = hi + lo (hi = bf16(x),
 // lo = bf16(x - hi)), and the product is taken as three tensor-core
 // products hi*hi + hi*lo + lo*hi accumulated in FP32 in tensor memory; the
-// FP32 partial sums of every 64-l chunk are drained into FP64 registers
-// (compensated accumulation across chunks).
+// FP32 partial sums of every 64-l chunk are drained into compensated
+// (Kahan) FP32 register sums, converted to FP64 once at the end (FP64
+// issue per chunk would bind the kernel on GB300's FP64 pipe).
 //
 // Data movement: the Pbar tables (per m, ring block of 128 pairs, l chunk)
 // are built once per plan directly in the shared-memory image the MMA
@@ -103,6 +104,19 @@ __device__ __forceinline__ void tc_fence_before() {
 __device__ __forceinline__ void tc_fence_after() {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
+
+// Compensated (Kahan) FP32 accumulation of the per-chunk partial sums:
+// the running sum s and the negated lost low part c, sum = s - c.
+struct KahanF {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float v) {
+    const float y = v - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
 
 // Shared-memory matrix descriptor: start, leading (k-group) and stride
 // (row-group) byte offsets, descriptor version 1, no swizzle.
@@ -237,7 +251,7 @@ __global__ void build_atab_kernel(TcGeometry g, const double2* __restrict__ fiel
 __global__ void __launch_bounds__(kThreads) synth_tc_kernel(TcGeometry g,
                                                             const unsigned char* __restrict__ ptab,
                                                             const unsigned char* __restrict__ atab,
-                                                            double2* __restrict__ S,
+                                                            float2* __restrict__ S,
                                                             int* __restrict__ status) {
   extern __shared__ __align__(1024) unsigned char smem[];
   unsigned char* sP = smem;                    // kPRecord bytes
@@ -265,9 +279,7 @@ __global__ void __launch_bounds__(kThreads) synth_tc_kernel(TcGeometry g,
   tc_fence_after();
   const uint32_t tmem = tmem_base_s;
   const uint32_t idesc = mma_idesc();
-  double accE[kNUsed], accO[kNUsed];
-#pragma unroll
-  for (int n = 0; n < kNUsed; ++n) accE[n] = accO[n] = 0.0;
+  KahanF accE[kNUsed], accO[kNUsed];
   const int nch = nchunks(L, m);
   uint32_t ph_load = 0, ph_mma = 0;
   for (int c = 0; c < nch; ++c) {
@@ -313,8 +325,8 @@ __global__ void __launch_bounds__(kThreads) synth_tc_kernel(TcGeometry g,
     tmem_ld32(tmem + lane_base + kN, vO);
 #pragma unroll
     for (int n = 0; n < kNUsed; ++n) {
-      accE[n] += (double)vE[n];
-      accO[n] += (double)vO[n];
+      accE[n].add(vE[n]);
+      accO[n].add(vO[n]);
     }
     tc_fence_before();
     __syncthreads();
@@ -329,10 +341,12 @@ __global__ void __launch_bounds__(kThreads) synth_tc_kernel(TcGeometry g,
       for (int f = 0; f < kNUsed / 2; ++f) {
         const int64_t base = (int64_t)f * (L + 1) * row_len;
         S[base + (int64_t)t * row_len + m] =
-            make_double2(accE[2 * f] + accO[2 * f], accE[2 * f + 1] + accO[2 * f + 1]);
+            make_float2((float)(accE[2 * f].value() + accO[2 * f].value()),
+                        (float)(accE[2 * f + 1].value() + accO[2 * f + 1].value()));
         if (L - t != t)
           S[base + (int64_t)(L - t) * row_len + m] =
-              make_double2(accE[2 * f] - accO[2 * f], accE[2 * f + 1] - accO[2 * f + 1]);
+              make_float2((float)(accE[2 * f].value() - accO[2 * f].value()),
+                          (float)(accE[2 * f + 1].value() - accO[2 * f + 1].value()));
       }
     }
   }
@@ -418,8 +432,9 @@ __global__ void build_ftab_kernel(TcFwdGeometry g, const double* __restrict__ ct
 }
 
 // Per transform: weighted, parity-folded fine-ring data -> X tile images
-// per (m, ring chunk).  fine: (4L, L) complex [j][m], rows 0..2L used.
-__global__ void build_xtab_kernel(TcFwdGeometry g, const double2* __restrict__ fine,
+// per (m, ring chunk).  fine: (4L, L) FP32 complex [j][m] from the FP32
+// ring FFTs, rows 0..2L used.
+__global__ void build_xtab_kernel(TcFwdGeometry g, const float2* __restrict__ fine,
                                   const double* __restrict__ w, unsigned char* __restrict__ xtab) {
   const int m = blockIdx.y;
   const int L = g.L;
@@ -430,10 +445,12 @@ __global__ void build_xtab_kernel(TcFwdGeometry g, const double2* __restrict__ f
     const int j = c * kKc + k;
     double v = 0.0;
     if (n < 2 && j <= L) {
-      const double2 a = fine[(int64_t)j * L + m];
+      const float2 af = fine[(int64_t)j * L + m];
+      const double2 a = make_double2(af.x, af.y);
       double2 s;
       if (j < L) {
-        const double2 b = fine[(int64_t)(2 * L - j) * L + m];
+        const float2 bf = fine[(int64_t)(2 * L - j) * L + m];
+        const double2 b = make_double2(bf.x, bf.y);
         s = par == 0 ? make_double2(a.x + b.x, a.y + b.y) : make_double2(a.x - b.x, a.y - b.y);
       } else {
         s = par == 0 ? a : make_double2(0.0, 0.0);
@@ -482,7 +499,7 @@ __global__ void __launch_bounds__(kThreads) analysis_tc_kernel(TcFwdGeometry g,
   tc_fence_after();
   const uint32_t tmem = tmem_base_s;
   const uint32_t idesc = mma_idesc_n16();
-  double aE0 = 0.0, aE1 = 0.0, aO0 = 0.0, aO1 = 0.0;
+  KahanF aE0, aE1, aO0, aO1;
   uint32_t ph_load = 0, ph_mma = 0;
   for (int c = 0; c < g.nck; ++c) {
     if (tid == 0) {
@@ -525,10 +542,10 @@ __global__ void __launch_bounds__(kThreads) analysis_tc_kernel(TcFwdGeometry g,
     const uint32_t lane_base = (uint32_t)(32 * warp) << 16;
     tmem_ld16(tmem + lane_base, vE);
     tmem_ld16(tmem + lane_base + kNA, vO);
-    aE0 += (double)vE[0];
-    aE1 += (double)vE[1];
-    aO0 += (double)vO[0];
-    aO1 += (double)vO[1];
+    aE0.add(vE[0]);
+    aE1.add(vE[1]);
+    aO0.add(vO[0]);
+    aO1.add(vO[1]);
     tc_fence_before();
     __syncthreads();
   }
@@ -537,8 +554,8 @@ __global__ void __launch_bounds__(kThreads) analysis_tc_kernel(TcFwdGeometry g,
   } else {
     const int i = lb * kM + tid;
     const int lE = m + 2 * i, lO = m + 1 + 2 * i;
-    if (lE < L) alm[(int64_t)m * L + lE] = make_double2(aE0, aE1);
-    if (lO < L) alm[(int64_t)m * L + lO] = make_double2(aO0, aO1);
+    if (lE < L) alm[(int64_t)m * L + lE] = make_double2(aE0.value(), aE1.value());
+    if (lO < L) alm[(int64_t)m * L + lO] = make_double2(aO0.value(), aO1.value());
   }
   tc_fence_before();
   __syncthreads();
@@ -638,7 +655,7 @@ size_t tc_plan_bytes(const TcPlan* p) {
   return p->ptab.bytes + p->atab.bytes + p->ftab.bytes + p->xtab.bytes;
 }
 
-int tc_synthesis(TcPlan* p, const double2* fields, double2* S, int* status, cudaStream_t s) {
+int tc_synthesis(TcPlan* p, const double2* fields, float2* S, int* status, cudaStream_t s) {
   TcGeometry g{p->L, p->npair, p->nrb, (const int*)p->cbase.p};
   build_atab_kernel<<<dim3(16, p->L), 256, 0, s>>>(g, fields, (unsigned char*)p->atab.p);
   int rc = check("build_atab_kernel");
@@ -650,7 +667,7 @@ int tc_synthesis(TcPlan* p, const double2* fields, double2* S, int* status, cuda
 
 // fine (4L, L) complex after the padded inverse transform, rows 0..2L;
 // w the 2L+1 Clenshaw-Curtis weights -> alm[m][l], l >= m.
-int tc_analysis(TcPlan* p, const double2* fine, const double* w, double2* alm, int* status,
+int tc_analysis(TcPlan* p, const float2* fine, const double* w, double2* alm, int* status,
                 cudaStream_t s) {
   const int L = p->L;
   TcFwdGeometry g{L, p->nck, (const int*)p->lbase.p};

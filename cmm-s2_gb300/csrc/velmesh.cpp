@@ -62,7 +62,7 @@ int build_latlon(int L, const double* theta, const double* phi, const double* gr
   if ((rc = m->verts.upload(vpad.data(), vpad.size() * 8))) return rc;
   if ((rc = m->tri_v.upload(tv.data(), tv.size() * sizeof(int4)))) return rc;
   if ((rc = m->tri_loc.upload(loc.data(), loc.size() * 8))) return rc;
-  if ((rc = m->tri_asm.upload(asmf.data(), asmf.size() * 8))) return rc;
+  if ((rc = upload_asm_factors(m->tri_asm, asmf, nt))) return rc;
   if ((rc = m->theta.upload(theta, (size_t)M * 8))) return rc;
   if ((rc = m->phi.upload(phi, (size_t)N * 8))) return rc;
   if ((rc = m->grid.upload(gpad.data(), gpad.size() * 8))) return rc;

@@ -233,9 +233,12 @@ int cmm_sht_destroy(cmm_sht* plan);
  * cmm_sht_inverse: CMM_SHT_FP64 (default; FP64 recurrence and sums) or
  * CMM_SHT_SPLIT_BF16: each factor split into bf16 hi + lo, products
  * hi*hi + hi*lo + lo*hi on the tensor cores (tcgen05) accumulated in FP32
- * per 64-degree chunk and in FP64 across chunks; Pbar tables (about
- * 1.5 GB at L = 1024) are built when the mode is first selected.  The
- * pyssht calls this replaces work in FP64. */
+ * per 64-term chunk and in FP64 across chunks, for both the forward
+ * analysis (cmm_sht_forward, the analysis inside cmm_sht_velocity) and the
+ * 12-field synthesis, whose ring FFTs then run in FP32; Pbar tables
+ * (about 4.4 GB at L = 1024) are built when the mode is first selected.
+ * Measured error about 4e-6 (analysis) and 6e-6 (synthesis) of the largest
+ * coefficient / sample.  The pyssht calls this replaces work in FP64. */
 #define CMM_SHT_FP64 0
 #define CMM_SHT_SPLIT_BF16 1
 int cmm_sht_set_precision(cmm_sht* plan, int mode);
@@ -270,6 +273,12 @@ int cmm_sht_velocity(cmm_sht* plan, const cmm_mesh* velmesh, const double* omega
  * (ncomp = 1) this builds the scalar spherical_spline of the field. */
 int cmm_sht_scalar_jets(cmm_sht* plan, const cmm_mesh* velmesh, const double* alm, double* jets,
                         void* stream);
+
+/* Angular power of a real field's coefficients alm (L,L) complex:
+ * power[l] = sum over m = -l..l of |a_lm|^2 (L doubles).  Enstrophy is
+ * sum_l power[l]; energy_spectrum (cmm_s2/core/spherical_harmonic_tools.py:
+ * 157-163) is power[0], power[l] / (l (l+1)). */
+int cmm_sht_power(cmm_sht* plan, const double* alm, double* power, void* stream);
 
 #ifdef __cplusplus
 }

@@ -97,3 +97,38 @@ def test_rossby_haurwitz_known_answer(sims):
     erro = np.abs(omo - rossby_wave(ph.reshape(-1), th.reshape(-1), t=1)).max()
     print(f"RH L_inf error: gpu {err:.6e} oracle {erro:.6e}")
     assert err < 0.5 and abs(err - erro) < 1e-9
+
+
+def test_diagnostics_rossby_haurwitz(sims):
+    """Run diagnostics on the travelling Rossby-Haurwitz wave: the L_inf
+    error on the MWSS grid against the exact solution, enstrophy and energy
+    drift; the split-BF16 form's errors stay within 2x of the FP64 form's."""
+    from cmm_gpu.meshgen import icosahedral_mesh
+    verts, tris = icosahedral_mesh(4)
+    L, Nt = 64, 42
+    out = {}
+    for form in ("fp64", "split_bf16"):
+        s = sims.BVESolver(verts, tris, 4, L, Nt, 1.0, "rossby_wave", n_maps=10, precision=form).run()
+        th, ph = np.meshgrid(np.pi * np.arange(L + 1) / L, np.pi * np.arange(2 * L) / L, indexing="ij")
+        d = s.diagnostics(omega_true=rossby_wave(ph, th, t=1))
+        print(form, d)
+        out[form] = d
+        assert d["linf_rel"] < 0.05
+        assert d["enstrophy_drift"] < 1e-3 and d["energy_drift"] < 1e-3
+    assert out["split_bf16"]["linf_rel"] < 2 * out["fp64"]["linf_rel"]
+    assert out["split_bf16"]["enstrophy_drift"] < 2 * out["fp64"]["enstrophy_drift"] + 1e-6
+
+
+def test_jacobian_determinant_converges(sims):
+    """The back-to-label map is area preserving; its spline's tangent
+    Jacobian determinant deviates from 1 by the interpolation error of the
+    derivative, which must fall with mesh refinement (O(h^2): about 4x per
+    level) on the Rossby-Haurwitz run."""
+    from cmm_gpu.meshgen import icosahedral_mesh
+    devs = []
+    for level in (3, 4, 5):
+        verts, tris = icosahedral_mesh(level)
+        s = sims.BVESolver(verts, tris, level, 64, 42, 1.0, "rossby_wave", n_maps=10).run()
+        devs.append(s.diagnostics(jacobian=True)["jac_det_dev"])
+    print("max |det DX - 1| at levels 3, 4, 5:", devs)
+    assert devs[1] < devs[0] / 2 and devs[2] < devs[1] / 2

@@ -197,3 +197,18 @@ def test_split_bf16_velocity_jets(nat):
     err = np.abs(got - ref).max() / np.abs(ref).max()
     print(f"split-BF16 velocity jets relative error {err:.3e}")
     assert err < 1e-4
+
+
+def test_power_matches_energy_spectrum(nat):
+    """cmm_sht_power against the oracle's energy_spectrum
+    (core/spherical_harmonic_tools.py:157-163) of the same coefficients:
+    power[0] = spectrum[0], power[l] = l (l+1) spectrum[l]; 1e-13 relative."""
+    L = 48
+    rng = np.random.default_rng(9)
+    a = np.tril(rng.standard_normal((L, L)) + 1j * rng.standard_normal((L, L)))
+    a[:, 0] = a[:, 0].real
+    spec = S.energy_spectrum(S.shifted_from_vec(S.full_from_half(a), L))
+    ell = np.arange(L)
+    ref = spec * np.where(ell > 0, ell * (ell + 1), 1)
+    got = nat.Sht(L).power(dev(mhalf(a))).cpu().numpy()
+    np.testing.assert_allclose(got, ref, rtol=1e-13, atol=0)
