@@ -276,37 +276,58 @@ def bench_gpu(args, rank, world):
 
 def bench_bve(args, dev):
     """Config: level 4, L=128, dt=1/200, 200 steps, remap every 20, random
-    real SH initial vorticity l=1..16 (N(0,1) l^-1.5, seed 0)."""
+    real SH initial vorticity l=1..16 (N(0,1) l^-1.5, seed 0), evaluated as
+    a pointwise series.  The whole run after the bootstrap (198 steps) is
+    timed with CUDA events in three ways: driven from the host through the
+    single calls (step_host), by the device-driven stepper (one
+    cmm_bve_step per step), and as one replayed CUDA graph per step."""
     import torch
     from cmm_gpu.meshgen import icosahedral_mesh
     from cmm_gpu.workloads import random_sh_vorticity
     from cmm_gpu.spherical_simulations import BVESolver, Vorticity
     _, a = random_sh_vorticity(16, seed=0)
     verts, tris = icosahedral_mesh(4)
-    s = BVESolver(verts, tris, 4, 128, 200, 1.0, Vorticity(sh=a), n_maps=20)
-    s.bootstrap()
-    for _ in range(3):
-        s.step()
-    torch.cuda.synchronize()
-    n = 60
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(n):
-        s.step()
-    e1.record()
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / n
-    return {"steps_per_s": 1e3 / ms, "ms_per_step": ms, "steps_timed": n,
-            "workload": "BVE level 4 (2562 vertices), L=128 MWSS 129x256, dt=1/200, remap every 20, "
-                        "random SH l<=16 initial vorticity; steps 5..64 after the bootstrap"}
+    out = {"workload": "BVE level 4 (2562 vertices), L=128 MWSS 129x256, dt=1/200, 200 steps, "
+                       "remap every 20, random SH l<=16 initial vorticity; the 198 steps after the "
+                       "bootstrap"}
+    omegas = {}
+    for mode in ("host", "device", "graph"):
+        s = BVESolver(verts, tris, 4, 128, 200, 1.0, Vorticity(sh=a), n_maps=20)
+        s.bootstrap()
+        if mode == "graph":
+            s.capture()
+        torch.cuda.synchronize()
+        n = s.Nt - 2
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        e0.record()
+        for _ in range(n):
+            s.step_host() if mode == "host" else s.step()
+        e1.record()
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        ms = e0.elapsed_time(e1) / n
+        out[mode] = {"steps_per_s": 1e3 / ms, "ms_per_step": ms, "wall_steps_per_s": n / wall}
+        omegas[mode] = s.omega.clone()
+        del s
+    out["steps_timed"] = 198
+    out["steps_per_s"] = out["graph"]["steps_per_s"]
+    out["ms_per_step"] = out["graph"]["ms_per_step"]
+    out["graph_equals_host"] = bool(torch.equal(omegas["graph"], omegas["host"]))
+    return out
 
 
-def bench_bve3(args, dev, steps=8):
-    """Config: level-7 mesh, L=1024 MWSS (1025 x 2048), 1000-step run with
-    remap every 10 (first steps timed); initial vorticity 4 zonal Gaussian
-    jets (width 0.1 rad at latitudes +-0.5, +-1.1 rad, amplitude 10) plus a
-    seeded l <= 64 perturbation with a k^-3 energy spectrum at 1 % of the
-    jets' amplitude (rms 0.1), evaluated through its scalar spline."""
+def bench_bve3(args, dev):
+    """Config: level-7 mesh, L=1024 MWSS (1025 x 2048), 1000 steps (dt =
+    1/1000, T = 1) with remap every 10 (n_maps = 10, the reference default:
+    up to 100 submaps composed at every step by the end); initial vorticity
+    4 zonal Gaussian jets (width 0.1 rad at latitudes +-0.5, +-1.1 rad,
+    amplitude 10) plus a seeded l <= 64 perturbation with a k^-3 energy
+    spectrum at 1 % of the jets' amplitude (rms 0.1), evaluated through its
+    scalar spline.  Each form runs the whole run (args.bve3_steps steps after
+    the 2-step bootstrap); steps/s = steps / CUDA-event time of the loop.
+    Also reported: the step time at the start (no submaps), the run's
+    diagnostics at the end and the split-vs-FP64 vorticity difference."""
     import torch
     from cmm_gpu.meshgen import icosahedral_mesh
     from cmm_gpu.workloads import spectral_perturbation
@@ -314,31 +335,38 @@ def bench_bve3(args, dev, steps=8):
     pert = spectral_perturbation(64, seed=3, slope=-2.0, rms=0.1)
     vort = Vorticity("gaussian_zonal_jets", (10.0, 0.1, 4, 0.5, -0.5, 1.1, -1.1), spline_sh=pert)
     verts, tris = icosahedral_mesh(7)
-    out = {"workload": "BVE level 7 (163842 vertices), L=1024 MWSS 1025x2048, remap every 10, "
-                       "4 Gaussian zonal jets + 1% k^-3 l<=64 perturbation (spline); steps 4..11"}
+    Nt = 1000
+    nsteps = min(args.bve3_steps, Nt - 2)
+    out = {"workload": "BVE level 7 (163842 vertices), L=1024 MWSS 1025x2048, 1000 steps of dt=1/1000, "
+                       "remap every 10, 4 Gaussian zonal jets + 1% k^-3 l<=64 perturbation (spline)",
+           "steps_timed": nsteps}
     omegas = {}
     for form in ("fp64", "split_bf16"):
         t0 = time.perf_counter()
-        s = BVESolver(verts, tris, 7, 1024, 1000, 1.0, vort, n_maps=10, precision=form)
+        s = BVESolver(verts, tris, 7, 1024, Nt, 1.0, vort, n_maps=10, precision=form)
         s.bootstrap()
-        s.step()
         torch.cuda.synchronize()
         setup = time.perf_counter() - t0
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        for _ in range(steps):
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        ev[0].record()
+        for k in range(nsteps):
             s.step()
-        e1.record()
+            if k == 7:
+                ev[1].record()
+        ev[2].record()
         torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1) / steps
+        ms = ev[0].elapsed_time(ev[2]) / nsteps
         ok = s.mesh.status() == 0 and s.vm.status() == 0 and s.sht.status() == 0
-        out[form] = {"steps_per_s": 1e3 / ms, "ms_per_step": ms, "steps_timed": steps,
-                     "setup_s": setup, "status_ok": ok}
+        d = s.diagnostics(jacobian=False)
+        out[form] = {"steps_per_s": 1e3 / ms, "ms_per_step": ms,
+                     "ms_per_step_first8": ev[0].elapsed_time(ev[1]) / 8 if nsteps > 8 else None,
+                     "submaps_at_end": s.Nc, "setup_s": setup, "status_ok": ok,
+                     "enstrophy_drift": d.get("enstrophy_drift"), "energy_drift": d.get("energy_drift")}
         omegas[form] = s.omega.clone()
         del s
         torch.cuda.empty_cache()
-    d = (omegas["split_bf16"] - omegas["fp64"]).abs().max().item()
-    out["split_vs_fp64_omega_rel"] = d / omegas["fp64"].abs().max().item()
+    dd = (omegas["split_bf16"] - omegas["fp64"]).abs().max().item()
+    out["split_vs_fp64_omega_rel"] = dd / omegas["fp64"].abs().max().item()
     out["speedup_split_over_fp64"] = out["split_bf16"]["steps_per_s"] / out["fp64"]["steps_per_s"]
     return out
 
@@ -471,6 +499,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-bve", action="store_true")
     ap.add_argument("--no-bve3", action="store_true", help="skip the level-7 / L=1024 BVE run")
+    ap.add_argument("--bve3-steps", type=int, default=998,
+                    help="steps of the level-7 / L=1024 run after its bootstrap (998 = the whole run)")
     ap.add_argument("--logq", type=int, default=24, help="log2 queries per GPU (profiling cases)")
     ap.add_argument("--no-kernels", action="store_true", help="skip the per-stage timings")
     ap.add_argument("--kernels-only", action="store_true",

@@ -19,6 +19,21 @@ if not os.path.exists(_LIB_PATH):
 lib = ctypes.CDLL(_LIB_PATH)
 
 _p, _i, _i64, _d = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_double
+
+
+class BveDesc(ctypes.Structure):
+    """cmm_bve_desc (include/cmm_gpu.h)."""
+    _fields_ = [("mesh", _p), ("velmesh", _p), ("sht", _p),
+                ("vort_kind", _i), ("nparams", _i), ("vort_params", _d * 12),
+                ("sh", _p), ("lmax", _i), ("spline", _p), ("rot_rate", _d),
+                ("tspan_step", _d), ("Nt", _i), ("n_maps", _i), ("eps", _d),
+                ("s_pts", _p), ("tan", _p), ("id_jets", _p), ("sample_pts", _p),
+                ("jets", _p), ("coeffs_cur", _p), ("work", _p), ("X", _p), ("omega", _p),
+                ("vel_jets", _p), ("vel", _p * 3), ("n_stack", _i), ("stack", _p),
+                ("stack_jets", _p), ("k", _i), ("count", _i), ("nc", _i), ("identity", _i),
+                ("ts0", _d)]
+
+
 _SIGS = {
     "cmm_last_error": (ctypes.c_char_p, []),
     "cmm_version": (_i, []),
@@ -43,6 +58,10 @@ _SIGS = {
     "cmm_sht_set_precision": (_i, [_p, _i]),
     "cmm_sht_status": (_i, [_p, _p, ctypes.POINTER(_i), _i]),
     "cmm_sht_power": (_i, [_p, _p, _p, _p]),
+    "cmm_bve_create": (_i, [ctypes.POINTER(BveDesc), ctypes.POINTER(_p)]),
+    "cmm_bve_destroy": (_i, [_p]),
+    "cmm_bve_step": (_i, [_p, _p]),
+    "cmm_bve_state": (_i, [_p, _p, ctypes.POINTER(_i), ctypes.POINTER(_i), ctypes.POINTER(_i)]),
     "cmm_sht_destroy": (_i, [_p]),
     "cmm_sht_forward": (_i, [_p, _p, _p, _p]),
     "cmm_sht_inverse": (_i, [_p, _p, _i, _p, _p]),

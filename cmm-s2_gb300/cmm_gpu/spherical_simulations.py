@@ -9,6 +9,7 @@ map update, the evaluation of submaps o current map at the MWSS sample
 points, the vorticity there, its inversion to velocity jets and the remap
 every n_maps steps.
 """
+import ctypes
 import math
 
 import numpy as np
@@ -60,7 +61,7 @@ class BVESolver:
         dev = self.device
         self.vort = Vorticity.from_reference(vorticity)
         self.sh = None if self.vort.sh is None else torch.from_numpy(self.vort.sh).to(dev)
-        self.L, self.Nt, self.T, self.rot = L, Nt, T, rot_rate
+        self.L, self.Nt, self.T, self.rot, self.n_maps = L, Nt, T, rot_rate, n_maps
         self.mesh = native.Mesh(verts, tris, level, device=dev.index)
         theta, phi, grid, vverts = latlon_mesh_arrays(L)
         self.vm = native.VelMesh(L, theta, phi, grid, vverts, device=dev.index)
@@ -88,7 +89,7 @@ class BVESolver:
         self.jets = self.id_jets.clone()
         self.coeffs_cur = self.mesh.new_coeffs()
         self.stack = [self.mesh.new_coeffs() for _ in ns]
-        self.stack_jets = [None for _ in ns]
+        self.stack_jets = [torch.empty_like(self.id_jets) for _ in ns]
         self.vel_coeffs = [self.vm.new_coeffs() for _ in range(3)]
         self.vel_jets = torch.empty((3, 4, self.vm.nv), **f64)
         self.work = torch.empty(native.lib.cmm_advect_workspace(self.mesh.h), **f64)
@@ -109,6 +110,8 @@ class BVESolver:
         self.count = 0
         self.step_index = 0
         self.launches = 0
+        self._bve = None        # device-driven stepper, made after the bootstrap
+        self.graph = None       # CUDA graph of one step (capture())
 
     # ------------------------------------------------------------ pieces
     def _project(self, X, n, rot=None):
@@ -156,14 +159,94 @@ class BVESolver:
         self.identity = False
         self.count = 2
         self.step_index = 2
+        self._make_stepper()
 
     def _sample_single(self):
         self.mesh.compose([self.coeffs_cur], self.sample_pts, out=self.X)
         self.launches += 1
         return self.X
 
+    def _make_stepper(self):
+        """The device-driven step (cmm_bve_create) from the post-bootstrap state."""
+        d = native.BveDesc()
+        d.mesh, d.velmesh, d.sht = self.mesh.h, self.vm.h, self.sht.h
+        d.vort_kind = self.vort.kind
+        d.nparams = len(self.vort.params)
+        for k, v in enumerate(self.vort.params[:12]):
+            d.vort_params[k] = float(v)
+        d.sh = self.sh.data_ptr() if self.sh is not None else None
+        d.lmax = self.sh.shape[0] - 1 if self.sh is not None else -1
+        d.spline = self.spline.data_ptr() if self.spline is not None else None
+        d.rot_rate = float(self.rot)
+        d.tspan_step = float(self.dt)
+        d.Nt, d.n_maps, d.eps = self.Nt, self.n_maps, 1e-5
+        for name in ("s_pts", "tan", "id_jets", "sample_pts", "jets", "coeffs_cur", "work", "X",
+                     "omega", "vel_jets"):
+            setattr(d, name, getattr(self, name).data_ptr())
+        for k in range(3):
+            d.vel[k] = self.vel_coeffs[k].data_ptr()
+        self._stack_arr = (ctypes.c_void_p * len(self.stack))(*[c.data_ptr() for c in self.stack])
+        self._jets_arr = (ctypes.c_void_p * len(self.stack))(*[j.data_ptr() for j in self.stack_jets])
+        d.n_stack = len(self.stack)
+        d.stack = ctypes.cast(self._stack_arr, ctypes.c_void_p)
+        d.stack_jets = ctypes.cast(self._jets_arr, ctypes.c_void_p)
+        d.k, d.count, d.nc, d.identity = self.step_index, self.count, self.Nc, int(self.identity)
+        d.ts0 = float(self.ts0)
+        h = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            native.check(native.lib.cmm_bve_create(ctypes.byref(d), ctypes.byref(h)), "cmm_bve_create")
+        self._bve = h
+
+    def __del__(self):
+        h = getattr(self, "_bve", None)
+        if h is not None and h.value:
+            native.lib.cmm_bve_destroy(h)
+            self._bve = None
+
+    def _advance_host(self):
+        """Host mirror of the driver's bookkeeping (spherical_simulations.py:
+        273-294), kept in step with the device state."""
+        self.ts0 = self.ts0 + self.dt
+        self.count += 1
+        self.identity = False
+        c = self.vel_coeffs
+        self.vel_coeffs = [c[1], c[2], c[0]]
+        if self.count in self.ns:
+            self.Nc = self.ns.index(self.count) + 1
+            self.identity = True
+        self.step_index += 1
+        self.launches += 13
+
     def step(self):
-        """One pass of the main loop (spherical_simulations.py:263-294)."""
+        """One pass of the main loop (spherical_simulations.py:263-294),
+        enqueued by the device-driven stepper (or replayed from the captured
+        CUDA graph after capture())."""
+        if self._bve is None:
+            self._make_stepper()
+        if self.graph is not None:
+            self.graph.replay()
+        else:
+            native.check(native.lib.cmm_bve_step(self._bve, native._stream(self.device)), "cmm_bve_step")
+        self._advance_host()
+
+    def capture(self):
+        """Capture one device-driven step into a CUDA graph; step() then
+        replays it (one graph launch per step)."""
+        g = torch.cuda.CUDAGraph()
+        torch.cuda.synchronize(self.device)
+        with torch.cuda.graph(g):
+            native.check(native.lib.cmm_bve_step(self._bve, native._stream(self.device)), "cmm_bve_step")
+        self.graph = g
+        return self
+
+    def step_host(self):
+        """The same step driven from the host through the single calls
+        (advect_project, assemble, compose, vorticity, velocity).  The
+        device-driven stepper (and any captured graph) is dropped and made
+        again from the host state at the next step()."""
+        if self._bve is not None:
+            native.lib.cmm_bve_destroy(self._bve)
+            self._bve, self.graph = None, None
         t = float(self.tspan[self.step_index])
         self._advect(native.RK4, t, None if self.identity else self.coeffs_cur)
         self._project(self._sample(), 2)
@@ -174,7 +257,7 @@ class BVESolver:
             idx = self.ns.index(self.count)
             self.Nc = idx + 1
             self.stack[idx].copy_(self.coeffs_cur)
-            self.stack_jets[idx] = self.jets.clone()
+            self.stack_jets[idx].copy_(self.jets)
             self.jets.copy_(self.id_jets)
             self.identity = True
         self.step_index += 1

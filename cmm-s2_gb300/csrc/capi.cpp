@@ -220,6 +220,20 @@ int cmm_sht_set_precision(cmm_sht* plan, int mode) {
   return sht_set_precision(plan, mode);
 }
 
+int cmm_bve_create(const cmm_bve_desc* desc, cmm_bve** out) { return bve_create(desc, out); }
+
+int cmm_bve_destroy(cmm_bve* bve) { return bve_destroy(bve); }
+
+int cmm_bve_step(cmm_bve* bve, void* stream) {
+  if (!bve) return arg_error("cmm_bve_step: null handle");
+  return bve_step(bve, (cudaStream_t)stream);
+}
+
+int cmm_bve_state(cmm_bve* bve, void* stream, int* count, int* nc, int* identity) {
+  if (!bve) return arg_error("cmm_bve_state: null handle");
+  return bve_state(bve, (cudaStream_t)stream, count, nc, identity);
+}
+
 int cmm_sht_power(cmm_sht* plan, const double* alm, double* power, void* stream) {
   if (!plan || !alm || !power) return arg_error("cmm_sht_power: null pointer");
   return sht_power(plan, (const double2*)alm, power, (cudaStream_t)stream);

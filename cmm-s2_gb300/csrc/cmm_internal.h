@@ -78,11 +78,17 @@ namespace cmm {
 // kernels (locate.cu)
 int launch_locate(const MeshView& m, const double* q, int64_t n, int32_t* tri, double* bcc,
                   cudaStream_t s);
+struct BveState;
+// st != NULL: write into st->vel[0] instead of coeffs.
 int launch_assemble(const MeshView& m, const double* jets, int ncomp, double* coeffs,
-                    cudaStream_t s);
+                    cudaStream_t s, const BveState* st = nullptr);
 int launch_compose(const MeshView& m, const double* const* coeffs, int S, const double* q,
                    int64_t n, double* out, int32_t* tri, int32_t* tri_all, double* jac,
                    cudaStream_t s);
+// Composition through the st->nc submaps of the device table `table`
+// (submap 0 first) followed by `last` (applied first), no Jacobian.
+int launch_compose_dev(const MeshView& m, const double* const* table, const BveState* st,
+                       const double* last, const double* q, int64_t n, double* out, cudaStream_t s);
 int launch_stencil_eval(const MeshView& m, const double* coeffs, const double* yn,
                         const double* st, int64_t nv, double* out, cudaStream_t s);
 // Host-side tables of an icosahedral mesh (before upload).
@@ -111,18 +117,35 @@ struct VelPtrs {
   const double* p[3];
 };
 TimeWeights time_weights(int nvs, double ts0, double dt, const double* times, int ntimes);
+
+// Device-resident state of a device-driven barotropic step (stepper.cu):
+// read by the kernels of a step in place of their host arguments, so one
+// captured CUDA graph replays every step; updated at the end of each step
+// by bve_advance_kernel.
+struct BveState {
+  double* vel[3];   // velocity coefficient slots, oldest first
+  TimeWeights tw;   // Lagrange weights of the next step's four RK4 stages
+  double ts0;       // time of the oldest velocity level
+  double step;      // tspan step (= dt)
+  int k;            // tspan index of the next step's start time
+  int count;        // steps taken (the driver's counter)
+  int nc;           // submaps in the stack
+  int identity;     // current map is the identity (right after a remap)
+};
 int launch_velocity_eval(const MeshView& vm, VelPtrs vc, int nvs, const TimeWeights& tw,
                          const double* x, int64_t n, double* out, cudaStream_t s);
 int launch_integrate(const MeshView& vm, VelPtrs vc, int nvs, const TimeWeights& tw, int scheme,
                      double dt, const double* x, int64_t n, double* out, cudaStream_t s);
 int launch_latlon_locate(const MeshView& vm, const double* q, int64_t n, int32_t* tri, double* bcc,
                          cudaStream_t s);
+// st != NULL: velocity slots and stage weights from st (advect), the
+// previous map dropped when st->identity (project).
 int launch_advect_points(const MeshView& mesh, const MeshView& vm, VelPtrs vc, int nvs,
                          const TimeWeights& tw, int scheme, double dt, const double* s_pts,
-                         double* work, cudaStream_t s);
+                         double* work, cudaStream_t s, const BveState* st = nullptr);
 int launch_project_jets(const MeshView& mesh, const double* prev_coeffs, const double* yn,
                         const double* sn, const double* tan, double eps, double* jets,
-                        cudaStream_t s);
+                        cudaStream_t s, const BveState* st = nullptr);
 
 // Allocation-free variant of the map update (velocity.cu): foot-point
 // scratch in a fixed device array sized for kNoAllocMaxVerts vertices.
@@ -148,6 +171,10 @@ int sht_velocity(cmm_sht* p, const cmm_mesh* vm, const double* omega, double2* p
                  double* jets, cudaStream_t s);
 int sht_scalar_jets(cmm_sht* p, const cmm_mesh* vm, const double2* alm, double* jets, cudaStream_t s);
 int sht_power(cmm_sht* p, const double2* alm, double* power, cudaStream_t s);
+int bve_create(const cmm_bve_desc* d, cmm_bve** out);
+int bve_step(cmm_bve* b, cudaStream_t s);
+int bve_destroy(cmm_bve* b);
+int bve_state(cmm_bve* b, cudaStream_t s, int* count, int* nc, int* identity);
 int sht_set_precision(cmm_sht* p, int mode);
 int sht_status(cmm_sht* p, cudaStream_t s, int* flags, int clear);
 

@@ -32,8 +32,20 @@ namespace {
 
 constexpr int kBlock = 256;
 
+// Submap lists: by value in the kernel parameters (host calls), or a
+// device table whose length comes from a device-driven step's state.
 struct SubmapPtrs {
   const double* p[CMM_MAX_SUBMAPS];
+  int S;
+  __device__ __forceinline__ int count() const { return S; }
+  __device__ __forceinline__ const double* at(int s, int) const { return p[s]; }
+};
+struct DevSubmaps {
+  const double* const* tab;
+  const BveState* st;
+  const double* last;
+  __device__ __forceinline__ int count() const { return st->nc + 1; }
+  __device__ __forceinline__ const double* at(int s, int S) const { return s < S - 1 ? tab[s] : last; }
 };
 
 // Tangent image of w under one normalised submap: dS = (dP - s (s.dP)) / |P|.
@@ -91,7 +103,9 @@ constexpr int kAsmTri = 64;   // triangles (threads) per block
 
 template <int NC>
 __global__ void __launch_bounds__(kAsmTri) assemble_kernel(MeshView m, const double* __restrict__ jets,
-                                                           double* __restrict__ coeffs) {
+                                                           double* __restrict__ coeffs,
+                                                           const BveState* __restrict__ st) {
+  if (st) coeffs = st->vel[0];
   constexpr int kStride = NC == 3 ? kCoeffStride3 : kCoeffStride1;
   constexpr int kRow = kStride + 1;
   __shared__ double rec[kAsmTri * kRow];
@@ -151,13 +165,14 @@ __global__ void __launch_bounds__(kAsmTri) assemble_kernel(MeshView m, const dou
   for (int i = tl; i < nblk * kStride; i += kAsmTri) dst[i] = rec[(i / kStride) * kRow + i % kStride];
 }
 
-template <bool JAC>
-__global__ void __launch_bounds__(kBlock) compose_kernel(MeshView m, SubmapPtrs cp, int S,
+template <bool JAC, class Src>
+__global__ void __launch_bounds__(kBlock) compose_kernel(MeshView m, Src cp,
                                                          const double* __restrict__ q, int64_t n,
                                                          double* __restrict__ out,
                                                          int32_t* __restrict__ tri,
                                                          int32_t* __restrict__ tri_all,
                                                          double* __restrict__ jac) {
+  const int S = cp.count();
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     double p[3] = {q[3 * i], q[3 * i + 1], q[3 * i + 2]};
@@ -194,7 +209,7 @@ __global__ void __launch_bounds__(kBlock) compose_kernel(MeshView m, SubmapPtrs 
       const Split sp = split_of(b);
       const Gam g = gamma_of(Lr, b, sp);
       Ords<3> o;
-      load_ords<3>(cp.p[s] + (int64_t)t * kCoeffStride3, sp, o);
+      load_ords<3>(cp.at(s, S) + (int64_t)t * kCoeffStride3, sp, o);
       double P[3];
       sbb<3>(o, g, P);
       const double inv_n = rsqrt(P[0] * P[0] + P[1] * P[1] + P[2] * P[2]);
@@ -266,12 +281,12 @@ int launch_locate(const MeshView& m, const double* q, int64_t n, int32_t* tri, d
 }
 
 int launch_assemble(const MeshView& m, const double* jets, int ncomp, double* coeffs,
-                    cudaStream_t s) {
+                    cudaStream_t s, const BveState* st) {
   const int blocks = (m.nt + kAsmTri - 1) / kAsmTri;
   if (ncomp == 3)
-    assemble_kernel<3><<<blocks, kAsmTri, 0, s>>>(m, jets, coeffs);
+    assemble_kernel<3><<<blocks, kAsmTri, 0, s>>>(m, jets, coeffs, st);
   else
-    assemble_kernel<1><<<blocks, kAsmTri, 0, s>>>(m, jets, coeffs);
+    assemble_kernel<1><<<blocks, kAsmTri, 0, s>>>(m, jets, coeffs, st);
   return check_launch("assemble_kernel");
 }
 
@@ -280,12 +295,22 @@ int launch_compose(const MeshView& m, const double* const* coeffs, int S, const 
                    cudaStream_t s) {
   if (n == 0) return CMM_OK;
   SubmapPtrs cp;
+  cp.S = S;
   for (int k = 0; k < S; ++k) cp.p[k] = coeffs[k];
   const int g = grid_for(n, kBlock);
   if (jac)
-    compose_kernel<true><<<g, kBlock, 0, s>>>(m, cp, S, q, n, out, tri, tri_all, jac);
+    compose_kernel<true><<<g, kBlock, 0, s>>>(m, cp, q, n, out, tri, tri_all, jac);
   else
-    compose_kernel<false><<<g, kBlock, 0, s>>>(m, cp, S, q, n, out, tri, tri_all, jac);
+    compose_kernel<false><<<g, kBlock, 0, s>>>(m, cp, q, n, out, tri, tri_all, jac);
+  return check_launch("compose_kernel");
+}
+
+int launch_compose_dev(const MeshView& m, const double* const* table, const BveState* st,
+                       const double* last, const double* q, int64_t n, double* out, cudaStream_t s) {
+  if (n == 0) return CMM_OK;
+  DevSubmaps cp{table, st, last};
+  compose_kernel<false><<<grid_for(n, kBlock), kBlock, 0, s>>>(m, cp, q, n, out, nullptr, nullptr,
+                                                                nullptr);
   return check_launch("compose_kernel");
 }
 

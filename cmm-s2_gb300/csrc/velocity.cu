@@ -171,7 +171,12 @@ __global__ void __launch_bounds__(kBlock) advect_points_kernel(MeshView mesh, Me
                                                                int nvs, TimeWeights tw, int scheme,
                                                                double dt,
                                                                const double* __restrict__ s_pts,
-                                                               double* __restrict__ work) {
+                                                               double* __restrict__ work,
+                                                               const BveState* __restrict__ st) {
+  if (st) {
+    vc = VelPtrs{{st->vel[0], st->vel[1], st->vel[2]}};
+    tw = st->tw;
+  }
   const int64_t nv = mesh.nv, n = 5 * nv;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
@@ -211,10 +216,12 @@ __global__ void __launch_bounds__(kBlock) project_jets_kernel(MeshView m, const 
                                                               const double* __restrict__ yn,
                                                               const double* __restrict__ sn,
                                                               const double* __restrict__ tan,
-                                                              double eps, double* __restrict__ jets) {
+                                                              double eps, double* __restrict__ jets,
+                                                              const BveState* __restrict__ st) {
   const int64_t nv = m.nv;
   const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (v >= nv) return;
+  if (st && st->identity) prev = nullptr;
   double S[4][3];
 #pragma unroll
   for (int k = 0; k < 4; ++k)
@@ -293,10 +300,10 @@ int launch_integrate(const MeshView& vm, VelPtrs vc, int nvs, const TimeWeights&
 
 int launch_advect_points(const MeshView& mesh, const MeshView& vm, VelPtrs vc, int nvs,
                          const TimeWeights& tw, int scheme, double dt, const double* s_pts,
-                         double* work, cudaStream_t s) {
+                         double* work, cudaStream_t s, const BveState* st) {
   const int64_t n = 5LL * mesh.nv;
   advect_points_kernel<<<grid_for(n, kBlock), kBlock, 0, s>>>(mesh, vm, vc, nvs, tw, scheme, dt,
-                                                               s_pts, work);
+                                                               s_pts, work, st);
   return check_launch("advect_points_kernel");
 }
 
@@ -354,10 +361,10 @@ int advect_project_noalloc(const MeshView& mesh, const MeshView& vm, VelPtrs vc,
 
 int launch_project_jets(const MeshView& mesh, const double* prev_coeffs, const double* yn,
                         const double* sn, const double* tan, double eps, double* jets,
-                        cudaStream_t s) {
+                        cudaStream_t s, const BveState* st) {
   const int64_t nv = mesh.nv;
   project_jets_kernel<<<(int)((nv + kBlock - 1) / kBlock), kBlock, 0, s>>>(mesh, prev_coeffs, yn, sn,
-                                                                           tan, eps, jets);
+                                                                           tan, eps, jets, st);
   return check_launch("project_jets_kernel");
 }
 

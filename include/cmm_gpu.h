@@ -274,6 +274,64 @@ int cmm_sht_velocity(cmm_sht* plan, const cmm_mesh* velmesh, const double* omega
 int cmm_sht_scalar_jets(cmm_sht* plan, const cmm_mesh* velmesh, const double* alm, double* jets,
                         void* stream);
 
+/* ---------------------------------------------- device-driven BVE steps */
+/* The main-loop body of euler_simulation_sphere_remapping
+ * (cmm_s2/core/spherical_simulations.py:263-294) as one enqueue per step:
+ * map update (RK4, cmm_advect_project), its assembly, the sample points
+ * through the submap stack and the current map (cmm_compose), the
+ * vorticity there (cmm_vorticity_eval), the velocity jets
+ * (cmm_sht_velocity) assembled into the oldest velocity slot, then the
+ * driver's bookkeeping (remap into the stack every n_maps steps and at
+ * step Nt, velocity-slot rotation, ts0, the next step's RK4 stage weights)
+ * done on the device.  The kernels read everything that varies between
+ * steps from a device-resident state, so the launches of every step are
+ * identical and a CUDA graph captured from one cmm_bve_step replays all
+ * later steps (several runs' graphs can be captured into one).  Results
+ * are bit-identical to the same run driven step by step from the host.
+ * No counterpart function in the reference (its loop is Python).
+ * All pointers are device buffers owned by the caller, except `stack` and
+ * `stack_jets`: host arrays of n_stack device pointers (copied at create;
+ * stack_jets may be NULL). */
+typedef struct cmm_bve cmm_bve;
+typedef struct {
+  const cmm_mesh* mesh;       /* icosahedral map mesh */
+  const cmm_mesh* velmesh;    /* MWSS velocity mesh of band-limit L */
+  cmm_sht* sht;               /* plan of band-limit L (precision as set) */
+  int vort_kind, nparams;     /* initial vorticity, as cmm_vorticity_eval */
+  double vort_params[12];
+  const double* sh;
+  int lmax;
+  const double* spline;
+  double rot_rate;
+  double tspan_step;          /* T / Nt: tspan[k] = k * tspan_step, dt */
+  int Nt, n_maps;
+  double eps;                 /* stencil half-width (1e-5) */
+  const double* s_pts;        /* (3,4,Nv) stencil points */
+  const double* tan;          /* (2,Nv,3) tangent frames */
+  const double* id_jets;      /* (3,4,Nv) identity jets */
+  const double* sample_pts;   /* (Q,3) MWSS sample points, Q = (L+1) 2L */
+  double* jets;               /* (3,4,Nv) current map jets */
+  double* coeffs_cur;         /* (Nt_map, 64) current map coefficients */
+  double* work;               /* cmm_advect_workspace(mesh) doubles */
+  double* X;                  /* (Q,3) back-traced sample points */
+  double* omega;              /* (L+1, 2L) vorticity samples */
+  double* vel_jets;           /* (3,4,Nv_u) velocity jets */
+  double* vel[3];             /* velocity coefficient slots, oldest first */
+  int n_stack;                /* stack slots (>= remaps of the run) */
+  double* const* stack;
+  double* const* stack_jets;
+  /* state after the bootstrap (spherical_simulations.py:216-261) */
+  int k;                      /* tspan index of the next step's start */
+  int count, nc, identity;
+  double ts0;
+} cmm_bve_desc;
+int cmm_bve_create(const cmm_bve_desc* desc, cmm_bve** out);
+int cmm_bve_destroy(cmm_bve* bve);
+/* Enqueue one step on `stream` (no host synchronisation, capturable). */
+int cmm_bve_step(cmm_bve* bve, void* stream);
+/* Read the device state (synchronises `stream`). */
+int cmm_bve_state(cmm_bve* bve, void* stream, int* count, int* nc, int* identity);
+
 /* Angular power of a real field's coefficients alm (L,L) complex:
  * power[l] = sum over m = -l..l of |a_lm|^2 (L doubles).  Enstrophy is
  * sum_l power[l]; energy_spectrum (cmm_s2/core/spherical_harmonic_tools.py:

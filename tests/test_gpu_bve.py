@@ -132,3 +132,66 @@ def test_jacobian_determinant_converges(sims):
         devs.append(s.diagnostics(jacobian=True)["jac_det_dev"])
     print("max |det DX - 1| at levels 3, 4, 5:", devs)
     assert devs[1] < devs[0] / 2 and devs[2] < devs[1] / 2
+
+
+def _small_solver(sims, precision="fp64"):
+    from cmm_gpu.meshgen import icosahedral_mesh
+    from cmm_gpu.workloads import random_sh_vorticity
+    verts, tris = icosahedral_mesh(3)
+    _, sh = random_sh_vorticity(8, seed=4)
+    vort = sims.Vorticity("rossby_wave", (0.0,), sh=sh)
+    return sims.BVESolver(verts, tris, 3, 16, 27, 1.0, vort, n_maps=5, precision=precision)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split_bf16"])
+def test_device_driven_step_matches_host_step(sims, precision):
+    """cmm_bve_step (device-resident state, device bookkeeping, stage
+    weights recomputed on the device) against the same run driven from the
+    host through the single calls: bit-identical maps, stack and vorticity,
+    including the remaps (n_maps = 5, Nt = 27: remaps at 5, 10, ..., 25, 27)."""
+    a, b = _small_solver(sims, precision), _small_solver(sims, precision)
+    a.bootstrap()
+    b.bootstrap()
+    for _ in range(a.Nt - 2):
+        a.step()
+        b.step_host()
+    assert a.Nc == b.Nc == len(a.ns) and a.count == b.count == a.Nt
+    for k in range(a.Nc):
+        assert torch.equal(a.stack[k], b.stack[k]), k
+        assert torch.equal(a.stack_jets[k], b.stack_jets[k]), k
+    assert torch.equal(a.omega, b.omega)
+    assert torch.equal(a.jets, b.jets)
+    cnt, nc, ident = [ctypes_int() for _ in range(3)]
+    from cmm_gpu import native
+    native.check(native.lib.cmm_bve_state(a._bve, native._stream(), *(byref(x) for x in (cnt, nc, ident))),
+                 "cmm_bve_state")
+    assert (cnt.value, nc.value, ident.value) == (a.count, a.Nc, int(a.identity))
+    assert a.mesh.status() == 0 and a.vm.status() == 0
+
+
+def test_captured_graph_replays_the_run(sims):
+    """One step captured into a CUDA graph and replayed for every later
+    step gives the run of the stepper called step by step, bit for bit."""
+    a, b = _small_solver(sims), _small_solver(sims)
+    a.bootstrap()
+    b.bootstrap()
+    b.capture()
+    for _ in range(a.Nt - 2):
+        a.step()
+        b.step()
+    torch.cuda.synchronize()
+    for k in range(a.Nc):
+        assert torch.equal(a.stack[k], b.stack[k]), k
+    assert torch.equal(a.omega, b.omega)
+    q = torch.nn.functional.normalize(torch.randn(1000, 3, dtype=torch.float64, device="cuda"), dim=1)
+    assert torch.equal(a.composite(q)[0], b.composite(q)[0])
+
+
+def ctypes_int():
+    import ctypes
+    return ctypes.c_int()
+
+
+def byref(x):
+    import ctypes
+    return ctypes.byref(x)
