@@ -258,7 +258,7 @@ def bench_gpu(args, rank, world):
             res["rh_error"] = bench_rh_error(dev)
         except Exception as exc:  # reported, the headline stands on its own
             res["bve"] = {"error": f"{type(exc).__name__}: {exc}"}
-    if rank == 0 and not (args.no_bve3 and args.no_kernels):
+    if rank == 0 and not (args.no_bve3 and args.no_kernels and args.no_ensemble):
         del q, mesh, cs
         torch.cuda.empty_cache()
     if rank == 0 and not args.no_kernels:
@@ -266,6 +266,13 @@ def bench_gpu(args, rank, world):
             res["kernels"] = bench_kernels(dev)
         except Exception as exc:
             res["kernels"] = {"error": f"{type(exc).__name__}: {exc}"}
+    if rank == 0 and not args.no_ensemble:
+        torch.cuda.empty_cache()
+        try:
+            res["ensemble"] = bench_ensemble(args, dev)
+        except Exception as exc:
+            res["ensemble"] = {"error": f"{type(exc).__name__}: {exc}"}
+        torch.cuda.empty_cache()
     if rank == 0 and not args.no_bve3:
         try:
             res["bve_l7_L1024"] = bench_bve3(args, dev)
@@ -371,6 +378,48 @@ def bench_bve3(args, dev):
     return out
 
 
+def bench_ensemble(args, dev):
+    """Config: batched ensemble of args.ens_members members (default 64) with
+    mesh levels 5-7 and band-limits {256, 512, 1024} drawn from a seed, each
+    from seeded k^-3 random vorticity over l <= 64 (RMS 5), 100 steps of
+    dt = 1/200, remap every 10, FP64 maps with the split-BF16 Legendre stage;
+    one CUDA graph replay advances every member by one step.  The autotuner
+    picks launch shapes per size class and the graph's branch count/member
+    order (its candidate replays are real steps of the run); the remaining
+    steps are timed.  value = member-steps per second."""
+    import torch
+    from cmm_gpu.ensemble import Ensemble
+    from cmm_gpu.autotune import Autotuner
+    t0 = time.perf_counter()
+    ens = Ensemble.from_seed(args.ens_members, seed=2024, Nt=100, T=0.5)
+    ens.bootstrap()
+    setup = time.perf_counter() - t0
+    tuner = Autotuner(reps=2)
+    tuner.tune_ensemble_kernels(ens)
+    tuner.tune_schedule(ens, stream_counts=(1, 2, 4, 8), steps_each=2)
+    n = ens.members[0].Nt - 2 - ens.count
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(n):
+        ens.step()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / n
+    classes = {}
+    for lv, L in ens.specs:
+        classes[f"level{lv}_L{L}"] = classes.get(f"level{lv}_L{L}", 0) + 1
+    ok = all(m.mesh.status() == 0 and m.vm.status() == 0 and m.sht.status() == 0 for m in ens.members)
+    return {"workload": f"{args.ens_members} members, levels 5-7 x L in {{256,512,1024}} (seed 2024), "
+                        "100 steps of dt=1/200, remap every 10, k^-3 l<=64 initial vorticity (spline), "
+                        "split-BF16 Legendre, FP32 velocity records, one graph replay per step",
+            "member_steps_per_s": len(ens.members) * 1e3 / ms, "ms_per_ensemble_step": ms,
+            "steps_timed": n, "members": len(ens.members), "classes": classes,
+            "device_memory_gb": torch.cuda.max_memory_allocated(dev) / 1e9, "setup_s": setup,
+            "schedule": tuner.log["schedule"]["best"], "launch_shapes": tuner.log["kernels"],
+            "status_ok": ok}
+
+
 def bench_rh_error(dev):
     """Rossby-Haurwitz wave (exact travelling solution, T=1): L_inf vorticity
     error of the FP64 and split-BF16 forms (level 4, L=64, 42 steps)."""
@@ -464,6 +513,14 @@ def bench_kernels(dev, level=7, L=1024, reps=5, stack=8, warm=True, nvtx=False):
         put(f"sht_forward_{form}", timed(lambda: s.sht.forward(s.omega)), flops=f_fwd)
         put(f"sht_velocity_{form}", timed(lambda: s.sht.velocity(s.vm, s.omega, jets=s.vel_jets)),
             flops=f_fwd + f_inv)
+        rb = 256 if form == "split_bf16" else 512   # FP32 / FP64 velocity records
+        put(f"assemble_vel_{form}", timed(lambda: s.vm.assemble(s.vel_jets, out=s.vel_coeffs[0])),
+            nbytes=nvu * 96 + ntu * (384 // (2 if rb == 256 else 1) + rb))
+        prev, jt = s.coeffs_cur.clone(), torch.empty_like(s.jets)
+        put(f"advect_rk4_{form}", timed(lambda: s.mesh.advect_project(
+            s.vm, s.vel_coeffs, s.ts0, native.RK4, 0.0, s.dt, s.s_pts, s.tan, prev, jets=jt,
+            work=s.work)),
+            nbytes=5 * nv * 48 + 96 * nv + min(288 * nvu, 20 * nv * 3 * 288))
         if form == "split_bf16":
             break
         q = torch.from_numpy(random_sphere_points(1 << 22, seed=5)).to(dev)
@@ -474,13 +531,6 @@ def bench_kernels(dev, level=7, L=1024, reps=5, stack=8, warm=True, nvtx=False):
             nbytes=Qg * 48 + stack * 96 * nv)
         put("assemble_map", timed(lambda: s.mesh.assemble(s.jets, out=s.stack[0])),
             nbytes=nv * 96 + nt * (384 + 512))
-        put("assemble_vel", timed(lambda: s.vm.assemble(s.vel_jets, out=s.vel_coeffs[0])),
-            nbytes=nvu * 96 + ntu * (384 + 512))
-        prev, jt = s.coeffs_cur.clone(), torch.empty_like(s.jets)
-        put("advect_rk4", timed(lambda: s.mesh.advect_project(
-            s.vm, s.vel_coeffs, s.ts0, native.RK4, 0.0, s.dt, s.s_pts, s.tan, prev, jets=jt,
-            work=s.work)),
-            nbytes=5 * nv * 48 + 96 * nv + min(288 * nvu, 20 * nv * 3 * 288))
         put("vorticity", timed(lambda: s.vm.vorticity(s.vort.kind, s.vort.params, s.X, s.rot,
                                                       omega=s.omega, spline=s.spline)),
             nbytes=Qg * 32 + 32 * nvu)
@@ -503,6 +553,9 @@ def main():
                     help="steps of the level-7 / L=1024 run after its bootstrap (998 = the whole run)")
     ap.add_argument("--logq", type=int, default=24, help="log2 queries per GPU (profiling cases)")
     ap.add_argument("--no-kernels", action="store_true", help="skip the per-stage timings")
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble run")
+    ap.add_argument("--ens-members", type=int, default=64)
+    ap.add_argument("--ensemble-only", action="store_true", help="print only the ensemble run")
     ap.add_argument("--kernels-only", action="store_true",
                     help="print only the per-stage timings of one BVE step (profiling runs)")
     ap.add_argument("--kernels-level", type=int, default=7)
@@ -541,6 +594,11 @@ def main():
         return
 
     import torch
+    if args.ensemble_only:
+        dev = torch.device("cuda", 0)
+        torch.cuda.set_device(dev)
+        print(json.dumps({"ensemble": bench_ensemble(args, dev)}))
+        return
     if args.kernels_only:
         dev = torch.device("cuda", 0)
         torch.cuda.set_device(dev)
@@ -584,7 +642,7 @@ def main():
                 "h2d_bytes_per_step": Q * 24, "d2h_bytes_per_step": Q * (24 + 4 + 72)},
         "clocks": r["clocks"], "gpu_launches": r["launches"],
     }
-    for key in ("bve", "rh_error", "bve_l7_L1024", "kernels"):
+    for key in ("bve", "rh_error", "bve_l7_L1024", "kernels", "ensemble"):
         if key in r:
             line[key] = r[key]
     print(json.dumps(line))

@@ -1,0 +1,114 @@
+"""Project-written autotuner: launch shapes of the tunable kernels per
+size class, and the schedule (branch count, member order) of an
+ensemble's captured graph, chosen from CUDA-event timings on the run's own
+data.
+
+Launch shapes (cmm_mesh_set_block) are set per mesh, i.e. per mesh level
+(composition, foot points) or band-limit (vorticity); every member of a
+size class shares the mesh and so the choice.  Candidates are timed on
+scratch outputs (the members' state is not touched).  A schedule candidate
+is timed by replaying its graph: those replays are real steps of the run
+(results do not depend on the schedule: every kernel is deterministic and
+the members are independent), so tuning costs no extra steps.
+"""
+import json
+
+import torch
+
+from . import native
+
+
+def _time(fn, reps, stream):
+    fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+class Autotuner:
+    BLOCKS = (64, 128, 192, 256)
+
+    def __init__(self, reps=3):
+        self.reps = reps
+        self.log = {"kernels": {}, "schedule": None}
+
+    # ------------------------------------------------------------ kernels
+    def tune_solver(self, s):
+        """Launch shapes for the size class (level, L) of solver s, after
+        its bootstrap; returns {kernel: (best threads, {threads: ms})}."""
+        dev = s.device
+        stream = torch.cuda.current_stream(dev)
+        X = torch.empty_like(s.X)
+        om = torch.empty_like(s.omega)
+        jets = torch.empty_like(s.jets)
+        work = torch.empty_like(s.work)
+        cs = s.stack[:s.Nc] + [s.coeffs_cur]
+        t = float(s.tspan[s.step_index])
+        prev = None if s.identity else s.coeffs_cur
+        stages = {
+            native.Mesh.TUNE_COMPOSE: (s.mesh, lambda: s.mesh.compose(cs, s.sample_pts, out=X)),
+            native.Mesh.TUNE_ADVECT: (s.mesh, lambda: s.mesh.advect_project(
+                s.vm, s.vel_coeffs, s.ts0, native.RK4, t, s.dt, s.s_pts, s.tan, prev, jets=jets,
+                work=work)),
+            native.Mesh.TUNE_VORTICITY: (s.vm, lambda: s.vm.vorticity(
+                s.vort.kind, s.vort.params, s.X, s.rot, sh=s.sh, omega=om, spline=s.spline)),
+        }
+        out = {}
+        for k, (mesh, fn) in stages.items():
+            times = {}
+            for b in self.BLOCKS:
+                mesh.set_block(k, b)
+                times[b] = _time(fn, self.reps, stream)
+            best = min(times, key=times.get)
+            mesh.set_block(k, best)
+            out[k] = (best, times)
+        self.log["kernels"][f"level{s.level}_L{s.L}"] = {
+            name: {"best": out[k][0], "ms": out[k][1]}
+            for name, k in (("compose", 0), ("advect", 1), ("vorticity", 2))}
+        return out
+
+    def tune_ensemble_kernels(self, ens):
+        """One representative member (the first) per (level, L) class."""
+        seen = set()
+        for m in ens.members:
+            key = (m.level, m.L)
+            if key in seen:
+                continue
+            seen.add(key)
+            self.tune_solver(m)
+        return self.log["kernels"]
+
+    # ----------------------------------------------------------- schedule
+    def tune_schedule(self, ens, stream_counts=(1, 2, 4, 8), steps_each=2):
+        """Capture the ensemble's graph for each branch count and member
+        order (as given; largest work first) and time `steps_each` replays
+        of each; keep the fastest.  Returns the timings."""
+        work = [m.sample_pts.shape[0] * (1 + m.n_maps) + m.mesh.nv * 20 for m in ens.members]
+        orders = {"given": list(range(len(ens.members))),
+                  "largest_first": sorted(range(len(ens.members)), key=lambda i: -work[i])}
+        stream = torch.cuda.current_stream(ens.device)
+        results = []
+        for name, order in orders.items():
+            for ns in stream_counts:
+                ens.capture(streams=ns, order=order)
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                for _ in range(steps_each):
+                    ens.step()
+                e1.record(stream)
+                torch.cuda.synchronize()
+                results.append({"order": name, "streams": ns, "ms_per_step": e0.elapsed_time(e1) / steps_each})
+        best = min(results, key=lambda r: r["ms_per_step"])
+        ens.capture(streams=best["streams"], order=orders[best["order"]])
+        self.log["schedule"] = {"best": best, "candidates": results}
+        return self.log["schedule"]
+
+    def save(self, path):
+        with open(path, "w") as f:
+            json.dump(self.log, f, indent=1)

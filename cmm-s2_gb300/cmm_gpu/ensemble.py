@@ -1,0 +1,157 @@
+"""Ensembles of barotropic runs of uneven sizes advanced together on one GPU.
+
+Each member is a BVESolver (its own map stack, velocity levels, vorticity
+and transform scratch); members of the same mesh level share the map mesh
+and its stencil frames, members of the same band-limit share the velocity
+mesh and the split-BF16 Pbar tables.  After every member's bootstrap, one
+device-driven step of all members (cmm_bve_step, whose varying state lives
+on the device) is captured into ONE CUDA graph, the members spread over
+parallel branches; every later step of the whole ensemble is one replay of
+that graph.  The branch count and member order of the graph and the launch
+shapes of the tunable kernels of each size class are chosen by the
+Autotuner from measured timings.
+
+No counterpart in the reference, which runs one simulation per process
+(cmm_s2/core/spherical_simulations.py); each member reproduces that
+driver's run.
+"""
+import time
+
+import numpy as np
+import torch
+
+from . import native
+from .meshgen import icosahedral_mesh, latlon_mesh_arrays, stencil_frames, identity_jets
+from .spherical_simulations import BVESolver, Vorticity
+from .workloads import spectral_perturbation
+
+
+class SharedResources:
+    """Read-only objects shared by the members: map meshes and stencil
+    frames per level, velocity meshes per band-limit (and record
+    precision), the MWSS sample points and the split-BF16 table owner per
+    band-limit."""
+
+    def __init__(self, device):
+        self.device = device
+        self._mesh, self._frames, self._vm, self._grid, self._sht = {}, {}, {}, {}, {}
+
+    def mesh(self, level):
+        if level not in self._mesh:
+            verts, tris = icosahedral_mesh(level)
+            self._mesh[level] = (verts, tris, native.Mesh(verts, tris, level, device=self.device.index))
+        return self._mesh[level]
+
+    def frames(self, level):
+        if level not in self._frames:
+            verts = self.mesh(level)[0]
+            tan, s_pts = stencil_frames(verts)
+            dev = self.device
+            self._frames[level] = (torch.from_numpy(np.ascontiguousarray(tan)).to(dev),
+                                   torch.from_numpy(np.ascontiguousarray(s_pts)).to(dev),
+                                   torch.from_numpy(identity_jets(verts)).to(dev))
+        return self._frames[level]
+
+    def velmesh(self, L, rec32):
+        key = (L, rec32)
+        if key not in self._vm:
+            theta, phi, grid, vverts = latlon_mesh_arrays(L)
+            vm = native.VelMesh(L, theta, phi, grid, vverts, device=self.device.index)
+            if rec32:
+                vm.set_records(native.VelMesh.REC_FP32)
+            self._vm[key] = (vm, grid)
+        return self._vm[key]
+
+    def sample_pts(self, L):
+        if L not in self._grid:
+            grid = latlon_mesh_arrays(L)[2]
+            self._grid[L] = torch.from_numpy(
+                np.ascontiguousarray(np.stack([g.reshape(-1) for g in grid], 1))).to(self.device)
+        return self._grid[L]
+
+    def sht_tables(self, L):
+        """The plan holding the split-BF16 tables of band-limit L, or None."""
+        return self._sht.get(L)
+
+    def set_sht_tables(self, L, sht):
+        self._sht.setdefault(L, sht)
+
+
+class Ensemble:
+    def __init__(self, members):
+        self.members = list(members)
+        self.device = self.members[0].device
+        self.graph = None
+        self.schedule = None
+        self.count = 0
+
+    @classmethod
+    def from_seed(cls, n, seed, levels=(5, 6, 7), bandlimits=(256, 512, 1024), Nt=100, T=0.5,
+                  lmax=64, rms=5.0, n_maps=10, precision="split_bf16", device=None):
+        """n members with mesh level and band-limit drawn from `seed`; each
+        starts from seeded random vorticity over l <= lmax with a k^-3
+        spectrum (coefficients N(0,1) l^-2, scaled to the given RMS),
+        evaluated through its scalar spline."""
+        device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
+        rng = np.random.default_rng(seed)
+        specs = [(int(rng.choice(levels)), int(rng.choice(bandlimits))) for _ in range(n)]
+        res = SharedResources(device)
+        members = []
+        for i, (level, L) in enumerate(specs):
+            pert = spectral_perturbation(lmax, seed=seed * 100003 + i, slope=-2.0, rms=rms)
+            members.append(BVESolver(None, None, level, L, Nt, T, Vorticity(spline_sh=pert),
+                                     n_maps=n_maps, precision=precision, resources=res))
+        ens = cls(members)
+        ens.specs = specs
+        ens.resources = res
+        return ens
+
+    # ----------------------------------------------------------------
+    def bootstrap(self):
+        for m in self.members:
+            m.bootstrap()
+            if m.precision_mode == native.Sht.SPLIT_BF16:
+                m.sht.trim()   # FP64 inverse scratch is needed only for the set-up
+        torch.cuda.synchronize(self.device)
+        return self
+
+    def capture(self, streams=4, order=None):
+        """One step of every member into one CUDA graph: members assigned
+        round-robin (in `order`, default as given) to `streams` parallel
+        branches forked from and joined into the capture stream."""
+        order = list(range(len(self.members))) if order is None else list(order)
+        g = torch.cuda.CUDAGraph()
+        side = [torch.cuda.Stream(self.device) for _ in range(streams)]
+        torch.cuda.synchronize(self.device)
+        with torch.cuda.graph(g):
+            cap = torch.cuda.current_stream(self.device)
+            for st in side:
+                st.wait_stream(cap)
+            for k, i in enumerate(order):
+                st = side[k % streams]
+                with torch.cuda.stream(st):
+                    native.check(native.lib.cmm_bve_step(self.members[i]._bve, native._stream(self.device)),
+                                 "cmm_bve_step")
+            for st in side:
+                cap.wait_stream(st)
+        self.graph, self.schedule = g, {"streams": streams, "order": order}
+        return self
+
+    def step(self):
+        """One step of every member: one graph launch."""
+        self.graph.replay()
+        for m in self.members:
+            m._advance_host()
+        self.count += 1
+
+    def run(self, nsteps=None):
+        n = self.members[0].Nt - 2 if nsteps is None else nsteps
+        for _ in range(n):
+            self.step()
+        return self
+
+    def member_steps(self):
+        return sum(m.count for m in self.members)
+
+    def memory_bytes(self):
+        return torch.cuda.memory_allocated(self.device)

@@ -58,6 +58,10 @@ _SIGS = {
     "cmm_sht_set_precision": (_i, [_p, _i]),
     "cmm_sht_status": (_i, [_p, _p, ctypes.POINTER(_i), _i]),
     "cmm_sht_power": (_i, [_p, _p, _p, _p]),
+    "cmm_sht_share_tables": (_i, [_p, _p]),
+    "cmm_sht_trim": (_i, [_p]),
+    "cmm_velmesh_set_records": (_i, [_p, _i]),
+    "cmm_mesh_set_block": (_i, [_p, _i, _i]),
     "cmm_bve_create": (_i, [ctypes.POINTER(BveDesc), ctypes.POINTER(_p)]),
     "cmm_bve_destroy": (_i, [_p]),
     "cmm_bve_step": (_i, [_p, _p]),
@@ -143,6 +147,13 @@ class Mesh:
             lib.cmm_mesh_destroy(h)
             self.h = None
 
+    TUNE_COMPOSE, TUNE_ADVECT, TUNE_VORTICITY, TUNE_LOCATE = 0, 1, 2, 3
+
+    def set_block(self, kernel, threads):
+        """Launch shape of a tunable kernel on this mesh (cmm_mesh_set_block)."""
+        check(lib.cmm_mesh_set_block(self.h, kernel, threads), "cmm_mesh_set_block")
+        return self
+
     # ------------------------------------------------------------------
     def status(self, clear=True):
         f = ctypes.c_int()
@@ -167,6 +178,9 @@ class Mesh:
         ncomp = jets.shape[0] if jets.dim() == 3 else 1
         if out is None:
             out = self.new_coeffs(ncomp)
+        want = torch.float32 if (ncomp == 3 and getattr(self, "rec32", False)) else torch.float64
+        if out.dtype != want or not out.is_contiguous():
+            raise TypeError(f"cmm_assemble: coefficient records must be contiguous {want}")
         check(lib.cmm_assemble(self.h, _ptr(jets), ncomp, _ptr(out), _stream(jets.device)),
               "cmm_assemble")
         return out
@@ -232,6 +246,20 @@ class VelMesh(Mesh):
         self.h = h
         self.stride = lib.cmm_coeff_stride(3)
 
+    REC_FP64, REC_FP32 = 0, 1
+
+    def set_records(self, precision):
+        """Velocity coefficient records in FP64 (default) or FP32
+        (cmm_velmesh_set_records)."""
+        with torch.cuda.device(self.device):
+            check(lib.cmm_velmesh_set_records(self.h, precision), "cmm_velmesh_set_records")
+        self.rec32 = precision == self.REC_FP32
+        return self
+
+    def new_coeffs(self, ncomp=3, batch=()):
+        dt = torch.float32 if (ncomp == 3 and getattr(self, "rec32", False)) else torch.float64
+        return torch.zeros((*batch, self.nt, lib.cmm_coeff_stride(ncomp)), dtype=dt, device=self.device)
+
     def vorticity(self, kind, params, X, rot_rate, sh=None, omega=None, spline=None):
         """omega (L+1, 2L) at the back-traced sample points X (Q,3)."""
         X = _dev(X)
@@ -285,6 +313,17 @@ class Sht:
     def set_precision(self, mode):
         with torch.cuda.device(self.device):
             check(lib.cmm_sht_set_precision(self.h, mode), "cmm_sht_set_precision")
+        return self
+
+    def share_tables(self, src):
+        """Split-BF16 mode on src's Pbar tables (cmm_sht_share_tables)."""
+        with torch.cuda.device(self.device):
+            check(lib.cmm_sht_share_tables(self.h, src.h), "cmm_sht_share_tables")
+        self._tables_from = src   # keep the owner alive
+        return self
+
+    def trim(self):
+        check(lib.cmm_sht_trim(self.h), "cmm_sht_trim")
         return self
 
     def status(self, clear=True):

@@ -56,35 +56,55 @@ class Vorticity:
 
 class BVESolver:
     def __init__(self, verts, tris, level, L, Nt, T, vorticity, rot_rate=2 * np.pi, n_maps=10,
-                 device=None, precision="fp64"):
+                 device=None, precision="fp64", resources=None):
+        """verts, tris: the icosahedral mesh of `level` (reference row order);
+        with `resources` (ensemble.SharedResources) they may be None and the
+        mesh, stencil frames, velocity mesh, sample points and split-BF16
+        tables are taken from (and shared through) it."""
         self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
         dev = self.device
+        if precision not in ("fp64", "split_bf16"):
+            raise ValueError("precision must be 'fp64' or 'split_bf16'")
+        split = precision == "split_bf16"
         self.vort = Vorticity.from_reference(vorticity)
         self.sh = None if self.vort.sh is None else torch.from_numpy(self.vort.sh).to(dev)
         self.L, self.Nt, self.T, self.rot, self.n_maps = L, Nt, T, rot_rate, n_maps
-        self.mesh = native.Mesh(verts, tris, level, device=dev.index)
-        theta, phi, grid, vverts = latlon_mesh_arrays(L)
-        self.vm = native.VelMesh(L, theta, phi, grid, vverts, device=dev.index)
-        self.sht = native.Sht(L, device=dev.index)
-        if precision == "split_bf16":
-            self.precision_mode = native.Sht.SPLIT_BF16
-            self.sht.set_precision(native.Sht.SPLIT_BF16)
-        elif precision == "fp64":
-            self.precision_mode = native.Sht.FP64
+        self.level = level
+        if resources is not None:
+            verts, tris, self.mesh = resources.mesh(level)
+            self.vm = resources.velmesh(L, split)[0]
+            self.tan, self.s_pts, self.id_jets = resources.frames(level)
+            self.sample_pts = resources.sample_pts(L)
         else:
-            raise ValueError("precision must be 'fp64' or 'split_bf16'")
-        tan, s_pts = stencil_frames(verts)
-        self.tan = torch.from_numpy(np.ascontiguousarray(tan)).to(dev)
-        self.s_pts = torch.from_numpy(np.ascontiguousarray(s_pts)).to(dev)
-        self.id_jets = torch.from_numpy(identity_jets(verts)).to(dev)
+            self.mesh = native.Mesh(verts, tris, level, device=dev.index)
+            theta, phi, grid, vverts = latlon_mesh_arrays(L)
+            self.vm = native.VelMesh(L, theta, phi, grid, vverts, device=dev.index)
+            if split:
+                # the mixed form keeps its velocity records in FP32
+                self.vm.set_records(native.VelMesh.REC_FP32)
+            tan, s_pts = stencil_frames(verts)
+            self.tan = torch.from_numpy(np.ascontiguousarray(tan)).to(dev)
+            self.s_pts = torch.from_numpy(np.ascontiguousarray(s_pts)).to(dev)
+            self.id_jets = torch.from_numpy(identity_jets(verts)).to(dev)
+            self.sample_pts = torch.from_numpy(
+                np.ascontiguousarray(np.stack([g.reshape(-1) for g in grid], 1))).to(dev)
+        self.sht = native.Sht(L, device=dev.index)
+        if split:
+            self.precision_mode = native.Sht.SPLIT_BF16
+            src = resources.sht_tables(L) if resources is not None else None
+            if src is not None:
+                self.sht.share_tables(src)
+            else:
+                self.sht.set_precision(native.Sht.SPLIT_BF16)
+                if resources is not None:
+                    resources.set_sht_tables(L, self.sht)
+        else:
+            self.precision_mode = native.Sht.FP64
         ns = [i for i in range(1, Nt) if i % n_maps == 0]
         ns.append(Nt)
         self.ns = ns
         self.tspan = np.linspace(0, T, Nt, endpoint=False)
         self.dt = self.tspan[1] - self.tspan[0]
-        self.sample_pts = torch.from_numpy(
-            np.ascontiguousarray(np.stack([g.reshape(-1) for g in grid], 1))).to(dev)
-        nv = len(verts)
         f64 = dict(dtype=torch.float64, device=dev)
         self.jets = self.id_jets.clone()
         self.coeffs_cur = self.mesh.new_coeffs()

@@ -220,6 +220,25 @@ int cmm_sht_set_precision(cmm_sht* plan, int mode) {
   return sht_set_precision(plan, mode);
 }
 
+int cmm_velmesh_set_records(cmm_mesh* velmesh, int precision) {
+  if (!velmesh || velmesh->view.kind != kLatLon) return arg_error("cmm_velmesh_set_records: velocity mesh expected");
+  if (precision != CMM_REC_FP64 && precision != CMM_REC_FP32)
+    return arg_error("cmm_velmesh_set_records: unknown precision");
+  if (precision == CMM_REC_FP32 && !velmesh->view.tri_asm_f) {
+    int rc = make_asm_f32(velmesh);
+    if (rc) return rc;
+  }
+  velmesh->view.rec32 = precision == CMM_REC_FP32 ? 1 : 0;
+  return CMM_OK;
+}
+
+int cmm_mesh_set_block(cmm_mesh* mesh, int kernel, int threads) {
+  if (!mesh || kernel < 0 || kernel > 3 || threads < 0 || threads > 256 || threads % 32 != 0)
+    return arg_error("cmm_mesh_set_block: bad argument");
+  mesh->view.block[kernel] = threads;
+  return CMM_OK;
+}
+
 int cmm_bve_create(const cmm_bve_desc* desc, cmm_bve** out) { return bve_create(desc, out); }
 
 int cmm_bve_destroy(cmm_bve* bve) { return bve_destroy(bve); }
@@ -237,6 +256,16 @@ int cmm_bve_state(cmm_bve* bve, void* stream, int* count, int* nc, int* identity
 int cmm_sht_power(cmm_sht* plan, const double* alm, double* power, void* stream) {
   if (!plan || !alm || !power) return arg_error("cmm_sht_power: null pointer");
   return sht_power(plan, (const double2*)alm, power, (cudaStream_t)stream);
+}
+
+int cmm_sht_share_tables(cmm_sht* plan, cmm_sht* src) {
+  if (!plan || !src) return arg_error("cmm_sht_share_tables: null plan");
+  return sht_share_tables(plan, src);
+}
+
+int cmm_sht_trim(cmm_sht* plan) {
+  if (!plan) return arg_error("cmm_sht_trim: null plan");
+  return sht_trim(plan);
 }
 
 int cmm_sht_status(cmm_sht* plan, void* stream, int* flags, int clear) {

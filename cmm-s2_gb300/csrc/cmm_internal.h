@@ -47,7 +47,18 @@ struct MeshView {
   const double* phi;        // (2L) longitudes
   const double* grid;       // ((L+1)*2L, 4) ring points x,y,z,0
   double dphi, dthe;
+  // velocity records (ncomp = 3) in FP32 (cmm_velmesh_set_records):
+  // (nt, 64) floats, assembled from the FP32 copy of the factors
+  int rec32;
+  const float* tri_asm_f;   // (kAsmFactors, nt), factor-major, when rec32
+  // launch shapes chosen by an autotuner (cmm_mesh_set_block), threads per
+  // block of the tunable kernels on this mesh; 0 = the library default
+  int block[4];
 };
+
+// Tunable kernels (index into MeshView::block).
+constexpr int kTuneCompose = 0, kTuneAdvect = 1, kTuneVorticity = 2, kTuneLocate = 3;
+inline int block_of(const MeshView& m, int k, int dflt) { return m.block[k] > 0 ? m.block[k] : dflt; }
 
 constexpr int kIcosahedral = 0;
 constexpr int kLatLon = 1;
@@ -64,6 +75,7 @@ struct DeviceBuffer {
   ~DeviceBuffer();
   int alloc(size_t n);
   int upload(const void* src, size_t n);
+  void release();
 };
 
 }  // namespace cmm
@@ -71,7 +83,7 @@ struct DeviceBuffer {
 struct cmm_mesh {
   cmm::MeshView view;
   cmm::DeviceBuffer verts, tri_v, tri_loc, tri_asm, root, root_f, root_adj, node_n, node_nf, leaf_row,
-      status, theta, phi, grid, cos_theta;
+      status, theta, phi, grid, cos_theta, tri_asm_f;
 };
 
 namespace cmm {
@@ -160,6 +172,8 @@ int launch_vorticity(int kind, const double* params, int nparams, const double* 
                      int64_t Q, int npr, const double* cos_ring, double* omega, cudaStream_t s);
 
 int launch_fp64_probe(int blocks, int iters, double* sink, cudaStream_t s);
+// FP32 copy of a mesh's factor table (velmesh records in FP32).
+int make_asm_f32(cmm_mesh* m);
 
 // spherical-harmonic transforms (sht.cu)
 int sht_create(int L, cmm_sht** out);
@@ -171,6 +185,8 @@ int sht_velocity(cmm_sht* p, const cmm_mesh* vm, const double* omega, double2* p
                  double* jets, cudaStream_t s);
 int sht_scalar_jets(cmm_sht* p, const cmm_mesh* vm, const double2* alm, double* jets, cudaStream_t s);
 int sht_power(cmm_sht* p, const double2* alm, double* power, cudaStream_t s);
+int sht_share_tables(cmm_sht* p, const cmm_sht* src);
+int sht_trim(cmm_sht* p);
 int bve_create(const cmm_bve_desc* d, cmm_bve** out);
 int bve_step(cmm_bve* b, cudaStream_t s);
 int bve_destroy(cmm_bve* b);
@@ -186,6 +202,7 @@ struct TcPlan;
 int tc_plan_create(int L, const double* ct_rings, const double* pmm_rings, const double* ct_fine,
                    const double* pmm_fine, const double* ra, const double* rb, TcPlan** out);
 void tc_plan_destroy(TcPlan* p);
+int tc_plan_share(const TcPlan* src, TcPlan** out);
 size_t tc_plan_bytes(const TcPlan* p);
 int tc_synthesis(TcPlan* p, const double2* fields, float2* S, int* status, cudaStream_t s);
 int tc_analysis(TcPlan* p, const float2* fine, const double* w, double2* alm, int* status,

@@ -171,6 +171,32 @@ __device__ __forceinline__ void sbb(const Ords<NC>& o, const Gam& g, double* P) 
            vc * o.c[5][c];
 }
 
+// FP32 velocity records: the six ordinates of the sub-triangle and the
+// patch in FP32 (the barycentrics and sub-triangle choice stay FP64).
+template <int NC>
+struct OrdsF {
+  float c[6][NC];
+};
+
+template <int NC>
+__device__ __forceinline__ void load_ords_f(const float* rec, const Split& sp, OrdsF<NC>& o) {
+  const int* id = kSplitOrd[sp.lo][sp.hi];
+#pragma unroll
+  for (int k = 0; k < 6; ++k)
+#pragma unroll
+    for (int c = 0; c < NC; ++c) o.c[k][c] = __ldg(rec + NC * id[k] + c);
+}
+
+template <int NC>
+__device__ __forceinline__ void sbb_f(const OrdsF<NC>& o, float V, float E, float C, float* P) {
+  const float vv = V * V, ee = E * E, cc = C * C;
+  const float ve = 2 * V * E, ec = 2 * E * C, vc = 2 * V * C;
+#pragma unroll
+  for (int c = 0; c < NC; ++c)
+    P[c] = vv * o.c[0][c] + ee * o.c[1][c] + cc * o.c[2][c] + ve * o.c[3][c] + ec * o.c[4][c] +
+           vc * o.c[5][c];
+}
+
 __device__ __forceinline__ void load_loc(const MeshView& m, int t, double* Lr) {
   const double* L = m.tri_loc + (int64_t)t * kLocStride;
 #pragma unroll

@@ -165,6 +165,68 @@ __global__ void __launch_bounds__(kAsmTri) assemble_kernel(MeshView m, const dou
   for (int i = tl; i < nblk * kStride; i += kAsmTri) dst[i] = rec[(i / kStride) * kRow + i % kStride];
 }
 
+// FP32 velocity records (velmesh with rec32, ncomp = 3): the same
+// ordinates from FP32 jets and the FP32 factor table, in FP32.
+__global__ void __launch_bounds__(kAsmTri) assemble_f32_kernel(MeshView m, const double* __restrict__ jets,
+                                                               float* __restrict__ coeffs,
+                                                               const BveState* __restrict__ st) {
+  if (st) coeffs = (float*)st->vel[0];
+  constexpr int kStride = kCoeffStride3;
+  constexpr int kRow = kStride + 1;
+  __shared__ float rec[kAsmTri * kRow];
+  const int t0 = blockIdx.x * kAsmTri;
+  const int nblk = min(kAsmTri, m.nt - t0);
+  const int tl = threadIdx.x, t = t0 + tl;
+  float* out = rec + tl * kRow;
+  if (tl < nblk) {
+    const int nv = m.nv, nt = m.nt;
+    const int4 tv = m.tri_v[t];
+    const int vid[3] = {tv.x, tv.y, tv.z};
+    const float* A = m.tri_asm_f + t;
+    const int corner[9] = {0, 0, 0, 1, 1, 1, 2, 2, 2};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      float f[3], c[19];
+#pragma unroll
+      for (int v = 0; v < 3; ++v) f[v] = (float)__ldg(jets + (int64_t)(k * 4) * nv + vid[v]);
+      c[0] = f[0];
+      c[1] = f[1];
+      c[2] = f[2];
+#pragma unroll
+      for (int o = 0; o < 9; ++o) {
+        const int v = vid[corner[o]];
+        const float gx = (float)__ldg(jets + (int64_t)(0 * 4 + 1 + k) * nv + v);
+        const float gy = (float)__ldg(jets + (int64_t)(1 * 4 + 1 + k) * nv + v);
+        const float gz = (float)__ldg(jets + (int64_t)(2 * 4 + 1 + k) * nv + v);
+        c[3 + o] = __ldg(A + (int64_t)(4 * o) * nt) * gx + __ldg(A + (int64_t)(4 * o + 1) * nt) * gy +
+                   __ldg(A + (int64_t)(4 * o + 2) * nt) * gz - __ldg(A + (int64_t)(4 * o + 3) * nt) * f[corner[o]];
+      }
+      float e[9];
+#pragma unroll
+      for (int j = 0; j < 9; ++j) e[j] = __ldg(A + (int64_t)(36 + j) * nt);
+      c[12] = e[0] * c[3] + e[1] * c[8];
+      c[13] = e[2] * c[6] + e[3] * c[11];
+      c[14] = e[5] * c[9] + e[4] * c[5];
+      c[15] = e[0] * c[4] + e[1] * c[7];
+      c[16] = e[2] * c[7] + e[3] * c[10];
+      c[17] = e[4] * c[4] + e[5] * c[10];
+      c[18] = e[6] * c[4] + e[7] * c[7] + e[8] * c[10];
+#pragma unroll
+      for (int o = 0; o < 19; ++o) out[3 * o + k] = c[o];
+    }
+#pragma unroll
+    for (int j = 57; j < kStride; ++j) out[j] = 0.f;
+  }
+  __syncthreads();
+  float* dst = coeffs + (int64_t)t0 * kStride;
+  for (int i = tl; i < nblk * kStride; i += kAsmTri) dst[i] = rec[(i / kStride) * kRow + i % kStride];
+}
+
+__global__ void to_f32_kernel(const double* __restrict__ a, int64_t n, float* __restrict__ b) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (float)a[i];
+}
+
 template <bool JAC, class Src>
 __global__ void __launch_bounds__(kBlock) compose_kernel(MeshView m, Src cp,
                                                          const double* __restrict__ q, int64_t n,
@@ -276,14 +338,17 @@ int check_launch(const char* what) {
 int launch_locate(const MeshView& m, const double* q, int64_t n, int32_t* tri, double* bcc,
                   cudaStream_t s) {
   if (n == 0) return CMM_OK;
-  locate_kernel<<<grid_for(n, kBlock), kBlock, 0, s>>>(m, q, n, tri, bcc);
+  const int b = block_of(m, kTuneLocate, kBlock);
+  locate_kernel<<<grid_for(n, b), b, 0, s>>>(m, q, n, tri, bcc);
   return check_launch("locate_kernel");
 }
 
 int launch_assemble(const MeshView& m, const double* jets, int ncomp, double* coeffs,
                     cudaStream_t s, const BveState* st) {
   const int blocks = (m.nt + kAsmTri - 1) / kAsmTri;
-  if (ncomp == 3)
+  if (ncomp == 3 && m.rec32)
+    assemble_f32_kernel<<<blocks, kAsmTri, 0, s>>>(m, jets, (float*)coeffs, st);
+  else if (ncomp == 3)
     assemble_kernel<3><<<blocks, kAsmTri, 0, s>>>(m, jets, coeffs, st);
   else
     assemble_kernel<1><<<blocks, kAsmTri, 0, s>>>(m, jets, coeffs, st);
@@ -297,19 +362,33 @@ int launch_compose(const MeshView& m, const double* const* coeffs, int S, const 
   SubmapPtrs cp;
   cp.S = S;
   for (int k = 0; k < S; ++k) cp.p[k] = coeffs[k];
-  const int g = grid_for(n, kBlock);
+  const int b = block_of(m, kTuneCompose, kBlock);
+  const int g = grid_for(n, b);
   if (jac)
-    compose_kernel<true><<<g, kBlock, 0, s>>>(m, cp, q, n, out, tri, tri_all, jac);
+    compose_kernel<true><<<g, b, 0, s>>>(m, cp, q, n, out, tri, tri_all, jac);
   else
-    compose_kernel<false><<<g, kBlock, 0, s>>>(m, cp, q, n, out, tri, tri_all, jac);
+    compose_kernel<false><<<g, b, 0, s>>>(m, cp, q, n, out, tri, tri_all, jac);
   return check_launch("compose_kernel");
+}
+
+int make_asm_f32(cmm_mesh* mesh) {
+  const int64_t n = (int64_t)kAsmFactors * mesh->view.nt;
+  int rc = mesh->tri_asm_f.alloc(n * sizeof(float));
+  if (rc) return rc;
+  to_f32_kernel<<<(int)((n + 255) / 256), 256>>>(mesh->view.tri_asm, n, (float*)mesh->tri_asm_f.p);
+  if ((rc = check_launch("to_f32_kernel"))) return rc;
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return cuda_fail(e, "make_asm_f32");
+  mesh->view.tri_asm_f = (const float*)mesh->tri_asm_f.p;
+  return CMM_OK;
 }
 
 int launch_compose_dev(const MeshView& m, const double* const* table, const BveState* st,
                        const double* last, const double* q, int64_t n, double* out, cudaStream_t s) {
   if (n == 0) return CMM_OK;
   DevSubmaps cp{table, st, last};
-  compose_kernel<false><<<grid_for(n, kBlock), kBlock, 0, s>>>(m, cp, q, n, out, nullptr, nullptr,
+  const int b = block_of(m, kTuneCompose, kBlock);
+  compose_kernel<false><<<grid_for(n, b), b, 0, s>>>(m, cp, q, n, out, nullptr, nullptr,
                                                                 nullptr);
   return check_launch("compose_kernel");
 }

@@ -38,6 +38,12 @@ DeviceBuffer::~DeviceBuffer() {
   if (p) cudaFree(p);
 }
 
+void DeviceBuffer::release() {
+  if (p) cudaFree(p);
+  p = nullptr;
+  bytes = 0;
+}
+
 int DeviceBuffer::alloc(size_t n) {
   if (p) cudaFree(p);
   p = nullptr;

@@ -540,8 +540,6 @@ int sht_create(int L, cmm_sht** out) {
   if ((rc = p->pad.alloc((size_t)4 * L * L * c16))) return fail(rc);
   if ((rc = p->alm.alloc((size_t)L * L * c16))) return fail(rc);
   if ((rc = p->fields.alloc((size_t)kFields * L * L * c16))) return fail(rc);
-  if ((rc = p->synth.alloc((size_t)kFields * (L + 1) * (L + 1) * c16))) return fail(rc);
-  if ((rc = p->samples.alloc((size_t)kFields * (L + 1) * 2 * L * 8))) return fail(rc);
   {
     const int zero = 0;
     if ((rc = p->status.upload(&zero, sizeof(int)))) return fail(rc);
@@ -579,6 +577,17 @@ static int set_streams(cmm_sht* p, cudaStream_t s) {
     cufftResult r = cufftSetStream(h[k], s);
     if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftSetStream");
   }
+  return CMM_OK;
+}
+
+// Scratch of the FP64 inverse (spectra and samples of 12 fields, about
+// 400 MB at L = 1024), allocated at its first use and released by
+// cmm_sht_trim.
+static int ensure_fp64_inverse(cmm_sht* p) {
+  const int L = p->L;
+  int rc;
+  if (!p->synth.p && (rc = p->synth.alloc((size_t)kFields * (L + 1) * (L + 1) * sizeof(double2)))) return rc;
+  if (!p->samples.p && (rc = p->samples.alloc((size_t)kFields * (L + 1) * 2 * L * 8))) return rc;
   return CMM_OK;
 }
 
@@ -677,6 +686,7 @@ int sht_inverse(cmm_sht* p, const double2* alm, int nf, double* samples, cudaStr
     }
     return CMM_OK;
   }
+  if ((rc = ensure_fp64_inverse(p))) return rc;
   double2* S = (double2*)p->synth.p;
   // all kFields spectra: the batched Z2D below transforms every row
   cudaError_t e = cudaMemsetAsync(S, 0, (size_t)kFields * (L + 1) * (L + 1) * sizeof(double2), s);
@@ -772,11 +782,36 @@ int sht_set_precision(cmm_sht* p, int mode) {
                             (const double*)p->ct_fine.p, (const double*)p->pmm_fine.p,
                             (const double*)p->ra.p, (const double*)p->rb.p, &p->tc);
     if (rc) return rc;
-    if ((rc = make_float_plans(p))) return rc;
+    if (!p->have_fplans[0] && (rc = make_float_plans(p))) return rc;
     cudaError_t e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return cuda_fail(e, "cmm_sht_set_precision");
   }
   p->precision = mode;
+  return CMM_OK;
+}
+
+int sht_share_tables(cmm_sht* p, const cmm_sht* src) {
+  if (!src->tc || src->L != p->L) {
+    set_last_error("cmm_sht_share_tables: source plan of the same L in CMM_SHT_SPLIT_BF16 mode expected");
+    return CMM_ERR_ARG;
+  }
+  if (p->tc) {
+    tc_plan_destroy(p->tc);
+    p->tc = nullptr;
+  }
+  int rc = tc_plan_share(src->tc, &p->tc);
+  if (rc) return rc;
+  if (!p->have_fplans[0] && (rc = make_float_plans(p))) return rc;
+  p->precision = CMM_SHT_SPLIT_BF16;
+  cudaError_t e = cudaDeviceSynchronize();
+  return e == cudaSuccess ? CMM_OK : cuda_fail(e, "cmm_sht_share_tables");
+}
+
+int sht_trim(cmm_sht* p) {
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return cuda_fail(e, "cmm_sht_trim");
+  p->synth.release();
+  p->samples.release();
   return CMM_OK;
 }
 

@@ -30,6 +30,7 @@
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 
+#include <memory>
 #include <vector>
 
 #include "cmm_internal.h"
@@ -220,19 +221,20 @@ __global__ void build_ptab_kernel(TcGeometry g, const double* __restrict__ ct,
 }
 
 // Per step: the 12 coefficient fields (12, L, L) [f][m][l] complex -> A tile
-// images per (m, chunk): column n = 2f + (0 re, 1 im), n >= 24 zero.
+// images per (m, chunk): column n = 2f + (0 re, 1 im); columns n >= 24 are
+// zeroed once when the plan is made and never written.
 __global__ void build_atab_kernel(TcGeometry g, const double2* __restrict__ fields,
                                   unsigned char* __restrict__ atab) {
   const int m = blockIdx.y;
   const int L = g.L;
   const int nch = nchunks(L, m);
-  const int per_chunk = 2 * kN * kKc;   // (par, n, k)
+  const int per_chunk = 2 * kNUsed * kKc;   // (par, n < 24, k)
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nch * per_chunk; e += gridDim.x * blockDim.x) {
     const int c = e / per_chunk, r = e % per_chunk;
-    const int par = r / (kN * kKc), n = (r / kKc) % kN, k = r % kKc;
+    const int par = r / (kNUsed * kKc), n = (r / kKc) % kNUsed, k = r % kKc;
     const int l = m + par + 2 * (c * kKc + k);
     double v = 0.0;
-    if (n < kNUsed && l < L) {
+    if (l < L) {
       const double2 a = fields[(int64_t)(n >> 1) * L * L + (int64_t)m * L + l];
       v = (n & 1) ? a.y : a.x;
     }
@@ -438,13 +440,15 @@ __global__ void build_xtab_kernel(TcFwdGeometry g, const float2* __restrict__ fi
                                   const double* __restrict__ w, unsigned char* __restrict__ xtab) {
   const int m = blockIdx.y;
   const int L = g.L;
-  const int total = g.nck * 2 * kNA * kKc;
+  // only the 2 used columns (re, im); columns 2..15 are zeroed once when
+  // the plan is made and never written
+  const int total = g.nck * 2 * 2 * kKc;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
-    const int c = e / (2 * kNA * kKc), r = e % (2 * kNA * kKc);
-    const int par = r / (kNA * kKc), n = (r / kKc) % kNA, k = r % kKc;
+    const int c = e / (2 * 2 * kKc), r = e % (2 * 2 * kKc);
+    const int par = r / (2 * kKc), n = (r / kKc) % 2, k = r % kKc;
     const int j = c * kKc + k;
     double v = 0.0;
-    if (n < 2 && j <= L) {
+    if (j <= L) {
       const float2 af = fine[(int64_t)j * L + m];
       const double2 a = make_double2(af.x, af.y);
       double2 s;
@@ -573,12 +577,19 @@ int check(const char* what) {
 }  // namespace
 
 // Host side --------------------------------------------------------------
+// The Pbar tables (read-only once built) may be shared by several plans
+// of the same band-limit (tc_plan_share); the per-call data tiles atab /
+// xtab are each plan's own, so plans sharing tables run concurrently.
+struct TcTables {
+  DeviceBuffer cbase, ptab, lbase, ftab;
+};
+
 struct TcPlan {
   int L = 0, npair = 0, nrb = 0, total_chunks = 0;
-  DeviceBuffer cbase, ptab, atab;
   // analysis: degree blocks of 128 per m (prefix sums), ring-pair chunks
   int nck = 0, total_lblocks = 0;
-  DeviceBuffer lbase, ftab, xtab;
+  std::shared_ptr<TcTables> tab;
+  DeviceBuffer atab, xtab;
 };
 
 static int tc_chunks(int L, int m) {
@@ -593,6 +604,7 @@ int tc_plan_create(int L, const double* ct_rings, const double* pmm_rings, const
     set_last_error("tc plan: out of host memory");
     return CMM_ERR_ARG;
   }
+  p->tab = std::make_shared<TcTables>();
   p->L = L;
   p->npair = L / 2 + 1;
   p->nrb = (p->npair + kM - 1) / kM;
@@ -600,16 +612,17 @@ int tc_plan_create(int L, const double* ct_rings, const double* pmm_rings, const
   for (int m = 0; m < L; ++m) cb[m + 1] = cb[m] + tc_chunks(L, m);
   p->total_chunks = cb[L];
   int rc;
-  if ((rc = p->cbase.upload(cb.data(), cb.size() * sizeof(int))) ||
-      (rc = p->ptab.alloc((size_t)p->total_chunks * p->nrb * kPRecord)) ||
+  if ((rc = p->tab->cbase.upload(cb.data(), cb.size() * sizeof(int))) ||
+      (rc = p->tab->ptab.alloc((size_t)p->total_chunks * p->nrb * kPRecord)) ||
       (rc = p->atab.alloc((size_t)p->total_chunks * kARecord))) {
     delete p;
     return rc;
   }
-  cudaMemset(p->ptab.p, 0, p->ptab.bytes);
-  TcGeometry g{L, p->npair, p->nrb, (const int*)p->cbase.p};
+  cudaMemset(p->tab->ptab.p, 0, p->tab->ptab.bytes);
+  cudaMemset(p->atab.p, 0, p->atab.bytes);
+  TcGeometry g{L, p->npair, p->nrb, (const int*)p->tab->cbase.p};
   dim3 grid((p->nrb * kM + 127) / 128, L);
-  build_ptab_kernel<<<grid, 128>>>(g, ct_rings, pmm_rings, ra, rb, (unsigned char*)p->ptab.p);
+  build_ptab_kernel<<<grid, 128>>>(g, ct_rings, pmm_rings, ra, rb, (unsigned char*)p->tab->ptab.p);
   if ((rc = check("build_ptab_kernel"))) {
     delete p;
     return rc;
@@ -625,16 +638,17 @@ int tc_plan_create(int L, const double* ct_rings, const double* pmm_rings, const
   std::vector<int> lb(L + 1, 0);
   for (int m = 0; m < L; ++m) lb[m + 1] = lb[m] + ((L - m + 1) / 2 + kM - 1) / kM;
   p->total_lblocks = lb[L];
-  if ((rc = p->lbase.upload(lb.data(), lb.size() * sizeof(int))) ||
-      (rc = p->ftab.alloc((size_t)p->total_lblocks * p->nck * kPRecord)) ||
+  if ((rc = p->tab->lbase.upload(lb.data(), lb.size() * sizeof(int))) ||
+      (rc = p->tab->ftab.alloc((size_t)p->total_lblocks * p->nck * kPRecord)) ||
       (rc = p->xtab.alloc((size_t)L * p->nck * kXRecord))) {
     delete p;
     return rc;
   }
-  cudaMemset(p->ftab.p, 0, p->ftab.bytes);
-  TcFwdGeometry gf{L, p->nck, (const int*)p->lbase.p};
+  cudaMemset(p->tab->ftab.p, 0, p->tab->ftab.bytes);
+  cudaMemset(p->xtab.p, 0, p->xtab.bytes);
+  TcFwdGeometry gf{L, p->nck, (const int*)p->tab->lbase.p};
   build_ftab_kernel<<<dim3((L + 1 + 127) / 128, L), 128>>>(gf, ct_fine, pmm_fine, ra, rb,
-                                                            (unsigned char*)p->ftab.p);
+                                                            (unsigned char*)p->tab->ftab.p);
   if ((rc = check("build_ftab_kernel"))) {
     delete p;
     return rc;
@@ -652,16 +666,45 @@ int tc_plan_create(int L, const double* ct_rings, const double* pmm_rings, const
 void tc_plan_destroy(TcPlan* p) { delete p; }
 
 size_t tc_plan_bytes(const TcPlan* p) {
-  return p->ptab.bytes + p->atab.bytes + p->ftab.bytes + p->xtab.bytes;
+  return p->tab->ptab.bytes + p->atab.bytes + p->tab->ftab.bytes + p->xtab.bytes;
+}
+
+// A plan of the same band-limit using src's Pbar tables and its own tiles.
+int tc_plan_share(const TcPlan* src, TcPlan** out) {
+  TcPlan* p = new (std::nothrow) TcPlan();
+  if (!p) {
+    set_last_error("tc plan: out of host memory");
+    return CMM_ERR_ARG;
+  }
+  p->L = src->L;
+  p->npair = src->npair;
+  p->nrb = src->nrb;
+  p->total_chunks = src->total_chunks;
+  p->nck = src->nck;
+  p->total_lblocks = src->total_lblocks;
+  p->tab = src->tab;
+  int rc;
+  if ((rc = p->atab.alloc(src->atab.bytes)) || (rc = p->xtab.alloc(src->xtab.bytes))) {
+    delete p;
+    return rc;
+  }
+  cudaError_t e = cudaMemset(p->atab.p, 0, p->atab.bytes);
+  if (e == cudaSuccess) e = cudaMemset(p->xtab.p, 0, p->xtab.bytes);
+  if (e != cudaSuccess) {
+    delete p;
+    return cuda_fail(e, "tc_plan_share");
+  }
+  *out = p;
+  return CMM_OK;
 }
 
 int tc_synthesis(TcPlan* p, const double2* fields, float2* S, int* status, cudaStream_t s) {
-  TcGeometry g{p->L, p->npair, p->nrb, (const int*)p->cbase.p};
+  TcGeometry g{p->L, p->npair, p->nrb, (const int*)p->tab->cbase.p};
   build_atab_kernel<<<dim3(16, p->L), 256, 0, s>>>(g, fields, (unsigned char*)p->atab.p);
   int rc = check("build_atab_kernel");
   if (rc) return rc;
   synth_tc_kernel<<<dim3(p->nrb, p->L), kThreads, kPRecord + kARecord, s>>>(
-      g, (const unsigned char*)p->ptab.p, (const unsigned char*)p->atab.p, S, status);
+      g, (const unsigned char*)p->tab->ptab.p, (const unsigned char*)p->atab.p, S, status);
   return check("synth_tc_kernel");
 }
 
@@ -670,13 +713,13 @@ int tc_synthesis(TcPlan* p, const double2* fields, float2* S, int* status, cudaS
 int tc_analysis(TcPlan* p, const float2* fine, const double* w, double2* alm, int* status,
                 cudaStream_t s) {
   const int L = p->L;
-  TcFwdGeometry g{L, p->nck, (const int*)p->lbase.p};
+  TcFwdGeometry g{L, p->nck, (const int*)p->tab->lbase.p};
   build_xtab_kernel<<<dim3(8, L), 256, 0, s>>>(g, fine, w, (unsigned char*)p->xtab.p);
   int rc = check("build_xtab_kernel");
   if (rc) return rc;
   const int maxlb = ((L + 1) / 2 + kM - 1) / kM;
   analysis_tc_kernel<<<dim3(maxlb, L), kThreads, kPRecord + kXRecord, s>>>(
-      g, (const unsigned char*)p->ftab.p, (const unsigned char*)p->xtab.p, alm, status);
+      g, (const unsigned char*)p->tab->ftab.p, (const unsigned char*)p->xtab.p, alm, status);
   return check("analysis_tc_kernel");
 }
 

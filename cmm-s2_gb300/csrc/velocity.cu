@@ -26,6 +26,7 @@ using namespace dev;
 namespace {
 
 constexpr int kBlock = 128;
+constexpr int kMaxBlock = 256;   // bound of the tunable advect kernel
 
 // Velocity at q: the Powell-Sabin patch of each time level, combined with
 // the stage's Lagrange weights w (spline_interp_velocity.__call__,
@@ -48,6 +49,26 @@ __device__ __forceinline__ void velocity_at(const MeshView& m, const VelPtrs& vc
   const Split sp = split_of(b);
   const Gam g = gamma_of(Lr, b, sp);
   V[0] = V[1] = V[2] = 0.0;
+  if (m.rec32) {  // FP32 records: patches and time combination in FP32
+    const float gV = (float)g.V, gE = (float)g.E, gC = (float)g.C;
+    float Vf[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int l = 0; l < 3; ++l) {
+      if (l >= nvs) break;
+      const float wl = (float)(l == 0 ? w.a : (l == 1 ? w.b : w.c));
+      OrdsF<3> o;
+      load_ords_f<3>((const float*)vc.p[l] + (int64_t)t * kCoeffStride3, sp, o);
+      float P[3];
+      sbb_f<3>(o, gV, gE, gC, P);
+      Vf[0] += wl * P[0];
+      Vf[1] += wl * P[1];
+      Vf[2] += wl * P[2];
+    }
+    V[0] = Vf[0];
+    V[1] = Vf[1];
+    V[2] = Vf[2];
+    return;
+  }
 #pragma unroll
   for (int l = 0; l < 3; ++l) {
     if (l >= nvs) break;
@@ -167,7 +188,7 @@ __global__ void __launch_bounds__(kBlock) integrate_kernel(MeshView m, VelPtrs v
 // (advect, cmm_s2/core/evolution_functions.py:117-133).  Point i < nv is
 // vertex i, point nv + k*nv + v is stencil point k of vertex v.  work:
 // yn (3,nv) followed by the stencil foot points (3,4,nv).
-__global__ void __launch_bounds__(kBlock) advect_points_kernel(MeshView mesh, MeshView vm, VelPtrs vc,
+__global__ void __launch_bounds__(kMaxBlock) advect_points_kernel(MeshView mesh, MeshView vm, VelPtrs vc,
                                                                int nvs, TimeWeights tw, int scheme,
                                                                double dt,
                                                                const double* __restrict__ s_pts,
@@ -302,7 +323,8 @@ int launch_advect_points(const MeshView& mesh, const MeshView& vm, VelPtrs vc, i
                          const TimeWeights& tw, int scheme, double dt, const double* s_pts,
                          double* work, cudaStream_t s, const BveState* st) {
   const int64_t n = 5LL * mesh.nv;
-  advect_points_kernel<<<grid_for(n, kBlock), kBlock, 0, s>>>(mesh, vm, vc, nvs, tw, scheme, dt,
+  const int b = block_of(mesh, kTuneAdvect, kBlock);
+  advect_points_kernel<<<grid_for(n, b), b, 0, s>>>(mesh, vm, vc, nvs, tw, scheme, dt,
                                                                s_pts, work, st);
   return check_launch("advect_points_kernel");
 }

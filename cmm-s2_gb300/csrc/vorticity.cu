@@ -97,7 +97,7 @@ __device__ double sh_value(const double* __restrict__ c, int lmax, double phi, d
   return out;
 }
 
-__global__ void vorticity_kernel(VortParams vp, const double* __restrict__ sh, int lmax,
+__global__ void __launch_bounds__(256) vorticity_kernel(VortParams vp, const double* __restrict__ sh, int lmax,
                                  MeshView vm, const double* __restrict__ spline, double rot,
                                  const double* __restrict__ X, int64_t Q, int npr,
                                  const double* __restrict__ cos_ring, double* __restrict__ omega) {
@@ -123,7 +123,8 @@ int launch_vorticity(int kind, const double* params, int nparams, const double* 
   VortParams vp{};
   vp.kind = kind;
   for (int k = 0; k < nparams && k < 12; ++k) vp.p[k] = params[k];
-  vorticity_kernel<<<grid_for(Q, 128), 128, 0, s>>>(vp, sh, lmax, vm, spline, rot, X, Q, npr,
+  const int b = block_of(vm, kTuneVorticity, 128);
+  vorticity_kernel<<<grid_for(Q, b), b, 0, s>>>(vp, sh, lmax, vm, spline, rot, X, Q, npr,
                                                     cos_ring, omega);
   note_launch();
   cudaError_t e = cudaGetLastError();

@@ -242,6 +242,15 @@ int cmm_sht_destroy(cmm_sht* plan);
 #define CMM_SHT_FP64 0
 #define CMM_SHT_SPLIT_BF16 1
 int cmm_sht_set_precision(cmm_sht* plan, int mode);
+/* Put `plan` in CMM_SHT_SPLIT_BF16 mode using the Pbar tables of `src`
+ * (same L, already in that mode) instead of building its own: plans of one
+ * band-limit share the ~4.4 GB of tables at L = 1024 and still run
+ * concurrently (each keeps its own data tiles and FFT scratch). */
+int cmm_sht_share_tables(cmm_sht* plan, cmm_sht* src);
+/* Release the FP64 inverse scratch (about 400 MB at L = 1024); it is
+ * allocated again at the next FP64 inverse (cmm_sht_inverse, the FP64
+ * velocity, cmm_sht_scalar_jets).  Synchronises the device. */
+int cmm_sht_trim(cmm_sht* plan);
 /* Read (and with clear != 0, reset) the plan's device status word
  * (CMM_FLAG_TIMEOUT); synchronises `stream`. */
 int cmm_sht_status(cmm_sht* plan, void* stream, int* flags, int clear);
@@ -273,6 +282,30 @@ int cmm_sht_velocity(cmm_sht* plan, const cmm_mesh* velmesh, const double* omega
  * (ncomp = 1) this builds the scalar spherical_spline of the field. */
 int cmm_sht_scalar_jets(cmm_sht* plan, const cmm_mesh* velmesh, const double* alm, double* jets,
                         void* stream);
+
+/* Storage of this velocity mesh's velocity coefficient records (ncomp = 3):
+ * CMM_REC_FP64 (default; (nt, 64) doubles) or CMM_REC_FP32 ((nt, 64)
+ * floats: cmm_assemble with ncomp = 3 writes FP32 ordinates computed in
+ * FP32 from the FP64 jets, and velocity evaluation forms the patches and
+ * their time combination in FP32; location, barycentrics, the RK4
+ * accumulation and the sphere projection stay FP64).  For the mixed form,
+ * whose velocities carry the split-BF16 transform's ~1e-5 relative error;
+ * halves the records' memory and traffic.  Scalar (ncomp = 1) records stay
+ * FP64.  Not a reference function: its velocity records are FP64. */
+#define CMM_REC_FP64 0
+#define CMM_REC_FP32 1
+int cmm_velmesh_set_records(cmm_mesh* velmesh, int precision);
+
+/* Threads per block of a tunable kernel launched on this mesh (set by an
+ * autotuner from measured timings; 0 restores the default): composition
+ * and location on a map mesh, the map update's foot-point kernel on a map
+ * mesh, the vorticity kernel on a velocity mesh.  threads: 0 or a multiple
+ * of 32 in [32, 256].  Launch shape only: results do not depend on it. */
+#define CMM_TUNE_COMPOSE 0
+#define CMM_TUNE_ADVECT 1
+#define CMM_TUNE_VORTICITY 2
+#define CMM_TUNE_LOCATE 3
+int cmm_mesh_set_block(cmm_mesh* mesh, int kernel, int threads);
 
 /* ---------------------------------------------- device-driven BVE steps */
 /* The main-loop body of euler_simulation_sphere_remapping

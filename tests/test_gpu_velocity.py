@@ -168,3 +168,29 @@ def test_advect_project_matches_reference(nat):
         np.testing.assert_allclose(j[:, 0], a[key][:, 0], rtol=0, atol=1e-12)
         np.testing.assert_allclose(j[:, 1:], a[key][:, 1:], rtol=0, atol=1e-9)
     assert mesh.status() == 0 and vm.status() == 0
+
+
+def test_fp32_velocity_records(nat):
+    """cmm_velmesh_set_records(CMM_REC_FP32): FP32 ordinates and FP32
+    patches against the FP64 records on the same velocity jets; stated
+    error 1e-6 of max |u| (FP32 rounding of ordinates ~1e-7 relative), and
+    the RK4 foot points (FP64 accumulation) within dt * 1e-6 * max |u|."""
+    from cmm_gpu.meshgen import random_sphere_points
+    d = golden("velocity_L8.npz")
+    vm64, _ = velmesh(nat, 8)
+    vm32, _ = velmesh(nat, 8)
+    vm32.set_records(nat.VelMesh.REC_FP32)
+    c64 = vel_coeffs(nat, vm64, d["vals"])
+    c32 = vel_coeffs(nat, vm32, d["vals"])
+    assert c32[0].dtype == torch.float32
+    np.testing.assert_allclose(host(c32[1]), host(c64[1]).astype(np.float32), rtol=2e-6, atol=1e-6)
+    x = random_sphere_points(20000, seed=11).T.copy()
+    u64 = host(vm64.velocity(c64, 0.0, 0.13, 0.1, dev(x)))
+    u32 = host(vm32.velocity(c32, 0.0, 0.13, 0.1, dev(x)))
+    scale = np.abs(u64).max()
+    err = np.abs(u32 - u64).max() / scale
+    print(f"FP32 velocity records: relative velocity error {err:.2e}")
+    assert 1e-10 < err < 1e-6
+    f64 = host(vm64.integrate(c64, 0.0, 2, 0.05, 0.1, dev(x)))
+    f32 = host(vm32.integrate(c32, 0.0, 2, 0.05, 0.1, dev(x)))
+    assert np.abs(f32 - f64).max() < 0.1 * 1e-6 * scale
