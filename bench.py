@@ -258,7 +258,7 @@ def bench_gpu(args, rank, world):
             res["rh_error"] = bench_rh_error(dev)
         except Exception as exc:  # reported, the headline stands on its own
             res["bve"] = {"error": f"{type(exc).__name__}: {exc}"}
-    if rank == 0 and not (args.no_bve3 and args.no_kernels and args.no_ensemble):
+    if rank == 0 and not (args.no_bve3 and args.no_kernels and args.no_ensemble and args.no_adjoint):
         del q, mesh, cs
         torch.cuda.empty_cache()
     if rank == 0 and not args.no_kernels:
@@ -272,6 +272,12 @@ def bench_gpu(args, rank, world):
             res["ensemble"] = bench_ensemble(args, dev)
         except Exception as exc:
             res["ensemble"] = {"error": f"{type(exc).__name__}: {exc}"}
+        torch.cuda.empty_cache()
+    if rank == 0 and not args.no_adjoint:
+        try:
+            res["adjoint"] = bench_adjoint(args, dev)
+        except Exception as exc:
+            res["adjoint"] = {"error": f"{type(exc).__name__}: {exc}"}
         torch.cuda.empty_cache()
     if rank == 0 and not args.no_bve3:
         try:
@@ -420,6 +426,64 @@ def bench_ensemble(args, dev):
             "status_ok": ok}
 
 
+def bench_adjoint(args, dev):
+    """Config: gradient of J = sum_x W (omega_T - omega_target)^2 over the
+    MWSS grid (W = sin(theta) (pi/L)^2) with respect to the initial real SH
+    coefficients (l <= 16, N(0,1) l^-1.5, seed 11), at L=512 on a level-6
+    mesh through 200 RK4 steps of dt = 1/200, remap every 20 steps (each
+    remap interval checkpointed, recomputed in the backward pass); target
+    = the same run from the coefficients + 10 % of a second seeded set.
+    FP64 form.  Checked against centred differences (h = 1e-6) on
+    args.adjoint_fd random coefficients."""
+    import torch
+    from cmm_gpu.adjoint import BVEGradient
+    from cmm_gpu.workloads import random_sh_vorticity
+    lmax = 16
+    run = BVEGradient(6, 512, 200, 1.0, n_maps=20)
+    _, a = random_sh_vorticity(lmax, seed=11)
+    _, b = random_sh_vorticity(lmax, seed=12)
+    sh = torch.from_numpy(a).to(dev)
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    with torch.no_grad():
+        e[0].record()
+        target = run.omega_T(sh + 0.1 * torch.from_numpy(b).to(dev))
+        e[1].record()
+    e[2].record()
+    J, grad = run.gradient(sh, target)
+    e[3].record()
+    torch.cuda.synchronize()
+    t_fwd, t_grad = e[0].elapsed_time(e[1]), e[2].elapsed_time(e[3])
+    rng = np.random.default_rng(13)
+    rel, best = [], []
+    for _ in range(args.adjoint_fd):
+        l = int(rng.integers(1, lmax + 1))
+        c = int(rng.integers(0, 2 * l + 1))
+        ad = float(grad[l, c])
+        errs = {}
+        for h in (1e-6, 1e-5, 1e-4):
+            sp, sm = sh.clone(), sh.clone()
+            sp[l, c] += h
+            sm[l, c] -= h
+            with torch.no_grad():
+                fd = (float(run.misfit(sp, target)) - float(run.misfit(sm, target))) / (2 * h)
+            errs[h] = abs(fd - ad) / max(abs(ad), 1e-300)
+        rel.append(errs[1e-6])
+        best.append(min(errs.values()))
+    return {"workload": "gradient of the final-vorticity misfit w.r.t. the initial SH coefficients "
+                        "(l<=16), L=512, level 6, 200 RK4 steps of dt=1/200, remap + checkpoint every "
+                        "20 steps, FP64",
+            "J": J, "forward_s": t_fwd / 1e3, "forward_backward_s": t_grad / 1e3,
+            "backward_over_forward": t_grad / t_fwd - 1.0,
+            "fd_coefficients": args.adjoint_fd,
+            "rel_err_h1e-6_max": max(rel) if rel else None,
+            "rel_err_h1e-6_median": float(np.median(rel)) if rel else None,
+            "rel_err_best_h_max": max(best) if best else None,
+            "rel_err_best_h_median": float(np.median(best)) if best else None,
+            "fd_note": "centred differences of J carry the map update's amplified rounding "
+                       "(1/(4 eps) = 2.5e4 on every step) and curvature; best_h = the smallest "
+                       "discrepancy over steps 1e-6, 1e-5, 1e-4"}
+
+
 def bench_rh_error(dev):
     """Rossby-Haurwitz wave (exact travelling solution, T=1): L_inf vorticity
     error of the FP64 and split-BF16 forms (level 4, L=64, 42 steps)."""
@@ -556,6 +620,10 @@ def main():
     ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble run")
     ap.add_argument("--ens-members", type=int, default=64)
     ap.add_argument("--ensemble-only", action="store_true", help="print only the ensemble run")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint run")
+    ap.add_argument("--adjoint-fd", type=int, default=2,
+                    help="coefficients checked by centred differences in the adjoint run")
+    ap.add_argument("--adjoint-only", action="store_true", help="print only the adjoint run")
     ap.add_argument("--kernels-only", action="store_true",
                     help="print only the per-stage timings of one BVE step (profiling runs)")
     ap.add_argument("--kernels-level", type=int, default=7)
@@ -594,6 +662,11 @@ def main():
         return
 
     import torch
+    if args.adjoint_only:
+        dev = torch.device("cuda", 0)
+        torch.cuda.set_device(dev)
+        print(json.dumps({"adjoint": bench_adjoint(args, dev)}))
+        return
     if args.ensemble_only:
         dev = torch.device("cuda", 0)
         torch.cuda.set_device(dev)
@@ -642,7 +715,7 @@ def main():
                 "h2d_bytes_per_step": Q * 24, "d2h_bytes_per_step": Q * (24 + 4 + 72)},
         "clocks": r["clocks"], "gpu_launches": r["launches"],
     }
-    for key in ("bve", "rh_error", "bve_l7_L1024", "kernels", "ensemble"):
+    for key in ("bve", "rh_error", "bve_l7_L1024", "kernels", "ensemble", "adjoint"):
         if key in r:
             line[key] = r[key]
     print(json.dumps(line))

@@ -58,7 +58,7 @@ class SharedResources:
             theta, phi, grid, vverts = latlon_mesh_arrays(L)
             vm = native.VelMesh(L, theta, phi, grid, vverts, device=self.device.index)
             if rec32:
-                vm.set_records(native.VelMesh.REC_FP32)
+                vm.set_records(native.VelMesh.REC_MIXED)
             self._vm[key] = (vm, grid)
         return self._vm[key]
 

@@ -61,6 +61,12 @@ _SIGS = {
     "cmm_sht_share_tables": (_i, [_p, _p]),
     "cmm_sht_trim": (_i, [_p]),
     "cmm_velmesh_set_records": (_i, [_p, _i]),
+    "cmm_assemble_bwd": (_i, [_p, _p, _p, _p]),
+    "cmm_compose_bwd": (_i, [_p, ctypes.POINTER(_p), _i, _p, _i64, _p, ctypes.POINTER(_p), _p, _p, _p]),
+    "cmm_vorticity_bwd": (_i, [_p, _p, _i, _d, _p, _p, _p, _p, _p]),
+    "cmm_sht_velocity_bwd": (_i, [_p, _p, _p, _p, _p]),
+    "cmm_advect_project_bwd": (_i, [_p, _p, ctypes.POINTER(_p), _i, _d, _i, _d, _d, _p, _p, _p, _d, _p,
+                                    ctypes.POINTER(_p), _p, _p, _p]),
     "cmm_mesh_set_block": (_i, [_p, _i, _i]),
     "cmm_bve_create": (_i, [ctypes.POINTER(BveDesc), ctypes.POINTER(_p)]),
     "cmm_bve_destroy": (_i, [_p]),
@@ -246,14 +252,14 @@ class VelMesh(Mesh):
         self.h = h
         self.stride = lib.cmm_coeff_stride(3)
 
-    REC_FP64, REC_FP32 = 0, 1
+    REC_FP64, REC_FP32, REC_MIXED = 0, 1, 2
 
     def set_records(self, precision):
         """Velocity coefficient records in FP64 (default) or FP32
         (cmm_velmesh_set_records)."""
         with torch.cuda.device(self.device):
             check(lib.cmm_velmesh_set_records(self.h, precision), "cmm_velmesh_set_records")
-        self.rec32 = precision == self.REC_FP32
+        self.rec32 = precision != self.REC_FP64
         return self
 
     def new_coeffs(self, ncomp=3, batch=()):

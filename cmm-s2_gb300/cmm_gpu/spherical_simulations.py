@@ -81,7 +81,7 @@ class BVESolver:
             self.vm = native.VelMesh(L, theta, phi, grid, vverts, device=dev.index)
             if split:
                 # the mixed form keeps its velocity records in FP32
-                self.vm.set_records(native.VelMesh.REC_FP32)
+                self.vm.set_records(native.VelMesh.REC_MIXED)
             tan, s_pts = stencil_frames(verts)
             self.tan = torch.from_numpy(np.ascontiguousarray(tan)).to(dev)
             self.s_pts = torch.from_numpy(np.ascontiguousarray(s_pts)).to(dev)

@@ -222,13 +222,14 @@ int cmm_sht_set_precision(cmm_sht* plan, int mode) {
 
 int cmm_velmesh_set_records(cmm_mesh* velmesh, int precision) {
   if (!velmesh || velmesh->view.kind != kLatLon) return arg_error("cmm_velmesh_set_records: velocity mesh expected");
-  if (precision != CMM_REC_FP64 && precision != CMM_REC_FP32)
+  if (precision != CMM_REC_FP64 && precision != CMM_REC_FP32 && precision != CMM_REC_MIXED)
     return arg_error("cmm_velmesh_set_records: unknown precision");
-  if (precision == CMM_REC_FP32 && !velmesh->view.tri_asm_f) {
+  if (precision != CMM_REC_FP64 && !velmesh->view.tri_asm_f) {
     int rc = make_asm_f32(velmesh);
     if (rc) return rc;
   }
-  velmesh->view.rec32 = precision == CMM_REC_FP32 ? 1 : 0;
+  velmesh->view.rec32 = precision != CMM_REC_FP64 ? 1 : 0;
+  velmesh->view.field32 = precision == CMM_REC_MIXED ? 1 : 0;
   return CMM_OK;
 }
 
@@ -251,6 +252,60 @@ int cmm_bve_step(cmm_bve* bve, void* stream) {
 int cmm_bve_state(cmm_bve* bve, void* stream, int* count, int* nc, int* identity) {
   if (!bve) return arg_error("cmm_bve_state: null handle");
   return bve_state(bve, (cudaStream_t)stream, count, nc, identity);
+}
+
+int cmm_assemble_bwd(const cmm_mesh* mesh, const double* grad_coeffs, double* grad_jets, void* stream) {
+  if (!mesh || !grad_coeffs || !grad_jets) return arg_error("cmm_assemble_bwd: null pointer");
+  if (mesh->view.rec32) return arg_error("cmm_assemble_bwd: FP64 records expected");
+  return launch_assemble_bwd(mesh->view, grad_coeffs, grad_jets, (cudaStream_t)stream);
+}
+
+int cmm_compose_bwd(const cmm_mesh* mesh, const double* const* coeffs, int S, const double* q, int64_t n,
+                    const double* grad_out, double* const* grad_coeffs, double* grad_q, double* work,
+                    void* stream) {
+  if (!mesh || S < 1 || S > kAdjMaxSubmaps || !coeffs || !grad_coeffs || n < 0 ||
+      (n > 0 && (!q || !grad_out || !work)))
+    return arg_error("cmm_compose_bwd: bad argument");
+  for (int k = 0; k < S; ++k)
+    if (!coeffs[k] || !grad_coeffs[k]) return arg_error("cmm_compose_bwd: null submap");
+  return launch_compose_bwd(mesh->view, coeffs, grad_coeffs, S, q, n, grad_out, grad_q, work,
+                            (cudaStream_t)stream);
+}
+
+int cmm_advect_project_bwd(const cmm_mesh* mesh, const cmm_mesh* velmesh, const double* const* vel_coeffs,
+                           int nvs, double ts0, int scheme, double t, double dt, const double* s_pts,
+                           const double* tan, const double* prev_coeffs, double eps, const double* grad_jets,
+                           double* const* grad_vel, double* grad_prev, double* work, void* stream) {
+  if (!mesh || mesh->view.kind != kIcosahedral) return arg_error("cmm_advect_project_bwd: map mesh expected");
+  VelPtrs vc;
+  int rc = vel_args(velmesh, vel_coeffs, nvs, &vc, "cmm_advect_project_bwd");
+  if (rc) return rc;
+  if (velmesh->view.rec32) return arg_error("cmm_advect_project_bwd: FP64 velocity records expected");
+  if (!s_pts || !tan || !grad_jets || !grad_vel || !work) return arg_error("cmm_advect_project_bwd: null pointer");
+  for (int l = 0; l < nvs; ++l)
+    if (!grad_vel[l]) return arg_error("cmm_advect_project_bwd: null velocity cotangent");
+  TimeWeights tw;
+  if ((rc = stage_weights(nvs, ts0, scheme, t, dt, &tw))) return rc;
+  return launch_advect_project_bwd(mesh->view, velmesh->view, vel_coeffs, grad_vel, nvs, tw, scheme, dt, s_pts,
+                                   tan, prev_coeffs, grad_prev, eps, grad_jets, work, (cudaStream_t)stream);
+}
+
+int cmm_vorticity_bwd(const cmm_mesh* velmesh, const double* dsh, int lmax, double rot_rate,
+                      const double* X, const double* grad_omega, double* grad_X, double* grad_sh,
+                      void* stream) {
+  if (!velmesh || velmesh->view.kind != kLatLon || !X || !grad_omega)
+    return arg_error("cmm_vorticity_bwd: bad argument");
+  const int L = velmesh->view.L;
+  const int64_t Q = (int64_t)(L + 1) * 2 * L;
+  return launch_vorticity_bwd(dsh, lmax, rot_rate, X, Q, grad_omega, grad_X, grad_sh, (cudaStream_t)stream);
+}
+
+int cmm_sht_velocity_bwd(cmm_sht* plan, const cmm_mesh* velmesh, const double* grad_jets, double* grad_omega,
+                         void* stream) {
+  if (!plan || !velmesh || velmesh->view.kind != kLatLon || velmesh->view.L != sht_L(plan) || !grad_jets ||
+      !grad_omega)
+    return arg_error("cmm_sht_velocity_bwd: bad argument");
+  return sht_velocity_bwd(plan, velmesh, grad_jets, grad_omega, (cudaStream_t)stream);
 }
 
 int cmm_sht_power(cmm_sht* plan, const double* alm, double* power, void* stream) {

@@ -51,6 +51,7 @@ struct MeshView {
   // (nt, 64) floats, assembled from the FP32 copy of the factors
   int rec32;
   const float* tri_asm_f;   // (kAsmFactors, nt), factor-major, when rec32
+  int field32;              // analytic initial vorticity fields in FP32
   // launch shapes chosen by an autotuner (cmm_mesh_set_block), threads per
   // block of the tunable kernels on this mesh; 0 = the library default
   int block[4];
@@ -172,6 +173,20 @@ int launch_vorticity(int kind, const double* params, int nparams, const double* 
                      int64_t Q, int npr, const double* cos_ring, double* omega, cudaStream_t s);
 
 int launch_fp64_probe(int blocks, int iters, double* sink, cudaStream_t s);
+
+// adjoints (adjoint.cu)
+constexpr int kAdjMaxSubmaps = 256;
+int launch_assemble_bwd(const MeshView& m, const double* gc, double* gj, cudaStream_t s);
+int launch_compose_bwd(const MeshView& m, const double* const* cs, double* const* gcs, int S,
+                       const double* q, int64_t n, const double* gout, double* gq, double* work,
+                       cudaStream_t s);
+int launch_vorticity_bwd(const double* dsh, int lmax, double rot, const double* X, int64_t Q,
+                         const double* gw, double* gX, double* gsh, cudaStream_t s);
+// work: cmm_advect_workspace (15 nv) + 12 nv doubles
+int launch_advect_project_bwd(const MeshView& mesh, const MeshView& vm, const double* const* vel,
+                              double* const* gvel, int nvs, const TimeWeights& tw, int scheme, double dt,
+                              const double* s_pts, const double* tan, const double* prev, double* gprev,
+                              double eps, const double* gjets, double* work, cudaStream_t s);
 // FP32 copy of a mesh's factor table (velmesh records in FP32).
 int make_asm_f32(cmm_mesh* m);
 
@@ -186,6 +201,7 @@ int sht_velocity(cmm_sht* p, const cmm_mesh* vm, const double* omega, double2* p
 int sht_scalar_jets(cmm_sht* p, const cmm_mesh* vm, const double2* alm, double* jets, cudaStream_t s);
 int sht_power(cmm_sht* p, const double2* alm, double* power, cudaStream_t s);
 int sht_share_tables(cmm_sht* p, const cmm_sht* src);
+int sht_velocity_bwd(cmm_sht* p, const cmm_mesh* vm, const double* gjets, double* gomega, cudaStream_t s);
 int sht_trim(cmm_sht* p);
 int bve_create(const cmm_bve_desc* d, cmm_bve** out);
 int bve_step(cmm_bve* b, cudaStream_t s);

@@ -274,6 +274,17 @@ __global__ void __launch_bounds__(kBlock) compose_kernel(MeshView m, Src cp,
       load_ords<3>(cp.at(s, S) + (int64_t)t * kCoeffStride3, sp, o);
       double P[3];
       sbb<3>(o, g, P);
+      if (!JAC && (s & 3) != 0) {
+        // Location, barycentrics and sub-triangle choice are invariant under
+        // p -> lambda p (lambda > 0) and the patch is homogeneous of degree
+        // 2, so the projection onto the sphere can wait: normalising every
+        // fourth submap (and the result) keeps |p| within ~1e-4 of 1
+        // (|P| = 1 + O(h^3) per submap) and saves the FP64 square root.
+        p[0] = P[0];
+        p[1] = P[1];
+        p[2] = P[2];
+        continue;
+      }
       const double inv_n = rsqrt(P[0] * P[0] + P[1] * P[1] + P[2] * P[2]);
       double sN[3] = {P[0] * inv_n, P[1] * inv_n, P[2] * inv_n};
       if (JAC) {

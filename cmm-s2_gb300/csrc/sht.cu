@@ -424,6 +424,295 @@ __global__ void jets_kernel(const R* __restrict__ fld, int L, const double* __re
   }
 }
 
+// ------------------------------------------------------------ adjoint
+// Transposes of the stages of sht_velocity (exact transposes of the
+// linear maps, complex arrays taken as pairs of reals).
+
+// sum over rings: out[m][l] = sum_{j=0..nr} w_j c_m Pbar_lm(theta_j) F[j][m],
+// rings j and nr-j paired (Pbar(pi - theta) = (-1)^(l+m) Pbar(theta)),
+// F row stride `row`, c_0 = 1 and c_m = cm (m > 0); w == NULL: unit weights.
+__global__ void __launch_bounds__(256) legendre_sum_kernel(const double2* __restrict__ F, int64_t row, int L,
+                                                           int nr, const double* __restrict__ w, double cm,
+                                                           const double* __restrict__ ct,
+                                                           const double* __restrict__ pmm, int pstride,
+                                                           const double* __restrict__ ra,
+                                                           const double* __restrict__ rb,
+                                                           double2* __restrict__ out) {
+  const int m = blockIdx.x;
+  const int npair = nr / 2 + 1;
+  constexpr int R = 8;
+  const double sc = m == 0 ? 1.0 : cm;
+  double2 E[R], O[R];
+  double x[R], p0[R], p1[R];
+  int nrr = 0;
+  for (int r = 0; r < R; ++r) {
+    const int j = threadIdx.x + r * blockDim.x;
+    if (j < npair) {
+      const double2 a = F[(int64_t)j * row + m];
+      double2 e, o;
+      if (j < nr - j) {
+        const double2 b = F[(int64_t)(nr - j) * row + m];
+        e = make_double2(a.x + b.x, a.y + b.y);
+        o = make_double2(a.x - b.x, a.y - b.y);
+      } else {
+        e = a;
+        o = make_double2(0.0, 0.0);
+      }
+      const double wj = (w ? w[j] : 1.0) * sc;
+      E[r] = cmul(e, wj);
+      O[r] = cmul(o, wj);
+      x[r] = ct[j];
+      p0[r] = pmm[(int64_t)m * pstride + j];
+      p1[r] = 0.0;
+      nrr = r + 1;
+    } else {
+      E[r] = O[r] = make_double2(0.0, 0.0);
+      x[r] = p0[r] = p1[r] = 0.0;
+    }
+  }
+  __shared__ double2 red[kLChunk][8];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int l0 = m; l0 < L; l0 += kLChunk) {
+    double2 acc[kLChunk];
+#pragma unroll
+    for (int q = 0; q < kLChunk; ++q) acc[q] = make_double2(0.0, 0.0);
+#pragma unroll
+    for (int q = 0; q < kLChunk; ++q) {
+      const int l = l0 + q;
+      if (l < L) {
+        const bool even = ((l - m) & 1) == 0;
+        double a = 0.0, b = 0.0;
+        if (l > m) {
+          a = ra[(int64_t)m * L + l];
+          b = rb[(int64_t)m * L + l];
+        }
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          if (r < nrr) {
+            double P;
+            if (l == m) {
+              P = p0[r];
+            } else if (l == m + 1) {
+              P = a * x[r] * p0[r];
+              p1[r] = p0[r];
+              p0[r] = P;
+            } else {
+              P = a * (x[r] * p0[r] - b * p1[r]);
+              p1[r] = p0[r];
+              p0[r] = P;
+            }
+            const double2 v = even ? E[r] : O[r];
+            acc[q].x += P * v.x;
+            acc[q].y += P * v.y;
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < kLChunk; ++q) {
+      double vx = acc[q].x, vy = acc[q].y;
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        vx += __shfl_down_sync(0xffffffffu, vx, off);
+        vy += __shfl_down_sync(0xffffffffu, vy, off);
+      }
+      if (lane == 0) red[q][warp] = make_double2(vx, vy);
+    }
+    __syncthreads();
+    if (threadIdx.x < kLChunk) {
+      const int q = threadIdx.x, l = l0 + q;
+      double2 s = make_double2(0.0, 0.0);
+      for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+        s.x += red[q][k].x;
+        s.y += red[q][k].y;
+      }
+      if (l < L) out[(int64_t)m * L + l] = s;
+    }
+    __syncthreads();
+  }
+}
+
+// ring synthesis with weights: out[j][m] = w_j sum_l Pbar_lm(theta_j)
+// a[m][l] for rings j = 0..nr (pairs j, nr-j), rows of length `row`.
+__global__ void __launch_bounds__(kSynthBlock) ring_synthesis_kernel(const double2* __restrict__ alm, int L,
+                                                                     int nr, const double* __restrict__ w,
+                                                                     const double* __restrict__ ct,
+                                                                     const double* __restrict__ pmm,
+                                                                     int pstride,
+                                                                     const double* __restrict__ ra,
+                                                                     const double* __restrict__ rb,
+                                                                     double2* __restrict__ out, int64_t row) {
+  const int m = blockIdx.x;
+  const int t = blockIdx.y * blockDim.x + threadIdx.x;
+  const int npair = nr / 2 + 1;
+  __shared__ double2 A[kLChunk];
+  double2 E = make_double2(0.0, 0.0), O = make_double2(0.0, 0.0);
+  const bool active = t < npair;
+  const double x = active ? ct[t] : 0.0;
+  double p0 = active ? pmm[(int64_t)m * pstride + t] : 0.0, p1 = 0.0;
+  for (int l0 = m; l0 < L; l0 += kLChunk) {
+    __syncthreads();
+    for (int e = threadIdx.x; e < kLChunk; e += blockDim.x) {
+      const int l = l0 + e;
+      A[e] = (l < L) ? alm[(int64_t)m * L + l] : make_double2(0.0, 0.0);
+    }
+    __syncthreads();
+    const int qn = min(kLChunk, L - l0);
+    for (int q = 0; q < qn; ++q) {
+      const int l = l0 + q;
+      double P;
+      if (l == m) {
+        P = p0;
+      } else if (l == m + 1) {
+        P = ra[(int64_t)m * L + l] * x * p0;
+        p1 = p0;
+        p0 = P;
+      } else {
+        P = ra[(int64_t)m * L + l] * (x * p0 - rb[(int64_t)m * L + l] * p1);
+        p1 = p0;
+        p0 = P;
+      }
+      if (((l - m) & 1) == 0) {
+        E.x += P * A[q].x;
+        E.y += P * A[q].y;
+      } else {
+        O.x += P * A[q].x;
+        O.y += P * A[q].y;
+      }
+    }
+  }
+  if (!active) return;
+  const double wt = w ? w[t] : 1.0;
+  out[(int64_t)t * row + m] = make_double2(wt * (E.x + O.x), wt * (E.y + O.y));
+  if (nr - t != t) out[(int64_t)(nr - t) * row + m] = make_double2(wt * (E.x - O.x), wt * (E.y - O.y));
+}
+
+// jets transpose: jet cotangents (3,4,Nv_u) -> field cotangents (12, L+1, 2L)
+// at the vertices' grid nodes (other pole samples stay 0): values, and
+// gbar = X x hbar for the tangent-gradient slots (the forward's projection
+// term (g x X).X vanishes identically).
+__global__ void jets_bwd_kernel(const double* __restrict__ gj, int L, const double* __restrict__ grid,
+                                double* __restrict__ gf) {
+  const int N = 2 * L;
+  const int64_t nv = 2 + (int64_t)(L - 1) * N;
+  const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  const int64_t node = v == 0 ? 0 : (v == nv - 1 ? (int64_t)L * N : N + (v - 1));
+  const int64_t fs = (int64_t)(L + 1) * N;
+  const double X0 = grid[4 * node], X1 = grid[4 * node + 1], X2 = grid[4 * node + 2];
+  for (int i = 0; i < 3; ++i) {
+    gf[i * fs + node] = gj[(int64_t)(i * 4) * nv + v];
+    const double h0 = gj[(int64_t)(0 * 4 + 1 + i) * nv + v], h1 = gj[(int64_t)(1 * 4 + 1 + i) * nv + v],
+                 h2 = gj[(int64_t)(2 * 4 + 1 + i) * nv + v];
+    gf[(3 + 3 * i) * fs + node] = X1 * h2 - X2 * h1;
+    gf[(4 + 3 * i) * fs + node] = X2 * h0 - X0 * h2;
+    gf[(5 + 3 * i) * fs + node] = X0 * h1 - X1 * h0;
+  }
+}
+
+// Transpose of `ladder` (gather form): cotangents ob[k] (k = x, y, z) of
+// the three outputs at every (m', l) -> cotangent of the input at (m, l).
+__device__ __forceinline__ double2 ladder_t(const double2* __restrict__ ox, const double2* __restrict__ oy,
+                                            const double2* __restrict__ oz, int L, int l, int m) {
+  const double ll = (double)l * (double)(l + 1);
+  auto idx = [&](int mm) { return (int64_t)mm * L + l; };
+  // up/dn cotangents of the output at m': up = (-i ox + oy)/2, dn = (-i ox - oy)/2
+  auto upb = [&](int mm) {
+    const double2 a = ox[idx(mm)], b = oy[idx(mm)];
+    return make_double2((a.y + b.x) / 2, (-a.x + b.y) / 2);
+  };
+  auto dnb = [&](int mm) {
+    const double2 a = ox[idx(mm)], b = oy[idx(mm)];
+    return make_double2((a.y - b.x) / 2, (-a.x - b.y) / 2);
+  };
+  double2 r = make_double2(0.0, 0.0);
+  // output m+1 reads a[m] as am1 (cu(l, m+1))
+  if (m + 1 <= l) {
+    const double cu = sqrt(ll - (double)(m + 1) * (double)m);
+    const double2 u = upb(m + 1);
+    r.x += cu * u.x;
+    r.y += cu * u.y;
+  }
+  // output m-1 reads a[m] as ap1 (cd(l, m-1))
+  if (m >= 1) {
+    const double cd = sqrt(ll - (double)(m - 1) * (double)m);
+    const double2 d = dnb(m - 1);
+    r.x += cd * d.x;
+    r.y += cd * d.y;
+  }
+  // output m = 0 reads a[1] as am1 = -conj(a[1]) (cu(l, 0))
+  if (m == 1) {
+    const double cu0 = sqrt(ll);
+    const double2 u = upb(0);
+    r.x += -cu0 * u.x;
+    r.y += cu0 * u.y;
+  }
+  // o_z = i m a
+  const double2 z = oz[idx(m)];
+  r.x += (double)m * z.y;
+  r.y += -(double)m * z.x;
+  return r;
+}
+
+// fields cotangents: fb[u] += ladder^T(fb[3+3u .. 5+3u]) (u = 0..2), then
+// psib = ladder^T(fb[0..2]); entries l < m are zero.
+__global__ void ladder2_bwd_kernel(double2* __restrict__ fb, int L) {
+  const int l = blockIdx.x * blockDim.x + threadIdx.x, m = blockIdx.y;
+  if (l >= L || l < m) return;
+  const int64_t fs = (int64_t)L * L, i = (int64_t)m * L + l;
+  for (int u = 0; u < 3; ++u) {
+    const double2 r = ladder_t(fb + (3 + 3 * u) * fs, fb + (4 + 3 * u) * fs, fb + (5 + 3 * u) * fs, L, l, m);
+    fb[u * fs + i].x += r.x;
+    fb[u * fs + i].y += r.y;
+  }
+}
+
+__global__ void ladder1_bwd_kernel(const double2* __restrict__ fb, int L, double2* __restrict__ psib) {
+  const int l = blockIdx.x * blockDim.x + threadIdx.x, m = blockIdx.y;
+  if (l >= L) return;
+  const int64_t fs = (int64_t)L * L, i = (int64_t)m * L + l;
+  psib[i] = (l < m) ? make_double2(0.0, 0.0) : ladder_t(fb, fb + fs, fb + 2 * fs, L, l, m);
+}
+
+// pad transpose: Hb (4L, L) -> Ghb (2L, L).
+__global__ void pad_bwd_kernel(const double2* __restrict__ Hb, int L, double2* __restrict__ Gb) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = blockIdx.y;  // 0..2L-1
+  if (m >= L || k >= 2 * L) return;
+  const double s = 1.0 / (2 * L);
+  double2 v;
+  if (k < L) {
+    v = Hb[(int64_t)k * L + m];
+  } else if (k == L) {
+    const double2 a = Hb[(int64_t)L * L + m], b = Hb[(int64_t)3 * L * L + m];
+    v = make_double2((a.x + b.x) / 2, (a.y + b.y) / 2);
+  } else {
+    v = Hb[(int64_t)(k + 2 * L) * L + m];
+  }
+  Gb[(int64_t)k * L + m] = cmul(v, s);
+}
+
+// torus transpose + C2R preparation: Gb (2L, L) -> X (L+1, L+1) with
+// specb[t][m] = (pi/L) (Gb[t][m] + [0<t<L] (-1)^m Gb[2L-t][m]), scaled by
+// 1/2 for 1 <= m < L (C2R doubles those), m = L zero.
+__global__ void torus_bwd_kernel(const double2* __restrict__ Gb, int L, double2* __restrict__ X) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = blockIdx.y;  // 0..L
+  if (m > L || t > L) return;
+  double2 v = make_double2(0.0, 0.0);
+  if (m < L) {
+    v = Gb[(int64_t)t * L + m];
+    if (t > 0 && t < L) {
+      double2 b = Gb[(int64_t)(2 * L - t) * L + m];
+      if (m & 1) b = make_double2(-b.x, -b.y);
+      v.x += b.x;
+      v.y += b.y;
+    }
+    v = cmul(v, M_PI / L * (m == 0 ? 1.0 : 0.5));
+  }
+  X[(int64_t)t * (L + 1) + m] = v;
+}
+
 int cufft_fail(cufftResult r, const char* what) {
   set_last_error(std::string(what) + ": cuFFT error " + std::to_string((int)r));
   return CMM_ERR_CUDA;
@@ -450,6 +739,9 @@ struct cmm_sht {
   cufftHandle f_ring_fwd = 0, f_torus_fwd = 0, f_pad_inv = 0, f_ring_inv = 0;
   bool have_fplans[4] = {false, false, false, false};
   cmm::DeviceBuffer f_in, f_spec, f_torus, f_pad, f_synth, f_samples;
+  // adjoint: D2Z over the 12 fields' rings, C2R over one field's rings
+  cufftHandle b_ring_fwd12 = 0, b_ring_inv1 = 0;
+  bool have_bplans = false;
   ~cmm_sht() {
     if (have_plans[0]) cufftDestroy(ring_fwd);
     if (have_plans[1]) cufftDestroy(torus_fwd);
@@ -459,6 +751,10 @@ struct cmm_sht {
     if (have_fplans[1]) cufftDestroy(f_torus_fwd);
     if (have_fplans[2]) cufftDestroy(f_pad_inv);
     if (have_fplans[3]) cufftDestroy(f_ring_inv);
+    if (have_bplans) {
+      cufftDestroy(b_ring_fwd12);
+      cufftDestroy(b_ring_inv1);
+    }
     if (tc) cmm::tc_plan_destroy(tc);
   }
 };
@@ -751,6 +1047,84 @@ int sht_velocity(cmm_sht* p, const cmm_mesh* vm, const double* omega, double2* p
     jets_kernel<double><<<(int)((nv + 127) / 128), 128, 0, s>>>((const double*)p->samples.p, L,
                                                                  vm->view.grid, jets);
   return check_launch("jets_kernel");
+}
+
+// Transpose of sht_velocity (omega -> velocity jets, FP64 form):
+// grad_jets (3,4,Nv_u) -> grad_omega (L+1, 2L), overwritten.
+int sht_velocity_bwd(cmm_sht* p, const cmm_mesh* vm, const double* gjets, double* gomega,
+                     cudaStream_t s) {
+  const int L = p->L;
+  int rc;
+  if ((rc = ensure_fp64_inverse(p))) return rc;
+  if (!p->have_bplans) {
+    int n2[1] = {2 * L}, inemb[1] = {2 * L}, onemb[1] = {L + 1}, cin[1] = {L + 1}, rout[1] = {2 * L};
+    cufftResult r = cufftPlanMany(&p->b_ring_fwd12, 1, n2, inemb, 1, 2 * L, onemb, 1, L + 1, CUFFT_D2Z,
+                                  kFields * (L + 1));
+    if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftPlanMany(b_ring_fwd12)");
+    r = cufftPlanMany(&p->b_ring_inv1, 1, n2, cin, 1, L + 1, rout, 1, 2 * L, CUFFT_Z2D, L + 1);
+    if (r != CUFFT_SUCCESS) {
+      cufftDestroy(p->b_ring_fwd12);
+      return cufft_fail(r, "cufftPlanMany(b_ring_inv1)");
+    }
+    p->have_bplans = true;
+  }
+  if ((rc = set_streams(p, s))) return rc;
+  cufftResult r = cufftSetStream(p->b_ring_fwd12, s);
+  if (r == CUFFT_SUCCESS) r = cufftSetStream(p->b_ring_inv1, s);
+  if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftSetStream");
+  double* gf = (double*)p->samples.p;             // (12, L+1, 2L)
+  double2* Sb = (double2*)p->synth.p;             // (12, L+1, L+1)
+  double2* Fb = (double2*)p->fields.p;            // (12, L, L)
+  double2* ab = (double2*)p->alm.p;               // (L, L)
+  const size_t fsz = (size_t)kFields * (L + 1) * 2 * L * sizeof(double);
+  cudaError_t e = cudaMemsetAsync(gf, 0, fsz, s);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+  const int64_t nv = 2 + (int64_t)(L - 1) * 2 * L;
+  jets_bwd_kernel<<<(int)((nv + 127) / 128), 128, 0, s>>>(gjets, L, vm->view.grid, gf);
+  if ((rc = check_launch("jets_bwd_kernel"))) return rc;
+  // C2R^T: spectra = c_m D2Z(samples)
+  r = cufftExecD2Z(p->b_ring_fwd12, (cufftDoubleReal*)gf, (cufftDoubleComplex*)Sb);
+  if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExecD2Z(adjoint)");
+  // synthesis^T: unit-weight Legendre sums over the L+1 rings, c_m = 2 for m > 0
+  for (int f = 0; f < kFields; ++f) {
+    legendre_sum_kernel<<<L, 256, 0, s>>>(Sb + (int64_t)f * (L + 1) * (L + 1), L + 1, L, L, nullptr, 2.0,
+                                          (const double*)p->ct_rings.p, (const double*)p->pmm_rings.p,
+                                          L + 1, (const double*)p->ra.p, (const double*)p->rb.p,
+                                          Fb + (int64_t)f * L * L);
+    if ((rc = check_launch("legendre_sum_kernel"))) return rc;
+  }
+  dim3 b(128), g((L + 127) / 128, L);
+  ladder2_bwd_kernel<<<g, b, 0, s>>>(Fb, L);
+  if ((rc = check_launch("ladder2_bwd_kernel"))) return rc;
+  ladder1_bwd_kernel<<<g, b, 0, s>>>(Fb, L, ab);
+  if ((rc = check_launch("ladder1_bwd_kernel"))) return rc;
+  dinv_kernel<<<g, b, 0, s>>>(ab, L);
+  if ((rc = check_launch("dinv_kernel"))) return rc;
+  // analysis^T: weighted synthesis on the 2L+1 fine rings
+  double2* H = (double2*)p->pad.p;                 // (4L, L)
+  e = cudaMemsetAsync(H, 0, (size_t)4 * L * L * sizeof(double2), s);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+  const int nfp = L + 1;   // ring pairs of the fine grid (nr = 2L)
+  ring_synthesis_kernel<<<dim3(L, (nfp + kSynthBlock - 1) / kSynthBlock), kSynthBlock, 0, s>>>(
+      ab, L, 2 * L, (const double*)p->w_fine.p, (const double*)p->ct_fine.p, (const double*)p->pmm_fine.p,
+      2 * L + 1, (const double*)p->ra.p, (const double*)p->rb.p, H, L);
+  if ((rc = check_launch("ring_synthesis_kernel"))) return rc;
+  // (Z2Z inverse 4L)^T = Z2Z forward 4L
+  r = cufftExecZ2Z(p->pad_inv, (cufftDoubleComplex*)H, (cufftDoubleComplex*)H, CUFFT_FORWARD);
+  if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExecZ2Z(adjoint pad)");
+  double2* Gb = (double2*)p->torus.p;              // (2L, L)
+  pad_bwd_kernel<<<dim3((L + 127) / 128, 2 * L), b, 0, s>>>(H, L, Gb);
+  if ((rc = check_launch("pad_bwd_kernel"))) return rc;
+  // (Z2Z forward 2L)^T = Z2Z inverse 2L
+  r = cufftExecZ2Z(p->torus_fwd, (cufftDoubleComplex*)Gb, (cufftDoubleComplex*)Gb, CUFFT_INVERSE);
+  if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExecZ2Z(adjoint torus)");
+  double2* X = (double2*)p->spec.p;                // (L+1, L+1)
+  torus_bwd_kernel<<<dim3((L + 1 + 127) / 128, L + 1), b, 0, s>>>(Gb, L, X);
+  if ((rc = check_launch("torus_bwd_kernel"))) return rc;
+  // D2Z^T: omega_bar[p] = Re sum_m specb_m e^{i m phi_p} (C2R of the prepared spectra)
+  r = cufftExecZ2D(p->b_ring_inv1, (cufftDoubleComplex*)X, (cufftDoubleReal*)gomega);
+  if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExecZ2D(adjoint)");
+  return CMM_OK;
 }
 
 int sht_power(cmm_sht* p, const double2* alm, double* power, cudaStream_t s) {

@@ -65,6 +65,51 @@ __device__ double omega0(const VortParams& v, double phi, double theta) {
   }
 }
 
+// The same fields in FP32 (mixed form, velmesh field32): angles from atan2f
+// and FP32 elementary functions; relative error ~1e-7, below the mixed
+// form's transform error (~1e-5).
+__device__ float jet_f(float theta, float theta_c) {
+  const float pi = 3.14159265358979f, beta2 = 144.0f;
+  const float u_lt = (pi / 2) * expf(-2 * beta2 * (1 - cosf(-theta + pi / 2 - theta_c)));
+  return (cosf(-theta + pi / 2) * (2 * beta2 * (cosf(theta_c) * sinf(-theta + pi / 2) -
+                                                sinf(theta_c) * cosf(-theta + pi / 2))) +
+          sinf(pi / 2 - theta)) *
+         u_lt;
+}
+
+__device__ float omega0_f(const VortParams& v, float phi, float theta) {
+  const float pi = 3.14159265358979f;
+  switch (v.kind) {
+    case CMM_VORT_ROSSBY_HAURWITZ: {
+      const float alpha = 1.0f / 30.0f, Omega = 2 * pi;
+      const float s = sinf(theta);
+      return 30 * cosf(theta) * cosf(4 * (phi + 2 * Omega * alpha * (float)v.p[0])) * (s * s * s * s);
+    }
+    case CMM_VORT_ZONAL_JET:
+      return jet_f(theta, pi / 4);
+    case CMM_VORT_PERTURBED_JET:
+      return jet_f(theta, pi / 4 + 0.01f * cosf(12 * phi));
+    case CMM_VORT_MULTI_JET:
+      return jet_f(theta, pi / 4 + 0.01f * cosf(12 * phi)) + jet_f(theta - pi / 8, pi / 4 + 0.01f * cosf(12 * phi));
+    case CMM_VORT_GAUSSIAN_VORTEX: {
+      const float x = sinf(theta) * cosf(phi), y = sinf(theta) * sinf(phi), z = cosf(theta);
+      return 4 * pi * expf(-((x - 1) * (x - 1) + y * y + z * z) / (1.0f / 16.0f));
+    }
+    case CMM_VORT_GAUSSIAN_JETS: {
+      const float lat = pi / 2 - theta;
+      float s = 0.0f;
+      const int n = (int)v.p[2];
+      for (int j = 0; j < n && j < 9; ++j) {
+        const float d = (lat - (float)v.p[3 + j]) / (float)v.p[1];
+        s += (float)v.p[0] * expf(-d * d);
+      }
+      return s;
+    }
+    default:
+      return 0.0f;
+  }
+}
+
 // Real orthonormal series: m = 0 -> Pbar_l0, m > 0 -> sqrt2 Pbar_lm cos(m
 // phi), m < 0 -> sqrt2 Pbar_l|m| sin(|m| phi); coefficients (lmax+1,
 // 2 lmax+1), column l+m.
@@ -104,12 +149,23 @@ __global__ void __launch_bounds__(256) vorticity_kernel(VortParams vp, const dou
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Q;
        i += (int64_t)gridDim.x * blockDim.x) {
     const double x = X[3 * i], y = X[3 * i + 1], z = X[3 * i + 2];
-    double phi, theta;
-    cart2sphere(x, y, z, &phi, &theta);
-    double w = omega0(vp, phi, theta);
-    if (sh) w += sh_value(sh, lmax, phi, theta);
+    double w, ct;
+    if (vm.field32 && !sh) {
+      const float xf = (float)x, yf = (float)y, zf = (float)z;
+      float phif = atan2f(yf, xf);
+      if (phif < 0.f) phif += 6.28318530717958647692f;
+      const float thf = atan2f(sqrtf(xf * xf + yf * yf), zf);
+      w = vp.kind == CMM_VORT_NONE ? 0.0 : (double)omega0_f(vp, phif, thf);
+      ct = z / sqrt(x * x + y * y + z * z);   // cos(theta), FP64
+    } else {
+      double phi, theta;
+      cart2sphere(x, y, z, &phi, &theta);
+      w = omega0(vp, phi, theta);
+      if (sh) w += sh_value(sh, lmax, phi, theta);
+      ct = cos(theta);
+    }
     if (spline) w += latlon_scalar(vm, spline, x, y, z);
-    const double r = w + 2 * rot * cos(theta) - 2 * rot * cos_ring[i / npr];
+    const double r = w + 2 * rot * ct - 2 * rot * cos_ring[i / npr];
     if (!isfinite(r)) atomicOr(vm.status, CMM_FLAG_NONFINITE);
     omega[i] = r;
   }

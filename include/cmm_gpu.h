@@ -294,6 +294,10 @@ int cmm_sht_scalar_jets(cmm_sht* plan, const cmm_mesh* velmesh, const double* al
  * FP64.  Not a reference function: its velocity records are FP64. */
 #define CMM_REC_FP64 0
 #define CMM_REC_FP32 1
+/* CMM_REC_FP32 plus the analytic initial-vorticity fields of
+ * cmm_vorticity_eval (not the SH series or the spline term) evaluated in
+ * FP32 from FP32 angles (relative error ~1e-7), cos(theta) as z/|X|. */
+#define CMM_REC_MIXED 2
 int cmm_velmesh_set_records(cmm_mesh* velmesh, int precision);
 
 /* Threads per block of a tunable kernel launched on this mesh (set by an
@@ -364,6 +368,43 @@ int cmm_bve_destroy(cmm_bve* bve);
 int cmm_bve_step(cmm_bve* bve, void* stream);
 /* Read the device state (synchronises `stream`). */
 int cmm_bve_state(cmm_bve* bve, void* stream, int* count, int* nc, int* identity);
+
+/* ------------------------------------------------------------ adjoints */
+/* Reverse-mode twins of the forward calls: each takes the cotangent of its
+ * forward call's output and accumulates (+=, unless stated) the cotangents
+ * of the inputs -- the exact transpose of the linearisation of the forward
+ * call's discrete arithmetic, with the piecewise choices (triangle,
+ * Powell-Sabin sub-triangle) held fixed.  Shared records are accumulated
+ * with FP64 atomics.  No counterpart in the reference, which has no
+ * derivatives; used by the gradient of a final-time vorticity misfit with
+ * respect to the initial spherical-harmonic coefficients. */
+/* cmm_assemble (ncomp = 3, FP64 records): grad_jets (3,4,Nv) += A^T grad_coeffs. */
+int cmm_assemble_bwd(const cmm_mesh* mesh, const double* grad_coeffs, double* grad_jets, void* stream);
+/* cmm_compose without Jacobians (S <= 256): grad_coeffs[s] (Nt, 64) and
+ * grad_q (n,3, may be NULL) += ; work: 3 S n doubles. */
+int cmm_compose_bwd(const cmm_mesh* mesh, const double* const* coeffs, int S, const double* q, int64_t n,
+                    const double* grad_out, double* const* grad_coeffs, double* grad_q, double* work,
+                    void* stream);
+/* cmm_vorticity_eval for kind CMM_VORT_NONE with a series sh (no spline):
+ * grad_X (Q,3) += omega_bar (grad omega0 + 2 rot grad cos theta) with
+ * grad omega0 = -X x (iL omega0)(X) from dsh, the three real series
+ * (3, lmax+1, 2 lmax+1) of iL_x, iL_y, iL_z applied to sh (NULL: the
+ * series term is left out); grad_sh (lmax+1, 2 lmax+1) += sum omega_bar Y. */
+int cmm_vorticity_bwd(const cmm_mesh* velmesh, const double* dsh, int lmax, double rot_rate,
+                      const double* X, const double* grad_omega, double* grad_X, double* grad_sh,
+                      void* stream);
+/* cmm_advect_project (FP64 velocity records): grad_vel[l] (Nt_u, 64) and
+ * grad_prev (Nt, 64; NULL when prev_coeffs is NULL or not wanted) += the
+ * transposes applied to grad_jets (3,4,Nv); the stencil and vertex start
+ * points are constants.  work: cmm_advect_workspace(mesh) + 12 Nv doubles. */
+int cmm_advect_project_bwd(const cmm_mesh* mesh, const cmm_mesh* velmesh, const double* const* vel_coeffs,
+                           int nvs, double ts0, int scheme, double t, double dt, const double* s_pts,
+                           const double* tan, const double* prev_coeffs, double eps, const double* grad_jets,
+                           double* const* grad_vel, double* grad_prev, double* work, void* stream);
+/* cmm_sht_velocity (omega -> velocity jets, FP64 plan): grad_omega
+ * (L+1, 2L) = transpose applied to grad_jets (3,4,Nv_u) (overwritten). */
+int cmm_sht_velocity_bwd(cmm_sht* plan, const cmm_mesh* velmesh, const double* grad_jets, double* grad_omega,
+                         void* stream);
 
 /* Angular power of a real field's coefficients alm (L,L) complex:
  * power[l] = sum over m = -l..l of |a_lm|^2 (L doubles).  Enstrophy is
