@@ -164,12 +164,36 @@ def cpu_rate(verts, tris, jets, nq, workers, steps=1, warmup=0):
 
 
 # ------------------------------------------------------------- GPU arm
+def bind_to_gpu_numa_node(index):
+    """Run this process on the host cores local to the GPU (from the PCI
+    device's local_cpulist), so pinned host buffers are allocated on the
+    GPU's NUMA node.  Returns the core count bound to, or None."""
+    try:
+        bus = subprocess.run(["nvidia-smi", "-i", str(index), "--query-gpu=pci.bus_id",
+                              "--format=csv,noheader"], capture_output=True, text=True,
+                             timeout=20).stdout.strip().lower()
+        dom, rest = bus.split(":", 1)
+        path = f"/sys/bus/pci/devices/{int(dom, 16):04x}:{rest}/local_cpulist"
+        cpus = set()
+        for part in open(path).read().strip().split(","):
+            a, _, b = part.partition("-")
+            cpus.update(range(int(a), int(b or a) + 1))
+        cpus &= os.sched_getaffinity(0)
+        if cpus:
+            os.sched_setaffinity(0, cpus)
+            return len(cpus)
+    except Exception:
+        pass
+    return None
+
+
 def bench_gpu(args, rank, world):
     import torch
     from cmm_gpu import native
 
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
     torch.cuda.set_device(dev)
+    numa_cores = bind_to_gpu_numa_node(dev.index)
     verts, tris, jets, rsp = workload()
     Q = 1 << args.logq
     mesh = native.Mesh(verts, tris, LEVEL)
@@ -250,7 +274,7 @@ def bench_gpu(args, rank, world):
     assert mesh.status() == 0
     del scratch
 
-    res = dict(ms=ms, value=value, ms_e2e=ms_e2e, launches=launches, clocks=clk.summary(),
+    res = dict(ms=ms, value=value, ms_e2e=ms_e2e, launches=launches, clocks=clk.summary(), numa_cores=numa_cores,
                nv=len(verts), nt=len(tris), Q=Q, fp64_fma_per_s=fp64_fma_per_s)
     if rank == 0 and not args.no_bve:
         try:
@@ -585,6 +609,9 @@ def bench_kernels(dev, level=7, L=1024, reps=5, stack=8, warm=True, nvtx=False):
             s.vm, s.vel_coeffs, s.ts0, native.RK4, 0.0, s.dt, s.s_pts, s.tan, prev, jets=jt,
             work=s.work)),
             nbytes=5 * nv * 48 + 96 * nv + min(288 * nvu, 20 * nv * 3 * 288))
+        put(f"vorticity_{form}", timed(lambda: s.vm.vorticity(s.vort.kind, s.vort.params, s.X, s.rot,
+                                                              omega=s.omega, spline=s.spline)),
+            nbytes=Qg * 32 + 32 * nvu)
         if form == "split_bf16":
             break
         q = torch.from_numpy(random_sphere_points(1 << 22, seed=5)).to(dev)
@@ -595,9 +622,6 @@ def bench_kernels(dev, level=7, L=1024, reps=5, stack=8, warm=True, nvtx=False):
             nbytes=Qg * 48 + stack * 96 * nv)
         put("assemble_map", timed(lambda: s.mesh.assemble(s.jets, out=s.stack[0])),
             nbytes=nv * 96 + nt * (384 + 512))
-        put("vorticity", timed(lambda: s.vm.vorticity(s.vort.kind, s.vort.params, s.X, s.rot,
-                                                      omega=s.omega, spline=s.spline)),
-            nbytes=Qg * 32 + 32 * nvu)
         del s, cs, prev, jt
         torch.cuda.empty_cache()
     return out
@@ -712,7 +736,8 @@ def main():
                  "peak_kind": "measured (FMA-chain probe in this run)"},
         "cpu_baseline": cpu,
         "e2e": {"value": world * Q * SUBMAPS / (r["ms_e2e"] / 1e3), "unit": "map evals/s",
-                "h2d_bytes_per_step": Q * 24, "d2h_bytes_per_step": Q * (24 + 4 + 72)},
+                "h2d_bytes_per_step": Q * 24, "d2h_bytes_per_step": Q * (24 + 4 + 72),
+                "host_cores_bound": r["numa_cores"]},
         "clocks": r["clocks"], "gpu_launches": r["launches"],
     }
     for key in ("bve", "rh_error", "bve_l7_L1024", "kernels", "ensemble", "adjoint"):
