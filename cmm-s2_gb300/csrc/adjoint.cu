@@ -178,58 +178,26 @@ __global__ void __launch_bounds__(kBlock) compose_bwd_kernel(MeshView m, AdjPtrs
 }
 
 // ---------------------------------------------------------- vorticity
-// Real orthonormal series value at (phi, theta) (as the forward kernel).
-__device__ double sh_series(const double* __restrict__ c, int lmax, double phi, double theta) {
-  const double x = cos(theta), s = sin(theta);
-  double out = 0.0, pmm = 0.28209479177387814;
-  const int w = 2 * lmax + 1;
-  for (int m = 0; m <= lmax; ++m) {
-    if (m > 0) pmm = -pmm * sqrt((2.0 * m + 1.0) / (2.0 * m)) * s;
-    double cm = 1.0, sm = 0.0;
-    if (m > 0) sincos(m * phi, &sm, &cm);
-    double p1 = 0.0, p = pmm;
-    for (int l = m; l <= lmax; ++l) {
-      if (l == m + 1) {
-        p1 = p;
-        p = sqrt(2.0 * m + 3.0) * x * pmm;
-      } else if (l > m + 1) {
-        const double a = sqrt((4.0 * l * l - 1.0) / ((double)l * l - (double)m * m));
-        const double b = sqrt(((l - 1.0) * (l - 1.0) - (double)m * m) / (4.0 * (l - 1.0) * (l - 1.0) - 1.0));
-        const double pn = a * (x * p - b * p1);
-        p1 = p;
-        p = pn;
-      }
-      if (m == 0)
-        out += c[(int64_t)l * w + l] * p;
-      else
-        out += 1.4142135623730951 * p * (c[(int64_t)l * w + l + m] * cm + c[(int64_t)l * w + l - m] * sm);
-    }
-  }
-  return out;
-}
-
 // grad_X = omega_bar * (grad omega0 + 2 Omega grad cos(theta)); grad omega0
 // = -X x (iL omega0)(X) with the three series dsh = iL_x, iL_y, iL_z of
-// the initial series (|X| = 1).
-__global__ void __launch_bounds__(kBlock) vorticity_bwd_x_kernel(const double* __restrict__ dsh, int lmax,
-                                                                 double rot, const double* __restrict__ X,
-                                                                 int64_t Q, const double* __restrict__ gw,
+// the initial series (|X| = 1), evaluated together.
+__global__ void __launch_bounds__(kBlock) vorticity_bwd_x_kernel(MeshView vm, const double* __restrict__ dsh,
+                                                                 int lmax, double rot,
+                                                                 const double* __restrict__ X, int64_t Q,
+                                                                 const double* __restrict__ gw,
                                                                  double* __restrict__ gX) {
-  const int64_t K = (int64_t)(lmax + 1) * (2 * lmax + 1);
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Q;
        i += (int64_t)gridDim.x * blockDim.x) {
     const double x = X[3 * i], y = X[3 * i + 1], z = X[3 * i + 2];
     const double wb = gw[i];
-    double phi, theta;
-    cart2sphere(x, y, z, &phi, &theta);
     double G[3] = {0.0, 0.0, 0.0};
     if (dsh) {
-      const double Lx = sh_series(dsh, lmax, phi, theta), Ly = sh_series(dsh + K, lmax, phi, theta),
-                   Lz = sh_series(dsh + 2 * K, lmax, phi, theta);
+      double Lv[3];
+      sh_series_n<3>(vm, dsh, lmax, sh_point(x, y, z), Lv);
       // -X x (Lx, Ly, Lz)
-      G[0] = -(y * Lz - z * Ly);
-      G[1] = -(z * Lx - x * Lz);
-      G[2] = -(x * Ly - y * Lx);
+      G[0] = -(y * Lv[2] - z * Lv[1]);
+      G[1] = -(z * Lv[0] - x * Lv[2]);
+      G[2] = -(x * Lv[1] - y * Lv[0]);
     }
     // cos(theta) = z / |X|
     const double r2 = x * x + y * y + z * z, r = sqrt(r2);
@@ -242,61 +210,62 @@ __global__ void __launch_bounds__(kBlock) vorticity_bwd_x_kernel(const double* _
   }
 }
 
-// grad_sh[l][l+-m] += sum_i omega_bar_i Y(X_i): one thread per order m,
-// the block's points staged in shared memory, per-(l, m) sums accumulated
-// privately in shared memory (no contention), then added to the output.
-constexpr int kPts = 64;
-__global__ void __launch_bounds__(kBlock) vorticity_bwd_sh_kernel(int lmax, const double* __restrict__ X,
-                                                                  int64_t Q, const double* __restrict__ gw,
-                                                                  double* __restrict__ gsh) {
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+  return v;
+}
+
+// grad_sh[l][l+-m] += sum_i omega_bar_i Y(X_i): one point per thread, each
+// basis value summed over the warp by shuffles, the warp sums gathered in
+// shared memory, one global atomic per coefficient per block.
+__global__ void __launch_bounds__(256) vorticity_bwd_sh_kernel(MeshView vm, int lmax,
+                                                               const double* __restrict__ X, int64_t Q,
+                                                               const double* __restrict__ gw,
+                                                               double* __restrict__ gsh) {
   extern __shared__ double acc[];   // (lmax+1) x (2 lmax + 1)
-  __shared__ double sx[kPts], ss[kPts], sphi[kPts], sw[kPts];
   const int w = 2 * lmax + 1;
   const int K = (lmax + 1) * w;
+  const int T = kShTableMax + 1;
   for (int k = threadIdx.x; k < K; k += blockDim.x) acc[k] = 0.0;
-  const int m = threadIdx.x;
-  for (int64_t base = (int64_t)blockIdx.x * kPts; base < Q; base += (int64_t)gridDim.x * kPts) {
-    __syncthreads();
-    if (threadIdx.x < kPts) {
-      const int64_t i = base + threadIdx.x;
-      if (i < Q) {
-        double phi, theta;
-        cart2sphere(X[3 * i], X[3 * i + 1], X[3 * i + 2], &phi, &theta);
-        sx[threadIdx.x] = cos(theta);
-        ss[threadIdx.x] = sin(theta);
-        sphi[threadIdx.x] = phi;
-        sw[threadIdx.x] = gw[i];
-      } else {
-        sx[threadIdx.x] = ss[threadIdx.x] = sphi[threadIdx.x] = sw[threadIdx.x] = 0.0;
-      }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < Q; base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = base + threadIdx.x;
+    double wb = 0.0;
+    ShPoint pt{1.0, 0.0, 1.0, 0.0};
+    if (i < Q) {
+      wb = gw[i];
+      pt = sh_point(X[3 * i], X[3 * i + 1], X[3 * i + 2]);
     }
-    __syncthreads();
-    if (m <= lmax) {
-      for (int j = 0; j < kPts; ++j) {
-        const double wb = sw[j];
-        if (wb == 0.0) continue;
-        const double x = sx[j], s = ss[j];
-        double pmm = 0.28209479177387814;
-        for (int mm = 1; mm <= m; ++mm) pmm = -pmm * sqrt((2.0 * mm + 1.0) / (2.0 * mm)) * s;
-        double cm = 1.0, sm = 0.0;
-        if (m > 0) sincos(m * sphi[j], &sm, &cm);
-        double p1 = 0.0, p = pmm;
-        for (int l = m; l <= lmax; ++l) {
-          if (l == m + 1) {
-            p1 = p;
-            p = sqrt(2.0 * m + 3.0) * x * pmm;
-          } else if (l > m + 1) {
-            const double a = sqrt((4.0 * l * l - 1.0) / ((double)l * l - (double)m * m));
-            const double b = sqrt(((l - 1.0) * (l - 1.0) - (double)m * m) / (4.0 * (l - 1.0) * (l - 1.0) - 1.0));
-            const double pn = a * (x * p - b * p1);
-            p1 = p;
-            p = pn;
-          }
-          if (m == 0) {
-            acc[l * w + l] += wb * p;
-          } else {
-            acc[l * w + l + m] += wb * 1.4142135623730951 * p * cm;
-            acc[l * w + l - m] += wb * 1.4142135623730951 * p * sm;
+    double pmm = 0.28209479177387814, cm = 1.0, sm = 0.0;
+    for (int m = 0; m <= lmax; ++m) {
+      if (m > 0) {
+        pmm = -pmm * __ldg(vm.sh_fm + m) * pt.st;
+        const double c2 = cm * pt.cp - sm * pt.sp;
+        sm = sm * pt.cp + cm * pt.sp;
+        cm = c2;
+      }
+      const double* ab = vm.sh_ab + 2 * (int64_t)m * T;
+      double p1 = 0.0, p = pmm;
+      for (int l = m; l <= lmax; ++l) {
+        if (l == m + 1) {
+          p1 = p;
+          p = __ldg(ab + 2 * l) * pt.ct * pmm;
+        } else if (l > m + 1) {
+          const double pn = __ldg(ab + 2 * l) * (pt.ct * p - __ldg(ab + 2 * l + 1) * p1);
+          p1 = p;
+          p = pn;
+        }
+        if (m == 0) {
+          const double v = warp_sum(wb * p);
+          if (lane == 0) atomicAdd(acc + l * w + l, v);
+        } else {
+          const double f = wb * 1.4142135623730951 * p;
+          const double vc = warp_sum(f * cm), vs = warp_sum(f * sm);
+          if (lane == 0) {
+            atomicAdd(acc + l * w + l + m, vc);
+            atomicAdd(acc + l * w + l - m, vs);
           }
         }
       }
@@ -635,27 +604,25 @@ int launch_advect_project_bwd(const MeshView& mesh, const MeshView& vm, const do
   return check("advect_points_bwd_kernel");
 }
 
-int launch_vorticity_bwd(const double* dsh, int lmax, double rot, const double* X, int64_t Q,
-                         const double* gw, double* gX, double* gsh, cudaStream_t s) {
+int launch_vorticity_bwd(const MeshView& vm, const double* dsh, int lmax, double rot, const double* X,
+                         int64_t Q, const double* gw, double* gX, double* gsh, cudaStream_t s) {
+  if (lmax > kShTableMax) {
+    set_last_error("cmm_vorticity_bwd: lmax must be <= 128");
+    return CMM_ERR_UNSUPPORTED;
+  }
   if (gX) {
-    vorticity_bwd_x_kernel<<<grid_for(Q, kBlock), kBlock, 0, s>>>(dsh, lmax, rot, X, Q, gw, gX);
+    vorticity_bwd_x_kernel<<<grid_for(Q, kBlock), kBlock, 0, s>>>(vm, dsh, lmax, rot, X, Q, gw, gX);
     int rc = check("vorticity_bwd_x_kernel");
     if (rc) return rc;
   }
   if (gsh && lmax >= 0) {
-    if (lmax >= kBlock) {
-      set_last_error("cmm_vorticity_bwd: lmax must be < 128");
-      return CMM_ERR_UNSUPPORTED;
-    }
     const size_t smem = sizeof(double) * (size_t)(lmax + 1) * (2 * lmax + 1);
     if (smem > 48 * 1024) {
       cudaError_t e = cudaFuncSetAttribute(vorticity_bwd_sh_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)smem);
       if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(vorticity_bwd_sh_kernel)");
     }
-    const int64_t blocks = (Q + kPts - 1) / kPts;
-    const int g = (int)(blocks < 152 * 4 ? blocks : 152 * 4);
-    vorticity_bwd_sh_kernel<<<g, kBlock, smem, s>>>(lmax, X, Q, gw, gsh);
+    vorticity_bwd_sh_kernel<<<grid_for(Q, 256), 256, smem, s>>>(vm, lmax, X, Q, gw, gsh);
     return check("vorticity_bwd_sh_kernel");
   }
   return CMM_OK;

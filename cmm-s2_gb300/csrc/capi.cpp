@@ -175,8 +175,8 @@ int cmm_vorticity_eval(const cmm_mesh* velmesh, int kind, const double* params, 
                        const double* X, double* omega, void* stream) {
   if (!velmesh || velmesh->view.kind != kLatLon) return arg_error("cmm_vorticity_eval: velocity mesh expected");
   if (!X || !omega || (nparams > 0 && !params) || nparams > 12 || kind < 0 || kind > 6 ||
-      (sh && lmax < 0))
-    return arg_error("cmm_vorticity_eval: bad argument");
+      (sh && (lmax < 0 || lmax > kShTableMax)))
+    return arg_error("cmm_vorticity_eval: bad argument (series degree lmax must be in [0, 128])");
   const int L = velmesh->view.L;
   const int64_t Q = (int64_t)(L + 1) * 2 * L;
   return launch_vorticity(kind, params, nparams, sh, lmax, velmesh->view, spline, rot_rate, X, Q,
@@ -297,7 +297,8 @@ int cmm_vorticity_bwd(const cmm_mesh* velmesh, const double* dsh, int lmax, doub
     return arg_error("cmm_vorticity_bwd: bad argument");
   const int L = velmesh->view.L;
   const int64_t Q = (int64_t)(L + 1) * 2 * L;
-  return launch_vorticity_bwd(dsh, lmax, rot_rate, X, Q, grad_omega, grad_X, grad_sh, (cudaStream_t)stream);
+  return launch_vorticity_bwd(velmesh->view, dsh, lmax, rot_rate, X, Q, grad_omega, grad_X, grad_sh,
+                              (cudaStream_t)stream);
 }
 
 int cmm_sht_velocity_bwd(cmm_sht* plan, const cmm_mesh* velmesh, const double* grad_jets, double* grad_omega,

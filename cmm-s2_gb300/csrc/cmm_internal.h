@@ -52,6 +52,11 @@ struct MeshView {
   int rec32;
   const float* tri_asm_f;   // (kAsmFactors, nt), factor-major, when rec32
   int field32;              // analytic initial vorticity fields in FP32
+  // recurrence table of the orthonormal associated Legendre functions for
+  // real SH series of degree <= kShTableMax: sh_ab[2 (m (kShTableMax+1) + l)]
+  // = (a_lm, b_lm), sh_fm[m] = sqrt((2m+1)/(2m))
+  const double* sh_ab;
+  const double* sh_fm;
   // launch shapes chosen by an autotuner (cmm_mesh_set_block), threads per
   // block of the tunable kernels on this mesh; 0 = the library default
   int block[4];
@@ -61,6 +66,7 @@ struct MeshView {
 constexpr int kTuneCompose = 0, kTuneAdvect = 1, kTuneVorticity = 2, kTuneLocate = 3;
 inline int block_of(const MeshView& m, int k, int dflt) { return m.block[k] > 0 ? m.block[k] : dflt; }
 
+constexpr int kShTableMax = 128;
 constexpr int kIcosahedral = 0;
 constexpr int kLatLon = 1;
 
@@ -84,7 +90,7 @@ struct DeviceBuffer {
 struct cmm_mesh {
   cmm::MeshView view;
   cmm::DeviceBuffer verts, tri_v, tri_loc, tri_asm, root, root_f, root_adj, node_n, node_nf, leaf_row,
-      status, theta, phi, grid, cos_theta, tri_asm_f;
+      status, theta, phi, grid, cos_theta, tri_asm_f, sh_ab, sh_fm;
 };
 
 namespace cmm {
@@ -180,8 +186,8 @@ int launch_assemble_bwd(const MeshView& m, const double* gc, double* gj, cudaStr
 int launch_compose_bwd(const MeshView& m, const double* const* cs, double* const* gcs, int S,
                        const double* q, int64_t n, const double* gout, double* gq, double* work,
                        cudaStream_t s);
-int launch_vorticity_bwd(const double* dsh, int lmax, double rot, const double* X, int64_t Q,
-                         const double* gw, double* gX, double* gsh, cudaStream_t s);
+int launch_vorticity_bwd(const MeshView& vm, const double* dsh, int lmax, double rot, const double* X,
+                         int64_t Q, const double* gw, double* gX, double* gsh, cudaStream_t s);
 // work: cmm_advect_workspace (15 nv) + 12 nv doubles
 int launch_advect_project_bwd(const MeshView& mesh, const MeshView& vm, const double* const* vel,
                               double* const* gvel, int nvs, const TimeWeights& tw, int scheme, double dt,

@@ -356,6 +356,71 @@ __device__ __forceinline__ double latlon_scalar(const MeshView& m, const double*
   return P[0];
 }
 
+// Real orthonormal spherical-harmonic series (coefficients (lmax+1,
+// 2 lmax+1), column l+m: m = 0 -> Pbar_l0, m > 0 -> sqrt2 Pbar_lm cos(m phi),
+// m < 0 -> sqrt2 Pbar_l|m| sin(|m| phi)) at the point (x, y, z), from the
+// velocity mesh's recurrence table, cos/sin(m phi) by rotation, no
+// transcendental calls.  NS series (coefficient arrays K = (lmax+1)(2lmax+1)
+// apart) share the Legendre recurrence.  lmax <= kShTableMax.
+struct ShPoint {
+  double ct, st, cp, sp;
+};
+
+__device__ __forceinline__ ShPoint sh_point(double x, double y, double z) {
+  const double rho = sqrt(x * x + y * y), r = sqrt(rho * rho + z * z);
+  ShPoint p;
+  p.ct = z / r;
+  p.st = rho / r;
+  if (rho > 0.0) {
+    p.cp = x / rho;
+    p.sp = y / rho;
+  } else {   // atan2(0, 0) = 0
+    p.cp = 1.0;
+    p.sp = 0.0;
+  }
+  return p;
+}
+
+template <int NS>
+__device__ __forceinline__ void sh_series_n(const MeshView& vm, const double* __restrict__ c, int lmax,
+                                            const ShPoint& pt, double* out) {
+  const int T = kShTableMax + 1;
+  const int w = 2 * lmax + 1;
+  const int64_t K = (int64_t)(lmax + 1) * w;
+#pragma unroll
+  for (int k = 0; k < NS; ++k) out[k] = 0.0;
+  double pmm = 0.28209479177387814;   // sqrt(1/(4 pi))
+  double cm = 1.0, sm = 0.0;          // cos(m phi), sin(m phi)
+  for (int m = 0; m <= lmax; ++m) {
+    if (m > 0) {
+      pmm = -pmm * __ldg(vm.sh_fm + m) * pt.st;
+      const double c2 = cm * pt.cp - sm * pt.sp;
+      sm = sm * pt.cp + cm * pt.sp;
+      cm = c2;
+    }
+    const double* ab = vm.sh_ab + 2 * (int64_t)m * T;
+    double p1 = 0.0, p = pmm;
+    for (int l = m; l <= lmax; ++l) {
+      if (l == m + 1) {
+        p1 = p;
+        p = __ldg(ab + 2 * l) * pt.ct * pmm;
+      } else if (l > m + 1) {
+        const double pn = __ldg(ab + 2 * l) * (pt.ct * p - __ldg(ab + 2 * l + 1) * p1);
+        p1 = p;
+        p = pn;
+      }
+      const int64_t i = (int64_t)l * w + l;
+#pragma unroll
+      for (int k = 0; k < NS; ++k) {
+        if (m == 0)
+          out[k] += c[k * K + i] * p;
+        else
+          out[k] += 1.4142135623730951 * p * (c[k * K + i + m] * cm + c[k * K + i - m] * sm);
+      }
+    }
+  }
+}
+
 inline int grid_for(int64_t n, int block) {
   int64_t b = (n + block - 1) / block;
   const int64_t cap = 152LL * 16;

@@ -410,17 +410,18 @@ __global__ void jets_kernel(const R* __restrict__ fld, int L, const double* __re
   else
     node = N + (v - 1);
   const int64_t fs = (int64_t)(L + 1) * N;
-  const double X0 = grid[4 * node], X1 = grid[4 * node + 1], X2 = grid[4 * node + 2];
-  const double nX = sqrt(X0 * X0 + X1 * X1 + X2 * X2);
+  // arithmetic in the samples' precision (FP32 in the mixed form)
+  const R X0 = (R)grid[4 * node], X1 = (R)grid[4 * node + 1], X2 = (R)grid[4 * node + 2];
+  const R nX = sqrt(X0 * X0 + X1 * X1 + X2 * X2);
   for (int i = 0; i < 3; ++i) {
     jets[(int64_t)(i * 4) * nv + v] = (double)fld[i * fs + node];
-    const double g0 = (double)fld[(3 + 3 * i) * fs + node], g1 = (double)fld[(4 + 3 * i) * fs + node],
-                 g2 = (double)fld[(5 + 3 * i) * fs + node];
-    const double c0 = g1 * X2 - g2 * X1, c1 = g2 * X0 - g0 * X2, c2 = g0 * X1 - g1 * X0;
-    const double sc = (c0 * X0 + c1 * X1 + c2 * X2) / nX;
-    jets[(int64_t)(0 * 4 + 1 + i) * nv + v] = c0 - sc * X0;
-    jets[(int64_t)(1 * 4 + 1 + i) * nv + v] = c1 - sc * X1;
-    jets[(int64_t)(2 * 4 + 1 + i) * nv + v] = c2 - sc * X2;
+    const R g0 = fld[(3 + 3 * i) * fs + node], g1 = fld[(4 + 3 * i) * fs + node],
+            g2 = fld[(5 + 3 * i) * fs + node];
+    const R c0 = g1 * X2 - g2 * X1, c1 = g2 * X0 - g0 * X2, c2 = g0 * X1 - g1 * X0;
+    const R sc = (c0 * X0 + c1 * X1 + c2 * X2) / nX;
+    jets[(int64_t)(0 * 4 + 1 + i) * nv + v] = (double)(c0 - sc * X0);
+    jets[(int64_t)(1 * 4 + 1 + i) * nv + v] = (double)(c1 - sc * X1);
+    jets[(int64_t)(2 * 4 + 1 + i) * nv + v] = (double)(c2 - sc * X2);
   }
 }
 
@@ -431,16 +432,21 @@ __global__ void jets_kernel(const R* __restrict__ fld, int L, const double* __re
 // sum over rings: out[m][l] = sum_{j=0..nr} w_j c_m Pbar_lm(theta_j) F[j][m],
 // rings j and nr-j paired (Pbar(pi - theta) = (-1)^(l+m) Pbar(theta)),
 // F row stride `row`, c_0 = 1 and c_m = cm (m > 0); w == NULL: unit weights.
+// blockIdx.y selects one of several fields (F + y fstride_in, out + y fstride_out);
+// R ring pairs per thread (256 R >= nr/2 + 1).
+template <int R, int C = 16>
 __global__ void __launch_bounds__(256) legendre_sum_kernel(const double2* __restrict__ F, int64_t row, int L,
                                                            int nr, const double* __restrict__ w, double cm,
                                                            const double* __restrict__ ct,
                                                            const double* __restrict__ pmm, int pstride,
                                                            const double* __restrict__ ra,
                                                            const double* __restrict__ rb,
-                                                           double2* __restrict__ out) {
+                                                           double2* __restrict__ out, int64_t fs_in,
+                                                           int64_t fs_out) {
   const int m = blockIdx.x;
+  F += blockIdx.y * fs_in;
+  out += blockIdx.y * fs_out;
   const int npair = nr / 2 + 1;
-  constexpr int R = 8;
   const double sc = m == 0 ? 1.0 : cm;
   double2 E[R], O[R];
   double x[R], p0[R], p1[R];
@@ -470,14 +476,14 @@ __global__ void __launch_bounds__(256) legendre_sum_kernel(const double2* __rest
       x[r] = p0[r] = p1[r] = 0.0;
     }
   }
-  __shared__ double2 red[kLChunk][8];
+  __shared__ double2 red[C][8];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int l0 = m; l0 < L; l0 += kLChunk) {
-    double2 acc[kLChunk];
+  for (int l0 = m; l0 < L; l0 += C) {
+    double2 acc[C];
 #pragma unroll
-    for (int q = 0; q < kLChunk; ++q) acc[q] = make_double2(0.0, 0.0);
+    for (int q = 0; q < C; ++q) acc[q] = make_double2(0.0, 0.0);
 #pragma unroll
-    for (int q = 0; q < kLChunk; ++q) {
+    for (int q = 0; q < C; ++q) {
       const int l = l0 + q;
       if (l < L) {
         const bool even = ((l - m) & 1) == 0;
@@ -509,7 +515,7 @@ __global__ void __launch_bounds__(256) legendre_sum_kernel(const double2* __rest
       }
     }
 #pragma unroll
-    for (int q = 0; q < kLChunk; ++q) {
+    for (int q = 0; q < C; ++q) {
       double vx = acc[q].x, vy = acc[q].y;
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) {
@@ -519,7 +525,7 @@ __global__ void __launch_bounds__(256) legendre_sum_kernel(const double2* __rest
       if (lane == 0) red[q][warp] = make_double2(vx, vy);
     }
     __syncthreads();
-    if (threadIdx.x < kLChunk) {
+    if (threadIdx.x < C) {
       const int q = threadIdx.x, l = l0 + q;
       double2 s = make_double2(0.0, 0.0);
       for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
@@ -1086,11 +1092,22 @@ int sht_velocity_bwd(cmm_sht* p, const cmm_mesh* vm, const double* gjets, double
   r = cufftExecD2Z(p->b_ring_fwd12, (cufftDoubleReal*)gf, (cufftDoubleComplex*)Sb);
   if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExecD2Z(adjoint)");
   // synthesis^T: unit-weight Legendre sums over the L+1 rings, c_m = 2 for m > 0
-  for (int f = 0; f < kFields; ++f) {
-    legendre_sum_kernel<<<L, 256, 0, s>>>(Sb + (int64_t)f * (L + 1) * (L + 1), L + 1, L, L, nullptr, 2.0,
-                                          (const double*)p->ct_rings.p, (const double*)p->pmm_rings.p,
-                                          L + 1, (const double*)p->ra.p, (const double*)p->rb.p,
-                                          Fb + (int64_t)f * L * L);
+  {
+    const int npair = L / 2 + 1;
+    const dim3 gl(L, kFields);
+    const int64_t fin = (int64_t)(L + 1) * (L + 1), fout = (int64_t)L * L;
+    const double* ct = (const double*)p->ct_rings.p;
+    const double* pm = (const double*)p->pmm_rings.p;
+    const double* ra = (const double*)p->ra.p;
+    const double* rb = (const double*)p->rb.p;
+    if (npair <= 256)
+      legendre_sum_kernel<1><<<gl, 256, 0, s>>>(Sb, L + 1, L, L, nullptr, 2.0, ct, pm, L + 1, ra, rb, Fb, fin, fout);
+    else if (npair <= 512)
+      legendre_sum_kernel<2><<<gl, 256, 0, s>>>(Sb, L + 1, L, L, nullptr, 2.0, ct, pm, L + 1, ra, rb, Fb, fin, fout);
+    else if (npair <= 1024)
+      legendre_sum_kernel<4><<<gl, 256, 0, s>>>(Sb, L + 1, L, L, nullptr, 2.0, ct, pm, L + 1, ra, rb, Fb, fin, fout);
+    else
+      legendre_sum_kernel<8><<<gl, 256, 0, s>>>(Sb, L + 1, L, L, nullptr, 2.0, ct, pm, L + 1, ra, rb, Fb, fin, fout);
     if ((rc = check_launch("legendre_sum_kernel"))) return rc;
   }
   dim3 b(128), g((L + 127) / 128, L);

@@ -120,7 +120,7 @@ int bve_create(const cmm_bve_desc* d, cmm_bve** out) {
       !d->tan || !d->id_jets || !d->sample_pts || !d->jets || !d->coeffs_cur || !d->work || !d->X ||
       !d->omega || !d->vel_jets || !d->vel[0] || !d->vel[1] || !d->vel[2] || d->n_stack < 1 ||
       !d->stack || d->n_maps < 1 || d->Nt < 3 || d->nparams < 0 || d->nparams > 12 ||
-      d->vort_kind < 0 || d->vort_kind > 6 || (d->sh && d->lmax < 0) || d->nc < 0 ||
+      d->vort_kind < 0 || d->vort_kind > 6 || (d->sh && (d->lmax < 0 || d->lmax > kShTableMax)) || d->nc < 0 ||
       d->nc > d->n_stack || d->n_stack > CMM_MAX_SUBMAPS - 1 || !(d->tspan_step > 0.0)) {
     set_last_error("cmm_bve_create: bad descriptor");
     return CMM_ERR_ARG;

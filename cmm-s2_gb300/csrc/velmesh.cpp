@@ -72,6 +72,28 @@ int build_latlon(int L, const double* theta, const double* phi, const double* gr
     if ((rc = m->cos_theta.upload(ct.data(), ct.size() * 8))) return rc;
   }
   if ((rc = m->status.upload(&zero, sizeof(int)))) return rc;
+  {
+    // Pbar_lm recurrence: l = m+1: a = sqrt(2m+3); l >= m+2:
+    // a = sqrt((4l^2-1)/(l^2-m^2)), b = sqrt(((l-1)^2-m^2)/(4(l-1)^2-1))
+    const int T = kShTableMax + 1;
+    std::vector<double> ab((size_t)2 * T * T, 0.0), fm(T, 0.0);
+    for (int mm = 0; mm < T; ++mm) {
+      if (mm > 0) fm[mm] = std::sqrt((2.0 * mm + 1.0) / (2.0 * mm));
+      for (int l = mm + 1; l < T; ++l) {
+        double a, b = 0.0;
+        if (l == mm + 1) {
+          a = std::sqrt(2.0 * mm + 3.0);
+        } else {
+          a = std::sqrt((4.0 * l * l - 1.0) / ((double)l * l - (double)mm * mm));
+          b = std::sqrt(((l - 1.0) * (l - 1.0) - (double)mm * mm) / (4.0 * (l - 1.0) * (l - 1.0) - 1.0));
+        }
+        ab[2 * ((size_t)mm * T + l)] = a;
+        ab[2 * ((size_t)mm * T + l) + 1] = b;
+      }
+    }
+    if ((rc = m->sh_ab.upload(ab.data(), ab.size() * 8))) return rc;
+    if ((rc = m->sh_fm.upload(fm.data(), fm.size() * 8))) return rc;
+  }
   MeshView& v = m->view;
   v = MeshView{};
   v.kind = kLatLon;
@@ -87,6 +109,8 @@ int build_latlon(int L, const double* theta, const double* phi, const double* gr
   v.phi = (const double*)m->phi.p;
   v.grid = (const double*)m->grid.p;
   v.status = (int*)m->status.p;
+  v.sh_ab = (const double*)m->sh_ab.p;
+  v.sh_fm = (const double*)m->sh_fm.p;
   // spacing as the reference computes it (mesh_functions.py:214-215)
   v.dphi = std::fabs(phi[1] - phi[0]);
   v.dthe = std::fabs(theta[1] - theta[0]);

@@ -110,38 +110,6 @@ __device__ float omega0_f(const VortParams& v, float phi, float theta) {
   }
 }
 
-// Real orthonormal series: m = 0 -> Pbar_l0, m > 0 -> sqrt2 Pbar_lm cos(m
-// phi), m < 0 -> sqrt2 Pbar_l|m| sin(|m| phi); coefficients (lmax+1,
-// 2 lmax+1), column l+m.
-__device__ double sh_value(const double* __restrict__ c, int lmax, double phi, double theta) {
-  const double x = cos(theta), s = sin(theta);
-  double out = 0.0, pmm = 0.28209479177387814;  // sqrt(1/(4 pi))
-  const int w = 2 * lmax + 1;
-  for (int m = 0; m <= lmax; ++m) {
-    if (m > 0) pmm = -pmm * sqrt((2.0 * m + 1.0) / (2.0 * m)) * s;
-    double cm = 1.0, sm = 0.0;
-    if (m > 0) sincos(m * phi, &sm, &cm);
-    double p1 = 0.0, p = pmm;
-    for (int l = m; l <= lmax; ++l) {
-      if (l == m + 1) {
-        p1 = p;
-        p = sqrt(2.0 * m + 3.0) * x * pmm;
-      } else if (l > m + 1) {
-        const double a = sqrt((4.0 * l * l - 1.0) / ((double)l * l - (double)m * m));
-        const double b = sqrt(((l - 1.0) * (l - 1.0) - (double)m * m) / (4.0 * (l - 1.0) * (l - 1.0) - 1.0));
-        const double pn = a * (x * p - b * p1);
-        p1 = p;
-        p = pn;
-      }
-      if (m == 0)
-        out += c[(int64_t)l * w + l] * p;
-      else
-        out += 1.4142135623730951 * p * (c[(int64_t)l * w + l + m] * cm + c[(int64_t)l * w + l - m] * sm);
-    }
-  }
-  return out;
-}
-
 __global__ void __launch_bounds__(256) vorticity_kernel(VortParams vp, const double* __restrict__ sh, int lmax,
                                  MeshView vm, const double* __restrict__ spline, double rot,
                                  const double* __restrict__ X, int64_t Q, int npr,
@@ -149,20 +117,26 @@ __global__ void __launch_bounds__(256) vorticity_kernel(VortParams vp, const dou
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < Q;
        i += (int64_t)gridDim.x * blockDim.x) {
     const double x = X[3 * i], y = X[3 * i + 1], z = X[3 * i + 2];
-    double w, ct;
-    if (vm.field32 && !sh) {
+    double w = 0.0, ct;
+    if (vm.field32) {
       const float xf = (float)x, yf = (float)y, zf = (float)z;
       float phif = atan2f(yf, xf);
       if (phif < 0.f) phif += 6.28318530717958647692f;
       const float thf = atan2f(sqrtf(xf * xf + yf * yf), zf);
-      w = vp.kind == CMM_VORT_NONE ? 0.0 : (double)omega0_f(vp, phif, thf);
+      if (vp.kind != CMM_VORT_NONE) w = (double)omega0_f(vp, phif, thf);
       ct = z / sqrt(x * x + y * y + z * z);   // cos(theta), FP64
-    } else {
+    } else if (vp.kind != CMM_VORT_NONE) {
       double phi, theta;
       cart2sphere(x, y, z, &phi, &theta);
       w = omega0(vp, phi, theta);
-      if (sh) w += sh_value(sh, lmax, phi, theta);
       ct = cos(theta);
+    } else {
+      ct = z / sqrt(x * x + y * y + z * z);
+    }
+    if (sh) {
+      double v;
+      sh_series_n<1>(vm, sh, lmax, sh_point(x, y, z), &v);
+      w += v;
     }
     if (spline) w += latlon_scalar(vm, spline, x, y, z);
     const double r = w + 2 * rot * ct - 2 * rot * cos_ring[i / npr];

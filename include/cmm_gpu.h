@@ -210,7 +210,7 @@ int cmm_advect_project_noalloc(const cmm_mesh* mesh, const cmm_mesh* velmesh,
  * 2 rot cos(theta_ring) (cmm_s2/core/spherical_simulations.py:269-272),
  * omega0 = field `kind` plus, when sh is not NULL, the real orthonormal
  * spherical-harmonic series sh (lmax+1, 2lmax+1) (column l+m; m>0 cos,
- * m<0 sin, both with sqrt2), plus, when spline is not NULL, the scalar
+ * m<0 sin, both with sqrt2; lmax <= 128), plus, when spline is not NULL, the scalar
  * Powell-Sabin spline with ncomp=1 coefficients `spline` on `velmesh`
  * (the spherical_spline a caller builds with cmm_sht_scalar_jets +
  * cmm_assemble, as project_onto_S12 does,

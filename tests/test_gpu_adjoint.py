@@ -186,7 +186,10 @@ def test_bve_gradient_against_differences(mods):
     update's amplified rounding (stencil differences over 4e-5 turn 1e-16
     into ~3e-12 per jet gradient, every step) and, at large steps, the
     curvature of J: their own error is ~1e-7..1e-5 depending on the step.
-    The check takes the best of steps 1e-4, 1e-5, 1e-6 and requires 2e-6."""
+    The check takes the best of steps 1e-4, 1e-5, 1e-6 and requires the
+    discrepancy below 2e-6 of the coefficient's derivative or, for the
+    small derivatives where the differences' own noise dominates, below
+    1e-7 of the largest derivative."""
     native, adj, meshgen, workloads = mods
     lmax = 6
     run = adj.BVEGradient(3, 16, 14, 0.1, n_maps=5)
@@ -198,6 +201,7 @@ def test_bve_gradient_against_differences(mods):
     J, grad = run.gradient(sh, target)
     rng = np.random.default_rng(5)
     idx = [(l, int(rng.integers(0, 2 * l + 1))) for l in rng.integers(1, lmax + 1, 8)]
+    gmax = float(grad.abs().max())
     for l, c in idx:
         ad = float(grad[l, c])
         errs = []
@@ -207,7 +211,7 @@ def test_bve_gradient_against_differences(mods):
             sm[l, c] -= h
             with torch.no_grad():
                 fd = (float(run.misfit(sp, target)) - float(run.misfit(sm, target))) / (2 * h)
-            errs.append(abs(fd - ad) / abs(ad))
+            errs.append(abs(fd - ad))
         print(f"coefficient ({l},{c - l}): adjoint {ad:.10e} rel err at h=1e-4,1e-5,1e-6: "
-              + " ".join(f"{e:.1e}" for e in errs))
-        assert min(errs) < 2e-6
+              + " ".join(f"{e / abs(ad):.1e}" for e in errs))
+        assert min(errs) < max(2e-6 * abs(ad), 1e-7 * gmax)
