@@ -52,6 +52,8 @@ struct MeshView {
   int rec32;
   const float* tri_asm_f;   // (kAsmFactors, nt), factor-major, when rec32
   int field32;              // analytic initial vorticity fields in FP32
+  const float* tri_loc_f;   // (nt, kLocStride) FP32 copy of the location records, when rec32
+  float phi0_f, dphi_f, the0_f, dthe_f;   // FP32 copies of phi[0], dphi, theta[0], dthe
   // recurrence table of the orthonormal associated Legendre functions for
   // real SH series of degree <= kShTableMax: sh_ab[2 (m (kShTableMax+1) + l)]
   // = (a_lm, b_lm), sh_fm[m] = sqrt((2m+1)/(2m))
@@ -90,7 +92,7 @@ struct DeviceBuffer {
 struct cmm_mesh {
   cmm::MeshView view;
   cmm::DeviceBuffer verts, tri_v, tri_loc, tri_asm, root, root_f, root_adj, node_n, node_nf, leaf_row,
-      status, theta, phi, grid, cos_theta, tri_asm_f, sh_ab, sh_fm;
+      status, theta, phi, grid, cos_theta, tri_asm_f, tri_loc_f, sh_ab, sh_fm;
 };
 
 namespace cmm {

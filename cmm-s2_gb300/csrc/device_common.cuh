@@ -147,6 +147,57 @@ __device__ __forceinline__ Gam gamma_of(const double* L, const Bcc& b, const Spl
   return Gam{bh - bm, edge_norm(L, sp.hi, sp.mid) * (bm - bl), L[9] * bl};
 }
 
+// FP32 barycentrics, sub-triangle and sub-triangle barycentrics from the
+// FP32 location record (velocity patches of the mixed form; the patch is
+// C1 across sub-triangles, so an FP32 ordering of nearly equal
+// barycentrics changes the value at rounding level only).
+struct BccF {
+  float b0, b1, b2;
+};
+
+__device__ __forceinline__ BccF bcc_of_f(const float* L, float x, float y, float z) {
+  return BccF{fmaf(L[0], x, fmaf(L[1], y, L[2] * z)), fmaf(L[3], x, fmaf(L[4], y, L[5] * z)),
+              fmaf(L[6], x, fmaf(L[7], y, L[8] * z))};
+}
+
+// b = Minv p = Minv (p - v1) + (1, 0, 0): the difference p - v1 (size of
+// the triangle) is formed in FP64 and the FP32 product then carries no
+// cancellation (Minv's rows are ~1/h long; Minv p in FP32 would lose
+// h^-1 * 6e-8 of b).
+__device__ __forceinline__ BccF bcc_rel_f(const MeshView& m, int t, const float* L, double x, double y,
+                                          double z) {
+  const int v1 = __ldg(&m.tri_v[t].x);
+  const double* v = m.verts + 4 * (int64_t)v1;
+  const float dx = (float)(x - __ldg(v)), dy = (float)(y - __ldg(v + 1)), dz = (float)(z - __ldg(v + 2));
+  BccF b = bcc_of_f(L, dx, dy, dz);
+  b.b0 += 1.0f;
+  return b;
+}
+
+__device__ __forceinline__ Split split_of_f(const BccF& b) {
+  int lo = 0, hi = 0;
+  float vlo = b.b0, vhi = b.b0;
+  if (b.b1 < vlo) { vlo = b.b1; lo = 1; }
+  if (b.b2 < vlo) { vlo = b.b2; lo = 2; }
+  if (b.b1 > vhi) { vhi = b.b1; hi = 1; }
+  if (b.b2 > vhi) { vhi = b.b2; hi = 2; }
+  if (lo == hi) { lo = 1; hi = 0; }
+  return Split{lo, 3 - lo - hi, hi};
+}
+
+__device__ __forceinline__ float pick_f(const BccF& b, int i) {
+  return i == 0 ? b.b0 : (i == 1 ? b.b1 : b.b2);
+}
+
+__device__ __forceinline__ void gamma_of_f(const float* L, const BccF& b, const Split& sp, float* g) {
+  const float bl = pick_f(b, sp.lo), bm = pick_f(b, sp.mid), bh = pick_f(b, sp.hi);
+  const int s = sp.hi + sp.mid;
+  const float en = s == 1 ? L[10] : (s == 3 ? L[11] : L[12]);
+  g[0] = bh - bm;
+  g[1] = en * (bm - bl);
+  g[2] = L[9] * bl;
+}
+
 template <int NC>
 struct Ords {
   double c[6][NC];
@@ -309,9 +360,9 @@ __device__ __forceinline__ int latlon_locate(const MeshView& m, double x, double
   float phif = atan2f(yf, xf);
   if (phif < 0.f) phif += 6.28318530717958647692f;
   const float thef = atan2f(sqrtf(xf * xf + yf * yf), zf);
-  const float u = (phif - (float)m.phi[0]) / (float)m.dphi;
-  const float v = (thef - (float)m.theta[0]) / (float)m.dthe;
-  const float du = 2e-6f / (float)m.dphi, dv = 2e-6f / (float)m.dthe;
+  const float u = (phif - m.phi0_f) / m.dphi_f;
+  const float v = (thef - m.the0_f) / m.dthe_f;
+  const float du = 2e-6f / m.dphi_f, dv = 2e-6f / m.dthe_f;
   const float uf = floorf(u), vf = floorf(v);
   const float fu = u - uf, fv = v - vf;
   const int phi_l = (int)uf;
@@ -419,6 +470,29 @@ __device__ __forceinline__ void sh_series_n(const MeshView& vm, const double* __
       }
     }
   }
+}
+
+// The scalar spline in FP32 (mixed form, field32 with FP32 location
+// records): FP32 barycentrics and patch from the FP64 ordinates.
+__device__ __forceinline__ double latlon_scalar_f(const MeshView& m, const double* __restrict__ coeffs,
+                                                  double x, double y, double z) {
+  const int t = latlon_locate(m, x, y, z);
+  const float* Lf = m.tri_loc_f + (int64_t)t * kLocStride;
+  float Lr[13];
+#pragma unroll
+  for (int k = 0; k < 13; ++k) Lr[k] = __ldg(Lf + k);
+  const BccF b = bcc_rel_f(m, t, Lr, x, y, z);
+  const Split sp = split_of_f(b);
+  float g[3];
+  gamma_of_f(Lr, b, sp, g);
+  const int* id = kSplitOrd[sp.lo][sp.hi];
+  const double* rec = coeffs + (int64_t)t * kCoeffStride1;
+  float o[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) o[k] = (float)__ldg(rec + id[k]);
+  const float V = g[0], E = g[1], C = g[2];
+  return (double)(V * V * o[0] + E * E * o[1] + C * C * o[2] + 2 * V * E * o[3] + 2 * E * C * o[4] +
+                  2 * V * C * o[5]);
 }
 
 inline int grid_for(int64_t n, int block) {

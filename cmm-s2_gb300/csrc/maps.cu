@@ -384,13 +384,17 @@ int launch_compose(const MeshView& m, const double* const* coeffs, int S, const 
 
 int make_asm_f32(cmm_mesh* mesh) {
   const int64_t n = (int64_t)kAsmFactors * mesh->view.nt;
+  const int64_t nl = (int64_t)kLocStride * mesh->view.nt;
   int rc = mesh->tri_asm_f.alloc(n * sizeof(float));
-  if (rc) return rc;
+  if (rc || (rc = mesh->tri_loc_f.alloc(nl * sizeof(float)))) return rc;
   to_f32_kernel<<<(int)((n + 255) / 256), 256>>>(mesh->view.tri_asm, n, (float*)mesh->tri_asm_f.p);
+  if ((rc = check_launch("to_f32_kernel"))) return rc;
+  to_f32_kernel<<<(int)((nl + 255) / 256), 256>>>(mesh->view.tri_loc, nl, (float*)mesh->tri_loc_f.p);
   if ((rc = check_launch("to_f32_kernel"))) return rc;
   cudaError_t e = cudaDeviceSynchronize();
   if (e != cudaSuccess) return cuda_fail(e, "make_asm_f32");
   mesh->view.tri_asm_f = (const float*)mesh->tri_asm_f.p;
+  mesh->view.tri_loc_f = (const float*)mesh->tri_loc_f.p;
   return CMM_OK;
 }
 

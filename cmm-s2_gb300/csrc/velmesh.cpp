@@ -114,6 +114,10 @@ int build_latlon(int L, const double* theta, const double* phi, const double* gr
   // spacing as the reference computes it (mesh_functions.py:214-215)
   v.dphi = std::fabs(phi[1] - phi[0]);
   v.dthe = std::fabs(theta[1] - theta[0]);
+  v.phi0_f = (float)phi[0];
+  v.dphi_f = (float)v.dphi;
+  v.the0_f = (float)theta[0];
+  v.dthe_f = (float)v.dthe;
   return CMM_OK;
 }
 

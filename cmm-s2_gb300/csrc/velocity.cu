@@ -43,14 +43,17 @@ __device__ __forceinline__ void velocity_at(const MeshView& m, const VelPtrs& vc
                                             const W3 w, double x, double y, double z,
                                             double* V) {
   const int t = latlon_locate(m, x, y, z);
-  double Lr[13];
-  load_loc(m, t, Lr);
-  const Bcc b = bcc_of(Lr, x, y, z);
-  const Split sp = split_of(b);
-  const Gam g = gamma_of(Lr, b, sp);
   V[0] = V[1] = V[2] = 0.0;
-  if (m.rec32) {  // FP32 records: patches and time combination in FP32
-    const float gV = (float)g.V, gE = (float)g.E, gC = (float)g.C;
+  if (m.rec32) {  // FP32 records: barycentrics, patches and time combination in FP32
+    const float* Lf = m.tri_loc_f + (int64_t)t * kLocStride;
+    float Lr[13];
+#pragma unroll
+    for (int k = 0; k < 13; ++k) Lr[k] = __ldg(Lf + k);
+    const BccF b = bcc_rel_f(m, t, Lr, x, y, z);
+    const Split sp = split_of_f(b);
+    float gg[3];
+    gamma_of_f(Lr, b, sp, gg);
+    const float gV = gg[0], gE = gg[1], gC = gg[2];
     float Vf[3] = {0.f, 0.f, 0.f};
 #pragma unroll
     for (int l = 0; l < 3; ++l) {
@@ -69,6 +72,11 @@ __device__ __forceinline__ void velocity_at(const MeshView& m, const VelPtrs& vc
     V[2] = Vf[2];
     return;
   }
+  double Lr[13];
+  load_loc(m, t, Lr);
+  const Bcc b = bcc_of(Lr, x, y, z);
+  const Split sp = split_of(b);
+  const Gam g = gamma_of(Lr, b, sp);
 #pragma unroll
   for (int l = 0; l < 3; ++l) {
     if (l >= nvs) break;

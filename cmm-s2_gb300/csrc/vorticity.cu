@@ -138,7 +138,8 @@ __global__ void __launch_bounds__(256) vorticity_kernel(VortParams vp, const dou
       sh_series_n<1>(vm, sh, lmax, sh_point(x, y, z), &v);
       w += v;
     }
-    if (spline) w += latlon_scalar(vm, spline, x, y, z);
+    if (spline) w += (vm.field32 && vm.tri_loc_f) ? latlon_scalar_f(vm, spline, x, y, z)
+                                                  : latlon_scalar(vm, spline, x, y, z);
     const double r = w + 2 * rot * ct - 2 * rot * cos_ring[i / npr];
     if (!isfinite(r)) atomicOr(vm.status, CMM_FLAG_NONFINITE);
     omega[i] = r;
