@@ -187,6 +187,18 @@ def bind_to_gpu_numa_node(index):
     return None
 
 
+def max_over_ranks(ms, device=None):
+    """The slowest rank's time (the job's time): all-reduce MAX over the
+    process group (NCCL on the GPUs, gloo in the CPU tests); ms alone
+    without a group."""
+    import torch
+    if not (torch.distributed.is_available() and torch.distributed.is_initialized()):
+        return ms
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
 def bench_gpu(args, rank, world):
     import torch
     from cmm_gpu import native
@@ -242,11 +254,7 @@ def bench_gpu(args, rank, world):
         torch.cuda.synchronize()
         barrier()
     launches = native.lib.cmm_launch_count() - n0
-    ms = e0.elapsed_time(e1) / args.steps
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, dev)
     value = world * Q * SUBMAPS / (ms / 1e3)
 
     # end to end through the host-buffer API
@@ -266,11 +274,7 @@ def bench_gpu(args, rank, world):
     e1.record(stream)
     torch.cuda.synchronize()
     barrier()
-    ms_e2e = e0.elapsed_time(e1) / args.steps
-    if world > 1:
-        t = torch.tensor([ms_e2e], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_e2e = float(t.item())
+    ms_e2e = max_over_ranks(e0.elapsed_time(e1) / args.steps, dev)
     assert mesh.status() == 0
     del scratch
 
