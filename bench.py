@@ -45,6 +45,10 @@ METRIC = "map evals/s"
 # capture of 2^22 queries summarised in profiles/compose_level7.md
 # (18.348 GB + 0.420 GB); the gathers scale with the number of queries.
 COMPOSE_TRAFFIC_PER_QUERY = (18.348423e9 + 0.420334e9) / (1 << 22)
+# The same with the queries grouped by coarse cell (cmm_query_order), from
+# the capture of 2^22 queries in profiles/compose_level7.md (2.856 GB read
+# + 0.719 GB written: the output rows are now scattered).
+COMPOSE_TRAFFIC_PER_QUERY_ORDERED = (2.856423424e9 + 0.719421696e9) / (1 << 22)
 # FP64 instructions per map evaluation (query x submap) with Jacobians,
 # from the same capture (FP64 pipe 88.6 % busy for 9.599 ms).
 FP64_INSTR_PER_EVAL = 152
@@ -216,11 +220,27 @@ def bench_gpu(args, rank, world):
     jac = torch.empty((Q, 3, 3), dtype=torch.float64, device=dev)
     arr = (native.ctypes.c_void_p * SUBMAPS)(*[c.data_ptr() for c in cs])
     stream = torch.cuda.current_stream(dev)
+    perm = torch.empty(Q, dtype=torch.int32, device=dev)
+    work = torch.empty(native.lib.cmm_query_order_workspace(Q), dtype=torch.int32, device=dev)
+    st = native.ctypes.c_void_p(stream.cuda_stream)
 
-    def step():
-        native.check(native.lib.cmm_compose(mesh.h, arr, SUBMAPS, native._ptr(q), Q, native._ptr(out),
-                                            native._ptr(tri), None, native._ptr(jac),
-                                            native.ctypes.c_void_p(stream.cuda_stream)), "cmm_compose")
+    def step(mark=None, ordered=False):
+        # caller order, or (ordered) the queries grouped by coarse cell
+        # inside the step, then the composition in that order; `mark`
+        # records an event before the composition
+        if not ordered:
+            if mark is not None:
+                mark.record(stream)
+            native.check(native.lib.cmm_compose(mesh.h, arr, SUBMAPS, native._ptr(q), Q, native._ptr(out),
+                                                native._ptr(tri), None, native._ptr(jac), st), "cmm_compose")
+            return
+        native.check(native.lib.cmm_query_order(mesh.h, native._ptr(q), Q, native._ptr(perm),
+                                                native._ptr(work), st), "cmm_query_order")
+        if mark is not None:
+            mark.record(stream)
+        native.check(native.lib.cmm_compose_ordered(mesh.h, arr, SUBMAPS, native._ptr(q), Q, native._ptr(perm),
+                                                    native._ptr(out), native._ptr(tri), None, native._ptr(jac),
+                                                    st), "cmm_compose_ordered")
 
     def barrier():
         if world > 1:
@@ -244,17 +264,61 @@ def bench_gpu(args, rank, world):
     assert mesh.status() == 0
     n0 = native.lib.cmm_launch_count()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    marks = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+             for _ in range(args.steps)]
     with ClockSampler(dev.index) as clk:
         barrier()
         torch.cuda.synchronize()
         e0.record(stream)
-        for _ in range(args.steps):
-            step()
+        for k in range(args.steps):
+            step(marks[k][0])
+            marks[k][1].record(stream)
         e1.record(stream)
         torch.cuda.synchronize()
         barrier()
     launches = native.lib.cmm_launch_count() - n0
     ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, dev)
+    # the composition kernel alone (the roofline's kernel)
+    ms_compose = sum(a.elapsed_time(b) for a, b in marks) / args.steps
+    # the same step with the queries grouped by coarse cell first
+    # (cmm_query_order + cmm_compose_ordered): a fifth of the DRAM traffic,
+    # reported beside the headline
+    for _ in range(2):
+        step(ordered=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for k in range(args.steps):
+        step(marks[k][0], ordered=True)
+        marks[k][1].record(stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ordered = {"ms_per_step": e0.elapsed_time(e1) / args.steps,
+               "compose_ms": sum(a.elapsed_time(b) for a, b in marks) / args.steps,
+               "traffic_per_launch": COMPOSE_TRAFFIC_PER_QUERY_ORDERED * Q}
+    # points only (no ids, no Jacobians): gather-bound, where the
+    # coarse-cell order pays
+    values = {}
+    for name, ordr in (("caller_order", False), ("cell_order", True)):
+        def vstep():
+            if ordr:
+                native.check(native.lib.cmm_query_order(mesh.h, native._ptr(q), Q, native._ptr(perm),
+                                                        native._ptr(work), st), "cmm_query_order")
+                native.check(native.lib.cmm_compose_ordered(mesh.h, arr, SUBMAPS, native._ptr(q), Q,
+                                                            native._ptr(perm), native._ptr(out), None, None,
+                                                            None, st), "cmm_compose_ordered")
+            else:
+                native.check(native.lib.cmm_compose(mesh.h, arr, SUBMAPS, native._ptr(q), Q, native._ptr(out),
+                                                    None, None, None, st), "cmm_compose")
+        for _ in range(3):
+            vstep()
+        e0.record(stream)
+        for _ in range(args.steps):
+            vstep()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        vms = e0.elapsed_time(e1) / args.steps
+        values[name] = {"ms_per_step": vms, "map_evals_per_s": Q * SUBMAPS / (vms / 1e3)}
+    assert mesh.status() == 0
     value = world * Q * SUBMAPS / (ms / 1e3)
 
     # end to end through the host-buffer API
@@ -264,13 +328,14 @@ def bench_gpu(args, rank, world):
     jh = torch.empty((Q, 3, 3), dtype=torch.float64).pin_memory()
     del out, jac, tri
     torch.cuda.empty_cache()
-    scratch, streams = native.compose_host(mesh, cs, qh, oh, th, jh)
+    scratch, streams = native.compose_host(mesh, cs, qh, oh, th, jh, order=False)
     torch.cuda.synchronize()
     barrier()
     t0 = time.perf_counter()
     e0.record(stream)
     for _ in range(args.steps):
-        scratch, streams = native.compose_host(mesh, cs, qh, oh, th, jh, scratch=scratch, streams=streams)
+        scratch, streams = native.compose_host(mesh, cs, qh, oh, th, jh, scratch=scratch, streams=streams,
+                                               order=False)
     e1.record(stream)
     torch.cuda.synchronize()
     barrier()
@@ -278,7 +343,7 @@ def bench_gpu(args, rank, world):
     assert mesh.status() == 0
     del scratch
 
-    res = dict(ms=ms, value=value, ms_e2e=ms_e2e, launches=launches, clocks=clk.summary(), numa_cores=numa_cores,
+    res = dict(ms=ms, ms_compose=ms_compose, ordered=ordered, values_only=values, value=value, ms_e2e=ms_e2e, launches=launches, clocks=clk.summary(), numa_cores=numa_cores,
                nv=len(verts), nt=len(tris), Q=Q, fp64_fma_per_s=fp64_fma_per_s)
     if rank == 0 and not args.no_bve:
         try:
@@ -286,7 +351,8 @@ def bench_gpu(args, rank, world):
             res["rh_error"] = bench_rh_error(dev)
         except Exception as exc:  # reported, the headline stands on its own
             res["bve"] = {"error": f"{type(exc).__name__}: {exc}"}
-    if rank == 0 and not (args.no_bve3 and args.no_kernels and args.no_ensemble and args.no_adjoint):
+    if rank == 0 and not (args.no_bve3 and args.no_kernels and args.no_ensemble and args.no_adjoint and
+                          args.no_transport):
         del q, mesh, cs
         torch.cuda.empty_cache()
     if rank == 0 and not args.no_kernels:
@@ -306,6 +372,12 @@ def bench_gpu(args, rank, world):
             res["adjoint"] = bench_adjoint(args, dev)
         except Exception as exc:
             res["adjoint"] = {"error": f"{type(exc).__name__}: {exc}"}
+        torch.cuda.empty_cache()
+    if rank == 0 and not args.no_transport:
+        try:
+            res["transport"] = bench_transport(args, dev)
+        except Exception as exc:
+            res["transport"] = {"error": f"{type(exc).__name__}: {exc}"}
         torch.cuda.empty_cache()
     if rank == 0 and not args.no_bve3:
         try:
@@ -452,6 +524,38 @@ def bench_ensemble(args, dev):
             "device_memory_gb": torch.cuda.max_memory_allocated(dev) / 1e9, "setup_s": setup,
             "schedule": tuner.log["schedule"]["best"], "launch_shapes": tuner.log["kernels"],
             "status_ok": ok}
+
+
+def bench_transport(args, dev):
+    """Linear transport (the loop of the reference's spherical transport
+    test) at level 7: u_deform_rot over T = 1 in 100 RK4 steps, remap every
+    10; steps/s of the map update after 3 warm-up steps, and the error of
+    the smooth test tracer through the 10 composed submaps at 2^20 random
+    points (the flow returns every particle at T)."""
+    import torch
+    from cmm_gpu import dynamical_fields as F
+    from cmm_gpu.spherical_transport import TransportSolver
+    s = TransportSolver(7, F.u_deform_rot, T=1.0, Nt=100, remapping=True, n_maps=10, device=dev.index)
+    s.run(3)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    n = s.Nt - s.count
+    e0.record()
+    s.run()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / n
+    from cmm_gpu.meshgen import random_sphere_points
+    q = torch.from_numpy(random_sphere_points(1 << 20, seed=77)).to(dev)
+    e0.record()
+    err = s.error(q)
+    e1.record()
+    torch.cuda.synchronize()
+    assert s.mesh.native.status() == 0
+    return {"workload": "level-7 mesh, u_deform_rot, T = 1, 100 RK4 steps, remap every 10",
+            "ms_per_step": ms, "steps_per_s": 1e3 / ms, "submaps": len(s.maps()),
+            "tracer_linf_error": err, "error_eval_ms": e0.elapsed_time(e1),
+            "error_points": 1 << 20}
 
 
 def bench_adjoint(args, dev):
@@ -649,6 +753,8 @@ def main():
     ap.add_argument("--ens-members", type=int, default=64)
     ap.add_argument("--ensemble-only", action="store_true", help="print only the ensemble run")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint run")
+    ap.add_argument("--no-transport", action="store_true", help="skip the linear-transport run")
+    ap.add_argument("--transport-only", action="store_true", help="print only the linear-transport run")
     ap.add_argument("--adjoint-fd", type=int, default=2,
                     help="coefficients checked by centred differences in the adjoint run")
     ap.add_argument("--adjoint-only", action="store_true", help="print only the adjoint run")
@@ -668,7 +774,8 @@ def main():
                        "FP64 points, int32 triangle ids, FP64 Jacobians",
            "level": LEVEL, "submaps": SUBMAPS, "queries_per_gpu": 1 << LOGQ,
            "l2": "inputs and outputs larger than L2 (queries 402 MB, Jacobians 1.2 GB), no flush",
-           "parallelism": f"replicas x{args.gpus} (independent queries per GPU)"}
+           "parallelism": f"replicas x{args.gpus} (independent queries per GPU)",
+           "query_order": "caller order (the coarse-cell order is reported under roofline.ordered)"}
 
     if args.impl == "reference":
         if rank != 0:
@@ -694,6 +801,11 @@ def main():
         dev = torch.device("cuda", 0)
         torch.cuda.set_device(dev)
         print(json.dumps({"adjoint": bench_adjoint(args, dev)}))
+        return
+    if args.transport_only:
+        dev = torch.device("cuda", 0)
+        torch.cuda.set_device(dev)
+        print(json.dumps({"transport": bench_transport(args, dev)}))
         return
     if args.ensemble_only:
         dev = torch.device("cuda", 0)
@@ -723,7 +835,8 @@ def main():
         return
     peak, how = peaks()
     algo = algorithmic_bytes(r["Q"], SUBMAPS, r["nv"], r["nt"])
-    achieved = algo / (r["ms"] / 1e3) / 1e9
+    achieved = algo / (r["ms_compose"] / 1e3) / 1e9
+    kernel_rate = r["Q"] * SUBMAPS / (r["ms_compose"] / 1e3)   # one GPU, composition kernel alone
     Q = r["Q"]
     line = {
         "metric": METRIC, "value": r["value"], "unit": "map evals/s", "n_gpus": world,
@@ -731,12 +844,13 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": how,
-                     "traffic": COMPOSE_TRAFFIC_PER_QUERY * Q, "algorithmic_bytes": algo},
+                     "traffic": COMPOSE_TRAFFIC_PER_QUERY * Q, "algorithmic_bytes": algo,
+                     "kernel": "compose_kernel", "kernel_ms": r["ms_compose"], "ordered": r["ordered"]},
         "fp64": {"bound": "fp64 pipe (binding on GB300)",
                  "instr_per_eval": FP64_INSTR_PER_EVAL,
-                 "achieved_tinstr_s": FP64_INSTR_PER_EVAL * r["value"] / world / 1e12,
+                 "achieved_tinstr_s": FP64_INSTR_PER_EVAL * kernel_rate / 1e12,
                  "peak_tinstr_s": r["fp64_fma_per_s"] / 1e12,
-                 "frac": FP64_INSTR_PER_EVAL * r["value"] / world / r["fp64_fma_per_s"],
+                 "frac": FP64_INSTR_PER_EVAL * kernel_rate / r["fp64_fma_per_s"],
                  "peak_kind": "measured (FMA-chain probe in this run)"},
         "cpu_baseline": cpu,
         "e2e": {"value": world * Q * SUBMAPS / (r["ms_e2e"] / 1e3), "unit": "map evals/s",
@@ -744,7 +858,8 @@ def main():
                 "host_cores_bound": r["numa_cores"]},
         "clocks": r["clocks"], "gpu_launches": r["launches"],
     }
-    for key in ("bve", "rh_error", "bve_l7_L1024", "kernels", "ensemble", "adjoint"):
+    line["points_only"] = r["values_only"]
+    for key in ("bve", "rh_error", "bve_l7_L1024", "kernels", "ensemble", "adjoint", "transport"):
         if key in r:
             line[key] = r[key]
     print(json.dumps(line))

@@ -47,6 +47,13 @@ _SIGS = {
     "cmm_locate": (_i, [_p, _p, _i64, _p, _p, _p]),
     "cmm_assemble": (_i, [_p, _p, _i, _p, _p]),
     "cmm_compose": (_i, [_p, ctypes.POINTER(_p), _i, _p, _i64, _p, _p, _p, _p, _p]),
+    "cmm_flow_velocity": (_i, [_p, _i, _d, _d, _d, _p, _i64, _p, _p]),
+    "cmm_flow_integrate": (_i, [_p, _i, _d, _d, _i, _d, _d, _p, _i64, _p, _p]),
+    "cmm_flow_advect_project": (_i, [_p, _i, _d, _d, _i, _d, _d, _p, _p, _p, _d, _p, _p, _p]),
+    "cmm_tracer_eval": (_i, [_p, _i, _d, _p, _i64, _p, _p]),
+    "cmm_query_order_workspace": (_i64, [_i64]),
+    "cmm_query_order": (_i, [_p, _p, _i64, _p, _p, _p]),
+    "cmm_compose_ordered": (_i, [_p, ctypes.POINTER(_p), _i, _p, _i64, _p, _p, _p, _p, _p, _p]),
     "cmm_stencil_eval": (_i, [_p, _p, _p, _p, _i64, _p, _p]),
     "cmm_velmesh_create": (_i, [_i, _p, _p, _p, _p, ctypes.POINTER(_p)]),
     "cmm_velocity_eval": (_i, [_p, ctypes.POINTER(_p), _i, _d, _d, _d, _p, _i64, _p, _p]),
@@ -191,8 +198,22 @@ class Mesh:
               "cmm_assemble")
         return out
 
-    def compose(self, coeffs, q, want_tri=False, want_tri_all=False, want_jac=False, out=None):
-        """coeffs: list of coefficient tensors, submap 0 first (applied last)."""
+    def query_order(self, q, work=None):
+        """Permutation grouping the queries by coarse hierarchy cell."""
+        q = _dev(q)
+        n = q.shape[0]
+        perm = torch.empty(n, dtype=torch.int32, device=q.device)
+        need = lib.cmm_query_order_workspace(n)
+        if work is None or work.numel() < need:
+            work = torch.empty(need, dtype=torch.int32, device=q.device)
+        check(lib.cmm_query_order(self.h, _ptr(q), n, _ptr(perm), _ptr(work), _stream(q.device)),
+              "cmm_query_order")
+        return perm
+
+    def compose(self, coeffs, q, want_tri=False, want_tri_all=False, want_jac=False, out=None,
+                perm=None):
+        """coeffs: list of coefficient tensors, submap 0 first (applied last).
+        perm: optional processing order (query_order), same results."""
         q = _dev(q)
         n = q.shape[0]
         S = len(coeffs)
@@ -201,8 +222,13 @@ class Mesh:
         tri = torch.empty(n, dtype=torch.int32, device=q.device) if want_tri else None
         tri_all = torch.empty((S, n), dtype=torch.int32, device=q.device) if want_tri_all else None
         jac = torch.empty((n, 3, 3), dtype=torch.float64, device=q.device) if want_jac else None
-        check(lib.cmm_compose(self.h, arr, S, _ptr(q), n, _ptr(out), _ptr(tri), _ptr(tri_all),
-                              _ptr(jac), _stream(q.device)), "cmm_compose")
+        if perm is None:
+            check(lib.cmm_compose(self.h, arr, S, _ptr(q), n, _ptr(out), _ptr(tri), _ptr(tri_all),
+                                  _ptr(jac), _stream(q.device)), "cmm_compose")
+        else:
+            check(lib.cmm_compose_ordered(self.h, arr, S, _ptr(q), n, _ptr(perm), _ptr(out), _ptr(tri),
+                                          _ptr(tri_all), _ptr(jac), _stream(q.device)),
+                  "cmm_compose_ordered")
         return out, tri, tri_all, jac
 
     def stencil_eval(self, coeffs, yn, st):
@@ -228,8 +254,51 @@ class Mesh:
                                      _ptr(work), _stream(s_pts.device)), "cmm_advect_project")
         return jets, work
 
+    # ---------------------------------------------------- linear transport
+    def flow_velocity(self, flow, t, x, T=1.0, alpha=0.0):
+        """Analytic flow velocity at x (3,n) -> (3,n)."""
+        x = _dev(x)
+        out = torch.empty_like(x)
+        check(lib.cmm_flow_velocity(self.h, flow, T, alpha, t, _ptr(x), x.shape[1], _ptr(out),
+                                    _stream(x.device)), "cmm_flow_velocity")
+        return out
 
-EULER, IMPROVED_EULER, RK4 = 0, 1, 2
+    def flow_integrate(self, flow, scheme, t, dt, x, T=1.0, alpha=0.0):
+        """Backward foot points of x (3,n) under an analytic flow."""
+        x = _dev(x)
+        out = torch.empty_like(x)
+        check(lib.cmm_flow_integrate(self.h, flow, T, alpha, scheme, t, dt, _ptr(x), x.shape[1], _ptr(out),
+                                     _stream(x.device)), "cmm_flow_integrate")
+        return out
+
+    def flow_advect_project(self, flow, scheme, t, dt, s_pts, tan, prev_coeffs, T=1.0, alpha=0.0,
+                            eps=1e-5, jets=None, work=None):
+        """One CMM map update under an analytic flow; returns (jets, work)."""
+        s_pts, tan = _dev(s_pts), _dev(tan)
+        if jets is None:
+            jets = torch.empty((3, 4, self.nv), dtype=torch.float64, device=s_pts.device)
+        if work is None:
+            work = torch.empty(lib.cmm_advect_workspace(self.h), dtype=torch.float64, device=s_pts.device)
+        check(lib.cmm_flow_advect_project(self.h, flow, T, alpha, scheme, t, dt, _ptr(s_pts), _ptr(tan),
+                                          _ptr(prev_coeffs), eps, _ptr(jets), _ptr(work),
+                                          _stream(s_pts.device)), "cmm_flow_advect_project")
+        return jets, work
+
+    def tracer(self, kind, X, t=0.0, out=None):
+        """Tracer field at points X (n,3) -> (n,)."""
+        X = _dev(X)
+        n = X.shape[0]
+        out = torch.empty(n, dtype=torch.float64, device=X.device) if out is None else out
+        check(lib.cmm_tracer_eval(self.h, kind, t, _ptr(X), n, _ptr(out), _stream(X.device)),
+              "cmm_tracer_eval")
+        return out
+
+
+EULER, IMPROVED_EULER, RK4, RK2 = 0, 1, 2, 3
+(FLOW_SOLID_BODY, FLOW_DEFORM, FLOW_DEFORM_ROT, FLOW_STATIC_VORTEX, FLOW_ROTATING_VORTEX,
+ FLOW_EQUATOR_VORTEX, FLOW_DIVERGENT) = range(7)
+(TRACER_COSINE_BELL, TRACER_SLOTTED_CYLINDERS, TRACER_STATIC_VORTEX, TRACER_ROTATING_VORTEX,
+ TRACER_SMOOTH_TEST) = range(5)
 (VORT_NONE, VORT_ROSSBY_HAURWITZ, VORT_ZONAL_JET, VORT_PERTURBED_JET, VORT_MULTI_JET,
  VORT_GAUSSIAN_VORTEX, VORT_GAUSSIAN_JETS) = range(7)
 
@@ -379,11 +448,16 @@ class Sht:
 
 
 def compose_host(mesh, coeffs, q_host, out_host, tri_host=None, jac_host=None, chunks=8,
-                 streams=None, scratch=None):
+                 streams=None, scratch=None, order=None):
     """Composition of host-resident queries (pinned (n,3) float64) into
     host-resident outputs, pipelined in `chunks` pieces over two CUDA
-    streams so the host<->device copies overlap the kernels.  Returns the
-    scratch dict for reuse."""
+    streams so the host<->device copies overlap the kernels.  order: each
+    chunk is processed grouped by coarse cell (cmm_query_order, same
+    results); by default only without Jacobians, where the gathers rather
+    than the FP64 pipe bound the kernel.  Returns the scratch dict for
+    reuse."""
+    if order is None:
+        order = jac_host is None
     n = q_host.shape[0]
     dev = mesh.device
     streams = streams or [torch.cuda.Stream(dev), torch.cuda.Stream(dev)]
@@ -395,7 +469,9 @@ def compose_host(mesh, coeffs, q_host, out_host, tri_host=None, jac_host=None, c
                 q=torch.empty((step, 3), dtype=torch.float64, device=dev),
                 out=torch.empty((step, 3), dtype=torch.float64, device=dev),
                 tri=torch.empty(step, dtype=torch.int32, device=dev) if tri_host is not None else None,
-                jac=torch.empty((step, 3, 3), dtype=torch.float64, device=dev) if jac_host is not None else None)
+                jac=torch.empty((step, 3, 3), dtype=torch.float64, device=dev) if jac_host is not None else None,
+                perm=torch.empty(step, dtype=torch.int32, device=dev),
+                work=torch.empty(lib.cmm_query_order_workspace(step), dtype=torch.int32, device=dev))
     arr = (ctypes.c_void_p * len(coeffs))(*[c.data_ptr() for c in coeffs])
     cur = torch.cuda.current_stream(dev)
     for s in streams:
@@ -409,9 +485,16 @@ def compose_host(mesh, coeffs, q_host, out_host, tri_host=None, jac_host=None, c
         m = hi - lo
         with torch.cuda.stream(s):
             b["q"][:m].copy_(q_host[lo:hi], non_blocking=True)
-            check(lib.cmm_compose(mesh.h, arr, len(coeffs), _ptr(b["q"]), m, _ptr(b["out"]),
-                                  _ptr(b["tri"]), None, _ptr(b["jac"]), ctypes.c_void_p(s.cuda_stream)),
-                  "cmm_compose")
+            st = ctypes.c_void_p(s.cuda_stream)
+            if order:
+                check(lib.cmm_query_order(mesh.h, _ptr(b["q"]), m, _ptr(b["perm"]), _ptr(b["work"]), st),
+                      "cmm_query_order")
+                check(lib.cmm_compose_ordered(mesh.h, arr, len(coeffs), _ptr(b["q"]), m, _ptr(b["perm"]),
+                                              _ptr(b["out"]), _ptr(b["tri"]), None, _ptr(b["jac"]), st),
+                      "cmm_compose_ordered")
+            else:
+                check(lib.cmm_compose(mesh.h, arr, len(coeffs), _ptr(b["q"]), m, _ptr(b["out"]),
+                                      _ptr(b["tri"]), None, _ptr(b["jac"]), st), "cmm_compose")
             out_host[lo:hi].copy_(b["out"][:m], non_blocking=True)
             if tri_host is not None:
                 tri_host[lo:hi].copy_(b["tri"][:m], non_blocking=True)

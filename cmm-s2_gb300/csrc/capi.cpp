@@ -123,25 +123,10 @@ int vel_args(const cmm_mesh* vm, const double* const* vc, int nvs, VelPtrs* out,
 }
 
 int stage_weights(int nvs, double ts0, int scheme, double t, double dt, TimeWeights* tw) {
-  // stage times of each integrator (cmm_s2/core/evolution_functions.py:19-67)
+  // stage times of each integrator (cmm_s2/core/evolution_functions.py:19-80)
   double times[4];
-  int nt;
-  if (scheme == CMM_EULER) {
-    times[0] = t;
-    nt = 1;
-  } else if (scheme == CMM_IMPROVED_EULER) {
-    times[0] = t;
-    times[1] = t + dt;
-    nt = 2;
-  } else if (scheme == CMM_RK4) {
-    times[0] = t + dt;
-    times[1] = t + dt / 2;
-    times[2] = t + 0.5 * dt;
-    times[3] = t;
-    nt = 4;
-  } else {
-    return arg_error("unknown integration scheme");
-  }
+  const int nt = stage_times(scheme, t, dt, times);
+  if (nt == 0) return arg_error("unknown integration scheme");
   *tw = time_weights(nvs, ts0, dt, times, nt);
   return CMM_OK;
 }
@@ -281,6 +266,8 @@ int cmm_advect_project_bwd(const cmm_mesh* mesh, const cmm_mesh* velmesh, const 
   int rc = vel_args(velmesh, vel_coeffs, nvs, &vc, "cmm_advect_project_bwd");
   if (rc) return rc;
   if (velmesh->view.rec32) return arg_error("cmm_advect_project_bwd: FP64 velocity records expected");
+  if (scheme != CMM_EULER && scheme != CMM_IMPROVED_EULER && scheme != CMM_RK4)
+    return arg_error("cmm_advect_project_bwd: scheme 0, 1 or 2 expected");
   if (!s_pts || !tan || !grad_jets || !grad_vel || !work) return arg_error("cmm_advect_project_bwd: null pointer");
   for (int l = 0; l < nvs; ++l)
     if (!grad_vel[l]) return arg_error("cmm_advect_project_bwd: null velocity cotangent");
@@ -388,6 +375,57 @@ int cmm_compose(const cmm_mesh* mesh, const double* const* coeffs, int S, const 
     if (!coeffs[k]) return arg_error("cmm_compose: null coefficient pointer");
   return launch_compose(mesh->view, coeffs, S, q, n, out, tri, tri_all, jac,
                         (cudaStream_t)stream);
+}
+
+int cmm_flow_velocity(const cmm_mesh* mesh, int flow, double T, double alpha, double t, const double* x,
+                      int64_t n, double* out, void* stream) {
+  if (!mesh || n < 0 || (n > 0 && (!x || !out))) return arg_error("cmm_flow_velocity: bad argument");
+  return flow_velocity(mesh->view, flow, T, alpha, t, x, n, out, (cudaStream_t)stream);
+}
+
+int cmm_flow_integrate(const cmm_mesh* mesh, int flow, double T, double alpha, int scheme, double t,
+                       double dt, const double* x, int64_t n, double* out, void* stream) {
+  if (!mesh || n < 0 || (n > 0 && (!x || !out))) return arg_error("cmm_flow_integrate: bad argument");
+  return flow_integrate(mesh->view, flow, T, alpha, scheme, t, dt, x, n, out, (cudaStream_t)stream);
+}
+
+int cmm_flow_advect_project(const cmm_mesh* mesh, int flow, double T, double alpha, int scheme, double t,
+                            double dt, const double* s_pts, const double* tan, const double* prev_coeffs,
+                            double eps, double* jets, double* work, void* stream) {
+  if (!mesh || mesh->view.kind != kIcosahedral) return arg_error("cmm_flow_advect_project: map mesh expected");
+  if (!s_pts || !tan || !jets || !work) return arg_error("cmm_flow_advect_project: null pointer");
+  cudaStream_t s = (cudaStream_t)stream;
+  int rc = flow_advect_points(mesh->view, flow, T, alpha, scheme, t, dt, s_pts, work, s);
+  if (rc) return rc;
+  const int64_t nv = mesh->view.nv;
+  return launch_project_jets(mesh->view, prev_coeffs, work, work + 3 * nv, tan, eps, jets, s);
+}
+
+int cmm_tracer_eval(const cmm_mesh* mesh, int tracer, double t, const double* X, int64_t n, double* out,
+                    void* stream) {
+  if (!mesh || n < 0 || (n > 0 && (!X || !out))) return arg_error("cmm_tracer_eval: bad argument");
+  return launch_tracer(mesh->view, tracer, t, X, n, out, (cudaStream_t)stream);
+}
+
+int64_t cmm_query_order_workspace(int64_t n) { return n < 0 ? -1 : order_workspace(n); }
+
+int cmm_query_order(const cmm_mesh* mesh, const double* q, int64_t n, int32_t* perm,
+                    int32_t* work, void* stream) {
+  if (!mesh || n < 0 || n > INT32_MAX || (n > 0 && (!q || !perm || !work)))
+    return arg_error("cmm_query_order: bad argument");
+  return launch_query_order(mesh->view, q, n, perm, work, (cudaStream_t)stream);
+}
+
+int cmm_compose_ordered(const cmm_mesh* mesh, const double* const* coeffs, int S, const double* q,
+                        int64_t n, const int32_t* perm, double* out, int32_t* tri,
+                        int32_t* tri_all, double* jac, void* stream) {
+  if (!mesh || S < 1 || S > CMM_MAX_SUBMAPS || !coeffs || n < 0 || n > INT32_MAX ||
+      (n > 0 && (!q || !out || !perm)))
+    return arg_error("cmm_compose_ordered: bad argument");
+  for (int k = 0; k < S; ++k)
+    if (!coeffs[k]) return arg_error("cmm_compose_ordered: null coefficient pointer");
+  return launch_compose(mesh->view, coeffs, S, q, n, out, tri, tri_all, jac,
+                        (cudaStream_t)stream, perm);
 }
 
 int cmm_stencil_eval(const cmm_mesh* mesh, const double* coeffs, const double* yn,

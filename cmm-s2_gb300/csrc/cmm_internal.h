@@ -105,7 +105,12 @@ int launch_assemble(const MeshView& m, const double* jets, int ncomp, double* co
                     cudaStream_t s, const BveState* st = nullptr);
 int launch_compose(const MeshView& m, const double* const* coeffs, int S, const double* q,
                    int64_t n, double* out, int32_t* tri, int32_t* tri_all, double* jac,
-                   cudaStream_t s);
+                   cudaStream_t s, const int32_t* perm = nullptr);
+// Query order by coarse cell (cmm_query_order): perm (n) and work
+// (order_workspace(n) int32).
+int64_t order_workspace(int64_t n);
+int launch_query_order(const MeshView& m, const double* q, int64_t n, int32_t* perm, int32_t* work,
+                       cudaStream_t s);
 // Composition through the st->nc submaps of the device table `table`
 // (submap 0 first) followed by `last` (applied first), no Jacobian.
 int launch_compose_dev(const MeshView& m, const double* const* table, const BveState* st,
@@ -138,6 +143,19 @@ struct VelPtrs {
   const double* p[3];
 };
 TimeWeights time_weights(int nvs, double ts0, double dt, const double* times, int ntimes);
+// Evaluation times of an integrator's stages (transport.cu); 0 = unknown.
+int stage_times(int scheme, double t, double dt, double* times);
+
+// Analytic transport flows and tracers (transport.cu); m is the map mesh
+// (status word only for the point kernels).
+int flow_velocity(const MeshView& m, int kind, double T, double alpha, double t, const double* x, int64_t n,
+                  double* out, cudaStream_t s);
+int flow_integrate(const MeshView& m, int kind, double T, double alpha, int scheme, double t, double dt,
+                   const double* x, int64_t n, double* out, cudaStream_t s);
+int flow_advect_points(const MeshView& mesh, int kind, double T, double alpha, int scheme, double t, double dt,
+                       const double* s_pts, double* work, cudaStream_t s);
+int launch_tracer(const MeshView& m, int kind, double t, const double* X, int64_t n, double* out,
+                  cudaStream_t s);
 
 // Device-resident state of a device-driven barotropic step (stepper.cu):
 // read by the kernels of a step in place of their host arguments, so one

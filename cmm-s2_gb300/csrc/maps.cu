@@ -227,16 +227,21 @@ __global__ void to_f32_kernel(const double* __restrict__ a, int64_t n, float* __
   if (i < n) b[i] = (float)a[i];
 }
 
+// perm (nullable): process the queries in this order (grouped by coarse
+// cell, cmm_query_order) so that neighbouring threads gather neighbouring
+// records; every query's own arithmetic and output slot are unchanged.
 template <bool JAC, class Src>
 __global__ void __launch_bounds__(kBlock) compose_kernel(MeshView m, Src cp,
                                                          const double* __restrict__ q, int64_t n,
                                                          double* __restrict__ out,
                                                          int32_t* __restrict__ tri,
                                                          int32_t* __restrict__ tri_all,
-                                                         double* __restrict__ jac) {
+                                                         double* __restrict__ jac,
+                                                         const int32_t* __restrict__ perm) {
   const int S = cp.count();
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n;
+       j += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = perm ? (int64_t)__ldg(perm + j) : j;
     double p[3] = {q[3 * i], q[3 * i + 1], q[3 * i + 2]};
     if (!finite3(p[0], p[1], p[2])) {
       flag(m, CMM_FLAG_NONFINITE);
@@ -338,6 +343,129 @@ __global__ void __launch_bounds__(kBlock) stencil_kernel(MeshView m, const doubl
   }
 }
 
+// ------------------------------------------------------- query order
+// Counting sort of the queries by coarse cell (the hierarchy node of level
+// kOrderLevel containing the query, FP32 descent, no FP64 filter: any
+// cell is a valid bucket) in four passes without global atomics:
+// per-block histograms, a scan along each cell's row of blocks, a scan of
+// the cell totals, a scatter.
+constexpr int kOrderLevel = 4;          // 20 * 4^4 = 5120 cells
+constexpr int kOrderCells = 20 << (2 * kOrderLevel);
+constexpr int kOrderBlock = 1024;       // threads per block of passes 1 and 3
+constexpr int kOrderPer = 16;           // queries per thread
+
+__device__ __forceinline__ int coarse_cell(const MeshView& m, double x, double y, double z) {
+  const float fx = (float)x, fy = (float)y, fz = (float)z;
+  const float* rf = m.root_f;
+  int f = 0;
+  float best = -4.0f;
+  for (int g = 0; g < 20; ++g) {
+    const float d = fmaf(rf[12 * g], fx, fmaf(rf[12 * g + 1], fy, rf[12 * g + 2] * fz));
+    if (d > best) {
+      best = d;
+      f = g;
+    }
+  }
+  int64_t off = 0, cnt = 20;
+  const int lv = m.level < kOrderLevel ? m.level : kOrderLevel;
+  for (int j = 0; j < lv; ++j) {
+    const float* nf = m.node_nf + 9 * (off + f);
+    int c;
+    if (plane_f(nf, fx, fy, fz) > 0.f) c = 0;
+    else if (plane_f(nf + 3, fx, fy, fz) > 0.f) c = 1;
+    else if (plane_f(nf + 6, fx, fy, fz) > 0.f) c = 2;
+    else c = 3;
+    off += cnt;
+    cnt *= 4;
+    f = 4 * f + c;
+  }
+  return f << (2 * (kOrderLevel - lv));
+}
+
+// pass 1: keys and per-block histograms hist[cell * nblk + block]
+__global__ void __launch_bounds__(kOrderBlock) order_count_kernel(MeshView m, const double* __restrict__ q,
+                                                                  int64_t n, int32_t* __restrict__ key,
+                                                                  int32_t* __restrict__ hist) {
+  __shared__ int h[kOrderCells];
+  for (int k = threadIdx.x; k < kOrderCells; k += blockDim.x) h[k] = 0;
+  __syncthreads();
+  const int64_t base = (int64_t)blockIdx.x * kOrderBlock * kOrderPer;
+  for (int r = 0; r < kOrderPer; ++r) {
+    const int64_t i = base + (int64_t)r * kOrderBlock + threadIdx.x;
+    if (i < n) {
+      const int c = coarse_cell(m, q[3 * i], q[3 * i + 1], q[3 * i + 2]);
+      key[i] = c;
+      atomicAdd(&h[c], 1);
+    }
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < kOrderCells; k += blockDim.x) hist[(int64_t)k * gridDim.x + blockIdx.x] = h[k];
+}
+
+// pass 2: per cell (one warp each) the exclusive scan of its row of block
+// counts in place, and the cell total
+__global__ void __launch_bounds__(256) order_rowscan_kernel(int32_t* __restrict__ hist, int nblk,
+                                                            int32_t* __restrict__ total) {
+  const int c = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (c >= kOrderCells) return;
+  int32_t* row = hist + (int64_t)c * nblk;
+  int carry = 0;
+  for (int b0 = 0; b0 < nblk; b0 += 32) {
+    const int b = b0 + lane;
+    const int v = b < nblk ? row[b] : 0;
+    int inc = v;
+    for (int d = 1; d < 32; d <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, inc, d);
+      if (lane >= d) inc += t;
+    }
+    if (b < nblk) row[b] = carry + inc - v;
+    carry += __shfl_sync(0xffffffffu, inc, 31);
+  }
+  if (lane == 0) total[c] = carry;
+}
+
+// pass 3: exclusive scan of the cell totals (one block)
+__global__ void __launch_bounds__(1024) order_cellscan_kernel(int32_t* __restrict__ total) {
+  constexpr int per = (kOrderCells + 1023) / 1024;
+  __shared__ int part[1024];
+  const int lo = threadIdx.x * per;
+  int v[per], s = 0;
+  for (int k = 0; k < per; ++k) {
+    v[k] = lo + k < kOrderCells ? total[lo + k] : 0;
+    s += v[k];
+  }
+  part[threadIdx.x] = s;
+  __syncthreads();
+  for (int d = 1; d < 1024; d <<= 1) {
+    const int t = threadIdx.x >= d ? part[threadIdx.x - d] : 0;
+    __syncthreads();
+    part[threadIdx.x] += t;
+    __syncthreads();
+  }
+  int acc = part[threadIdx.x] - s;
+  for (int k = 0; k < per; ++k)
+    if (lo + k < kOrderCells) {
+      total[lo + k] = acc;
+      acc += v[k];
+    }
+}
+
+// pass 4: scatter the query ids into their cells' ranges
+__global__ void __launch_bounds__(kOrderBlock) order_scatter_kernel(const int32_t* __restrict__ key, int64_t n,
+                                                                    const int32_t* __restrict__ hist,
+                                                                    const int32_t* __restrict__ cbase,
+                                                                    int32_t* __restrict__ perm) {
+  __shared__ int h[kOrderCells];
+  for (int k = threadIdx.x; k < kOrderCells; k += blockDim.x)
+    h[k] = cbase[k] + hist[(int64_t)k * gridDim.x + blockIdx.x];
+  __syncthreads();
+  const int64_t base = (int64_t)blockIdx.x * kOrderBlock * kOrderPer;
+  for (int r = 0; r < kOrderPer; ++r) {
+    const int64_t i = base + (int64_t)r * kOrderBlock + threadIdx.x;
+    if (i < n) perm[atomicAdd(&h[key[i]], 1)] = (int32_t)i;
+  }
+}
+
 int check_launch(const char* what) {
   note_launch();
   cudaError_t e = cudaGetLastError();
@@ -368,7 +496,7 @@ int launch_assemble(const MeshView& m, const double* jets, int ncomp, double* co
 
 int launch_compose(const MeshView& m, const double* const* coeffs, int S, const double* q,
                    int64_t n, double* out, int32_t* tri, int32_t* tri_all, double* jac,
-                   cudaStream_t s) {
+                   cudaStream_t s, const int32_t* perm) {
   if (n == 0) return CMM_OK;
   SubmapPtrs cp;
   cp.S = S;
@@ -376,9 +504,9 @@ int launch_compose(const MeshView& m, const double* const* coeffs, int S, const 
   const int b = block_of(m, kTuneCompose, kBlock);
   const int g = grid_for(n, b);
   if (jac)
-    compose_kernel<true><<<g, b, 0, s>>>(m, cp, q, n, out, tri, tri_all, jac);
+    compose_kernel<true><<<g, b, 0, s>>>(m, cp, q, n, out, tri, tri_all, jac, perm);
   else
-    compose_kernel<false><<<g, b, 0, s>>>(m, cp, q, n, out, tri, tri_all, jac);
+    compose_kernel<false><<<g, b, 0, s>>>(m, cp, q, n, out, tri, tri_all, jac, perm);
   return check_launch("compose_kernel");
 }
 
@@ -398,13 +526,36 @@ int make_asm_f32(cmm_mesh* mesh) {
   return CMM_OK;
 }
 
+int64_t order_workspace(int64_t n) {
+  const int64_t nblk = (n + (int64_t)kOrderBlock * kOrderPer - 1) / ((int64_t)kOrderBlock * kOrderPer);
+  return n + (int64_t)kOrderCells * ((nblk < 1 ? 1 : nblk) + 1);
+}
+
+int launch_query_order(const MeshView& m, const double* q, int64_t n, int32_t* perm, int32_t* work,
+                       cudaStream_t s) {
+  if (n == 0) return CMM_OK;
+  const int64_t nblk = (n + (int64_t)kOrderBlock * kOrderPer - 1) / ((int64_t)kOrderBlock * kOrderPer);
+  int32_t* key = work;
+  int32_t* hist = work + n;
+  int32_t* total = hist + (int64_t)kOrderCells * nblk;
+  order_count_kernel<<<(int)nblk, kOrderBlock, 0, s>>>(m, q, n, key, hist);
+  int rc = check_launch("order_count_kernel");
+  if (rc) return rc;
+  order_rowscan_kernel<<<kOrderCells / 8, 256, 0, s>>>(hist, (int)nblk, total);
+  if ((rc = check_launch("order_rowscan_kernel"))) return rc;
+  order_cellscan_kernel<<<1, 1024, 0, s>>>(total);
+  if ((rc = check_launch("order_cellscan_kernel"))) return rc;
+  order_scatter_kernel<<<(int)nblk, kOrderBlock, 0, s>>>(key, n, hist, total, perm);
+  return check_launch("order_scatter_kernel");
+}
+
 int launch_compose_dev(const MeshView& m, const double* const* table, const BveState* st,
                        const double* last, const double* q, int64_t n, double* out, cudaStream_t s) {
   if (n == 0) return CMM_OK;
   DevSubmaps cp{table, st, last};
   const int b = block_of(m, kTuneCompose, kBlock);
   compose_kernel<false><<<grid_for(n, b), b, 0, s>>>(m, cp, q, n, out, nullptr, nullptr,
-                                                                nullptr);
+                                                                nullptr, nullptr);
   return check_launch("compose_kernel");
 }
 

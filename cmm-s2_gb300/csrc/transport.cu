@@ -1,0 +1,452 @@
+// Linear transport on the sphere with the reference's analytic test flows
+// and tracer fields (sm_103a): the velocity fields of
+// cmm_s2/core/dynamical_fields.py:18-107 evaluated in closed form inside
+// the backward integrators, so the CMM map update of
+// cmm_s2/tests/test_spherical_transport.py (advect_project_sphere with
+// U = u_deform_rot, ...) runs without a velocity mesh; and the tracer
+// initial conditions (:85-159, and the smooth test function of
+// tests/test_spherical_transport.py:36-38) evaluated at composed points.
+//
+// Time-dependent rotation matrices and cos(pi t / T) factors are computed
+// on the host once per stage time (FlowSpec), in FP64 with the reference's
+// formulas; the kernels see only products and sums.
+#include <cuda_runtime.h>
+
+#include <cmath>
+
+#include "cmm_internal.h"
+#include "device_common.cuh"
+#include "integrators.cuh"
+
+namespace cmm {
+
+using namespace dev;
+
+namespace {
+
+constexpr int kBlock = 128;
+constexpr double kPi = 3.141592653589793;
+constexpr double kRho0 = 3.0;  // rho_0, dynamical_fields.py:44
+
+struct FlowStage {
+  double fwd[9];   // rotation into the moving frame
+  double back[9];  // rotation back
+  double c1;       // 2 k cos(pi t / T), k = 2 (u_deform)
+  double cdiv;     // cos(pi t / T) (u_div)
+};
+
+struct FlowSpec {
+  int kind;
+  double wx, wz;   // solid-body rotation vector (c sin(alpha), 0, c cos(alpha)), c = -2 pi / T
+  FlowStage st[4];
+};
+
+__device__ __forceinline__ void rotate3(const double* L, double x, double y, double z, double* o) {
+  o[0] = L[0] * x + L[1] * y + L[2] * z;
+  o[1] = L[3] * x + L[4] * y + L[5] * z;
+  o[2] = L[6] * x + L[7] * y + L[8] * z;
+}
+
+// utils.cross(a, b) with b = (bx, by, bz)
+__device__ __forceinline__ void cross3(double ax, double ay, double az, double bx, double by, double bz,
+                                       double* o) {
+  o[0] = ay * bz - az * by;
+  o[1] = az * bx - ax * bz;
+  o[2] = ax * by - ay * bx;
+}
+
+__device__ __forceinline__ void u_sbr(const FlowSpec& f, double x, double y, double z, double* V) {
+  cross3(x, y, z, f.wx, 0.0, f.wz, V);  // :18-22
+}
+
+__device__ __forceinline__ void u_deform(double c1, double x, double y, double z, double* V) {
+  cross3(x, y, z, 0.0 * x, c1 * y, 0.0 * z, V);  // :24-30
+}
+
+// omega_r (:48-55): angular speed of the static vortex at colatitude theta
+__device__ __forceinline__ double omega_r(double theta) {
+  if (theta == 0.0) return 0.0;
+  const double c = sin(theta);
+  const double a = kRho0 * c;
+  const double sech = 1.0 / cosh(a);
+  return (2 * kPi) * sqrt(3.0) * (3.0 / 2.0) * (1.0 / a) * tanh(a) * (sech * sech);
+}
+
+__device__ __forceinline__ void u_static_vortex(double x, double y, double z, double* V) {
+  double phi, theta;  // :57-65
+  cart2sphere(x, y, z, &phi, &theta);
+  const double w = omega_r(theta);
+  V[0] = -y * w;
+  V[1] = x * w;
+  V[2] = 0.0 * z;
+}
+
+// tan_proj (utils.py:29-34)
+__device__ __forceinline__ void tan_proj(double x, double y, double z, const double* A, double* o) {
+  o[0] = (1 - x * x) * A[0] + (-x * y) * A[1] + (-x * z) * A[2];
+  o[1] = (-x * y) * A[0] + (1 - y * y) * A[1] + (-y * z) * A[2];
+  o[2] = (-x * z) * A[0] + (-y * z) * A[1] + (1 - z * z) * A[2];
+}
+
+__device__ void flow_at(const FlowSpec& f, int s, double x, double y, double z, double* V) {
+  const FlowStage& g = f.st[s];
+  switch (f.kind) {
+    case CMM_FLOW_SOLID_BODY:
+      u_sbr(f, x, y, z, V);
+      return;
+    case CMM_FLOW_DEFORM:
+      u_deform(g.c1, x, y, z, V);
+      return;
+    case CMM_FLOW_DEFORM_ROT: {  // :32-42
+      double r[3], u[3], w[3];
+      rotate3(g.fwd, x, y, z, r);
+      u_deform(g.c1, r[0], r[1], r[2], u);
+      rotate3(g.back, u[0], u[1], u[2], w);
+      u_sbr(f, x, y, z, V);
+      V[0] = w[0] + V[0];
+      V[1] = w[1] + V[1];
+      V[2] = w[2] + V[2];
+      return;
+    }
+    case CMM_FLOW_STATIC_VORTEX:
+      u_static_vortex(x, y, z, V);
+      return;
+    case CMM_FLOW_ROTATING_VORTEX:  // :67-76
+    case CMM_FLOW_EQUATOR_VORTEX: {  // :78-83
+      double r[3], u[3], w[3];
+      rotate3(g.fwd, x, y, z, r);
+      u_static_vortex(r[0], r[1], r[2], u);
+      rotate3(g.back, u[0], u[1], u[2], w);
+      if (f.kind == CMM_FLOW_EQUATOR_VORTEX) {
+        V[0] = w[0];
+        V[1] = w[1];
+        V[2] = w[2];
+        return;
+      }
+      u_sbr(f, x, y, z, V);
+      V[0] = w[0] + V[0];
+      V[1] = w[1] + V[1];
+      V[2] = w[2] + V[2];
+      return;
+    }
+    case CMM_FLOW_DIVERGENT: {  // :97-107
+      double phi, theta;
+      cart2sphere(x, y, z, &phi, &theta);
+      const double sp2 = sin(phi / 2), st = sin(theta), ct = cos(theta), sph = sin(phi), cph = cos(phi);
+      const double u = -(sp2 * sp2) * sin(2 * theta) * st * g.cdiv;
+      const double v = (-0.5) * sph * (st * st * st) * g.cdiv;
+      const double A[3] = {ct * cph * v - st * sph * u, ct * sph * v + st * cph * u, -st * v};
+      tan_proj(x, y, z, A, V);
+      return;
+    }
+    default:
+      V[0] = V[1] = V[2] = 0.0;
+  }
+}
+
+struct FlowVel {
+  const FlowSpec& f;
+  __device__ __forceinline__ void operator()(int s, double x, double y, double z, double* V) const {
+    flow_at(f, s, x, y, z, V);
+  }
+};
+
+// x, out: (3,n) component-major
+__global__ void __launch_bounds__(kBlock) flow_velocity_kernel(MeshView m, FlowSpec f,
+                                                               const double* __restrict__ x, int64_t n,
+                                                               double* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double px = x[i], py = x[n + i], pz = x[2 * n + i];
+    double V[3] = {nan(""), nan(""), nan("")};
+    if (finite3(px, py, pz))
+      flow_at(f, 0, px, py, pz, V);
+    if (!finite3(V[0], V[1], V[2])) flag(m, CMM_FLAG_NONFINITE);
+    out[i] = V[0];
+    out[n + i] = V[1];
+    out[2 * n + i] = V[2];
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) flow_integrate_kernel(MeshView m, FlowSpec f, int scheme, double dt,
+                                                                const double* __restrict__ x, int64_t n,
+                                                                double* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double p[3] = {x[i], x[n + i], x[2 * n + i]};
+    if (finite3(p[0], p[1], p[2])) integrate_back(FlowVel{f}, scheme, dt, p);
+    if (!finite3(p[0], p[1], p[2])) flag(m, CMM_FLAG_NONFINITE);
+    out[i] = p[0];
+    out[n + i] = p[1];
+    out[2 * n + i] = p[2];
+  }
+}
+
+// Foot points of the vertices and stencil points (advect,
+// evolution_functions.py:117-133), the layout of advect_points_kernel:
+// work = yn (3,nv) followed by the stencil foot points (3,4,nv).
+__global__ void __launch_bounds__(kBlock) flow_advect_points_kernel(MeshView mesh, FlowSpec f, int scheme,
+                                                                    double dt, const double* __restrict__ s_pts,
+                                                                    double* __restrict__ work) {
+  const int64_t nv = mesh.nv, n = 5 * nv;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double p[3];
+    const int64_t j = i - nv;
+    if (i < nv) {
+      p[0] = mesh.verts[4 * i];
+      p[1] = mesh.verts[4 * i + 1];
+      p[2] = mesh.verts[4 * i + 2];
+    } else {
+      p[0] = s_pts[j];
+      p[1] = s_pts[4 * nv + j];
+      p[2] = s_pts[8 * nv + j];
+    }
+    integrate_back(FlowVel{f}, scheme, dt, p);
+    if (!finite3(p[0], p[1], p[2])) flag(mesh, CMM_FLAG_NONFINITE);
+    if (i < nv) {
+      work[i] = p[0];
+      work[nv + i] = p[1];
+      work[2 * nv + i] = p[2];
+    } else {
+      double* sn = work + 3 * nv;
+      sn[j] = p[0];
+      sn[4 * nv + j] = p[1];
+      sn[8 * nv + j] = p[2];
+    }
+  }
+}
+
+// ----------------------------------------------------------------- tracers
+struct TracerSpec {
+  int kind;
+  double t;
+  double rot[9];   // rotating_vort_IC: Rot_x(pi/2) Rot_z(0)^T
+};
+
+// great-circle distance of (phi, theta) to a bell centre (:124-127)
+__device__ __forceinline__ double bell_r(double phi, double theta, double phic, double thec) {
+  const double arg = sin(thec - kPi / 2) * sin(theta - kPi / 2) +
+                     cos(thec - kPi / 2) * cos(theta - kPi / 2) * cos(phi - phic);
+  return acos(arg);  // NaN outside [-1, 1], as numpy's arccos; NaN < R is false
+}
+
+__device__ double tracer_at(const TracerSpec& ts, double x, double y, double z) {
+  const double phic1 = kPi + kPi / 6, phic2 = kPi - kPi / 6, thec = kPi / 2, R = 0.5, h0 = 1.0;
+  switch (ts.kind) {
+    case CMM_TRACER_COSINE_BELL: {  // :122-137
+      double phi, theta;
+      cart2sphere(x, y, z, &phi, &theta);
+      const double r1 = bell_r(phi, theta, phic1, thec), r2 = bell_r(phi, theta, phic2, thec);
+      const double o1 = r1 < R ? (h0 / 2) * (1 + cos(r1 * kPi / R)) : 0.0;
+      const double o2 = r2 < R ? (h0 / 2) * (1 + cos(r2 * kPi / R)) : 0.0;
+      return 0.9 * (o1 + o2) + 0.1;
+    }
+    case CMM_TRACER_SLOTTED_CYLINDERS: {  // :139-157
+      double phi, theta;
+      cart2sphere(x, y, z, &phi, &theta);
+      const double r1 = bell_r(phi, theta, phic1, thec), r2 = bell_r(phi, theta, phic2, thec);
+      double o1 = 0.0, o2 = 0.0;
+      if (r1 <= R && fabs(phi - phic1) >= R / 6) o1 = 0.9;
+      if (r1 <= R && fabs(phi - phic1) < R / 6 && theta < (-5 * R / 12 + kPi / 2)) o1 = 0.9;
+      if (r2 <= R && fabs(phi - phic2) >= R / 6) o2 = 0.9;
+      if (r2 <= R && fabs(phi - phic2) < R / 6 && theta > (5 * R / 12 + kPi / 2)) o2 = 0.9;
+      return o1 + o2 + 0.1;
+    }
+    case CMM_TRACER_STATIC_VORTEX:      // static_vort_IC, :85-88
+    case CMM_TRACER_ROTATING_VORTEX: {  // rotating_vort_IC, :90-95
+      double p[3] = {x, y, z};
+      if (ts.kind == CMM_TRACER_ROTATING_VORTEX) rotate3(ts.rot, x, y, z, p);
+      double phi, theta;
+      cart2sphere(p[0], p[1], p[2], &phi, &theta);
+      const double rho = kRho0 * sin(theta);
+      return 1 - tanh((rho / 5) * sin(phi - omega_r(theta) * ts.t));
+    }
+    case CMM_TRACER_SMOOTH_TEST: {  // tests/test_spherical_transport.py:36-38
+      const double y7 = y * y * y * y * y * y * y, z5 = z * z * z * z * z;
+      return sin(x * x) * (10 * cos(y - 2)) + cos(10 * z5) + 2 * sin(x * 3 * (z - 0.1) + y7);
+    }
+    default:
+      return 0.0;
+  }
+}
+
+// X (n,3) points -> out (n,)
+__global__ void __launch_bounds__(kBlock) tracer_kernel(MeshView m, TracerSpec ts, const double* __restrict__ X,
+                                                        int64_t n, double* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double x = X[3 * i], y = X[3 * i + 1], z = X[3 * i + 2];
+    double v = nan("");
+    if (finite3(x, y, z)) v = tracer_at(ts, x, y, z);
+    if (!isfinite(v)) flag(m, CMM_FLAG_NONFINITE);
+    out[i] = v;
+  }
+}
+
+// ------------------------------------------------------------------ host
+// utils.Rot_x/Rot_y/Rot_z (utils.py:109-116), row-major
+void rot_x(double a, double* R) {
+  const double c = std::cos(a), s = std::sin(a);
+  const double M[9] = {1, 0, 0, 0, c, -s, 0, s, c};
+  for (int k = 0; k < 9; ++k) R[k] = M[k];
+}
+void rot_y(double a, double* R) {
+  const double c = std::cos(a), s = std::sin(a);
+  const double M[9] = {c, 0, -s, 0, 1, 0, s, 0, c};
+  for (int k = 0; k < 9; ++k) R[k] = M[k];
+}
+void rot_z(double a, double* R) {
+  const double c = std::cos(a), s = std::sin(a);
+  const double M[9] = {c, -s, 0, s, c, 0, 0, 0, 1};
+  for (int k = 0; k < 9; ++k) R[k] = M[k];
+}
+void transpose3(const double* A, double* T) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) T[3 * j + i] = A[3 * i + j];
+}
+void matmul3(const double* A, const double* B, double* C) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) C[3 * i + j] = A[3 * i] * B[j] + A[3 * i + 1] * B[3 + j] + A[3 * i + 2] * B[6 + j];
+}
+
+void stage_setup(int kind, double T, double alpha, double t, FlowStage* g) {
+  g->c1 = 2 * 2 * std::cos(kPi * t / T);
+  g->cdiv = std::cos(kPi * t / T);
+  double A[9], B[9], At[9], Bt[9];
+  for (int k = 0; k < 9; ++k) g->fwd[k] = g->back[k] = k % 4 == 0 ? 1.0 : 0.0;
+  if (kind == CMM_FLOW_DEFORM_ROT) {  // tau = 2 pi t
+    rot_z(2 * kPi * t, A);
+    rot_y(alpha, B);
+    transpose3(A, At);
+    transpose3(B, Bt);
+    matmul3(At, B, g->fwd);
+    matmul3(Bt, A, g->back);
+  } else if (kind == CMM_FLOW_ROTATING_VORTEX) {  // tau = 2 pi t / T
+    rot_x(kPi / 2, A);
+    rot_z(2 * kPi * t / T, B);
+    transpose3(A, At);
+    transpose3(B, Bt);
+    matmul3(A, Bt, g->fwd);
+    matmul3(B, At, g->back);
+  } else if (kind == CMM_FLOW_EQUATOR_VORTEX) {
+    rot_x(kPi / 2, A);
+    for (int k = 0; k < 9; ++k) g->fwd[k] = A[k];
+    transpose3(A, g->back);
+  }
+}
+
+int make_spec(int kind, double T, double alpha, int scheme, double t, double dt, FlowSpec* f);
+int check_launch(const char* what);
+
+}  // namespace
+
+// stage times of each scheme, in the order the integrators call V
+// (evolution_functions.py:19-80); 0 for an unknown scheme
+int stage_times(int scheme, double t, double dt, double* times) {
+  switch (scheme) {
+    case CMM_EULER:
+      times[0] = t;
+      return 1;
+    case CMM_IMPROVED_EULER:
+      times[0] = t;
+      times[1] = t + dt;
+      return 2;
+    case CMM_RK4:
+      times[0] = t + dt;
+      times[1] = t + dt / 2;
+      times[2] = t + 0.5 * dt;
+      times[3] = t;
+      return 4;
+    case CMM_RK2:
+      times[0] = t + dt;
+      times[1] = t + dt / 2;
+      return 2;
+    default:
+      return 0;
+  }
+}
+
+namespace {
+
+int make_spec(int kind, double T, double alpha, int scheme, double t, double dt, FlowSpec* f) {
+  if (kind < CMM_FLOW_SOLID_BODY || kind > CMM_FLOW_DIVERGENT) {
+    set_last_error("unknown transport flow");
+    return CMM_ERR_ARG;
+  }
+  if (!(T != 0.0) || !std::isfinite(T) || !std::isfinite(alpha)) {
+    set_last_error("transport flow: period T must be finite and nonzero, alpha finite");
+    return CMM_ERR_ARG;
+  }
+  double times[4];
+  const int nt = scheme < 0 ? 1 : stage_times(scheme, t, dt, times);
+  if (scheme < 0) times[0] = t;
+  if (nt == 0) {
+    set_last_error("unknown integration scheme");
+    return CMM_ERR_ARG;
+  }
+  *f = FlowSpec{};
+  f->kind = kind;
+  const double c = -2 * kPi / T;
+  f->wx = c * std::sin(alpha);
+  f->wz = c * std::cos(alpha);
+  for (int s = 0; s < nt; ++s) stage_setup(kind, T, alpha, times[s], &f->st[s]);
+  return CMM_OK;
+}
+
+int check_launch(const char* what) {
+  note_launch();
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? CMM_OK : cuda_fail(e, what);
+}
+
+}  // namespace
+
+int flow_velocity(const MeshView& m, int kind, double T, double alpha, double t, const double* x, int64_t n,
+                  double* out, cudaStream_t s) {
+  FlowSpec f;
+  int rc = make_spec(kind, T, alpha, -1, t, 0.0, &f);
+  if (rc || n == 0) return rc;
+  flow_velocity_kernel<<<grid_for(n, kBlock), kBlock, 0, s>>>(m, f, x, n, out);
+  return check_launch("flow_velocity_kernel");
+}
+
+int flow_integrate(const MeshView& m, int kind, double T, double alpha, int scheme, double t, double dt,
+                   const double* x, int64_t n, double* out, cudaStream_t s) {
+  FlowSpec f;
+  int rc = make_spec(kind, T, alpha, scheme, t, dt, &f);
+  if (rc || n == 0) return rc;
+  flow_integrate_kernel<<<grid_for(n, kBlock), kBlock, 0, s>>>(m, f, scheme, dt, x, n, out);
+  return check_launch("flow_integrate_kernel");
+}
+
+int flow_advect_points(const MeshView& mesh, int kind, double T, double alpha, int scheme, double t, double dt,
+                       const double* s_pts, double* work, cudaStream_t s) {
+  FlowSpec f;
+  int rc = make_spec(kind, T, alpha, scheme, t, dt, &f);
+  if (rc) return rc;
+  const int64_t n = 5LL * mesh.nv;
+  flow_advect_points_kernel<<<grid_for(n, kBlock), kBlock, 0, s>>>(mesh, f, scheme, dt, s_pts, work);
+  return check_launch("flow_advect_points_kernel");
+}
+
+int launch_tracer(const MeshView& m, int kind, double t, const double* X, int64_t n, double* out,
+                  cudaStream_t s) {
+  if (kind < CMM_TRACER_COSINE_BELL || kind > CMM_TRACER_SMOOTH_TEST) {
+    set_last_error("cmm_tracer_eval: unknown tracer");
+    return CMM_ERR_ARG;
+  }
+  TracerSpec ts{};
+  ts.kind = kind;
+  ts.t = t;
+  double A[9], B[9], Bt[9];
+  rot_x(kPi / 2, A);
+  rot_z(0.0, B);
+  transpose3(B, Bt);
+  matmul3(A, Bt, ts.rot);
+  if (n == 0) return CMM_OK;
+  tracer_kernel<<<grid_for(n, kBlock), kBlock, 0, s>>>(m, ts, X, n, out);
+  return check_launch("tracer_kernel");
+}
+
+}  // namespace cmm

@@ -18,6 +18,7 @@
 #include "cmm_internal.h"
 #include "device_common.cuh"
 #include "geom.h"
+#include "integrators.cuh"
 
 namespace cmm {
 
@@ -91,45 +92,22 @@ __device__ __forceinline__ void velocity_at(const MeshView& m, const VelPtrs& vc
   }
 }
 
-__device__ __forceinline__ void sphere_proj(double* x) {
-  const double r = 1.0 / sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
-  x[0] *= r;
-  x[1] *= r;
-  x[2] *= r;
-}
+// The spline velocity as the integrators' velocity source: stage s uses
+// the Lagrange weights of the scheme's s-th evaluation time.
+struct SplineVel {
+  const MeshView& m;
+  const VelPtrs& vc;
+  int nvs;
+  const TimeWeights& tw;
+  __device__ __forceinline__ void operator()(int s, double x, double y, double z, double* V) const {
+    velocity_at(m, vc, nvs, stage(tw, s), x, y, z, V);
+  }
+};
 
-// Backward integrators (cmm_s2/core/evolution_functions.py:19-67):
-// scheme 0 Euler_step_proj, 1 improved_Euler_proj, 2 RK4_proj.
 __device__ __forceinline__ void integrate_point(const MeshView& m, const VelPtrs& vc, int nvs,
                                                 const TimeWeights& tw, int scheme, double dt,
                                                 double* x) {
-  double v1[3], v2[3], s[3];
-  velocity_at(m, vc, nvs, stage(tw, 0), x[0], x[1], x[2], v1);
-  if (scheme == 0) {
-    for (int c = 0; c < 3; ++c) x[c] = x[c] - dt * v1[c];
-    sphere_proj(x);
-    return;
-  }
-  if (scheme == 1) {
-    for (int c = 0; c < 3; ++c) s[c] = x[c] - dt * v1[c];
-    sphere_proj(s);
-    velocity_at(m, vc, nvs, stage(tw, 1), s[0], s[1], s[2], v2);
-    for (int c = 0; c < 3; ++c) x[c] = x[c] - (dt / 2) * (v1[c] + v2[c]);
-    sphere_proj(x);
-    return;
-  }
-  double v3[3], v4[3];
-  for (int c = 0; c < 3; ++c) s[c] = x[c] - dt * v1[c] / 2;
-  sphere_proj(s);
-  velocity_at(m, vc, nvs, stage(tw, 1), s[0], s[1], s[2], v2);
-  for (int c = 0; c < 3; ++c) s[c] = x[c] - (dt / 2) * v2[c];
-  sphere_proj(s);
-  velocity_at(m, vc, nvs, stage(tw, 2), s[0], s[1], s[2], v3);
-  for (int c = 0; c < 3; ++c) s[c] = x[c] - dt * v3[c];
-  sphere_proj(s);
-  velocity_at(m, vc, nvs, stage(tw, 3), s[0], s[1], s[2], v4);
-  for (int c = 0; c < 3; ++c) x[c] = x[c] - (dt / 6) * (v1[c] + 2 * v2[c] + 2 * v3[c] + v4[c]);
-  sphere_proj(x);
+  integrate_back(SplineVel{m, vc, nvs, tw}, scheme, dt, x);
 }
 
 __global__ void __launch_bounds__(kBlock) latlon_locate_kernel(MeshView m, const double* __restrict__ q,

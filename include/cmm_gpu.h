@@ -114,6 +114,65 @@ int cmm_compose(const cmm_mesh* mesh, const double* const* coeffs, int S, const 
                 int64_t n, double* out, int32_t* tri, int32_t* tri_all, double* jac,
                 void* stream);
 
+/* ------------------------------------------------- linear transport */
+/* The analytic test flows of cmm_s2/core/dynamical_fields.py, in closed
+ * form inside the backward integrators, for linear advection of a tracer
+ * (cmm_s2/tests/test_spherical_transport.py).  T: period (the module's
+ * T = 1), alpha: tilt of the solid-body rotation (the module's alpha = 0).
+ * mesh: the map mesh (its status word receives CMM_FLAG_NONFINITE). */
+#define CMM_FLOW_SOLID_BODY 0      /* u_sbr, :18-22 */
+#define CMM_FLOW_DEFORM 1          /* u_deform, :24-30 */
+#define CMM_FLOW_DEFORM_ROT 2      /* u_deform_rot, :32-42 */
+#define CMM_FLOW_STATIC_VORTEX 3   /* u_static_vortex, :57-65 */
+#define CMM_FLOW_ROTATING_VORTEX 4 /* u_rotating_vortex, :67-76 */
+#define CMM_FLOW_EQUATOR_VORTEX 5  /* equator_vortex, :78-83 */
+#define CMM_FLOW_DIVERGENT 6       /* u_div, :97-107 */
+
+/* Velocity V(t, x) of a flow at x (3,n) -> out (3,n). */
+int cmm_flow_velocity(const cmm_mesh* mesh, int flow, double T, double alpha, double t, const double* x,
+                      int64_t n, double* out, void* stream);
+
+/* cmm_integrate with an analytic flow (any scheme, CMM_RK2 included). */
+int cmm_flow_integrate(const cmm_mesh* mesh, int flow, double T, double alpha, int scheme, double t,
+                       double dt, const double* x, int64_t n, double* out, void* stream);
+
+/* cmm_advect_project with an analytic flow: advect_project_sphere(interp,
+ * integrator, t, dt, U, identity) of evolution_functions.py:136-142 with
+ * U one of the flows above.  work: 15*nv doubles. */
+int cmm_flow_advect_project(const cmm_mesh* mesh, int flow, double T, double alpha, int scheme, double t,
+                            double dt, const double* s_pts, const double* tan, const double* prev_coeffs,
+                            double eps, double* jets, double* work, void* stream);
+
+/* Tracer fields at points X (n,3) -> out (n,): the initial conditions of
+ * dynamical_fields.py and the smooth test function of
+ * tests/test_spherical_transport.py:36-38.  t: time argument of the vortex
+ * fields (ignored by the others). */
+#define CMM_TRACER_COSINE_BELL 0        /* cosine_bell, :122-137 */
+#define CMM_TRACER_SLOTTED_CYLINDERS 1  /* IC_SC, :139-157 */
+#define CMM_TRACER_STATIC_VORTEX 2      /* static_vort_IC, :85-88 */
+#define CMM_TRACER_ROTATING_VORTEX 3    /* rotating_vort_IC, :90-95 */
+#define CMM_TRACER_SMOOTH_TEST 4        /* test_func of the transport test */
+int cmm_tracer_eval(const cmm_mesh* mesh, int tracer, double t, const double* X, int64_t n, double* out,
+                    void* stream);
+
+/* Query order for cmm_compose_ordered: perm (n,) int32 receives the query
+ * ids grouped by the level-4 hierarchy cell holding each query (a counting
+ * sort; the order inside a cell is unspecified), so that neighbouring threads of the
+ * composition gather neighbouring coefficient records and share them in
+ * L1/L2 instead of re-reading DRAM.  work: cmm_query_order_workspace(n)
+ * int32 device scratch.  n <= INT32_MAX.  No counterpart in the reference
+ * (its queries are processed in caller order by numpy). */
+int64_t cmm_query_order_workspace(int64_t n);
+int cmm_query_order(const cmm_mesh* mesh, const double* q, int64_t n, int32_t* perm,
+                    int32_t* work, void* stream);
+
+/* cmm_compose with the queries processed in the order perm (a permutation
+ * of 0..n-1, e.g. from cmm_query_order); every output stays in its query's
+ * own slot and is bitwise equal to cmm_compose's. */
+int cmm_compose_ordered(const cmm_mesh* mesh, const double* const* coeffs, int S, const double* q,
+                        int64_t n, const int32_t* perm, double* out, int32_t* tri,
+                        int32_t* tri_all, double* jac, void* stream);
+
 /* Stencil evaluation: locate each vertex foot point yn[:,v] (3,nv), then
  * evaluate the 4 stencil foot points st (3,4,nv) in that same Powell-Sabin
  * sub-triangle, un-normalised -> out (3,4,nv).  Replaces
@@ -142,11 +201,14 @@ int cmm_velocity_eval(const cmm_mesh* velmesh, const double* const* vel_coeffs, 
 
 /* Backward foot points of x (3,n) over one step from t+dt to t, projected
  * onto the sphere after each stage -> out (3,n).  scheme 0: Euler_step_proj,
- * 1: improved_Euler_proj, 2: RK4_proj
- * (cmm_s2/core/evolution_functions.py:19-67). */
+ * 1: improved_Euler_proj, 2: RK4_proj, 3: RK2_proj
+ * (cmm_s2/core/evolution_functions.py:19-80; RK3_proj :35-47 passes three
+ * arguments to the one-argument div_norm and cannot run, so it has no
+ * counterpart).  The adjoint entry points take schemes 0-2. */
 #define CMM_EULER 0
 #define CMM_IMPROVED_EULER 1
 #define CMM_RK4 2
+#define CMM_RK2 3
 int cmm_integrate(const cmm_mesh* velmesh, const double* const* vel_coeffs, int nvs, double ts0,
                   int scheme, double t, double dt, const double* x, int64_t n, double* out,
                   void* stream);

@@ -35,6 +35,14 @@ def rk4_back(t, dt, x, V):
     return _proj(x - (dt / 6) * (v1 + 2 * v2 + 2 * v3 + v4))
 
 
+def rk2_back(t, dt, x, V):
+    """RK2_proj (:68-78)."""
+    v1 = V(t + dt, dt, x)
+    s1 = _proj(x - (dt / 2) * v1)
+    v2 = V(t + dt / 2, dt, s1)
+    return _proj(x - dt * v2)
+
+
 def jets_from_stencil(s_evals, tan, eps=1e-5):
     """spline_proj_sphere (:90-113): new jets (3,4,Nv) from the 4 stencil
     images s_evals (3,4,Nv) and the vertex tangent frames tan (2,Nv,3)."""

@@ -210,6 +210,53 @@ def main():
     save("scalar_L8.npz", alm_half=half, vals=sp.vals, coeffs=sp.coeffs, phi=PH, theta=TH,
          value=sp(PH.copy(), TH.copy()))
 
+    # ---- linear transport: analytic flows, tracers, a remapped run ----------
+    m = ref_mesh(3)
+    tris = np.asarray(m.simplices)
+    X = np.concatenate([random_sphere_points(600, seed=31), special_points(m.vertices, tris),
+                        [[0, 0, 1.0], [0, 0, -1.0], [0, 1.0, 0], [-1.0, 0, 0]]])
+    flows = ["u_sbr", "u_deform", "u_deform_rot", "u_static_vortex", "u_rotating_vortex", "equator_vortex",
+             "u_div"]
+    out = dict(X=X)
+    for name in flows:
+        for k, t in enumerate([0.0, 0.37]):
+            out[f"vel_{name}_{k}"] = np.asarray(getattr(rfields, name)(t, 0.05, X.T.copy()))
+    phi, theta = rutils.cart2sphere(X.T)
+    out["tr_cosine_bell"] = rfields.cosine_bell(phi, theta)
+    out["tr_IC_SC"] = rfields.IC_SC(phi, theta)
+    out["tr_static_vort_IC"] = rfields.static_vort_IC(0.4, X.T.copy())
+    out["tr_rotating_vort_IC"] = rfields.rotating_vort_IC(0.4, X.T.copy())
+    # the loop of tests/test_spherical_transport.py at level 3 (Nt = 2^3 + 10
+    # steps of RK4 over T = 1, u_deform_rot) with remapping every 5 steps
+    verts = m.vertices
+    jet0 = np.zeros((3, 4, len(verts)))
+    jet0[:, 0, :] = verts.T
+    jet0[:, 1:, :] = np.array([rutils.grad_x(verts.T), rutils.grad_y(verts.T), rutils.grad_z(verts.T)])
+    nt = len(tris)
+    map0 = rspl.sphere_diffeomorphism(m, jet0.copy(), np.zeros((3, 19, nt)))
+    Nt = 2 ** 3 + 10
+    tspan = np.linspace(0, 1, Nt, endpoint=False)
+    dt = tspan[1] - tspan[0]
+    remaps, mapping, identity = [], map0, True
+    for count, t in enumerate(tspan, start=1):
+        mapping = revol.advect_project_sphere(mapping, revol.RK4_proj, t, dt, rfields.u_deform_rot, identity)
+        identity = False
+        if count % 5 == 0:
+            remaps.append(mapping.vals.copy())
+            mapping = rspl.sphere_diffeomorphism(m, jet0.copy(), np.zeros((3, 19, nt)))
+            identity = True
+    if not identity:
+        remaps.append(mapping.vals.copy())
+    q = random_sphere_points(400, seed=32)
+    ev = q.copy()
+    for vals in remaps[::-1]:
+        ev = rspl.sphere_diffeomorphism(m, vals.copy(), np.zeros((3, 19, nt)))(ev.copy()).T
+    out.update(jet0=jet0, remaps=np.stack(remaps), q=q, evals=ev, dt=dt, Nt=Nt)
+    # one RK2 step of the solid-body rotation from the identity
+    rk2 = revol.advect_project_sphere(map0, revol.RK2_proj, 0.0, 0.05, rfields.u_sbr, True)
+    out["jets_rk2_sbr"] = rk2.vals
+    save("transport_l3.npz", **out)
+
     # ---- a short barotropic run (restated transforms stand in for pyssht) ---
     m2 = ref_mesh(2)
     subs = rsim.euler_simulation_sphere_remapping(8, 12, 1.0, m2, rfields.rossby_wave,

@@ -174,3 +174,50 @@ def test_project_onto_s12_scalar_spline():
     bcc, tri, vs = mu.query(q)
     val = SP.eval_patch(co, tri, bcc, vs, q)
     np.testing.assert_allclose(val, d["value"].reshape(-1), rtol=0, atol=1e-12)
+
+
+def test_transport_flows_and_tracers():
+    """The restated analytic flows and tracer fields against the reference's
+    dynamical_fields outputs."""
+    from oracle import transport as TR
+    d = load("transport_l3.npz")
+    X = d["X"]
+    for name in TR.FLOWS:
+        V = TR.make_flow(name)
+        for k, t in enumerate([0.0, 0.37]):
+            np.testing.assert_allclose(V(t, 0.05, X.T.copy()), d[f"vel_{name}_{k}"], rtol=0, atol=1e-14,
+                                       err_msg=name)
+    for name in ("cosine_bell", "IC_SC", "static_vort_IC", "rotating_vort_IC"):
+        np.testing.assert_allclose(TR.tracer(name, X, t=0.4), d[f"tr_{name}"], rtol=0, atol=1e-14, err_msg=name)
+
+
+def test_transport_run_with_remaps():
+    """The linear-advection loop of tests/test_spherical_transport.py
+    (u_deform_rot, RK4, 18 steps over T = 1) with a remap every 5 steps,
+    replayed by the oracle: every remapped submap and the composed images."""
+    from oracle import transport as TR
+    d, m = load("transport_l3.npz"), load("mesh_l3.npz")
+    verts, tris = m["verts"], m["tris"]
+    loc = G.QhullLocator(verts)
+    tan, s_pts = G.stencil_points(verts)
+    U = TR.make_flow("u_deform_rot")
+    Nt = int(d["Nt"])
+    tspan = np.linspace(0, 1, Nt, endpoint=False)
+    dt = tspan[1] - tspan[0]
+    assert dt == d["dt"]
+    remaps, prev, identity = [], None, True
+    for count, t in enumerate(tspan, start=1):
+        jets = EV.advect_project(prev, EV.rk4_back, t, dt, U, verts, s_pts, tan, identity)
+        prev, identity = SP.MapOracle(verts, tris, loc, jets), False
+        if count % 5 == 0:
+            remaps.append(jets)
+            prev, identity = None, True
+    if not identity:
+        remaps.append(prev.vals)
+    assert len(remaps) == len(d["remaps"])
+    for a, b in zip(remaps, d["remaps"]):
+        np.testing.assert_allclose(a, b, rtol=0, atol=1e-11)
+    comp = SP.CompositeOracle(verts, tris, loc, np.stack(remaps))
+    np.testing.assert_allclose(comp(d["q"]), d["evals"], rtol=0, atol=1e-13)
+    rk2 = EV.advect_project(None, EV.rk2_back, 0.0, 0.05, TR.make_flow("u_sbr"), verts, s_pts, tan, True)
+    np.testing.assert_allclose(rk2, d["jets_rk2_sbr"], rtol=0, atol=1e-10)
