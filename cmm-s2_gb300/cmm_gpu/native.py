@@ -300,7 +300,7 @@ EULER, IMPROVED_EULER, RK4, RK2 = 0, 1, 2, 3
 (TRACER_COSINE_BELL, TRACER_SLOTTED_CYLINDERS, TRACER_STATIC_VORTEX, TRACER_ROTATING_VORTEX,
  TRACER_SMOOTH_TEST) = range(5)
 (VORT_NONE, VORT_ROSSBY_HAURWITZ, VORT_ZONAL_JET, VORT_PERTURBED_JET, VORT_MULTI_JET,
- VORT_GAUSSIAN_VORTEX, VORT_GAUSSIAN_JETS) = range(7)
+ VORT_GAUSSIAN_VORTEX, VORT_GAUSSIAN_JETS, VORT_PERTURBED_RH) = range(8)
 
 
 class VelMesh(Mesh):

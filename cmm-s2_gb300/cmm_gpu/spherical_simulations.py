@@ -25,6 +25,7 @@ _FIELDS = {
     "multi_jet": native.VORT_MULTI_JET,
     "gaussian_vortex": native.VORT_GAUSSIAN_VORTEX,
     "gaussian_zonal_jets": native.VORT_GAUSSIAN_JETS,
+    "perturbed_rossby_wave": native.VORT_PERTURBED_RH,
 }
 
 
@@ -360,3 +361,69 @@ class BVESolver:
 
     def stack_coeffs(self):
         return self.stack[:self.Nc]
+
+    def submaps(self, mesh):
+        """The reference driver's return value (:297): a
+        composite_sphere_diffeomorphism over the remapped submaps (jets,
+        coefficient records, ns, Nc) on `mesh`, the spherical_triangulation
+        this run was built from."""
+        from .spherical_spline import composite_sphere_diffeomorphism
+        comp = composite_sphere_diffeomorphism(mesh, [j.clone() for j in self.stack_jets],
+                                               coeffs=[c.clone() for c in self.stack], ns=list(self.ns))
+        comp.Nc = self.Nc
+        return comp
+
+    # ------------------------------------------------- checkpoint/resume
+    def save_state(self, path):
+        """Checkpoint between steps (state_io.save_bve_state)."""
+        from .state_io import save_bve_state
+        save_bve_state(self, path)
+
+    def load_state(self, path):
+        """Resume a checkpoint into this (not bootstrapped) solver."""
+        from .state_io import load_bve_state
+        return load_bve_state(self, path)
+
+
+def _solver_for(mesh, L, Nt, T, vorticity, rot_rate, n_maps, precision):
+    return BVESolver(mesh.vertices, mesh.simplices, mesh.level, L, Nt, T, vorticity, rot_rate=rot_rate,
+                     n_maps=n_maps, device=mesh.device.index, precision=precision)
+
+
+def euler_simulation_sphere_remapping(L, Nt, T, mesh, vorticity, rot_rate=2 * np.pi, n_maps=10,
+                                      precision="fp64"):
+    """The reference driver (spherical_simulations.py:144-297) on the GPU:
+    `mesh` a spherical_triangulation of this package, `vorticity` a
+    reference field function (or its name, or a Vorticity); returns the
+    composite_sphere_diffeomorphism of the remapped submaps."""
+    s = _solver_for(mesh, L, Nt, T, vorticity, rot_rate, n_maps, precision).run()
+    return s.submaps(mesh)
+
+
+def euler_simulation_sphere(L, Nt, T, mesh, vorticity, rot_rate=2 * np.pi, precision="fp64"):
+    """The driver without remapping (spherical_simulations.py:20-141, whose
+    own body cannot run: it reads ``mesh_u.verticess``, :56): one map
+    over the whole run, returned as a sphere_diffeomorphism."""
+    from .spherical_spline import sphere_diffeomorphism
+    s = _solver_for(mesh, L, Nt, T, vorticity, rot_rate, Nt, precision).run()
+    return sphere_diffeomorphism(mesh, s.stack_jets[0].clone(), s.stack[0].clone())
+
+
+def euler_simulation_sphere_remapping_video(L, Nt, T, mesh, vorticity, rot_rate, n_maps, file_name, save_steps,
+                                            precision="fp64"):
+    """spherical_simulations.py:301-457: the remapping driver that also
+    writes the current map every `save_steps` steps (except at remaps) as
+    the reference's snapshot pickle ``file_name + "<count>.txt"`` =
+    {"vals": (3,4,Nv), "Nc"}.  The final submap stack goes to
+    ``file_name + "_all_maps.npz"`` (vals, ns, Nc, mesh) instead of a
+    pickled reference object.  Returns the composite, as the remapping
+    driver."""
+    from .state_io import write_reference_snapshot, write_submaps
+    s = _solver_for(mesh, L, Nt, T, vorticity, rot_rate, n_maps, precision)
+    s.bootstrap()
+    for _ in range(Nt - 2):
+        s.step()
+        if s.count % save_steps == 0 and s.count not in s.ns:
+            write_reference_snapshot(file_name + "%s" % s.count + ".txt", s.jets, s.Nc)
+    write_submaps(file_name + "_all_maps.npz", s.stack_jets, s.ns, s.Nc, mesh.vertices, mesh.simplices)
+    return s.submaps(mesh)

@@ -159,7 +159,7 @@ int cmm_vorticity_eval(const cmm_mesh* velmesh, int kind, const double* params, 
                        const double* sh, int lmax, const double* spline, double rot_rate,
                        const double* X, double* omega, void* stream) {
   if (!velmesh || velmesh->view.kind != kLatLon) return arg_error("cmm_vorticity_eval: velocity mesh expected");
-  if (!X || !omega || (nparams > 0 && !params) || nparams > 12 || kind < 0 || kind > 6 ||
+  if (!X || !omega || (nparams > 0 && !params) || nparams > 12 || kind < 0 || kind > 7 ||
       (sh && (lmax < 0 || lmax > kShTableMax)))
     return arg_error("cmm_vorticity_eval: bad argument (series degree lmax must be in [0, 128])");
   const int L = velmesh->view.L;

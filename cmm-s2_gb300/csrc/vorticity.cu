@@ -50,6 +50,10 @@ __device__ double omega0(const VortParams& v, double phi, double theta) {
       const double x = sin(theta) * cos(phi), y = sin(theta) * sin(phi), z = cos(theta);
       return 4 * kPi * exp(-((x - 1) * (x - 1) + y * y + z * z) / (1.0 / 16.0));
     }
+    case CMM_VORT_PERTURBED_RH: {  // dynamical_fields.py:213-215
+      const double s = sin(theta);
+      return 30 * cos(theta) * cos(4 * phi) * (s * s * s * s) + 0.1 * sin(theta) * cos(30 * theta);
+    }
     case CMM_VORT_GAUSSIAN_JETS: {  // p = amplitude, width, n, lat_1..lat_n
       const double lat = kPi / 2 - theta;
       double s = 0.0;
@@ -94,6 +98,10 @@ __device__ float omega0_f(const VortParams& v, float phi, float theta) {
     case CMM_VORT_GAUSSIAN_VORTEX: {
       const float x = sinf(theta) * cosf(phi), y = sinf(theta) * sinf(phi), z = cosf(theta);
       return 4 * pi * expf(-((x - 1) * (x - 1) + y * y + z * z) / (1.0f / 16.0f));
+    }
+    case CMM_VORT_PERTURBED_RH: {
+      const float s = sinf(theta);
+      return 30 * cosf(theta) * cosf(4 * phi) * (s * s * s * s) + 0.1f * sinf(theta) * cosf(30 * theta);
     }
     case CMM_VORT_GAUSSIAN_JETS: {
       const float lat = pi / 2 - theta;

@@ -266,6 +266,7 @@ int cmm_advect_project_noalloc(const cmm_mesh* mesh, const cmm_mesh* velmesh,
 #define CMM_VORT_GAUSSIAN_VORTEX 5 /* gaussian_vortex, :200-203 */
 #define CMM_VORT_GAUSSIAN_JETS 6   /* params: amplitude, width (rad), n <= 9,
                                       latitudes (rad): sum A exp(-((lat-l_j)/w)^2) */
+#define CMM_VORT_PERTURBED_RH 7    /* perturbed_rossby_wave, :213-215 */
 
 /* omega at the sample rings of `velmesh` (L+1,2L) from the back-traced
  * sample points X ((L+1)*2L, 3): omega0(X) + 2 rot cos(theta(X)) -

@@ -15,6 +15,11 @@ def rossby_wave(phi, theta, t=0.0):
     return 30 * np.cos(theta) * np.cos(4 * (phi + 2 * Omega * alpha * t)) * np.sin(theta) ** 4
 
 
+def perturbed_rossby_wave(phi, theta):
+    """dynamical_fields.py:213-215."""
+    return 30 * np.cos(theta) * np.cos(4 * phi) * np.sin(theta) ** 4 + 0.1 * np.sin(theta) * np.cos(30 * theta)
+
+
 def zonal_jet(phi, theta):
     """dynamical_fields.py:181-186."""
     beta2 = 12 ** 2

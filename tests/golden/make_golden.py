@@ -210,6 +210,16 @@ def main():
     save("scalar_L8.npz", alm_half=half, vals=sp.vals, coeffs=sp.coeffs, phi=PH, theta=TH,
          value=sp(PH.copy(), TH.copy()))
 
+    # ---- initial vorticity fields at scattered points ----------------------
+    Xf = random_sphere_points(400, seed=41)
+    phi, theta = rutils.cart2sphere(Xf.T)
+    fields = dict(X=Xf, rossby_wave=rfields.rossby_wave(phi, theta, t=0.3), zonal_jet=rfields.zonal_jet(phi, theta),
+                  perturbed_zonal_jet=rfields.perturbed_zonal_jet(phi, theta),
+                  multi_jet=rfields.multi_jet(phi, theta), gaussian_vortex=rfields.gaussian_vortex(phi, theta),
+                  perturbed_rossby_wave=rfields.perturbed_rossby_wave(phi, theta),
+                  rotating_frame=rfields.rotating_frame(phi, theta))
+    save("fields.npz", **fields)
+
     # ---- linear transport: analytic flows, tracers, a remapped run ----------
     m = ref_mesh(3)
     tris = np.asarray(m.simplices)
@@ -263,6 +273,20 @@ def main():
                                                   rot_rate=2 * np.pi, n_maps=5)
     qe = random_sphere_points(500, seed=99)
     save("bve_l2_L8.npz", vals=subs.vals[:subs.Nc], Nc=subs.Nc, ns=np.array(subs.ns), q=qe, img=subs(qe.copy()))
+
+    # ---- the reference's own files: the video driver's snapshot pickles and
+    # its pickled submap stack (read back by cmm_gpu.state_io)
+    import shutil
+    import tempfile
+    tmp = tempfile.mkdtemp()
+    try:
+        rsim.euler_simulation_sphere_remapping_video(8, 12, 1.0, m2, rfields.rossby_wave, 2 * np.pi, 5,
+                                                     os.path.join(tmp, "run"), 3)
+        for name in sorted(os.listdir(tmp)):
+            shutil.copy(os.path.join(tmp, name), os.path.join(HERE, "ref_video_l2_" + name.replace(".txt", ".pkl")))
+            print("wrote", os.path.join(HERE, "ref_video_l2_" + name.replace(".txt", ".pkl")))
+    finally:
+        shutil.rmtree(tmp)
 
 
 if __name__ == "__main__":

@@ -195,3 +195,90 @@ def ctypes_int():
 def byref(x):
     import ctypes
     return ctypes.byref(x)
+
+
+def test_vorticity_fields_match_reference(sims):
+    """Every built-in initial-vorticity field at scattered points (with the
+    planetary term off) against the reference's dynamical_fields values."""
+    from cmm_gpu import native
+    from cmm_gpu.meshgen import latlon_mesh_arrays
+    d = np.load(os.path.join(GOLDEN, "fields.npz"))
+    X = d["X"]
+    L = 14                                  # (L+1) 2L = 420 >= 400 sample slots
+    theta, phi, grid, vverts = latlon_mesh_arrays(L)
+    vm = native.VelMesh(L, theta, phi, grid, vverts)
+    Xp = np.concatenate([X, np.tile([[0.0, 0.0, 1.0]], ((L + 1) * 2 * L - len(X), 1))])
+    cases = [(native.VORT_ROSSBY_HAURWITZ, [0.3], "rossby_wave"), (native.VORT_ZONAL_JET, [], "zonal_jet"),
+             (native.VORT_PERTURBED_JET, [], "perturbed_zonal_jet"), (native.VORT_MULTI_JET, [], "multi_jet"),
+             (native.VORT_GAUSSIAN_VORTEX, [], "gaussian_vortex"),
+             (native.VORT_PERTURBED_RH, [], "perturbed_rossby_wave")]
+    for kind, params, name in cases:
+        om = vm.vorticity(kind, params, dev(Xp), 0.0).cpu().numpy().reshape(-1)[:len(X)]
+        scale = np.abs(d[name]).max()
+        np.testing.assert_allclose(om, d[name], rtol=0, atol=1e-12 * scale + 1e-14, err_msg=name)
+    assert vm.status() == 0
+
+
+def _ref_mesh_l2():
+    """The level-2 mesh with the reference's (Qhull) triangle table."""
+    from cmm_gpu.meshgen import icosahedral_mesh
+    from cmm_gpu.mesh_functions import spherical_triangulation
+    verts, _ = icosahedral_mesh(2)
+    return spherical_triangulation(verts, OG.QhullLocator(verts).tris)
+
+
+def test_video_driver_writes_the_reference_snapshots(sims, tmp_path):
+    """euler_simulation_sphere_remapping_video: the snapshot pickles at
+    steps 3, 6, 9 against the ones the reference's video driver wrote for
+    the same run, and the returned submaps against its pickled stack."""
+    from cmm_gpu import state_io
+    mesh = _ref_mesh_l2()
+    comp = sims.euler_simulation_sphere_remapping_video(8, 12, 1.0, mesh, "rossby_wave", 2 * np.pi, 5,
+                                                        str(tmp_path / "run"), 3)
+    for count in (3, 6, 9):
+        ours = state_io.read_reference_snapshot(str(tmp_path / f"run{count}.txt"))
+        ref = state_io.read_reference_snapshot(os.path.join(GOLDEN, f"ref_video_l2_run{count}.pkl"))
+        assert ours["Nc"] == ref["Nc"]
+        np.testing.assert_allclose(ours["vals"][:, 0], ref["vals"][:, 0], rtol=0, atol=1e-9)
+    stack = np.load(str(tmp_path / "run_all_maps.npz"))
+    r = state_io.reference_submaps(os.path.join(GOLDEN, "ref_video_l2_run_all_maps.pkl"))
+    assert int(stack["Nc"]) == r["Nc"] == comp.Nc and list(stack["ns"]) == r["ns"]
+    np.testing.assert_allclose(stack["vals"][:r["Nc"], :, 0], r["vals"][:r["Nc"], :, 0], rtol=0, atol=1e-9)
+
+
+def test_reference_submap_pickle_evaluates_on_the_gpu(sims):
+    """The reference's pickled composite, loaded by the restricted reader and
+    assembled on the GPU, maps query points as the reference's object did."""
+    from cmm_gpu import state_io
+    d = np.load(os.path.join(GOLDEN, "bve_l2_L8.npz"))
+    mesh, comp = state_io.composite_from_reference(os.path.join(GOLDEN, "ref_video_l2_run_all_maps.pkl"))
+    img = comp(dev(d["q"])).cpu().numpy()
+    np.testing.assert_allclose(img, d["img"], rtol=0, atol=1e-12)
+    assert mesh.native.status() == 0
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split_bf16"])
+def test_checkpoint_resume_is_bit_identical(sims, tmp_path, precision):
+    """Stop after 7 of 22 steps, write the checkpoint, resume it in a fresh
+    solver: the rest of the run is bit-identical to the uninterrupted one."""
+    from cmm_gpu.meshgen import icosahedral_mesh
+    verts, tris = icosahedral_mesh(3)
+    args = (verts, tris, 3, 16, 24, 0.5, "rossby_wave")
+    kw = dict(n_maps=5, precision=precision)
+    a = sims.BVESolver(*args, **kw).run()
+    b = sims.BVESolver(*args, **kw)
+    b.bootstrap()
+    for _ in range(7):
+        b.step()
+    b.save_state(str(tmp_path / "ck.npz"))
+    del b
+    c = sims.BVESolver(*args, **kw).load_state(str(tmp_path / "ck.npz"))
+    for _ in range(24 - 2 - 7):
+        c.step()
+    assert (c.count, c.Nc, c.identity) == (a.count, a.Nc, a.identity)
+    q = dev(np.random.default_rng(8).standard_normal((500, 3)))
+    q = q / q.norm(dim=1, keepdim=True)
+    assert torch.equal(a.composite(q)[0], c.composite(q)[0])
+    assert torch.equal(a.omega, c.omega)
+    with pytest.raises(ValueError):
+        sims.BVESolver(verts, tris, 3, 16, 24, 0.5, "zonal_jet", **kw).load_state(str(tmp_path / "ck.npz"))

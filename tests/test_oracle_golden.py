@@ -221,3 +221,13 @@ def test_transport_run_with_remaps():
     np.testing.assert_allclose(comp(d["q"]), d["evals"], rtol=0, atol=1e-13)
     rk2 = EV.advect_project(None, EV.rk2_back, 0.0, 0.05, TR.make_flow("u_sbr"), verts, s_pts, tan, True)
     np.testing.assert_allclose(rk2, d["jets_rk2_sbr"], rtol=0, atol=1e-10)
+
+
+def test_vorticity_fields():
+    """The restated initial-vorticity fields against dynamical_fields."""
+    from oracle import fields as F
+    d = load("fields.npz")
+    phi, theta = G.cart2sphere(d["X"].T)
+    np.testing.assert_allclose(F.rossby_wave(phi, theta, t=0.3), d["rossby_wave"], rtol=1e-13, atol=1e-13)
+    for name in ("zonal_jet", "perturbed_zonal_jet", "multi_jet", "gaussian_vortex", "perturbed_rossby_wave"):
+        np.testing.assert_allclose(getattr(F, name)(phi, theta), d[name], rtol=1e-13, atol=1e-13, err_msg=name)
