@@ -229,3 +229,44 @@ def test_ordered_compose_bitwise_equal(nat, level, n):
         step = np.linalg.norm(pts[1:] - pts[:-1], axis=1)
         assert np.median(step) < 0.1, np.median(step)
     assert mesh.status(clear=True) == 0
+
+
+def test_full_size_composition_properties(nat):
+    """The map-evaluation workload at full size (level 7, 8 submaps, 2^24
+    queries, ids and Jacobians), through size-independent properties:
+    images on the sphere; composing the stack in two launches (submaps 4-7,
+    then 0-3) gives the same points bit for bit and the chain-rule product
+    of the two Jacobians; the ids of the first submap applied equal plain
+    location; and a 4096-query sample matches the oracle (1e-12 points,
+    1e-10 relative Jacobians)."""
+    from cmm_gpu.meshgen import icosahedral_mesh, random_sphere_points, stencil_frames
+    from cmm_gpu.workloads import submap_stack
+    verts, tris = icosahedral_mesh(7)
+    tan, s_pts = stencil_frames(verts)
+    jets = submap_stack(s_pts, tan, 8, seed=1)
+    m = nat.Mesh(verts, tris, 7)
+    cs = [m.assemble(dev(j)) for j in jets]
+    q = dev(random_sphere_points(1 << 24, seed=3))
+    X, tri, _, J = m.compose(cs, q, want_tri=True, want_jac=True)
+    assert float((X.norm(dim=1) - 1).abs().max()) < 1e-15
+    Y, _, _, JB = m.compose(cs[4:], q, want_jac=True)
+    X2, _, _, JA = m.compose(cs[:4], Y, want_jac=True)
+    assert torch.equal(X, X2)
+    del X2, Y
+    JJ = torch.bmm(JA, JB)
+    del JA, JB
+    rel = float(((JJ - J).abs().amax(dim=(1, 2)) / J.abs().amax(dim=(1, 2))).max())
+    assert rel < 1e-12, rel
+    del JJ
+    t0, _ = m.locate(q)
+    assert torch.equal(t0, tri)
+    assert m.status() == 0
+    # oracle on a sample
+    idx = np.random.default_rng(0).choice(1 << 24, 4096, replace=False)
+    qs = host(q[torch.from_numpy(idx).cuda()])
+    comp = OS.CompositeOracle(verts, tris, OG.ConeLocator(verts, tris), jets, tie_fix=True)
+    np.testing.assert_allclose(host(X)[idx], comp(qs), rtol=0, atol=1e-12)
+    _, Jo = OS.composite_jacobian(comp, qs)
+    Jg = host(J)[idx]
+    scale = np.abs(Jo).max(axis=(1, 2))[:, None, None]
+    np.testing.assert_allclose(Jg / scale, Jo / scale, rtol=0, atol=1e-10)
