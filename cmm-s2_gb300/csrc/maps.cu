@@ -48,25 +48,21 @@ struct DevSubmaps {
   __device__ __forceinline__ const double* at(int s, int S) const { return s < S - 1 ? tab[s] : last; }
 };
 
-// Tangent image of w under one normalised submap: dS = (dP - s (s.dP)) / |P|.
-__device__ __forceinline__ void push_tangent(const double* L, const Split& sp, const Gam& g,
-                                             const Ords<3>& o, const double* s, double inv_n,
-                                             double* w) {
+// Half the patch derivative along w, DP(p)[w] / 2, with the partials
+// dP/dgamma / 2 of the three components given (pd[c] = (pV, pE, pC)).  The
+// composition chains these unprojected, unnormalised derivatives and
+// projects and rescales only where it normalises the point (below).
+__device__ __forceinline__ void push_half(const double* L, const Split& sp, const double (*pd)[3],
+                                          double* w) {
   const Bcc d = bcc_of(L, w[0], w[1], w[2]);
   const double dl = pick(d, sp.lo), dm = pick(d, sp.mid), dh = pick(d, sp.hi);
-  double dV = dh - dm, dE = edge_norm(L, sp.hi, sp.mid) * (dm - dl), dC = L[9] * dl;
-  double dP[3];
+  const double dV = dh - dm, dE = edge_norm(L, sp.hi, sp.mid) * (dm - dl), dC = L[9] * dl;
 #pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    double pV = g.V * o.c[0][c] + g.E * o.c[3][c] + g.C * o.c[5][c];
-    double pE = g.E * o.c[1][c] + g.V * o.c[3][c] + g.C * o.c[4][c];
-    double pC = g.C * o.c[2][c] + g.E * o.c[4][c] + g.V * o.c[5][c];
-    dP[c] = 2 * (pV * dV + pE * dE + pC * dC);
-  }
-  double sd = s[0] * dP[0] + s[1] * dP[1] + s[2] * dP[2];
-#pragma unroll
-  for (int c = 0; c < 3; ++c) w[c] = (dP[c] - s[c] * sd) * inv_n;
+  for (int c = 0; c < 3; ++c) w[c] = pd[c][0] * dV + pd[c][1] * dE + pd[c][2] * dC;
 }
+
+// 2^m as a double, from its bit pattern (0 <= m <= 4 here)
+__device__ __forceinline__ double pow2(int m) { return __longlong_as_double((long long)(1023 + m) << 52); }
 
 __global__ void __launch_bounds__(kBlock) locate_kernel(MeshView m, const double* __restrict__ q,
                                                         int64_t n, int32_t* __restrict__ tri,
@@ -254,6 +250,7 @@ __global__ void __launch_bounds__(kBlock) compose_kernel(MeshView m, Src cp,
       continue;
     }
     double t1[3], t2[3], w1[3], w2[3];
+    int since = 0;   // submaps pushed since the last normalisation
     if (JAC) {  // orthonormal tangent basis at q
       double ax = fabs(p[2]) < 0.9 ? 0.0 : 1.0, az = 1.0 - ax;
       t1[0] = p[1] * az;
@@ -279,26 +276,48 @@ __global__ void __launch_bounds__(kBlock) compose_kernel(MeshView m, Src cp,
       load_ords<3>(cp.at(s, S) + (int64_t)t * kCoeffStride3, sp, o);
       double P[3];
       sbb<3>(o, g, P);
-      if (!JAC && (s & 3) != 0) {
-        // Location, barycentrics and sub-triangle choice are invariant under
-        // p -> lambda p (lambda > 0) and the patch is homogeneous of degree
-        // 2, so the projection onto the sphere can wait: normalising every
-        // fourth submap (and the result) keeps |p| within ~1e-4 of 1
-        // (|P| = 1 + O(h^3) per submap) and saves the FP64 square root.
+      if (JAC) {
+        double pd[3][3];   // dP/dgamma / 2 per component
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          pd[c][0] = g.V * o.c[0][c] + g.E * o.c[3][c] + g.C * o.c[5][c];
+          pd[c][1] = g.E * o.c[1][c] + g.V * o.c[3][c] + g.C * o.c[4][c];
+          pd[c][2] = g.C * o.c[2][c] + g.E * o.c[4][c] + g.V * o.c[5][c];
+        }
+        push_half(Lr, sp, pd, w1);
+        push_half(Lr, sp, pd, w2);
+        ++since;
+      }
+      // Location, barycentrics and sub-triangle choice are invariant under
+      // p -> lambda p (lambda > 0) and the patch is homogeneous of degree 2,
+      // so the projection onto the sphere can wait: normalising every fourth
+      // submap (and the result) keeps |p| within ~1e-4 of 1 (|P| = 1 +
+      // O(h^3) per submap) and saves the FP64 square root.  The tangent
+      // pushes then carry exactly the factor |p| / 2^(submaps since the last
+      // normalisation) against the normalised chain, and their components
+      // along p stay along p (DP(p)[p] = 2 P); both are removed where the
+      // point is normalised.
+      if ((s & 3) != 0) {
         p[0] = P[0];
         p[1] = P[1];
         p[2] = P[2];
         continue;
       }
       const double inv_n = rsqrt(P[0] * P[0] + P[1] * P[1] + P[2] * P[2]);
-      double sN[3] = {P[0] * inv_n, P[1] * inv_n, P[2] * inv_n};
+      p[0] = P[0] * inv_n;
+      p[1] = P[1] * inv_n;
+      p[2] = P[2] * inv_n;
       if (JAC) {
-        push_tangent(Lr, sp, g, o, sN, inv_n, w1);
-        push_tangent(Lr, sp, g, o, sN, inv_n, w2);
+        const double sc = inv_n * pow2(since);
+        since = 0;
+        const double d1 = p[0] * w1[0] + p[1] * w1[1] + p[2] * w1[2];
+        const double d2 = p[0] * w2[0] + p[1] * w2[1] + p[2] * w2[2];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          w1[c] = (w1[c] - p[c] * d1) * sc;
+          w2[c] = (w2[c] - p[c] * d2) * sc;
+        }
       }
-      p[0] = sN[0];
-      p[1] = sN[1];
-      p[2] = sN[2];
     }
     if (!finite3(p[0], p[1], p[2])) flag(m, CMM_FLAG_NONFINITE);
     out[3 * i] = p[0];
