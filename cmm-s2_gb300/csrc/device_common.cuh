@@ -37,9 +37,21 @@ __device__ __forceinline__ bool plane_pos(const float* nf, const double* nd, flo
   return td > 0.0;
 }
 
+// x as a float truncated toward zero (0 below 2^-126; |x| < 2^128), from
+// its bit pattern on the integer pipe: a rounding conversion would occupy
+// the FP64 pipe, the one that bounds the composition.  Within one FP32 ulp
+// of x, which the filter bound kFilter covers with margin.
+__device__ __forceinline__ float to_f32_trunc(double x) {
+  const long long b = __double_as_longlong(x);
+  const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+  const unsigned mag = hi & 0x7fffffffu;
+  const unsigned f = mag < (897u << 20) ? 0u : (((mag - (896u << 20)) << 3) | (lo >> 29));
+  return __uint_as_float((hi & 0x80000000u) | f);
+}
+
 // Reference row of the icosahedral triangle containing q.
 __device__ __forceinline__ int locate_row(const MeshView& m, double x, double y, double z) {
-  const float fx = (float)x, fy = (float)y, fz = (float)z;
+  const float fx = to_f32_trunc(x), fy = to_f32_trunc(y), fz = to_f32_trunc(z);
   // root face: nearest face centre (FP32), then exact edge checks with a
   // bounded walk across a violated edge
   const float* rf = m.root_f;

@@ -275,18 +275,24 @@ __global__ void __launch_bounds__(kBlock) compose_kernel(MeshView m, Src cp,
       Ords<3> o;
       load_ords<3>(cp.at(s, S) + (int64_t)t * kCoeffStride3, sp, o);
       double P[3];
-      sbb<3>(o, g, P);
       if (JAC) {
+        // The patch is the quadratic form P_c = gamma^T M_c gamma of the
+        // symmetric ordinate matrix M_c; its half gradient M_c gamma (9
+        // FMA-chains) serves the two tangent pushes and gives the value
+        // with three more operations per component.
         double pd[3][3];   // dP/dgamma / 2 per component
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
           pd[c][0] = g.V * o.c[0][c] + g.E * o.c[3][c] + g.C * o.c[5][c];
           pd[c][1] = g.E * o.c[1][c] + g.V * o.c[3][c] + g.C * o.c[4][c];
           pd[c][2] = g.C * o.c[2][c] + g.E * o.c[4][c] + g.V * o.c[5][c];
+          P[c] = g.V * pd[c][0] + g.E * pd[c][1] + g.C * pd[c][2];
         }
         push_half(Lr, sp, pd, w1);
         push_half(Lr, sp, pd, w2);
         ++since;
+      } else {
+        sbb<3>(o, g, P);
       }
       // Location, barycentrics and sub-triangle choice are invariant under
       // p -> lambda p (lambda > 0) and the patch is homogeneous of degree 2,
