@@ -48,17 +48,19 @@ struct DevSubmaps {
   __device__ __forceinline__ const double* at(int s, int S) const { return s < S - 1 ? tab[s] : last; }
 };
 
-// Half the patch derivative along w, DP(p)[w] / 2, with the partials
-// dP/dgamma / 2 of the three components given (pd[c] = (pV, pE, pC)).  The
-// composition chains these unprojected, unnormalised derivatives and
-// projects and rescales only where it normalises the point (below).
-__device__ __forceinline__ void push_half(const double* L, const Split& sp, const double (*pd)[3],
-                                          double* w) {
-  const Bcc d = bcc_of(L, w[0], w[1], w[2]);
-  const double dl = pick(d, sp.lo), dm = pick(d, sp.mid), dh = pick(d, sp.hi);
-  const double dV = dh - dm, dE = edge_norm(L, sp.hi, sp.mid) * (dm - dl), dC = L[9] * dl;
-#pragma unroll
-  for (int c = 0; c < 3; ++c) w[c] = pd[c][0] * dV + pd[c][1] * dE + pd[c][2] * dC;
+// Orthonormal tangent basis (t1, t2) at the unit point p.
+__device__ __forceinline__ void tangent_basis(const double* p, double* t1, double* t2) {
+  const double ax = fabs(p[2]) < 0.9 ? 0.0 : 1.0, az = 1.0 - ax;
+  t1[0] = p[1] * az;
+  t1[1] = p[2] * ax - p[0] * az;
+  t1[2] = -p[1] * ax;
+  const double in = rsqrt(t1[0] * t1[0] + t1[1] * t1[1] + t1[2] * t1[2]);
+  t1[0] *= in;
+  t1[1] *= in;
+  t1[2] *= in;
+  t2[0] = p[1] * t1[2] - p[2] * t1[1];
+  t2[1] = p[2] * t1[0] - p[0] * t1[2];
+  t2[2] = p[0] * t1[1] - p[1] * t1[0];
 }
 
 // 2^m as a double, from its bit pattern (0 <= m <= 4 here)
@@ -258,20 +260,9 @@ __global__ void __launch_bounds__(kBlock, ComposeOccupancy<JAC>::kMinBlocks) com
         for (int k = 0; k < 9; ++k) jac[9 * i + k] = nan("");
       continue;
     }
-    double t1[3], t2[3], w1[3], w2[3];
+    double w1[3], w2[3];
     int since = 0;   // submaps pushed since the last normalisation
-    if (JAC) {  // orthonormal tangent basis at q
-      double ax = fabs(p[2]) < 0.9 ? 0.0 : 1.0, az = 1.0 - ax;
-      t1[0] = p[1] * az;
-      t1[1] = p[2] * ax - p[0] * az;
-      t1[2] = -p[1] * ax;
-      double in = rsqrt(t1[0] * t1[0] + t1[1] * t1[1] + t1[2] * t1[2]);
-      t1[0] *= in; t1[1] *= in; t1[2] *= in;
-      t2[0] = p[1] * t1[2] - p[2] * t1[1];
-      t2[1] = p[2] * t1[0] - p[0] * t1[2];
-      t2[2] = p[0] * t1[1] - p[1] * t1[0];
-      for (int c = 0; c < 3; ++c) { w1[c] = t1[c]; w2[c] = t2[c]; }
-    }
+    if (JAC) tangent_basis(p, w1, w2);   // pushed from the tangent basis at q
     for (int s = S - 1; s >= 0; --s) {
       const int t = locate_row(m, p[0], p[1], p[2]);
       if (s == S - 1 && tri) tri[i] = t;
@@ -281,26 +272,35 @@ __global__ void __launch_bounds__(kBlock, ComposeOccupancy<JAC>::kMinBlocks) com
       const Bcc b = bcc_of(Lr, p[0], p[1], p[2]);
       const Split sp = split_of(b);
       const Gam g = gamma_of(Lr, b, sp);
-      Ords<3> o;
-      load_ords<3>(cp.at(s, S) + (int64_t)t * kCoeffStride3, sp, o);
+      const double* rec = cp.at(s, S) + (int64_t)t * kCoeffStride3;
       double P[3];
       if (JAC) {
         // The patch is the quadratic form P_c = gamma^T M_c gamma of the
-        // symmetric ordinate matrix M_c; its half gradient M_c gamma (9
-        // FMA-chains) serves the two tangent pushes and gives the value
-        // with three more operations per component.
-        double pd[3][3];   // dP/dgamma / 2 per component
+        // symmetric ordinate matrix M_c; its half gradient M_c gamma serves
+        // the two tangent pushes (half derivatives along dgamma = T L w) and
+        // gives the value with three more operations per component.  The
+        // pushes' barycentric directions are formed first and the ordinates
+        // consumed one component at a time, which keeps the loop within 64
+        // registers.
+        const Gam e1 = gamma_of(Lr, bcc_of(Lr, w1[0], w1[1], w1[2]), sp);
+        const Gam e2 = gamma_of(Lr, bcc_of(Lr, w2[0], w2[1], w2[2]), sp);
+        const int* id = kSplitOrd[sp.lo][sp.hi];
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-          pd[c][0] = g.V * o.c[0][c] + g.E * o.c[3][c] + g.C * o.c[5][c];
-          pd[c][1] = g.E * o.c[1][c] + g.V * o.c[3][c] + g.C * o.c[4][c];
-          pd[c][2] = g.C * o.c[2][c] + g.E * o.c[4][c] + g.V * o.c[5][c];
-          P[c] = g.V * pd[c][0] + g.E * pd[c][1] + g.C * pd[c][2];
+          double o[6];
+#pragma unroll
+          for (int k = 0; k < 6; ++k) o[k] = __ldg(rec + 3 * id[k] + c);
+          const double pV = g.V * o[0] + g.E * o[3] + g.C * o[5];
+          const double pE = g.E * o[1] + g.V * o[3] + g.C * o[4];
+          const double pC = g.C * o[2] + g.E * o[4] + g.V * o[5];
+          P[c] = g.V * pV + g.E * pE + g.C * pC;
+          w1[c] = pV * e1.V + pE * e1.E + pC * e1.C;
+          w2[c] = pV * e2.V + pE * e2.E + pC * e2.C;
         }
-        push_half(Lr, sp, pd, w1);
-        push_half(Lr, sp, pd, w2);
         ++since;
       } else {
+        Ords<3> o;
+        load_ords<3>(rec, sp, o);
         sbb<3>(o, g, P);
       }
       // Location, barycentrics and sub-triangle choice are invariant under
@@ -339,6 +339,11 @@ __global__ void __launch_bounds__(kBlock, ComposeOccupancy<JAC>::kMinBlocks) com
     out[3 * i + 1] = p[1];
     out[3 * i + 2] = p[2];
     if (JAC) {
+      // the basis again, from q re-read (cheaper than keeping it in
+      // registers across the submap loop)
+      const double q0[3] = {q[3 * i], q[3 * i + 1], q[3 * i + 2]};
+      double t1[3], t2[3];
+      tangent_basis(q0, t1, t2);
 #pragma unroll
       for (int a = 0; a < 3; ++a)
 #pragma unroll
