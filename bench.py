@@ -43,15 +43,15 @@ LEVEL, SUBMAPS = 7, 8
 METRIC = "map evals/s"
 # DRAM bytes (read + write) of one compose launch per query, from the ncu
 # capture of 2^22 queries summarised in profiles/compose_level7.md
-# (18.348 GB + 0.420 GB); the gathers scale with the number of queries.
-COMPOSE_TRAFFIC_PER_QUERY = (18.348423e9 + 0.420334e9) / (1 << 22)
+# (18.671 GB + 1.118 GB); the gathers scale with the number of queries.
+COMPOSE_TRAFFIC_PER_QUERY = (18.671e9 + 1.118e9) / (1 << 22)
 # The same with the queries grouped by coarse cell (cmm_query_order), from
-# the capture of 2^22 queries in profiles/compose_level7.md (2.856 GB read
-# + 0.719 GB written: the output rows are now scattered).
-COMPOSE_TRAFFIC_PER_QUERY_ORDERED = (2.856423424e9 + 0.719421696e9) / (1 << 22)
-# FP64 instructions per map evaluation (query x submap) with Jacobians,
-# from the same capture (FP64 pipe 88.6 % busy for 9.599 ms).
-FP64_INSTR_PER_EVAL = 152
+# the same capture (3.101 GB read + 0.961 GB written: the output rows are
+# scattered).
+COMPOSE_TRAFFIC_PER_QUERY_ORDERED = (3.101e9 + 0.961e9) / (1 << 22)
+# FP64-pipe instructions per map evaluation (query x submap) with the
+# Jacobian, from the same capture (sm__thread_inst_executed_pipe_fp64).
+FP64_INSTR_PER_EVAL = 110.4
 
 
 def peaks():
