@@ -94,7 +94,7 @@ for _name, (_res, _args) in _SIGS.items():
 
 STATUS = {0: "OK", 1: "ERR_ARG", 2: "ERR_MESH", 3: "ERR_CUDA", 4: "ERR_NONFINITE", 5: "ERR_LOCATE",
           6: "ERR_TIMEOUT", 7: "ERR_UNSUPPORTED"}
-FLAG_NONFINITE, FLAG_LOCATE = 1, 2
+FLAG_NONFINITE, FLAG_LOCATE, FLAG_TIMEOUT, FLAG_INDEX = 1, 2, 4, 8
 
 
 class CmmError(RuntimeError):

@@ -249,6 +249,10 @@ __global__ void __launch_bounds__(kBlock, ComposeOccupancy<JAC>::kMinBlocks) com
   for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n;
        j += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = perm ? (int64_t)__ldg(perm + j) : j;
+    if ((uint64_t)i >= (uint64_t)n) {   // a bad permutation entry
+      flag(m, CMM_FLAG_INDEX);
+      continue;
+    }
     double p[3] = {q[3 * i], q[3 * i + 1], q[3 * i + 2]};
     if (!finite3(p[0], p[1], p[2])) {
       flag(m, CMM_FLAG_NONFINITE);

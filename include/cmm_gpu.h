@@ -47,6 +47,7 @@ typedef enum {
 #define CMM_FLAG_NONFINITE 1
 #define CMM_FLAG_LOCATE 2
 #define CMM_FLAG_TIMEOUT 4   /* a bounded wait inside a kernel ran out */
+#define CMM_FLAG_INDEX 8     /* an index argument (a permutation entry) was out of range; skipped */
 
 const char* cmm_last_error(void);
 int cmm_version(void);
@@ -168,7 +169,8 @@ int cmm_query_order(const cmm_mesh* mesh, const double* q, int64_t n, int32_t* p
 
 /* cmm_compose with the queries processed in the order perm (a permutation
  * of 0..n-1, e.g. from cmm_query_order); every output stays in its query's
- * own slot and is bitwise equal to cmm_compose's. */
+ * own slot and is bitwise equal to cmm_compose's.  An entry outside
+ * [0, n) is skipped and sets CMM_FLAG_INDEX. */
 int cmm_compose_ordered(const cmm_mesh* mesh, const double* const* coeffs, int S, const double* q,
                         int64_t n, const int32_t* perm, double* out, int32_t* tri,
                         int32_t* tri_all, double* jac, void* stream);

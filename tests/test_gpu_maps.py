@@ -270,3 +270,26 @@ def test_full_size_composition_properties(nat):
     Jg = host(J)[idx]
     scale = np.abs(Jo).max(axis=(1, 2))[:, None, None]
     np.testing.assert_allclose(Jg / scale, Jo / scale, rtol=0, atol=1e-10)
+
+
+def test_ordered_compose_rejects_bad_permutation_entries(nat):
+    """Entries outside [0, n) are skipped by the kernel's own bounds check and
+    reported as CMM_FLAG_INDEX; every other query is composed as usual."""
+    from cmm_gpu.meshgen import icosahedral_mesh, random_sphere_points
+    from cmm_gpu.workloads import submap_stack
+    verts, tris = icosahedral_mesh(3)
+    mesh = nat.Mesh(verts, tris, 3)
+    tan, s_pts = OG.stencil_points(verts)
+    coeffs = [mesh.assemble(dev(j)) for j in submap_stack(s_pts, tan, 2, seed=5)]
+    n = 1000
+    q = dev(random_sphere_points(n, seed=8))
+    perm = torch.arange(n, dtype=torch.int32, device="cuda")
+    perm[3], perm[5] = n + 7, -2          # queries 3 and 5 are then never visited
+    ref = mesh.compose(coeffs, q)[0]
+    out = torch.full((n, 3), 7.0, dtype=torch.float64, device="cuda")
+    mesh.compose(coeffs, q, out=out, perm=perm)
+    assert mesh.status(clear=True) == nat.FLAG_INDEX
+    keep = torch.ones(n, dtype=torch.bool, device="cuda")
+    keep[[3, 5]] = False
+    assert torch.equal(out[keep], ref[keep])
+    assert bool((out[~keep] == 7.0).all())
