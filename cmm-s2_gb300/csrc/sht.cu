@@ -391,6 +391,139 @@ __global__ void __launch_bounds__(kSynthBlock) synthesis_kernel(const double2* _
   }
 }
 
+// ------------------------------------- small band-limits: Pbar tables
+// At L <= kTabMaxL the recurrence kernels above run a few warps per SM
+// (one block per m, one thread per ring pair) and are latency-bound.  There
+// the Pbar_lm values are tabulated once per plan (FP64, the same
+// recurrence) and both Legendre stages become table contractions with one
+// thread per (m, l) (analysis) or per (m, ring pair, field group)
+// (synthesis): L^3/2 and L^3/4 doubles, 68 + 34 MB at L = 256.
+constexpr int kTabMaxL = 256;
+
+// offset of order m in a table with nj entries per (m, l): nj sum_{m'<m} (L - m')
+__device__ __host__ __forceinline__ int64_t tab_off(int m, int L, int nj) {
+  return (int64_t)nj * ((int64_t)m * L - (int64_t)m * (m - 1) / 2);
+}
+
+// One thread per (m, ring j): Pbar_{l,m}(theta_j), l = m..L-1.  lmajor:
+// layout [m][l-m][j] (synthesis) else [m][j][l-m] (analysis).
+__global__ void build_pbar_kernel(int L, int nj, const double* __restrict__ ct, const double* __restrict__ pmm,
+                                  int pmm_stride, const double* __restrict__ ra, const double* __restrict__ rb,
+                                  bool lmajor, double* __restrict__ tab) {
+  const int m = blockIdx.y, j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= nj) return;
+  const double x = ct[j];
+  double p0 = pmm[(int64_t)m * pmm_stride + j], p1 = 0.0;
+  double* base = tab + tab_off(m, L, nj);
+  const int nl = L - m;
+  for (int l = m; l < L; ++l) {
+    double P;
+    if (l == m) {
+      P = p0;
+    } else if (l == m + 1) {
+      P = ra[(int64_t)m * L + l] * x * p0;
+      p1 = p0;
+      p0 = P;
+    } else {
+      P = ra[(int64_t)m * L + l] * (x * p0 - rb[(int64_t)m * L + l] * p1);
+      p1 = p0;
+      p0 = P;
+    }
+    const int i = l - m;
+    base[lmajor ? (int64_t)i * nj + j : (int64_t)j * nl + i] = P;
+  }
+}
+
+// Analysis from the table: block (m, tile of 64 degrees), thread l; the
+// weighted even/odd ring spectra of order m staged in shared memory.
+constexpr int kTabBlock = 64;
+__global__ void __launch_bounds__(kTabBlock) analysis_tab_kernel(const double2* __restrict__ fine, int L,
+                                                                 const double* __restrict__ w,
+                                                                 const double* __restrict__ tab,
+                                                                 double2* __restrict__ alm) {
+  __shared__ double2 E[kTabMaxL + 1], O[kTabMaxL + 1];
+  const int m = blockIdx.x, l = m + blockIdx.y * kTabBlock + threadIdx.x;
+  if (m + (int)blockIdx.y * kTabBlock >= L) return;   // the whole tile is past l = L-1
+  const int npair = L + 1;
+  for (int j = threadIdx.x; j < npair; j += blockDim.x) {
+    const double2 a = fine[(int64_t)j * L + m];
+    double2 e, o;
+    if (j < L) {
+      const double2 b = fine[(int64_t)(2 * L - j) * L + m];
+      e = make_double2(a.x + b.x, a.y + b.y);
+      o = make_double2(a.x - b.x, a.y - b.y);
+    } else {
+      e = a;
+      o = make_double2(0.0, 0.0);
+    }
+    E[j] = cmul(e, w[j]);
+    O[j] = cmul(o, w[j]);
+  }
+  __syncthreads();
+  if (l >= L) return;
+  const int nl = L - m, i = l - m;
+  const double* P = tab + tab_off(m, L, npair) + i;
+  const double2* V = (i & 1) == 0 ? E : O;
+  double2 acc = make_double2(0.0, 0.0);
+  for (int j = 0; j < npair; ++j) {
+    const double pj = __ldg(P + (int64_t)j * nl);
+    acc.x += pj * V[j].x;
+    acc.y += pj * V[j].y;
+  }
+  alm[(int64_t)m * L + l] = acc;
+}
+
+// Synthesis from the table: block (m, tile of ring pairs, group of G
+// fields); each thread one ring pair (t, L-t) and G fields.
+template <int G>
+__global__ void __launch_bounds__(kTabBlock) synthesis_tab_kernel(const double2* __restrict__ alm, int L,
+                                                                  const double* __restrict__ tab,
+                                                                  double2* __restrict__ S) {
+  const int m = blockIdx.x, t = blockIdx.y * blockDim.x + threadIdx.x, f0 = blockIdx.z * G;
+  const int npair = L / 2 + 1;
+  const int64_t fs = (int64_t)L * L;
+  __shared__ double2 A[kLChunk][G];
+  double2 E[G], O[G];
+#pragma unroll
+  for (int f = 0; f < G; ++f) E[f] = O[f] = make_double2(0.0, 0.0);
+  const bool active = t < npair;
+  const double* P = tab + tab_off(m, L, npair) + (active ? t : 0);
+  for (int l0 = m; l0 < L; l0 += kLChunk) {
+    __syncthreads();
+    for (int e = threadIdx.x; e < kLChunk * G; e += blockDim.x) {
+      const int q = e / G, f = e % G, l = l0 + q;
+      A[q][f] = (l < L) ? alm[(f0 + f) * fs + (int64_t)m * L + l] : make_double2(0.0, 0.0);
+    }
+    __syncthreads();
+    const int qn = min(kLChunk, L - l0);
+    for (int q = 0; q < qn; ++q) {
+      const int l = l0 + q;
+      const double pv = active ? __ldg(P + (int64_t)(l - m) * npair) : 0.0;
+      if (((l - m) & 1) == 0) {
+#pragma unroll
+        for (int f = 0; f < G; ++f) {
+          E[f].x += pv * A[q][f].x;
+          E[f].y += pv * A[q][f].y;
+        }
+      } else {
+#pragma unroll
+        for (int f = 0; f < G; ++f) {
+          O[f].x += pv * A[q][f].x;
+          O[f].y += pv * A[q][f].y;
+        }
+      }
+    }
+  }
+  if (!active) return;
+  const int64_t row = L + 1;
+#pragma unroll
+  for (int f = 0; f < G; ++f) {
+    const int64_t base = (int64_t)(f0 + f) * (L + 1) * row;
+    S[base + (int64_t)t * row + m] = make_double2(E[f].x + O[f].x, E[f].y + O[f].y);
+    if (L - t != t) S[base + (int64_t)(L - t) * row + m] = make_double2(E[f].x - O[f].x, E[f].y - O[f].y);
+  }
+}
+
 // Velocity jets (project_stream, spherical_harmonic_tools.py:81-101) from
 // the 12 synthesised fields on the grid: vals[i][0] = u_i and, with
 // g = (iLx, iLy, iLz) u_i, vals[c][1+i] = (g x X - ((g x X).X/|X|) X)_c;
@@ -739,6 +872,7 @@ struct cmm_sht {
   cufftHandle ring_fwd = 0, torus_fwd = 0, pad_inv = 0, ring_inv = 0;
   bool have_plans[4] = {false, false, false, false};
   cmm::DeviceBuffer ct_rings, ct_fine, w_fine, pmm_rings, pmm_fine, ra, rb;
+  cmm::DeviceBuffer tab_a, tab_s;   // Pbar tables of the FP64 stages at small L
   cmm::DeviceBuffer spec, torus, pad, alm, fields, synth, samples, status;
   cmm::TcPlan* tc = nullptr;
   // split-BF16 form: FP32 ring FFTs and buffers, made with the tc plan
@@ -836,6 +970,24 @@ int sht_create(int L, cmm_sht** out) {
   if ((rc = p->pmm_fine.upload(pmm_f.data(), pmm_f.size() * 8))) return fail(rc);
   if ((rc = p->ra.upload(ra.data(), ra.size() * 8))) return fail(rc);
   if ((rc = p->rb.upload(rb.data(), rb.size() * 8))) return fail(rc);
+  if (L <= kTabMaxL) {
+    const int64_t tri = (int64_t)L * (L + 1) / 2;
+    const int na = L + 1, ns = L / 2 + 1;
+    if ((rc = p->tab_a.alloc((size_t)tri * na * 8)) || (rc = p->tab_s.alloc((size_t)tri * ns * 8)))
+      return fail(rc);
+    build_pbar_kernel<<<dim3((na + 127) / 128, L), 128>>>(L, na, (const double*)p->ct_fine.p,
+                                                          (const double*)p->pmm_fine.p, 2 * L + 1,
+                                                          (const double*)p->ra.p, (const double*)p->rb.p,
+                                                          false, (double*)p->tab_a.p);
+    if ((rc = check_launch("build_pbar_kernel"))) return fail(rc);
+    build_pbar_kernel<<<dim3((ns + 127) / 128, L), 128>>>(L, ns, (const double*)p->ct_rings.p,
+                                                          (const double*)p->pmm_rings.p, L + 1,
+                                                          (const double*)p->ra.p, (const double*)p->rb.p,
+                                                          true, (double*)p->tab_s.p);
+    if ((rc = check_launch("build_pbar_kernel"))) return fail(rc);
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return fail(cuda_fail(e, "cudaDeviceSynchronize"));
+  }
   const size_t c16 = sizeof(double2);
   if ((rc = p->spec.alloc((size_t)(L + 1) * (L + 1) * c16))) return fail(rc);
   if ((rc = p->torus.alloc((size_t)2 * L * L * c16))) return fail(rc);
@@ -962,6 +1114,11 @@ int sht_forward(cmm_sht* p, const double* samples, double2* out, cudaStream_t s)
     set_last_error("sht_forward: L too large for the analysis kernel");
     return CMM_ERR_UNSUPPORTED;
   }
+  if (p->tab_a.p) {
+    analysis_tab_kernel<<<dim3(L, (L + kTabBlock - 1) / kTabBlock), kTabBlock, 0, s>>>(
+        (const double2*)p->pad.p, L, (const double*)p->w_fine.p, (const double*)p->tab_a.p, out);
+    return check_launch("analysis_tab_kernel");
+  }
   analysis_kernel<<<L, 256, 0, s>>>((const double2*)p->pad.p, L, (const double*)p->w_fine.p,
                                     (const double*)p->ct_fine.p, (const double*)p->pmm_fine.p,
                                     (const double*)p->ra.p, (const double*)p->rb.p, out);
@@ -994,6 +1151,15 @@ int sht_inverse(cmm_sht* p, const double2* alm, int nf, double* samples, cudaStr
   cudaError_t e = cudaMemsetAsync(S, 0, (size_t)kFields * (L + 1) * (L + 1) * sizeof(double2), s);
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
   const int npair = L / 2 + 1;
+  if (p->tab_s.p && (nf == kFields || nf == 4 || nf == 1)) {
+    const int G = nf == kFields ? 3 : 1;
+    dim3 gt(L, (npair + kTabBlock - 1) / kTabBlock, nf / G);
+    if (G == 3)
+      synthesis_tab_kernel<3><<<gt, kTabBlock, 0, s>>>(alm, L, (const double*)p->tab_s.p, S);
+    else
+      synthesis_tab_kernel<1><<<gt, kTabBlock, 0, s>>>(alm, L, (const double*)p->tab_s.p, S);
+    if ((rc = check_launch("synthesis_tab_kernel"))) return rc;
+  } else {
   dim3 g(L, (npair + kSynthBlock - 1) / kSynthBlock);
   if (nf == kFields)
     synthesis_kernel<kFields><<<g, kSynthBlock, 0, s>>>(alm, L, (const double*)p->ct_rings.p,
@@ -1012,6 +1178,7 @@ int sht_inverse(cmm_sht* p, const double2* alm, int nf, double* samples, cudaStr
     return CMM_ERR_ARG;
   }
   if ((rc = check_launch("synthesis_kernel"))) return rc;
+  }
   // Z2D over kFields*(L+1) rows; only the first nf*(L+1) rows matter
   cufftResult r = cufftExecZ2D(p->ring_inv, (cufftDoubleComplex*)S, (cufftDoubleReal*)p->samples.p);
   if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExecZ2D");
