@@ -440,7 +440,11 @@ def bench_bve3(args, dev):
     scalar spline.  Each form runs the whole run (args.bve3_steps steps after
     the 2-step bootstrap); steps/s = steps / CUDA-event time of the loop.
     Also reported: the step time at the start (no submaps), the run's
-    diagnostics at the end and the split-vs-FP64 vorticity difference."""
+    diagnostics at the end and the split-vs-FP64 vorticity difference.  A
+    third run, `fp64_tables`, is the FP64 form with its Legendre stages
+    contracted against 6.5 GB of tabulated Pbar (cmm_sht_set_tables) instead
+    of the on-the-fly recurrence: the split form's speed-up over it is
+    reported beside the one over the plain FP64 form."""
     import torch
     from cmm_gpu.meshgen import icosahedral_mesh
     from cmm_gpu.workloads import spectral_perturbation
@@ -454,9 +458,11 @@ def bench_bve3(args, dev):
                        "remap every 10, 4 Gaussian zonal jets + 1% k^-3 l<=64 perturbation (spline)",
            "steps_timed": nsteps}
     omegas = {}
-    for form in ("fp64", "split_bf16"):
+    for form in ("fp64", "fp64_tables", "split_bf16"):
         t0 = time.perf_counter()
-        s = BVESolver(verts, tris, 7, 1024, Nt, 1.0, vort, n_maps=10, precision=form)
+        s = BVESolver(verts, tris, 7, 1024, Nt, 1.0, vort, n_maps=10,
+                      precision="split_bf16" if form == "split_bf16" else "fp64",
+                      fp64_tables=True if form == "fp64_tables" else None)
         s.bootstrap()
         torch.cuda.synchronize()
         setup = time.perf_counter() - t0
@@ -481,6 +487,9 @@ def bench_bve3(args, dev):
     dd = (omegas["split_bf16"] - omegas["fp64"]).abs().max().item()
     out["split_vs_fp64_omega_rel"] = dd / omegas["fp64"].abs().max().item()
     out["speedup_split_over_fp64"] = out["split_bf16"]["steps_per_s"] / out["fp64"]["steps_per_s"]
+    out["speedup_split_over_fp64_tables"] = out["split_bf16"]["steps_per_s"] / out["fp64_tables"]["steps_per_s"]
+    out["fp64_tables_vs_fp64_omega_rel"] = ((omegas["fp64_tables"] - omegas["fp64"]).abs().max().item() /
+                                            omegas["fp64"].abs().max().item())
     return out
 
 

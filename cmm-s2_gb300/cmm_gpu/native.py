@@ -67,6 +67,7 @@ _SIGS = {
     "cmm_sht_power": (_i, [_p, _p, _p, _p]),
     "cmm_sht_share_tables": (_i, [_p, _p]),
     "cmm_sht_trim": (_i, [_p]),
+    "cmm_sht_set_tables": (_i, [_p, _i]),
     "cmm_velmesh_set_records": (_i, [_p, _i]),
     "cmm_assemble_bwd": (_i, [_p, _p, _p, _p]),
     "cmm_compose_bwd": (_i, [_p, ctypes.POINTER(_p), _i, _p, _i64, _p, ctypes.POINTER(_p), _p, _p, _p]),
@@ -399,6 +400,14 @@ class Sht:
 
     def trim(self):
         check(lib.cmm_sht_trim(self.h), "cmm_sht_trim")
+        return self
+
+    TABLES_AUTO, TABLES_ALWAYS, TABLES_NEVER = 0, 1, -1
+
+    def set_tables(self, mode):
+        """FP64 Legendre stages from Pbar tables (cmm_sht_set_tables)."""
+        with torch.cuda.device(self.device):
+            check(lib.cmm_sht_set_tables(self.h, int(mode)), "cmm_sht_set_tables")
         return self
 
     def status(self, clear=True):

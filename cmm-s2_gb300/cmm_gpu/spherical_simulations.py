@@ -57,11 +57,13 @@ class Vorticity:
 
 class BVESolver:
     def __init__(self, verts, tris, level, L, Nt, T, vorticity, rot_rate=2 * np.pi, n_maps=10,
-                 device=None, precision="fp64", resources=None):
+                 device=None, precision="fp64", resources=None, fp64_tables=None):
         """verts, tris: the icosahedral mesh of `level` (reference row order);
         with `resources` (ensemble.SharedResources) they may be None and the
         mesh, stencil frames, velocity mesh, sample points and split-BF16
-        tables are taken from (and shared through) it."""
+        tables are taken from (and shared through) it.  fp64_tables: the
+        FP64 Legendre stages from Pbar tables (True), from the recurrence
+        (False) or by band-limit (None: tables for L <= 512)."""
         self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
         dev = self.device
         if precision not in ("fp64", "split_bf16"):
@@ -90,6 +92,8 @@ class BVESolver:
             self.sample_pts = torch.from_numpy(
                 np.ascontiguousarray(np.stack([g.reshape(-1) for g in grid], 1))).to(dev)
         self.sht = native.Sht(L, device=dev.index)
+        if fp64_tables is not None:
+            self.sht.set_tables(native.Sht.TABLES_ALWAYS if fp64_tables else native.Sht.TABLES_NEVER)
         if split:
             self.precision_mode = native.Sht.SPLIT_BF16
             src = resources.sht_tables(L) if resources is not None else None

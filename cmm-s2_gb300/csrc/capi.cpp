@@ -205,6 +205,11 @@ int cmm_sht_set_precision(cmm_sht* plan, int mode) {
   return sht_set_precision(plan, mode);
 }
 
+int cmm_sht_set_tables(cmm_sht* plan, int mode) {
+  if (!plan) return arg_error("cmm_sht_set_tables: null pointer");
+  return sht_set_tables(plan, mode);
+}
+
 int cmm_velmesh_set_records(cmm_mesh* velmesh, int precision) {
   if (!velmesh || velmesh->view.kind != kLatLon) return arg_error("cmm_velmesh_set_records: velocity mesh expected");
   if (precision != CMM_REC_FP64 && precision != CMM_REC_FP32 && precision != CMM_REC_MIXED)

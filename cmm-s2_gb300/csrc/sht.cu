@@ -392,13 +392,17 @@ __global__ void __launch_bounds__(kSynthBlock) synthesis_kernel(const double2* _
 }
 
 // ------------------------------------- small band-limits: Pbar tables
-// At L <= kTabMaxL the recurrence kernels above run a few warps per SM
-// (one block per m, one thread per ring pair) and are latency-bound.  There
-// the Pbar_lm values are tabulated once per plan (FP64, the same
+// At small L the recurrence kernels above run a few warps per SM (one
+// block per m, one thread per ring pair) and are latency-bound, and the
+// analysis spends 3 FP64 operations of recurrence per 2 of contraction.
+// With tables the Pbar_lm values are computed once per plan (FP64, the same
 // recurrence) and both Legendre stages become table contractions with one
 // thread per (m, l) (analysis) or per (m, ring pair, field group)
-// (synthesis): L^3/2 and L^3/4 doubles, 68 + 34 MB at L = 256.
-constexpr int kTabMaxL = 256;
+// (synthesis): L^3/2 and L^3/4 doubles, 68 + 34 MB at L = 256, 0.54 + 0.27
+// GB at L = 512, 4.3 + 2.2 GB at L = 1024.  By default (cmm_sht_set_tables)
+// plans with L <= kTabMaxL use them.
+constexpr int kTabMaxL = 512;
+constexpr int kTabShared = 1024;   // largest L the analysis kernel's shared arrays hold
 
 // offset of order m in a table with nj entries per (m, l): nj sum_{m'<m} (L - m')
 __device__ __host__ __forceinline__ int64_t tab_off(int m, int L, int nj) {
@@ -441,7 +445,7 @@ __global__ void __launch_bounds__(kTabBlock) analysis_tab_kernel(const double2* 
                                                                  const double* __restrict__ w,
                                                                  const double* __restrict__ tab,
                                                                  double2* __restrict__ alm) {
-  __shared__ double2 E[kTabMaxL + 1], O[kTabMaxL + 1];
+  __shared__ double2 E[kTabShared + 1], O[kTabShared + 1];
   const int m = blockIdx.x, l = m + blockIdx.y * kTabBlock + threadIdx.x;
   if (m + (int)blockIdx.y * kTabBlock >= L) return;   // the whole tile is past l = L-1
   const int npair = L + 1;
@@ -872,7 +876,8 @@ struct cmm_sht {
   cufftHandle ring_fwd = 0, torus_fwd = 0, pad_inv = 0, ring_inv = 0;
   bool have_plans[4] = {false, false, false, false};
   cmm::DeviceBuffer ct_rings, ct_fine, w_fine, pmm_rings, pmm_fine, ra, rb;
-  cmm::DeviceBuffer tab_a, tab_s;   // Pbar tables of the FP64 stages at small L
+  cmm::DeviceBuffer tab_a, tab_s;   // Pbar tables of the FP64 stages
+  int tab_mode = 0;                 // cmm_sht_set_tables: 0 auto, 1 always, -1 never
   cmm::DeviceBuffer spec, torus, pad, alm, fields, synth, samples, status;
   cmm::TcPlan* tc = nullptr;
   // split-BF16 form: FP32 ring FFTs and buffers, made with the tc plan
@@ -970,24 +975,6 @@ int sht_create(int L, cmm_sht** out) {
   if ((rc = p->pmm_fine.upload(pmm_f.data(), pmm_f.size() * 8))) return fail(rc);
   if ((rc = p->ra.upload(ra.data(), ra.size() * 8))) return fail(rc);
   if ((rc = p->rb.upload(rb.data(), rb.size() * 8))) return fail(rc);
-  if (L <= kTabMaxL) {
-    const int64_t tri = (int64_t)L * (L + 1) / 2;
-    const int na = L + 1, ns = L / 2 + 1;
-    if ((rc = p->tab_a.alloc((size_t)tri * na * 8)) || (rc = p->tab_s.alloc((size_t)tri * ns * 8)))
-      return fail(rc);
-    build_pbar_kernel<<<dim3((na + 127) / 128, L), 128>>>(L, na, (const double*)p->ct_fine.p,
-                                                          (const double*)p->pmm_fine.p, 2 * L + 1,
-                                                          (const double*)p->ra.p, (const double*)p->rb.p,
-                                                          false, (double*)p->tab_a.p);
-    if ((rc = check_launch("build_pbar_kernel"))) return fail(rc);
-    build_pbar_kernel<<<dim3((ns + 127) / 128, L), 128>>>(L, ns, (const double*)p->ct_rings.p,
-                                                          (const double*)p->pmm_rings.p, L + 1,
-                                                          (const double*)p->ra.p, (const double*)p->rb.p,
-                                                          true, (double*)p->tab_s.p);
-    if ((rc = check_launch("build_pbar_kernel"))) return fail(rc);
-    cudaError_t e = cudaDeviceSynchronize();
-    if (e != cudaSuccess) return fail(cuda_fail(e, "cudaDeviceSynchronize"));
-  }
   const size_t c16 = sizeof(double2);
   if ((rc = p->spec.alloc((size_t)(L + 1) * (L + 1) * c16))) return fail(rc);
   if ((rc = p->torus.alloc((size_t)2 * L * L * c16))) return fail(rc);
@@ -1031,6 +1018,45 @@ static int set_streams(cmm_sht* p, cudaStream_t s) {
     cufftResult r = cufftSetStream(h[k], s);
     if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftSetStream");
   }
+  return CMM_OK;
+}
+
+// Pbar tables of the FP64 Legendre stages at L <= kTabMaxL, built at their
+// first use on `s` (a call inside a stream capture keeps the recurrence
+// kernels, since a capture cannot allocate); released by cmm_sht_trim.
+static int ensure_tables(cmm_sht* p, cudaStream_t s, bool* ok) {
+  *ok = false;
+  const int L = p->L;
+  if (p->tab_mode < 0 || (p->tab_mode == 0 && L > kTabMaxL) || L > kTabShared) return CMM_OK;
+  if (p->tab_a.p && p->tab_s.p) {
+    *ok = true;
+    return CMM_OK;
+  }
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cs) != cudaSuccess) {
+    cudaGetLastError();
+    return CMM_OK;
+  }
+  if (cs != cudaStreamCaptureStatusNone) return CMM_OK;
+  const int64_t tri = (int64_t)L * (L + 1) / 2;
+  const int na = L + 1, ns = L / 2 + 1;
+  int rc;
+  if ((rc = p->tab_a.alloc((size_t)tri * na * 8)) || (rc = p->tab_s.alloc((size_t)tri * ns * 8))) {
+    p->tab_a.release();
+    p->tab_s.release();
+    return rc;
+  }
+  build_pbar_kernel<<<dim3((na + 127) / 128, L), 128, 0, s>>>(L, na, (const double*)p->ct_fine.p,
+                                                              (const double*)p->pmm_fine.p, 2 * L + 1,
+                                                              (const double*)p->ra.p, (const double*)p->rb.p,
+                                                              false, (double*)p->tab_a.p);
+  if ((rc = check_launch("build_pbar_kernel"))) return rc;
+  build_pbar_kernel<<<dim3((ns + 127) / 128, L), 128, 0, s>>>(L, ns, (const double*)p->ct_rings.p,
+                                                              (const double*)p->pmm_rings.p, L + 1,
+                                                              (const double*)p->ra.p, (const double*)p->rb.p,
+                                                              true, (double*)p->tab_s.p);
+  if ((rc = check_launch("build_pbar_kernel"))) return rc;
+  *ok = true;
   return CMM_OK;
 }
 
@@ -1114,7 +1140,9 @@ int sht_forward(cmm_sht* p, const double* samples, double2* out, cudaStream_t s)
     set_last_error("sht_forward: L too large for the analysis kernel");
     return CMM_ERR_UNSUPPORTED;
   }
-  if (p->tab_a.p) {
+  bool tab;
+  if ((rc = ensure_tables(p, s, &tab))) return rc;
+  if (tab) {
     analysis_tab_kernel<<<dim3(L, (L + kTabBlock - 1) / kTabBlock), kTabBlock, 0, s>>>(
         (const double2*)p->pad.p, L, (const double*)p->w_fine.p, (const double*)p->tab_a.p, out);
     return check_launch("analysis_tab_kernel");
@@ -1151,7 +1179,9 @@ int sht_inverse(cmm_sht* p, const double2* alm, int nf, double* samples, cudaStr
   cudaError_t e = cudaMemsetAsync(S, 0, (size_t)kFields * (L + 1) * (L + 1) * sizeof(double2), s);
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
   const int npair = L / 2 + 1;
-  if (p->tab_s.p && (nf == kFields || nf == 4 || nf == 1)) {
+  bool tab;
+  if ((rc = ensure_tables(p, s, &tab))) return rc;
+  if (tab && (nf == kFields || nf == 4 || nf == 1)) {
     const int G = nf == kFields ? 3 : 1;
     dim3 gt(L, (npair + kTabBlock - 1) / kTabBlock, nf / G);
     if (G == 3)
@@ -1348,6 +1378,25 @@ int sht_set_precision(cmm_sht* p, int mode) {
   return CMM_OK;
 }
 
+int sht_set_tables(cmm_sht* p, int mode) {
+  if (mode < -1 || mode > 1) {
+    set_last_error("cmm_sht_set_tables: mode must be -1, 0 or 1");
+    return CMM_ERR_ARG;
+  }
+  if (mode == 1 && p->L > kTabShared) {
+    set_last_error("cmm_sht_set_tables: FP64 Pbar tables are limited to L <= 1024");
+    return CMM_ERR_UNSUPPORTED;
+  }
+  p->tab_mode = mode;
+  if (mode < 0 || (mode == 0 && p->L > kTabMaxL)) {
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return cuda_fail(e, "cmm_sht_set_tables");
+    p->tab_a.release();
+    p->tab_s.release();
+  }
+  return CMM_OK;
+}
+
 int sht_share_tables(cmm_sht* p, const cmm_sht* src) {
   if (!src->tc || src->L != p->L) {
     set_last_error("cmm_sht_share_tables: source plan of the same L in CMM_SHT_SPLIT_BF16 mode expected");
@@ -1370,6 +1419,8 @@ int sht_trim(cmm_sht* p) {
   if (e != cudaSuccess) return cuda_fail(e, "cmm_sht_trim");
   p->synth.release();
   p->samples.release();
+  p->tab_a.release();
+  p->tab_s.release();
   return CMM_OK;
 }
 

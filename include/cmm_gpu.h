@@ -312,9 +312,17 @@ int cmm_sht_set_precision(cmm_sht* plan, int mode);
  * band-limit share the ~4.4 GB of tables at L = 1024 and still run
  * concurrently (each keeps its own data tiles and FFT scratch). */
 int cmm_sht_share_tables(cmm_sht* plan, cmm_sht* src);
-/* Release the FP64 inverse scratch (about 400 MB at L = 1024); it is
- * allocated again at the next FP64 inverse (cmm_sht_inverse, the FP64
- * velocity, cmm_sht_scalar_jets).  Synchronises the device. */
+/* FP64 Legendre stages from tabulated Pbar_lm (analysis and synthesis as
+ * table contractions; 0.8 GB at L = 512, 6.5 GB at L = 1024) instead of
+ * the on-the-fly recurrence: mode 0 (default) for L <= 512, 1 for any
+ * L <= 1024, -1 never.  The tables are built at the next FP64 stage that
+ * runs outside a stream capture.  No counterpart in the reference. */
+int cmm_sht_set_tables(cmm_sht* plan, int mode);
+/* Release the FP64 inverse scratch (about 400 MB at L = 1024) and, at
+ * the FP64 Pbar tables (cmm_sht_set_tables); each is allocated
+ * again at its next use (the tables only by a call outside a stream
+ * capture; inside one the FP64 stages use their recurrence kernels).
+ * Synchronises the device. */
 int cmm_sht_trim(cmm_sht* plan);
 /* Read (and with clear != 0, reset) the plan's device status word
  * (CMM_FLAG_TIMEOUT); synchronises `stream`. */
