@@ -7,7 +7,8 @@ mesh and the split-BF16 Pbar tables.  After every member's bootstrap, one
 device-driven step of all members (cmm_bve_step, whose varying state lives
 on the device) is captured into ONE CUDA graph, the members spread over
 parallel branches; every later step of the whole ensemble is one replay of
-that graph.  The branch count and member order of the graph and the launch
+that graph, or the whole remaining run is captured as one graph and
+launched once (run_persistent).  The branch count and member order of the graph and the launch
 shapes of the tunable kernels of each size class are chosen by the
 Autotuner from measured timings.
 
@@ -115,10 +116,14 @@ class Ensemble:
         torch.cuda.synchronize(self.device)
         return self
 
-    def capture(self, streams=4, order=None):
-        """One step of every member into one CUDA graph: members assigned
-        round-robin (in `order`, default as given) to `streams` parallel
-        branches forked from and joined into the capture stream."""
+    def capture(self, streams=4, order=None, steps=1):
+        """`steps` steps of every member into one CUDA graph: members
+        assigned round-robin (in `order`, default as given) to `streams`
+        parallel branches forked from and joined into the capture stream;
+        each branch runs its members' steps in order (a member's step k+1
+        after its step k on the same branch; members never wait on each
+        other).  Every step's state lives on the device (cmm_bve_step), so
+        the whole remaining run can be one graph: one launch."""
         order = list(range(len(self.members))) if order is None else list(order)
         g = torch.cuda.CUDAGraph()
         side = [torch.cuda.Stream(self.device) for _ in range(streams)]
@@ -127,26 +132,40 @@ class Ensemble:
             cap = torch.cuda.current_stream(self.device)
             for st in side:
                 st.wait_stream(cap)
-            for k, i in enumerate(order):
-                st = side[k % streams]
-                with torch.cuda.stream(st):
-                    native.check(native.lib.cmm_bve_step(self.members[i]._bve, native._stream(self.device)),
-                                 "cmm_bve_step")
+            for _ in range(steps):
+                for k, i in enumerate(order):
+                    st = side[k % streams]
+                    with torch.cuda.stream(st):
+                        native.check(native.lib.cmm_bve_step(self.members[i]._bve,
+                                                             native._stream(self.device)), "cmm_bve_step")
             for st in side:
                 cap.wait_stream(st)
-        self.graph, self.schedule = g, {"streams": streams, "order": order}
+        self.graph, self.schedule = g, {"streams": streams, "order": order, "steps": steps}
         return self
 
     def step(self):
-        """One step of every member: one graph launch."""
+        """One graph launch: schedule["steps"] steps of every member."""
         self.graph.replay()
-        for m in self.members:
-            m._advance_host()
-        self.count += 1
+        for _ in range(self.schedule.get("steps", 1)):
+            for m in self.members:
+                m._advance_host()
+            self.count += 1
+
+    def run_persistent(self, nsteps=None):
+        """The remaining run (or `nsteps` steps) as one captured graph on the
+        current schedule, launched once."""
+        n = self.members[0].Nt - 2 - self.count if nsteps is None else nsteps
+        sched = self.schedule or {"streams": 4, "order": None}
+        self.capture(streams=sched["streams"], order=sched["order"], steps=n)
+        self.step()
+        return self
 
     def run(self, nsteps=None):
         n = self.members[0].Nt - 2 if nsteps is None else nsteps
-        for _ in range(n):
+        per = self.schedule.get("steps", 1) if self.schedule else 1
+        if n % per:
+            raise ValueError(f"{n} steps is not a multiple of the graph's {per}")
+        for _ in range(n // per):
             self.step()
         return self
 

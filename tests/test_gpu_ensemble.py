@@ -27,14 +27,21 @@ def _alone(mods, spec, i, seed, Nt, T, lmax, rms, n_maps):
     return s.run()
 
 
-def test_ensemble_graph_matches_members_alone(mods):
+@pytest.mark.parametrize("persistent", [False, True])
+def test_ensemble_graph_matches_members_alone(mods, persistent):
+    """One graph replay per step, or (persistent) the whole remaining run
+    captured as one graph and launched once."""
     ensemble, sims, autotune, _, _ = mods
     kw = dict(levels=(2, 3), bandlimits=(16, 32), Nt=14, T=0.1, lmax=8, rms=3.0, n_maps=4)
     ens = ensemble.Ensemble.from_seed(5, seed=7, **kw).bootstrap()
     tuner = autotune.Autotuner(reps=1)
     tuner.tune_ensemble_kernels(ens)
     tuner.tune_schedule(ens, stream_counts=(1, 3), steps_each=1)
-    ens.run(ens.members[0].Nt - 2 - ens.count)
+    if persistent:
+        ens.run_persistent()
+        assert ens.schedule["steps"] > 1
+    else:
+        ens.run(ens.members[0].Nt - 2 - ens.count)
     torch.cuda.synchronize()
     assert ens.count == ens.members[0].Nt - 2
     for i, (m, spec) in enumerate(zip(ens.members, ens.specs)):
