@@ -391,9 +391,10 @@ def bench_bve(args, dev):
     """Config: level 4, L=128, dt=1/200, 200 steps, remap every 20, random
     real SH initial vorticity l=1..16 (N(0,1) l^-1.5, seed 0), evaluated as
     a pointwise series.  The whole run after the bootstrap (198 steps) is
-    timed with CUDA events in three ways: driven from the host through the
+    timed with CUDA events in four ways: driven from the host through the
     single calls (step_host), by the device-driven stepper (one
-    cmm_bve_step per step), and as one replayed CUDA graph per step."""
+    cmm_bve_step per step), as one replayed CUDA graph per step, and as one
+    graph of the whole run launched once."""
     import torch
     from cmm_gpu.meshgen import icosahedral_mesh
     from cmm_gpu.workloads import random_sh_vorticity
@@ -404,17 +405,19 @@ def bench_bve(args, dev):
                        "remap every 20, random SH l<=16 initial vorticity; the 198 steps after the "
                        "bootstrap"}
     omegas = {}
-    for mode in ("host", "device", "graph"):
+    for mode in ("host", "device", "graph", "graph_run"):
         s = BVESolver(verts, tris, 4, 128, 200, 1.0, Vorticity(sh=a), n_maps=20)
         s.bootstrap()
+        n = s.Nt - 2
         if mode == "graph":
             s.capture()
+        elif mode == "graph_run":
+            s.capture(steps=n)        # the whole run: one graph, one launch
         torch.cuda.synchronize()
-        n = s.Nt - 2
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         t0 = time.perf_counter()
         e0.record()
-        for _ in range(n):
+        for _ in range(1 if mode == "graph_run" else n):
             s.step_host() if mode == "host" else s.step()
         e1.record()
         torch.cuda.synchronize()
@@ -424,9 +427,11 @@ def bench_bve(args, dev):
         omegas[mode] = s.omega.clone()
         del s
     out["steps_timed"] = 198
-    out["steps_per_s"] = out["graph"]["steps_per_s"]
-    out["ms_per_step"] = out["graph"]["ms_per_step"]
-    out["graph_equals_host"] = bool(torch.equal(omegas["graph"], omegas["host"]))
+    best = max(("graph", "graph_run"), key=lambda k: out[k]["steps_per_s"])
+    out["steps_per_s"] = out[best]["steps_per_s"]
+    out["ms_per_step"] = out[best]["ms_per_step"]
+    out["graph_equals_host"] = bool(torch.equal(omegas["graph"], omegas["host"]) and
+                                    torch.equal(omegas["graph_run"], omegas["host"]))
     return out
 
 

@@ -136,7 +136,8 @@ class BVESolver:
         self.step_index = 0
         self.launches = 0
         self._bve = None        # device-driven stepper, made after the bootstrap
-        self.graph = None       # CUDA graph of one step (capture())
+        self.graph = None       # CUDA graph of graph_steps steps (capture())
+        self.graph_steps = 1
 
     # ------------------------------------------------------------ pieces
     def _project(self, X, n, rot=None):
@@ -250,18 +251,24 @@ class BVESolver:
             self._make_stepper()
         if self.graph is not None:
             self.graph.replay()
-        else:
-            native.check(native.lib.cmm_bve_step(self._bve, native._stream(self.device)), "cmm_bve_step")
+            for _ in range(self.graph_steps):
+                self._advance_host()
+            return
+        native.check(native.lib.cmm_bve_step(self._bve, native._stream(self.device)), "cmm_bve_step")
         self._advance_host()
 
-    def capture(self):
-        """Capture one device-driven step into a CUDA graph; step() then
-        replays it (one graph launch per step)."""
+    def capture(self, steps=1):
+        """Capture `steps` device-driven steps into one CUDA graph; step()
+        then replays it (one graph launch per `steps` steps; the whole
+        remaining run when steps = Nt - 2 - count)."""
+        if self._bve is None:
+            self._make_stepper()
         g = torch.cuda.CUDAGraph()
         torch.cuda.synchronize(self.device)
         with torch.cuda.graph(g):
-            native.check(native.lib.cmm_bve_step(self._bve, native._stream(self.device)), "cmm_bve_step")
-        self.graph = g
+            for _ in range(steps):
+                native.check(native.lib.cmm_bve_step(self._bve, native._stream(self.device)), "cmm_bve_step")
+        self.graph, self.graph_steps = g, steps
         return self
 
     def step_host(self):

@@ -169,17 +169,23 @@ def test_device_driven_step_matches_host_step(sims, precision):
     assert a.mesh.status() == 0 and a.vm.status() == 0
 
 
-def test_captured_graph_replays_the_run(sims):
+@pytest.mark.parametrize("whole_run", [False, True])
+def test_captured_graph_replays_the_run(sims, whole_run):
     """One step captured into a CUDA graph and replayed for every later
-    step gives the run of the stepper called step by step, bit for bit."""
+    step, or (whole_run) every remaining step captured into one graph and
+    launched once, gives the run of the stepper called step by step, bit
+    for bit."""
     a, b = _small_solver(sims), _small_solver(sims)
     a.bootstrap()
     b.bootstrap()
-    b.capture()
-    for _ in range(a.Nt - 2):
+    n = a.Nt - 2
+    b.capture(steps=n if whole_run else 1)
+    for _ in range(n):
         a.step()
+    for _ in range(1 if whole_run else n):
         b.step()
     torch.cuda.synchronize()
+    assert (a.count, a.Nc, a.identity) == (b.count, b.Nc, b.identity)
     for k in range(a.Nc):
         assert torch.equal(a.stack[k], b.stack[k]), k
     assert torch.equal(a.omega, b.omega)
