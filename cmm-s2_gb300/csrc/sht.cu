@@ -675,6 +675,60 @@ __global__ void __launch_bounds__(256) legendre_sum_kernel(const double2* __rest
   }
 }
 
+// legendre_sum_kernel on the synthesis Pbar table (unit weights, the L+1
+// MWSS rings, pairs (t, L-t)) for NF fields: block (m, tile of 64 degrees,
+// group of G fields), one thread per degree l; the group's weighted even/odd
+// ring values of order m staged in shared memory, the thread's table row
+// streamed over the ring pairs.
+template <int G>
+__global__ void __launch_bounds__(kTabBlock) legendre_sum_tab_kernel(const double2* __restrict__ F,
+                                                                     int64_t row, int L, double cm,
+                                                                     const double* __restrict__ tab,
+                                                                     double2* __restrict__ out, int64_t fs_in,
+                                                                     int64_t fs_out) {
+  constexpr int kMaxPair = kTabShared / 2 + 1;
+  __shared__ double2 E[G][kMaxPair], O[G][kMaxPair];
+  const int m = blockIdx.x, l = m + blockIdx.y * kTabBlock + threadIdx.x, f0 = blockIdx.z * G;
+  if (m + (int)blockIdx.y * kTabBlock >= L) return;   // the whole tile is past l = L-1
+  const int nr = L, npair = nr / 2 + 1;
+  const double sc = m == 0 ? 1.0 : cm;
+  for (int e = threadIdx.x; e < G * npair; e += blockDim.x) {
+    const int f = e / npair, j = e % npair;
+    const double2* Ff = F + (int64_t)(f0 + f) * fs_in;
+    const double2 a = Ff[(int64_t)j * row + m];
+    double2 ev, od;
+    if (j < nr - j) {
+      const double2 b = Ff[(int64_t)(nr - j) * row + m];
+      ev = make_double2(a.x + b.x, a.y + b.y);
+      od = make_double2(a.x - b.x, a.y - b.y);
+    } else {
+      ev = a;
+      od = make_double2(0.0, 0.0);
+    }
+    E[f][j] = cmul(ev, sc);
+    O[f][j] = cmul(od, sc);
+  }
+  __syncthreads();
+  if (l >= L) return;
+  const int i = l - m;
+  const double* P = tab + tab_off(m, L, npair) + (int64_t)i * npair;
+  const bool even = (i & 1) == 0;
+  double2 acc[G];
+#pragma unroll
+  for (int f = 0; f < G; ++f) acc[f] = make_double2(0.0, 0.0);
+  for (int j = 0; j < npair; ++j) {
+    const double pj = __ldg(P + j);
+#pragma unroll
+    for (int f = 0; f < G; ++f) {
+      const double2 v = even ? E[f][j] : O[f][j];
+      acc[f].x += pj * v.x;
+      acc[f].y += pj * v.y;
+    }
+  }
+#pragma unroll
+  for (int f = 0; f < G; ++f) out[(int64_t)(f0 + f) * fs_out + (int64_t)m * L + l] = acc[f];
+}
+
 // ring synthesis with weights: out[j][m] = w_j sum_l Pbar_lm(theta_j)
 // a[m][l] for rings j = 0..nr (pairs j, nr-j), rows of length `row`.
 __global__ void __launch_bounds__(kSynthBlock) ring_synthesis_kernel(const double2* __restrict__ alm, int L,
@@ -1297,7 +1351,13 @@ int sht_velocity_bwd(cmm_sht* p, const cmm_mesh* vm, const double* gjets, double
     const double* pm = (const double*)p->pmm_rings.p;
     const double* ra = (const double*)p->ra.p;
     const double* rb = (const double*)p->rb.p;
-    if (npair <= 256)
+    bool tab;
+    if ((rc = ensure_tables(p, s, &tab))) return rc;
+    if (tab) {
+      const dim3 gt(L, (L + kTabBlock - 1) / kTabBlock, kFields / 2);
+      legendre_sum_tab_kernel<2><<<gt, kTabBlock, 0, s>>>(Sb, L + 1, L, 2.0, (const double*)p->tab_s.p, Fb, fin,
+                                                          fout);
+    } else if (npair <= 256)
       legendre_sum_kernel<1><<<gl, 256, 0, s>>>(Sb, L + 1, L, L, nullptr, 2.0, ct, pm, L + 1, ra, rb, Fb, fin, fout);
     else if (npair <= 512)
       legendre_sum_kernel<2><<<gl, 256, 0, s>>>(Sb, L + 1, L, L, nullptr, 2.0, ct, pm, L + 1, ra, rb, Fb, fin, fout);
