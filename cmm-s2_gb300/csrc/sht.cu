@@ -82,6 +82,45 @@ __global__ void pad_kernel(const C* __restrict__ Gh, int L, C* __restrict__ H) {
   H[(int64_t)k * L + m] = cmul(v, s);
 }
 
+// The FP64 form keeps the torus and padded spectra order-major, G[m][t]
+// (L, 2L) and H[m][k] (L, 4L), so that cuFFT transforms L contiguous rows
+// (the strided column transforms of the layout above run a few blocks at
+// small L).  Same values as torus_kernel / pad_kernel.
+__global__ void torus_t_kernel(const double2* __restrict__ F, int L, double2* __restrict__ G) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = blockIdx.y;
+  if (m >= L || t >= 2 * L) return;
+  const double s = M_PI / L;
+  double2 v;
+  if (t <= L) {
+    v = F[(int64_t)t * (L + 1) + m];
+  } else {
+    v = F[(int64_t)(2 * L - t) * (L + 1) + m];
+    if (m & 1) {
+      v.x = -v.x;
+      v.y = -v.y;
+    }
+  }
+  G[(int64_t)m * 2 * L + t] = cmul(v, s);
+}
+
+__global__ void pad_t_kernel(const double2* __restrict__ Gh, int L, double2* __restrict__ H) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;  // 0..4L-1
+  const int m = blockIdx.y;
+  if (k >= 4 * L || m >= L) return;
+  const double s = 1.0 / (2 * L);
+  const double2* g = Gh + (int64_t)m * 2 * L;
+  double2 v = make_double2(0.0, 0.0);
+  if (k < L) {
+    v = g[k];
+  } else if (k == L || k == 3 * L) {
+    v = cmul(g[L], 0.5);
+  } else if (k > 3 * L) {
+    v = g[k - 2 * L];
+  }
+  H[(int64_t)m * 4 * L + k] = cmul(v, s);
+}
+
 // Zero the m = L column of nrows spectra rows of length L+1 (an
 // out-of-place C2R transform may overwrite its input).
 __global__ void zero_nyquist_kernel(float2* __restrict__ S, int L, int nrows) {
@@ -101,7 +140,8 @@ __global__ void to_double_kernel(const float* __restrict__ a, int64_t n, double*
 }
 
 // Legendre analysis: one block per m; ring pairs (j, 2L-j) of the fine grid
-// with the quadrature weights folded in.  fine (4L, L): rows 0..2L used.
+// with the quadrature weights folded in.  fine (L, 4L) order-major: rings
+// 0..2L of each order used.
 __global__ void __launch_bounds__(256) analysis_kernel(const double2* __restrict__ fine, int L,
                                                        const double* __restrict__ w,
                                                        const double* __restrict__ ct,
@@ -118,10 +158,10 @@ __global__ void __launch_bounds__(256) analysis_kernel(const double2* __restrict
   for (int r = 0; r < R; ++r) {
     const int j = threadIdx.x + r * blockDim.x;
     if (j < npair) {
-      const double2 a = fine[(int64_t)j * L + m];
+      const double2 a = fine[(int64_t)m * 4 * L + j];
       double2 e, o;
       if (j < L) {
-        const double2 b = fine[(int64_t)(2 * L - j) * L + m];
+        const double2 b = fine[(int64_t)m * 4 * L + 2 * L - j];
         e = make_double2(a.x + b.x, a.y + b.y);
         o = make_double2(a.x - b.x, a.y - b.y);
       } else {
@@ -450,10 +490,10 @@ __global__ void __launch_bounds__(kTabBlock) analysis_tab_kernel(const double2* 
   if (m + (int)blockIdx.y * kTabBlock >= L) return;   // the whole tile is past l = L-1
   const int npair = L + 1;
   for (int j = threadIdx.x; j < npair; j += blockDim.x) {
-    const double2 a = fine[(int64_t)j * L + m];
+    const double2 a = fine[(int64_t)m * 4 * L + j];
     double2 e, o;
     if (j < L) {
-      const double2 b = fine[(int64_t)(2 * L - j) * L + m];
+      const double2 b = fine[(int64_t)m * 4 * L + 2 * L - j];
       e = make_double2(a.x + b.x, a.y + b.y);
       o = make_double2(a.x - b.x, a.y - b.y);
     } else {
@@ -929,6 +969,9 @@ struct cmm_sht {
   int precision = CMM_SHT_FP64;
   cufftHandle ring_fwd = 0, torus_fwd = 0, pad_inv = 0, ring_inv = 0;
   bool have_plans[4] = {false, false, false, false};
+  // FP64 forward on order-major rows (torus_t_kernel / pad_t_kernel)
+  cufftHandle torus_fwd_t = 0, pad_inv_t = 0;
+  bool have_tplans[2] = {false, false};
   cmm::DeviceBuffer ct_rings, ct_fine, w_fine, pmm_rings, pmm_fine, ra, rb;
   cmm::DeviceBuffer tab_a, tab_s;   // Pbar tables of the FP64 stages
   int tab_mode = 0;                 // cmm_sht_set_tables: 0 auto, 1 always, -1 never
@@ -946,6 +989,8 @@ struct cmm_sht {
     if (have_plans[1]) cufftDestroy(torus_fwd);
     if (have_plans[2]) cufftDestroy(pad_inv);
     if (have_plans[3]) cufftDestroy(ring_inv);
+    if (have_tplans[0]) cufftDestroy(torus_fwd_t);
+    if (have_tplans[1]) cufftDestroy(pad_inv_t);
     if (have_fplans[0]) cufftDestroy(f_ring_fwd);
     if (have_fplans[1]) cufftDestroy(f_torus_fwd);
     if (have_fplans[2]) cufftDestroy(f_pad_inv);
@@ -1060,6 +1105,12 @@ int sht_create(int L, cmm_sht** out) {
   r = cufftPlanMany(&p->ring_inv, 1, n2, cin, 1, L + 1, rout, 1, 2 * L, CUFFT_Z2D, kFields * (L + 1));
   if (r != CUFFT_SUCCESS) return fail(cufft_fail(r, "cufftPlanMany(ring_inv)"));
   p->have_plans[3] = true;
+  r = cufftPlanMany(&p->torus_fwd_t, 1, n2, tn, 1, 2 * L, tn, 1, 2 * L, CUFFT_Z2Z, L);
+  if (r != CUFFT_SUCCESS) return fail(cufft_fail(r, "cufftPlanMany(torus_fwd_t)"));
+  p->have_tplans[0] = true;
+  r = cufftPlanMany(&p->pad_inv_t, 1, n4, pn, 1, 4 * L, pn, 1, 4 * L, CUFFT_Z2Z, L);
+  if (r != CUFFT_SUCCESS) return fail(cufft_fail(r, "cufftPlanMany(pad_inv_t)"));
+  p->have_tplans[1] = true;
   *out = p;
   return CMM_OK;
 }
@@ -1070,6 +1121,12 @@ static int set_streams(cmm_sht* p, cudaStream_t s) {
   for (int k = 0; k < 8; ++k) {
     if (k >= 4 && !p->have_fplans[k - 4]) continue;
     cufftResult r = cufftSetStream(h[k], s);
+    if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftSetStream");
+  }
+  cufftHandle ht[2] = {p->torus_fwd_t, p->pad_inv_t};
+  for (int k = 0; k < 2; ++k) {
+    if (!p->have_tplans[k]) continue;
+    cufftResult r = cufftSetStream(ht[k], s);
     if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftSetStream");
   }
   return CMM_OK;
@@ -1181,14 +1238,14 @@ int sht_forward(cmm_sht* p, const double* samples, double2* out, cudaStream_t s)
   }
   cufftResult r = cufftExecD2Z(p->ring_fwd, (cufftDoubleReal*)samples, (cufftDoubleComplex*)p->spec.p);
   if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExecD2Z");
-  torus_kernel<double2><<<g1, b, 0, s>>>((const double2*)p->spec.p, L, (double2*)p->torus.p);
-  if ((rc = check_launch("torus_kernel"))) return rc;
-  r = cufftExecZ2Z(p->torus_fwd, (cufftDoubleComplex*)p->torus.p, (cufftDoubleComplex*)p->torus.p,
+  torus_t_kernel<<<g1, b, 0, s>>>((const double2*)p->spec.p, L, (double2*)p->torus.p);
+  if ((rc = check_launch("torus_t_kernel"))) return rc;
+  r = cufftExecZ2Z(p->torus_fwd_t, (cufftDoubleComplex*)p->torus.p, (cufftDoubleComplex*)p->torus.p,
                    CUFFT_FORWARD);
   if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExecZ2Z(torus)");
-  pad_kernel<double2><<<g2, b, 0, s>>>((const double2*)p->torus.p, L, (double2*)p->pad.p);
-  if ((rc = check_launch("pad_kernel"))) return rc;
-  r = cufftExecZ2Z(p->pad_inv, (cufftDoubleComplex*)p->pad.p, (cufftDoubleComplex*)p->pad.p, CUFFT_INVERSE);
+  pad_t_kernel<<<dim3((4 * L + 127) / 128, L), b, 0, s>>>((const double2*)p->torus.p, L, (double2*)p->pad.p);
+  if ((rc = check_launch("pad_t_kernel"))) return rc;
+  r = cufftExecZ2Z(p->pad_inv_t, (cufftDoubleComplex*)p->pad.p, (cufftDoubleComplex*)p->pad.p, CUFFT_INVERSE);
   if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExecZ2Z(pad)");
   if (L + 1 > 8 * 256) {
     set_last_error("sht_forward: L too large for the analysis kernel");
