@@ -167,6 +167,28 @@ def cpu_rate(verts, tris, jets, nq, workers, steps=1, warmup=0):
     return steps * nq * len(jets) / dt, workers
 
 
+def cpu_bve_rate(steps=8):
+    """BVE steps/s of the oracle (the restated reference driver) on the
+    barotropic configuration of bench_bve (level 4, L=128, dt=1/200, remap
+    every 20, the same random SH initial vorticity evaluated as a series),
+    one host thread: `steps` steps after the bootstrap."""
+    from cmm_gpu.meshgen import icosahedral_mesh
+    from cmm_gpu.workloads import random_sh_vorticity
+    from oracle.bve import BVEOracle
+    from oracle import geometry as OG, fields as OF
+    verts, tris = icosahedral_mesh(4)
+    _, a = random_sh_vorticity(16, seed=0)
+    o = BVEOracle(verts, tris, OG.ConeLocator(verts, tris), 128, 200, 1.0, OF.sh_series(a), n_maps=20)
+    o.bootstrap()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        o.step()
+    dt = time.perf_counter() - t0
+    return {"value": steps / dt, "unit": "BVE steps/s", "cores": 1, "kind": "port",
+            "sample": f"{steps} steps after the bootstrap of the level-4 / L=128 run, numpy oracle "
+                      "(restated reference driver), 1 thread"}
+
+
 # ------------------------------------------------------------- GPU arm
 def bind_to_gpu_numa_node(index):
     """Run this process on the host cores local to the GPU (from the PCI
@@ -843,7 +865,7 @@ def main():
         return
     if world > 1:
         torch.distributed.init_process_group("nccl")
-    cpu = None
+    cpu = cpu_bve = None
     if rank == 0 and not args.no_cpu:
         # timed before any CUDA work so the spawn pool starts cleanly
         verts, tris, jets, _ = workload()
@@ -851,6 +873,8 @@ def main():
         cpu = {"value": rate, "unit": "map evals/s", "cores": used, "kind": "port",
                "sample": f"{max(1024, args.cpu_queries // 8)} queries x {SUBMAPS} submaps with "
                          "Jacobians, numpy oracle (restated reference), 1 thread"}
+        if not args.no_bve:
+            cpu_bve = cpu_bve_rate()
     r = bench_gpu(args, rank, world)
     if rank != 0:
         torch.distributed.destroy_process_group()
@@ -884,6 +908,8 @@ def main():
     for key in ("bve", "rh_error", "bve_l7_L1024", "kernels", "ensemble", "adjoint", "transport"):
         if key in r:
             line[key] = r[key]
+    if cpu_bve is not None and isinstance(line.get("bve"), dict):
+        line["bve"]["cpu_baseline"] = cpu_bve
     print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
