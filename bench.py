@@ -558,6 +558,20 @@ def bench_ensemble(args, dev):
     for lv, L in ens.specs:
         classes[f"level{lv}_L{L}"] = classes.get(f"level{lv}_L{L}", 0) + 1
     ok = all(m.mesh.status() == 0 and m.vm.status() == 0 and m.sht.status() == 0 for m in ens.members)
+    # the split-BF16 error, stated: the smallest member rerun alone in the
+    # FP64 form, its final vorticity against the ensemble's
+    from cmm_gpu.meshgen import icosahedral_mesh
+    from cmm_gpu.spherical_simulations import BVESolver, Vorticity
+    from cmm_gpu.workloads import spectral_perturbation
+    i0 = min(range(len(ens.members)), key=lambda i: (ens.specs[i][1], ens.specs[i][0]))
+    m0 = ens.members[i0]
+    lv0, L0 = ens.specs[i0]
+    v0, tri0 = icosahedral_mesh(lv0)
+    pert0 = spectral_perturbation(64, seed=2024 * 100003 + i0, slope=-2.0, rms=5.0)
+    ref = BVESolver(v0, tri0, lv0, L0, m0.Nt, m0.T, Vorticity(spline_sh=pert0), n_maps=m0.n_maps,
+                    precision="fp64").run()
+    err0 = float((m0.omega - ref.omega).abs().max() / ref.omega.abs().max())
+    del ref
     return {"workload": f"{args.ens_members} members, levels 5-7 x L in {{256,512,1024}} (seed 2024), "
                         "100 steps of dt=1/200, remap every 10, k^-3 l<=64 initial vorticity (spline), "
                         "split-BF16 Legendre, FP32 velocity records; the timed steps are one captured "
@@ -566,6 +580,7 @@ def bench_ensemble(args, dev):
             "steps_timed": n, "members": len(ens.members), "classes": classes,
             "device_memory_gb": torch.cuda.max_memory_allocated(dev) / 1e9, "setup_s": setup,
             "graph_steps": n, "graph_capture_s": capture_s,
+            "split_vs_fp64_omega_rel": {"member": i0, "level": lv0, "L": L0, "value": err0},
             "schedule": tuner.log["schedule"]["best"], "launch_shapes": tuner.log["kernels"],
             "status_ok": ok}
 
