@@ -68,6 +68,7 @@ _SIGS = {
     "cmm_sht_share_tables": (_i, [_p, _p]),
     "cmm_sht_trim": (_i, [_p]),
     "cmm_sht_set_tables": (_i, [_p, _i]),
+    "cmm_sht_timeout_selftest": (_i, [_p, _i64, _p]),
     "cmm_velmesh_set_records": (_i, [_p, _i]),
     "cmm_assemble_bwd": (_i, [_p, _p, _p, _p]),
     "cmm_compose_bwd": (_i, [_p, ctypes.POINTER(_p), _i, _p, _i64, _p, ctypes.POINTER(_p), _p, _p, _p]),
@@ -400,6 +401,11 @@ class Sht:
 
     def trim(self):
         check(lib.cmm_sht_trim(self.h), "cmm_sht_trim")
+        return self
+
+    def timeout_selftest(self, polls=1000):
+        """Make the bounded tensor-core wait run out (cmm_sht_timeout_selftest)."""
+        check(lib.cmm_sht_timeout_selftest(self.h, int(polls), _stream(self.device)), "cmm_sht_timeout_selftest")
         return self
 
     TABLES_AUTO, TABLES_ALWAYS, TABLES_NEVER = 0, 1, -1

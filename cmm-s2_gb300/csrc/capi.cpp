@@ -205,6 +205,12 @@ int cmm_sht_set_precision(cmm_sht* plan, int mode) {
   return sht_set_precision(plan, mode);
 }
 
+int cmm_sht_timeout_selftest(cmm_sht* plan, long long polls, void* stream) {
+  if (!plan || polls < 1 || polls > (1LL << 20))
+    return arg_error("cmm_sht_timeout_selftest: polls must be in [1, 2^20]");
+  return tc_wait_timeout_probe(polls, sht_status_word(plan), (cudaStream_t)stream);
+}
+
 int cmm_sht_set_tables(cmm_sht* plan, int mode) {
   if (!plan) return arg_error("cmm_sht_set_tables: null pointer");
   return sht_set_tables(plan, mode);

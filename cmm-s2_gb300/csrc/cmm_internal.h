@@ -226,6 +226,7 @@ int sht_velocity(cmm_sht* p, const cmm_mesh* vm, const double* omega, double2* p
                  double* jets, cudaStream_t s);
 int sht_scalar_jets(cmm_sht* p, const cmm_mesh* vm, const double2* alm, double* jets, cudaStream_t s);
 int sht_power(cmm_sht* p, const double2* alm, double* power, cudaStream_t s);
+int* sht_status_word(cmm_sht* p);
 int sht_set_tables(cmm_sht* p, int mode);
 int sht_share_tables(cmm_sht* p, const cmm_sht* src);
 int sht_velocity_bwd(cmm_sht* p, const cmm_mesh* vm, const double* gjets, double* gomega, cudaStream_t s);
@@ -250,4 +251,5 @@ size_t tc_plan_bytes(const TcPlan* p);
 int tc_synthesis(TcPlan* p, const double2* fields, float2* S, int* status, cudaStream_t s);
 int tc_analysis(TcPlan* p, const float2* fine, const double* w, double2* alm, int* status,
                 cudaStream_t s);
+int tc_wait_timeout_probe(long long polls, int* status, cudaStream_t s);
 }  // namespace cmm

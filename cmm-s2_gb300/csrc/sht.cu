@@ -1541,6 +1541,8 @@ int sht_trim(cmm_sht* p) {
   return CMM_OK;
 }
 
+int* sht_status_word(cmm_sht* p) { return (int*)p->status.p; }
+
 int sht_status(cmm_sht* p, cudaStream_t s, int* flags, int clear) {
   int h = 0;
   cudaError_t e = cudaMemcpyAsync(&h, p->status.p, sizeof(int), cudaMemcpyDeviceToHost, s);

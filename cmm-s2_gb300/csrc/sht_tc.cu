@@ -85,8 +85,8 @@ __device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
 }
 
 // Bounded wait; false on timeout.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  for (long long i = 0; i < kSpinLimit; ++i)
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long long limit = kSpinLimit) {
+  for (long long i = 0; i < limit; ++i)
     if (mbar_test(bar, parity)) return true;
   return false;
 }
@@ -696,6 +696,28 @@ int tc_plan_share(const TcPlan* src, TcPlan** out) {
   }
   *out = p;
   return CMM_OK;
+}
+
+namespace {
+
+// Self-test of the timeout path: the tensor-core kernels' bounded wait on
+// an mbarrier that no copy or MMA will ever complete (nothing arrives on
+// it), with a limit of `polls`; on the timeout the block records
+// CMM_FLAG_TIMEOUT in the status word and returns, as those kernels do.
+__global__ void wait_timeout_probe_kernel(long long polls, int* __restrict__ status) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) mbar_init(&bar, 1);
+  __syncthreads();
+  const bool ok = mbar_wait(&bar, 0, polls);
+  __syncthreads();
+  if (threadIdx.x == 0 && !ok) atomicOr(status, CMM_FLAG_TIMEOUT);
+}
+
+}  // namespace
+
+int tc_wait_timeout_probe(long long polls, int* status, cudaStream_t s) {
+  wait_timeout_probe_kernel<<<1, 32, 0, s>>>(polls, status);
+  return check("wait_timeout_probe_kernel");
 }
 
 int tc_synthesis(TcPlan* p, const double2* fields, float2* S, int* status, cudaStream_t s) {

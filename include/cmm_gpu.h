@@ -312,6 +312,12 @@ int cmm_sht_set_precision(cmm_sht* plan, int mode);
  * band-limit share the ~4.4 GB of tables at L = 1024 and still run
  * concurrently (each keeps its own data tiles and FFT scratch). */
 int cmm_sht_share_tables(cmm_sht* plan, cmm_sht* src);
+/* Failure-path self-test: runs the tensor-core kernels' bounded mbarrier
+ * wait on a barrier that nothing ever completes, with a limit of `polls`
+ * (1..2^20) polls; the wait runs out, the block sets CMM_FLAG_TIMEOUT in the
+ * plan's status word (read with cmm_sht_status) and returns, leaving the
+ * context usable.  No counterpart in the reference. */
+int cmm_sht_timeout_selftest(cmm_sht* plan, long long polls, void* stream);
 /* FP64 Legendre stages from tabulated Pbar_lm (analysis and synthesis as
  * table contractions; 0.8 GB at L = 512, 6.5 GB at L = 1024) instead of
  * the on-the-fly recurrence: mode 0 (default) for L <= 512, 1 for any

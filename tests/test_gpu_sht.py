@@ -243,3 +243,22 @@ def test_fp64_table_and_recurrence_stages_agree(nat, L):
         j1 = nat.Sht(L).velocity(vm, dev(om)).cpu().numpy()
         s = np.abs(j0).max()
         np.testing.assert_allclose(j1 / s, j0 / s, rtol=0, atol=1e-13)
+
+
+def test_bounded_wait_timeout_sets_status_and_context_survives(nat):
+    """The tensor-core kernels' bounded mbarrier wait, run on a barrier that
+    nothing completes (cmm_sht_timeout_selftest, 1000 polls), runs out, sets
+    CMM_FLAG_TIMEOUT in the plan's status word and returns; the context
+    stays usable (a split-BF16 transform afterwards is still correct)."""
+    L = 32
+    tc = nat.Sht(L).set_precision(nat.Sht.SPLIT_BF16)
+    assert tc.status() == 0
+    tc.timeout_selftest(1000)
+    assert tc.status(clear=True) == nat.FLAG_TIMEOUT
+    assert tc.status() == 0
+    f = np.random.default_rng(3).standard_normal((L + 1, 2 * L))
+    f[0], f[-1] = f[0, 0], f[-1, 0]
+    a64 = nat.Sht(L).forward(dev(f))
+    a16 = tc.forward(dev(f))
+    rel = float((a16 - a64).abs().max() / a64.abs().max())
+    assert 1e-9 < rel < 1e-4 and tc.status() == 0
