@@ -288,3 +288,24 @@ def test_checkpoint_resume_is_bit_identical(sims, tmp_path, precision):
     assert torch.equal(a.omega, c.omega)
     with pytest.raises(ValueError):
         sims.BVESolver(verts, tris, 3, 16, 24, 0.5, "zonal_jet", **kw).load_state(str(tmp_path / "ck.npz"))
+
+
+def test_nonfinite_initial_condition_is_reported(sims):
+    """Fault injection on the host: a NaN among the initial SH coefficients
+    propagates through vorticity, transform, velocity and map update without
+    any out-of-range access (every location path maps NaN to a valid cell)
+    and is reported as CMM_FLAG_NONFINITE; a clean run afterwards in the same
+    context is unaffected."""
+    from cmm_gpu import native
+    from cmm_gpu.meshgen import icosahedral_mesh
+    from cmm_gpu.workloads import random_sh_vorticity
+    verts, tris = icosahedral_mesh(2)
+    _, a = random_sh_vorticity(4, seed=1)
+    bad = a.copy()
+    bad[3, 4] = np.nan
+    s = sims.BVESolver(verts, tris, 2, 8, 8, 1.0, sims.Vorticity(sh=bad), n_maps=3).run()
+    flags = s.mesh.status(clear=True) | s.vm.status(clear=True)
+    assert flags & native.FLAG_NONFINITE
+    good = sims.BVESolver(verts, tris, 2, 8, 8, 1.0, sims.Vorticity(sh=a), n_maps=3).run()
+    assert good.mesh.status() == 0 and good.vm.status() == 0
+    assert bool(torch.isfinite(good.omega).all())
