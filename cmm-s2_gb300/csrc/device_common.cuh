@@ -463,6 +463,11 @@ __device__ __forceinline__ void sh_series_n(const MeshView& vm, const double* __
     }
     const double* ab = vm.sh_ab + 2 * (int64_t)m * T;
     double p1 = 0.0, p = pmm;
+    // sum_l Pbar_lm (c_l,m cos + c_l,-m sin) = cos * sum_l Pbar_lm c_l,m +
+    // sin * sum_l Pbar_lm c_l,-m: two FMAs per degree, the angle once per m
+    double ac[NS], as[NS];
+#pragma unroll
+    for (int k = 0; k < NS; ++k) ac[k] = as[k] = 0.0;
     for (int l = m; l <= lmax; ++l) {
       if (l == m + 1) {
         p1 = p;
@@ -475,12 +480,13 @@ __device__ __forceinline__ void sh_series_n(const MeshView& vm, const double* __
       const int64_t i = (int64_t)l * w + l;
 #pragma unroll
       for (int k = 0; k < NS; ++k) {
-        if (m == 0)
-          out[k] += c[k * K + i] * p;
-        else
-          out[k] += 1.4142135623730951 * p * (c[k * K + i + m] * cm + c[k * K + i - m] * sm);
+        ac[k] += c[k * K + i + m] * p;
+        if (m > 0) as[k] += c[k * K + i - m] * p;
       }
     }
+#pragma unroll
+    for (int k = 0; k < NS; ++k)
+      out[k] += m == 0 ? ac[k] : 1.4142135623730951 * (ac[k] * cm + as[k] * sm);
   }
 }
 
