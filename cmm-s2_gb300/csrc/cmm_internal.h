@@ -67,6 +67,19 @@ struct MeshView {
 // Tunable kernels (index into MeshView::block).
 constexpr int kTuneCompose = 0, kTuneAdvect = 1, kTuneVorticity = 2, kTuneLocate = 3;
 inline int block_of(const MeshView& m, int k, int dflt) { return m.block[k] > 0 ? m.block[k] : dflt; }
+// Threads per block for n work items: the tuned size when one is set, else
+// the default, or for small n a smaller multiple of 32 so that the grid
+// covers each of the 152 SMs twice (a few thousand FP64-heavy points in
+// default-size blocks would leave most SMs idle).
+constexpr int kNumSMs = 152;
+inline int small_block(int64_t n, int dflt) {
+  const int64_t want = (n + 2 * kNumSMs - 1) / (2 * kNumSMs);
+  const int b = (int)((want + 31) / 32 * 32);
+  return b < 32 ? 32 : (b > dflt ? dflt : b);
+}
+inline int block_for(const MeshView& m, int k, int dflt, int64_t n) {
+  return m.block[k] > 0 ? m.block[k] : small_block(n, dflt);
+}
 
 constexpr int kShTableMax = 128;
 constexpr int kIcosahedral = 0;

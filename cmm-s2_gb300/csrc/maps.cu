@@ -520,7 +520,7 @@ int check_launch(const char* what) {
 int launch_locate(const MeshView& m, const double* q, int64_t n, int32_t* tri, double* bcc,
                   cudaStream_t s) {
   if (n == 0) return CMM_OK;
-  const int b = block_of(m, kTuneLocate, kBlock);
+  const int b = block_for(m, kTuneLocate, kBlock, n);
   locate_kernel<<<grid_for(n, b), b, 0, s>>>(m, q, n, tri, bcc);
   return check_launch("locate_kernel");
 }
@@ -544,7 +544,7 @@ int launch_compose(const MeshView& m, const double* const* coeffs, int S, const 
   SubmapPtrs cp;
   cp.S = S;
   for (int k = 0; k < S; ++k) cp.p[k] = coeffs[k];
-  const int b = block_of(m, kTuneCompose, kBlock);
+  const int b = block_for(m, kTuneCompose, kBlock, n);
   const int g = grid_for(n, b);
   if (jac)
     compose_kernel<true><<<g, b, 0, s>>>(m, cp, q, n, out, tri, tri_all, jac, perm);
@@ -596,7 +596,7 @@ int launch_compose_dev(const MeshView& m, const double* const* table, const BveS
                        const double* last, const double* q, int64_t n, double* out, cudaStream_t s) {
   if (n == 0) return CMM_OK;
   DevSubmaps cp{table, st, last};
-  const int b = block_of(m, kTuneCompose, kBlock);
+  const int b = block_for(m, kTuneCompose, kBlock, n);
   compose_kernel<false><<<grid_for(n, b), b, 0, s>>>(m, cp, q, n, out, nullptr, nullptr,
                                                                 nullptr, nullptr);
   return check_launch("compose_kernel");

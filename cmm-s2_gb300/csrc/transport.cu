@@ -426,7 +426,8 @@ int flow_advect_points(const MeshView& mesh, int kind, double T, double alpha, i
   int rc = make_spec(kind, T, alpha, scheme, t, dt, &f);
   if (rc) return rc;
   const int64_t n = 5LL * mesh.nv;
-  flow_advect_points_kernel<<<grid_for(n, kBlock), kBlock, 0, s>>>(mesh, f, scheme, dt, s_pts, work);
+  const int b = small_block(n, kBlock);
+  flow_advect_points_kernel<<<grid_for(n, b), b, 0, s>>>(mesh, f, scheme, dt, s_pts, work);
   return check_launch("flow_advect_points_kernel");
 }
 

@@ -309,7 +309,7 @@ int launch_advect_points(const MeshView& mesh, const MeshView& vm, VelPtrs vc, i
                          const TimeWeights& tw, int scheme, double dt, const double* s_pts,
                          double* work, cudaStream_t s, const BveState* st) {
   const int64_t n = 5LL * mesh.nv;
-  const int b = block_of(mesh, kTuneAdvect, kBlock);
+  const int b = block_for(mesh, kTuneAdvect, kBlock, n);
   advect_points_kernel<<<grid_for(n, b), b, 0, s>>>(mesh, vm, vc, nvs, tw, scheme, dt,
                                                                s_pts, work, st);
   return check_launch("advect_points_kernel");
@@ -371,8 +371,8 @@ int launch_project_jets(const MeshView& mesh, const double* prev_coeffs, const d
                         const double* sn, const double* tan, double eps, double* jets,
                         cudaStream_t s, const BveState* st) {
   const int64_t nv = mesh.nv;
-  project_jets_kernel<<<(int)((nv + kBlock - 1) / kBlock), kBlock, 0, s>>>(mesh, prev_coeffs, yn, sn,
-                                                                           tan, eps, jets, st);
+  const int b = small_block(nv, kBlock);
+  project_jets_kernel<<<(int)((nv + b - 1) / b), b, 0, s>>>(mesh, prev_coeffs, yn, sn, tan, eps, jets, st);
   return check_launch("project_jets_kernel");
 }
 

@@ -162,7 +162,7 @@ int launch_vorticity(int kind, const double* params, int nparams, const double* 
   VortParams vp{};
   vp.kind = kind;
   for (int k = 0; k < nparams && k < 12; ++k) vp.p[k] = params[k];
-  const int b = block_of(vm, kTuneVorticity, 128);
+  const int b = block_for(vm, kTuneVorticity, 128, Q);
   vorticity_kernel<<<grid_for(Q, b), b, 0, s>>>(vp, sh, lmax, vm, spline, rot, X, Q, npr,
                                                     cos_ring, omega);
   note_launch();
