@@ -71,7 +71,7 @@ def test_latlon_locate_matches_reference(nat):
     print(f"{diff.sum()} of {len(tri)} edge/vertex queries resolved to another container")
 
 
-@pytest.mark.parametrize("L", [16, 128])
+@pytest.mark.parametrize("L", [16, 128, 1024])
 def test_latlon_locate_random(nat, L):
     from cmm_gpu.meshgen import random_sphere_points
     q = random_sphere_points(100_000, seed=L)
