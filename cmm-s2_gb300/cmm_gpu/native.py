@@ -462,7 +462,7 @@ class Sht:
         return jets
 
 
-def compose_host(mesh, coeffs, q_host, out_host, tri_host=None, jac_host=None, chunks=8,
+def compose_host(mesh, coeffs, q_host, out_host, tri_host=None, jac_host=None, chunks=16,
                  streams=None, scratch=None, order=None):
     """Composition of host-resident queries (pinned (n,3) float64) into
     host-resident outputs, pipelined in `chunks` pieces over two CUDA
