@@ -646,11 +646,12 @@ def bench_adjoint(args, dev):
     t_fwd, t_grad = e[0].elapsed_time(e[1]), e[2].elapsed_time(e[3])
     rng = np.random.default_rng(13)
     rel, best = [], []
+    ads, fd6, fdb = [], [], []
     for _ in range(args.adjoint_fd):
         l = int(rng.integers(1, lmax + 1))
         c = int(rng.integers(0, 2 * l + 1))
         ad = float(grad[l, c])
-        errs = {}
+        errs, fds = {}, {}
         for h in (1e-6, 1e-5, 1e-4):
             sp, sm = sh.clone(), sh.clone()
             sp[l, c] += h
@@ -658,6 +659,10 @@ def bench_adjoint(args, dev):
             with torch.no_grad():
                 fd = (float(run.misfit(sp, target)) - float(run.misfit(sm, target))) / (2 * h)
             errs[h] = abs(fd - ad) / max(abs(ad), 1e-300)
+            fds[h] = fd
+        ads.append(ad)
+        fd6.append(fds[1e-6])
+        fdb.append(fds[min(errs, key=errs.get)])
         rel.append(errs[1e-6])
         best.append(min(errs.values()))
     return {"workload": "gradient of the final-vorticity misfit w.r.t. the initial SH coefficients "
@@ -670,6 +675,11 @@ def bench_adjoint(args, dev):
             "rel_err_h1e-6_median": float(np.median(rel)) if rel else None,
             "rel_err_best_h_max": max(best) if best else None,
             "rel_err_best_h_median": float(np.median(best)) if best else None,
+            # the sampled gradient as a vector: |fd - ad|_2 / |fd|_2
+            "vector_rel_err_h1e-6": (float(np.linalg.norm(np.subtract(fd6, ads)) / np.linalg.norm(fd6))
+                                     if ads else None),
+            "vector_rel_err_best_h": (float(np.linalg.norm(np.subtract(fdb, ads)) / np.linalg.norm(fdb))
+                                      if ads else None),
             "fd_note": "centred differences of J carry the map update's amplified rounding "
                        "(1/(4 eps) = 2.5e4 on every step) and curvature; best_h = the smallest "
                        "discrepancy over steps 1e-6, 1e-5, 1e-4"}
