@@ -838,6 +838,12 @@ def main():
     LOGQ = args.logq
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
+    if world > 1 and args.impl != "reference":
+        # the scaling line is the map-evaluation metric alone: the other
+        # configurations and the CPU baseline are single-GPU measurements
+        # that would hold every rank's GPU while rank 0 ran them
+        args.no_cpu = args.no_bve = args.no_bve3 = args.no_kernels = True
+        args.no_ensemble = args.no_adjoint = args.no_transport = True
     cfg = {"workload": f"flow-map evaluation: level-{LEVEL} icosahedral mesh (163842 vertices, "
                        f"327680 triangles), {SUBMAPS} composed submaps, 2^{LOGQ} uniform queries; "
                        "FP64 points, int32 triangle ids, FP64 Jacobians",
