@@ -276,6 +276,86 @@ __global__ void __launch_bounds__(256) vorticity_bwd_sh_kernel(MeshView vm, int 
     if (acc[k] != 0.0) atomicAdd(gsh + k, acc[k]);
 }
 
+// The same sums for lmax <= kShTiledMax without warp shuffles: each warp
+// takes 32 points at a time, stages their weighted basis values of one order
+// m in shared memory (one row per point), and lane v then sums column v
+// over the 32 points into the warp's own coefficient accumulators; the
+// block's warps are added at the end, one global atomic per coefficient per
+// block.  About half the FP64 work of the shuffle form.
+constexpr int kShTiledMax = 32;
+constexpr int kShTiledWarps = 4;
+
+__global__ void __launch_bounds__(32 * kShTiledWarps) vorticity_bwd_sh_tiled_kernel(
+    MeshView vm, int lmax, const double* __restrict__ X, int64_t Q, const double* __restrict__ gw,
+    double* __restrict__ gsh) {
+  extern __shared__ double sbuf[];
+  const int w = 2 * lmax + 1;
+  const int K = (lmax + 1) * w;
+  const int T = kShTableMax + 1;
+  const int ncol = 2 * (lmax + 1) + 1;   // odd row length against bank conflicts
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double* stage = sbuf + (int64_t)warp * (32 * ncol + K);
+  double* acc = stage + 32 * ncol;
+  for (int k = lane; k < K; k += 32) acc[k] = 0.0;
+  __syncwarp();
+  const int64_t nw = (int64_t)gridDim.x * kShTiledWarps;
+  for (int64_t base = ((int64_t)blockIdx.x * kShTiledWarps + warp) * 32; base < Q; base += nw * 32) {
+    const int64_t i = base + lane;
+    double wb = 0.0;
+    ShPoint pt{1.0, 0.0, 1.0, 0.0};
+    if (i < Q) {
+      wb = gw[i];
+      pt = sh_point(X[3 * i], X[3 * i + 1], X[3 * i + 2]);
+    }
+    double* row = stage + lane * ncol;
+    double pmm = 0.28209479177387814, cm = 1.0, sm = 0.0;
+    for (int m = 0; m <= lmax; ++m) {
+      if (m > 0) {
+        pmm = -pmm * __ldg(vm.sh_fm + m) * pt.st;
+        const double c2 = cm * pt.cp - sm * pt.sp;
+        sm = sm * pt.cp + cm * pt.sp;
+        cm = c2;
+      }
+      const double* ab = vm.sh_ab + 2 * (int64_t)m * T;
+      const int nl = lmax - m + 1;
+      double p1 = 0.0, p = pmm;
+      for (int l = m; l <= lmax; ++l) {
+        if (l == m + 1) {
+          p1 = p;
+          p = __ldg(ab + 2 * l) * pt.ct * pmm;
+        } else if (l > m + 1) {
+          const double pn = __ldg(ab + 2 * l) * (pt.ct * p - __ldg(ab + 2 * l + 1) * p1);
+          p1 = p;
+          p = pn;
+        }
+        if (m == 0) {
+          row[l] = wb * p;
+        } else {
+          const double f = wb * 1.4142135623730951 * p;
+          row[l - m] = f * cm;
+          row[nl + l - m] = f * sm;
+        }
+      }
+      __syncwarp();
+      const int nvals = m == 0 ? nl : 2 * nl;
+      for (int v = lane; v < nvals; v += 32) {
+        double sum = 0.0;
+#pragma unroll 8
+        for (int q = 0; q < 32; ++q) sum += stage[q * ncol + v];
+        const int j = v < nl ? v : v - nl, l = m + j;
+        acc[l * w + l + (v < nl ? m : -m)] += sum;
+      }
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < K; k += blockDim.x) {
+    double t = 0.0;
+    for (int wp = 0; wp < kShTiledWarps; ++wp) t += sbuf[(int64_t)wp * (32 * ncol + K) + 32 * ncol + k];
+    if (t != 0.0) atomicAdd(gsh + k, t);
+  }
+}
+
 // ---------------------------------------------------------- map update
 // Gradient of a patch P(gamma(b(p))) at p (fixed sub-triangle): given the
 // cotangents (Vb, Eb, Cb) of the sub-triangle barycentrics, pbar += Minv^T
@@ -614,6 +694,18 @@ int launch_vorticity_bwd(const MeshView& vm, const double* dsh, int lmax, double
     vorticity_bwd_x_kernel<<<grid_for(Q, kBlock), kBlock, 0, s>>>(vm, dsh, lmax, rot, X, Q, gw, gX);
     int rc = check("vorticity_bwd_x_kernel");
     if (rc) return rc;
+  }
+  if (gsh && lmax >= 0 && lmax <= kShTiledMax) {
+    const int ncol = 2 * (lmax + 1) + 1;
+    const size_t smem = sizeof(double) * (size_t)kShTiledWarps *
+                        (32 * ncol + (size_t)(lmax + 1) * (2 * lmax + 1));
+    cudaError_t e = cudaFuncSetAttribute(vorticity_bwd_sh_tiled_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(vorticity_bwd_sh_tiled_kernel)");
+    const int64_t chunks = (Q + 32 * kShTiledWarps - 1) / (32 * kShTiledWarps);
+    const int g = (int)(chunks < 2 * 152 ? chunks : 2 * 152);
+    vorticity_bwd_sh_tiled_kernel<<<g, 32 * kShTiledWarps, smem, s>>>(vm, lmax, X, Q, gw, gsh);
+    return check("vorticity_bwd_sh_tiled_kernel");
   }
   if (gsh && lmax >= 0) {
     const size_t smem = sizeof(double) * (size_t)(lmax + 1) * (2 * lmax + 1);
