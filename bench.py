@@ -385,13 +385,17 @@ def bench_gpu(args, rank, world):
     if rank == 0 and not args.no_ensemble:
         torch.cuda.empty_cache()
         try:
-            res["ensemble"] = bench_ensemble(args, dev)
+            with ClockSampler(dev.index) as clk:
+                res["ensemble"] = bench_ensemble(args, dev)
+            res["ensemble"]["clocks"] = clk.summary()
         except Exception as exc:
             res["ensemble"] = {"error": f"{type(exc).__name__}: {exc}"}
         torch.cuda.empty_cache()
     if rank == 0 and not args.no_adjoint:
         try:
-            res["adjoint"] = bench_adjoint(args, dev)
+            with ClockSampler(dev.index) as clk:
+                res["adjoint"] = bench_adjoint(args, dev)
+            res["adjoint"]["clocks"] = clk.summary()
         except Exception as exc:
             res["adjoint"] = {"error": f"{type(exc).__name__}: {exc}"}
         torch.cuda.empty_cache()
@@ -403,7 +407,9 @@ def bench_gpu(args, rank, world):
         torch.cuda.empty_cache()
     if rank == 0 and not args.no_bve3:
         try:
-            res["bve_l7_L1024"] = bench_bve3(args, dev)
+            with ClockSampler(dev.index) as clk:
+                res["bve_l7_L1024"] = bench_bve3(args, dev)
+            res["bve_l7_L1024"]["clocks"] = clk.summary()
         except Exception as exc:
             res["bve_l7_L1024"] = {"error": f"{type(exc).__name__}: {exc}"}
     return res
