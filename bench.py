@@ -648,6 +648,8 @@ def bench_adjoint(args, dev):
         e[0].record()
         run.omega_T(sh)
         e[1].record()
+    run.gradient(sh, target)              # warm-up: the allocator's pools, the adjoint's FFT plans
+    torch.cuda.synchronize()
     e[2].record()
     J, grad = run.gradient(sh, target)
     e[3].record()
