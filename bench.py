@@ -630,8 +630,9 @@ def bench_adjoint(args, dev):
     mesh through 200 RK4 steps of dt = 1/200, remap every 20 steps (each
     remap interval checkpointed, recomputed in the backward pass); target
     = the same run from the coefficients + 10 % of a second seeded set.
-    FP64 form.  Checked against centred differences (h = 1e-6) on
-    args.adjoint_fd random coefficients."""
+    FP64 form.  The forward and the gradient are each timed after one
+    untimed pass (the target run; a first gradient).  Checked against
+    centred differences (h = 1e-6) on args.adjoint_fd random coefficients."""
     import torch
     from cmm_gpu.adjoint import BVEGradient
     from cmm_gpu.workloads import random_sh_vorticity
