@@ -309,3 +309,20 @@ def test_nonfinite_initial_condition_is_reported(sims):
     good = sims.BVESolver(verts, tris, 2, 8, 8, 1.0, sims.Vorticity(sh=a), n_maps=3).run()
     assert good.mesh.status() == 0 and good.vm.status() == 0
     assert bool(torch.isfinite(good.omega).all())
+
+
+def test_reference_drivers(sims):
+    """euler_simulation_sphere_remapping with the reference's signature
+    against the reference's own run (bve_l2_L8.npz, its 12-step run), and
+    euler_simulation_sphere (no remapping) equal to the solver's one-map run."""
+    d = np.load(os.path.join(GOLDEN, "bve_l2_L8.npz"))
+    mesh = _ref_mesh_l2()
+    comp = sims.euler_simulation_sphere_remapping(8, 12, 1.0, mesh, "rossby_wave", rot_rate=2 * np.pi, n_maps=5)
+    assert comp.Nc == int(d["Nc"]) and list(comp.ns) == list(d["ns"])
+    img = comp(dev(d["q"])).cpu().numpy()
+    np.testing.assert_allclose(img, d["img"], rtol=0, atol=5e-9)
+    one = sims.euler_simulation_sphere(8, 12, 1.0, mesh, "rossby_wave")
+    s = sims.BVESolver(mesh.vertices, mesh.simplices, 2, 8, 12, 1.0, "rossby_wave", n_maps=12).run()
+    assert s.Nc == 1
+    q = dev(d["q"])
+    assert torch.equal(one(q).T.contiguous(), s.composite(q)[0])
