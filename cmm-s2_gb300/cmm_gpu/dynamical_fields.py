@@ -110,3 +110,10 @@ def smooth_test(xyz):
     points xyz (N,3)."""
     dev = _device_of(xyz)
     return _status_mesh(dev).tracer(native.TRACER_SMOOTH_TEST, as_device(xyz, dev))
+
+
+def random_initial_condition(xyz):
+    """The random smooth field of :158-172 at points xyz (3,N): the series
+    sum_{1<=l<=32, -l<=m<l} c_lm Re Y_l^m with c numpy's seed-42 uniform(-1, 1)
+    draws, the coefficients regenerated inside the library (MT19937)."""
+    return _tracer_xyz(native.TRACER_RANDOM_SH, xyz)

@@ -300,7 +300,7 @@ EULER, IMPROVED_EULER, RK4, RK2 = 0, 1, 2, 3
 (FLOW_SOLID_BODY, FLOW_DEFORM, FLOW_DEFORM_ROT, FLOW_STATIC_VORTEX, FLOW_ROTATING_VORTEX,
  FLOW_EQUATOR_VORTEX, FLOW_DIVERGENT) = range(7)
 (TRACER_COSINE_BELL, TRACER_SLOTTED_CYLINDERS, TRACER_STATIC_VORTEX, TRACER_ROTATING_VORTEX,
- TRACER_SMOOTH_TEST) = range(5)
+ TRACER_SMOOTH_TEST, TRACER_RANDOM_SH) = range(6)
 (VORT_NONE, VORT_ROSSBY_HAURWITZ, VORT_ZONAL_JET, VORT_PERTURBED_JET, VORT_MULTI_JET,
  VORT_GAUSSIAN_VORTEX, VORT_GAUSSIAN_JETS, VORT_PERTURBED_RH) = range(8)
 

@@ -13,6 +13,8 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdint>
+#include <mutex>
 
 #include "cmm_internal.h"
 #include "device_common.cuh"
@@ -271,6 +273,42 @@ __device__ double tracer_at(const TracerSpec& ts, double x, double y, double z) 
   }
 }
 
+// random_initial_condition (:158-172): sum over 1 <= l <= 32, -l <= m < l
+// of c_lm Re Y_l^m(phi, theta), c the first 1056 of numpy's legacy
+// uniform(-1, 1, 33^2) draws after seed(42).  Re Y_l^-m = (-1)^m Re Y_l^m,
+// so the field is a cosine series sum_{m>=0} cos(m phi) sum_l A_lm Pbar_lm
+// (orthonormal Pbar with the Condon-Shortley phase, as scipy's sph_harm).
+// Tables [m][l] in constant memory: every lane reads the same entry.
+constexpr int kRandL = 32, kRandW = kRandL + 1;
+__constant__ double c_rand_A[kRandW * kRandW];       // A_lm at [m][l]
+__constant__ double c_rand_ab[2 * kRandW * kRandW];  // (a_lm, 1 / a_{l-1,m}) at [m][l]
+__constant__ double c_rand_fm[kRandW];               // sqrt((2m+1)/(2m))
+
+__device__ double random_sh_at(double x, double y, double z) {
+  const ShPoint pt = sh_point(x, y, z);
+  double f = 0.0, pmm = 0.28209479177387814;  // sqrt(1/(4 pi))
+  double cm = 1.0, sm = 0.0;
+  for (int m = 0; m <= kRandL; ++m) {
+    if (m > 0) {
+      pmm = -pmm * c_rand_fm[m] * pt.st;
+      const double c2 = cm * pt.cp - sm * pt.sp;
+      sm = sm * pt.cp + cm * pt.sp;
+      cm = c2;
+    }
+    const double* A = c_rand_A + m * kRandW;
+    const double* ab = c_rand_ab + 2 * m * kRandW;
+    double p1 = 0.0, p = pmm, acc = A[m] * pmm;
+    for (int l = m + 1; l <= kRandL; ++l) {
+      const double pn = ab[2 * l] * (pt.ct * p - ab[2 * l + 1] * p1);
+      p1 = p;
+      p = pn;
+      acc += A[l] * p;
+    }
+    f += acc * cm;
+  }
+  return f;
+}
+
 // X (n,3) points -> out (n,)
 __global__ void __launch_bounds__(kBlock) tracer_kernel(MeshView m, TracerSpec ts, const double* __restrict__ X,
                                                         int64_t n, double* __restrict__ out) {
@@ -278,7 +316,7 @@ __global__ void __launch_bounds__(kBlock) tracer_kernel(MeshView m, TracerSpec t
        i += (int64_t)gridDim.x * blockDim.x) {
     const double x = X[3 * i], y = X[3 * i + 1], z = X[3 * i + 2];
     double v = nan("");
-    if (finite3(x, y, z)) v = tracer_at(ts, x, y, z);
+    if (finite3(x, y, z)) v = ts.kind == CMM_TRACER_RANDOM_SH ? random_sh_at(x, y, z) : tracer_at(ts, x, y, z);
     if (!isfinite(v)) flag(m, CMM_FLAG_NONFINITE);
     out[i] = v;
   }
@@ -431,9 +469,98 @@ int flow_advect_points(const MeshView& mesh, int kind, double T, double alpha, i
   return check_launch("flow_advect_points_kernel");
 }
 
+namespace {
+
+// MT19937 (Matsumoto & Nishimura 1998) seeded by init_genrand, and the
+// 53-bit double of numpy's legacy random_sample ((a >> 5) 2^26 + (b >> 6))
+// / 2^53: the generator behind np.random.seed(42); np.random.uniform.
+class Mt19937 {
+ public:
+  explicit Mt19937(uint32_t seed) {
+    s_[0] = seed;
+    for (int i = 1; i < kN; ++i) s_[i] = 1812433253u * (s_[i - 1] ^ (s_[i - 1] >> 30)) + (uint32_t)i;
+  }
+  uint32_t next() {
+    if (i_ >= kN) {
+      for (int k = 0; k < kN; ++k) {
+        const uint32_t y = (s_[k] & 0x80000000u) | (s_[(k + 1) % kN] & 0x7fffffffu);
+        s_[k] = s_[(k + 397) % kN] ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
+      }
+      i_ = 0;
+    }
+    uint32_t y = s_[i_++];
+    y ^= y >> 11;
+    y ^= (y << 7) & 0x9d2c5680u;
+    y ^= (y << 15) & 0xefc60000u;
+    y ^= y >> 18;
+    return y;
+  }
+  double sample() {
+    const uint32_t a = next() >> 5, b = next() >> 6;
+    return (a * 67108864.0 + b) / 9007199254740992.0;
+  }
+
+ private:
+  static constexpr int kN = 624;
+  uint32_t s_[kN];
+  int i_ = kN;
+};
+
+// Uploads the tables of the random tracer once per device, outside a
+// stream capture (a capture that meets them missing gets CMM_ERR_ARG).
+int ensure_random_tables(cudaStream_t s) {
+  static std::mutex mu;
+  static bool done[64] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cmm_tracer_eval");
+  if (dev < 0 || dev >= 64) {
+    set_last_error("cmm_tracer_eval: device ordinal out of range");
+    return CMM_ERR_ARG;
+  }
+  std::lock_guard<std::mutex> lock(mu);
+  if (done[dev]) return CMM_OK;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if ((e = cudaStreamIsCapturing(s, &cs)) != cudaSuccess) return cuda_fail(e, "cmm_tracer_eval");
+  if (cs != cudaStreamCaptureStatusNone) {
+    set_last_error("cmm_tracer_eval: call the random tracer once outside a stream capture first");
+    return CMM_ERR_ARG;
+  }
+  // coefficient lm = l(l-1) + l + m, the order of the reference's double loop
+  Mt19937 rng(42);
+  double c[kRandW * kRandW];
+  for (double& v : c) v = -1.0 + 2.0 * rng.sample();
+  double A[kRandW * kRandW] = {}, ab[2 * kRandW * kRandW] = {}, fm[kRandW] = {};
+  for (int l = 1; l <= kRandL; ++l) {
+    const int base = l * (l - 1) + l;
+    A[l] = c[base];                                        // m = 0
+    for (int m = 1; m < l; ++m)
+      A[m * kRandW + l] = c[base + m] + ((m & 1) ? -c[base - m] : c[base - m]);
+    A[l * kRandW + l] = (l & 1) ? -c[base - l] : c[base - l];  // m = l: only Y_l^-l
+  }
+  for (int m = 0; m <= kRandL; ++m) {
+    if (m > 0) fm[m] = std::sqrt((2.0 * m + 1) / (2.0 * m));
+    double a_prev = 0.0;
+    for (int l = m + 1; l <= kRandL; ++l) {
+      const double a = std::sqrt((4.0 * l * l - 1) / ((double)l * l - (double)m * m));
+      ab[2 * (m * kRandW + l)] = a;
+      ab[2 * (m * kRandW + l) + 1] = a_prev > 0.0 ? 1.0 / a_prev : 0.0;
+      a_prev = a;
+    }
+  }
+  if ((e = cudaMemcpyToSymbol(c_rand_A, A, sizeof(A))) != cudaSuccess ||
+      (e = cudaMemcpyToSymbol(c_rand_ab, ab, sizeof(ab))) != cudaSuccess ||
+      (e = cudaMemcpyToSymbol(c_rand_fm, fm, sizeof(fm))) != cudaSuccess)
+    return cuda_fail(e, "cmm_tracer_eval: random tracer tables");
+  done[dev] = true;
+  return CMM_OK;
+}
+
+}  // namespace
+
 int launch_tracer(const MeshView& m, int kind, double t, const double* X, int64_t n, double* out,
                   cudaStream_t s) {
-  if (kind < CMM_TRACER_COSINE_BELL || kind > CMM_TRACER_SMOOTH_TEST) {
+  if (kind < CMM_TRACER_COSINE_BELL || kind > CMM_TRACER_RANDOM_SH) {
     set_last_error("cmm_tracer_eval: unknown tracer");
     return CMM_ERR_ARG;
   }
@@ -446,6 +573,10 @@ int launch_tracer(const MeshView& m, int kind, double t, const double* X, int64_
   transpose3(B, Bt);
   matmul3(A, Bt, ts.rot);
   if (n == 0) return CMM_OK;
+  if (kind == CMM_TRACER_RANDOM_SH) {
+    const int rc = ensure_random_tables(s);
+    if (rc) return rc;
+  }
   tracer_kernel<<<grid_for(n, kBlock), kBlock, 0, s>>>(m, ts, X, n, out);
   return check_launch("tracer_kernel");
 }

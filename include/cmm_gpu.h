@@ -153,6 +153,9 @@ int cmm_flow_advect_project(const cmm_mesh* mesh, int flow, double T, double alp
 #define CMM_TRACER_STATIC_VORTEX 2      /* static_vort_IC, :85-88 */
 #define CMM_TRACER_ROTATING_VORTEX 3    /* rotating_vort_IC, :90-95 */
 #define CMM_TRACER_SMOOTH_TEST 4        /* test_func of the transport test */
+#define CMM_TRACER_RANDOM_SH 5          /* random_initial_condition, :158-172: the
+                                           degree-32 series of numpy's seed-42 draws;
+                                           first call outside a stream capture */
 int cmm_tracer_eval(const cmm_mesh* mesh, int tracer, double t, const double* X, int64_t n, double* out,
                     void* stream);
 

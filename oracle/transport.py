@@ -155,10 +155,28 @@ def smooth_test(xyz):
     return np.sin(x ** 2) * (10 * np.cos(y - 2)) + np.cos(10 * z ** 5) + 2 * np.sin(x * 3 * (z - 0.1) + y ** 7)
 
 
+def random_initial_condition(xyz):
+    """dynamical_fields.py:158-172; xyz (3, N).  The module-level draws
+    (np.random.seed(42); uniform(-1, 1, 33**2)) taken from a private
+    RandomState with the same seed, so the global generator is untouched;
+    scipy's sph_harm(m, l, phi, theta) is sph_harm_y(l, m, theta, phi)."""
+    from scipy.special import sph_harm_y
+    coeffs = np.random.RandomState(42).uniform(-1, 1, 33 ** 2)
+    phi, theta = _cart2sphere(xyz)
+    out, lm = 0, 0
+    for l in range(33):
+        for m in range(-l, l):
+            out = out + coeffs[lm] * sph_harm_y(l, m, theta, phi).real
+            lm += 1
+    return out
+
+
 def tracer(kind, X, t=0.0):
     """Tracer `kind` at points X (N, 3)."""
     if kind == "smooth_test":
         return smooth_test(X)
+    if kind == "random_initial_condition":
+        return random_initial_condition(X.T)
     if kind == "static_vort_IC":
         return static_vort_ic(t, X.T)
     if kind == "rotating_vort_IC":
@@ -167,4 +185,5 @@ def tracer(kind, X, t=0.0):
     return {"cosine_bell": cosine_bell, "IC_SC": slotted_cylinders}[kind](phi, theta)
 
 
-TRACERS = ["cosine_bell", "IC_SC", "static_vort_IC", "rotating_vort_IC", "smooth_test"]
+TRACERS = ["cosine_bell", "IC_SC", "static_vort_IC", "rotating_vort_IC", "smooth_test",
+           "random_initial_condition"]

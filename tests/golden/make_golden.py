@@ -236,6 +236,7 @@ def main():
     out["tr_IC_SC"] = rfields.IC_SC(phi, theta)
     out["tr_static_vort_IC"] = rfields.static_vort_IC(0.4, X.T.copy())
     out["tr_rotating_vort_IC"] = rfields.rotating_vort_IC(0.4, X.T.copy())
+    out["tr_random_initial_condition"] = rfields.random_initial_condition(X.T.copy())
     # the loop of tests/test_spherical_transport.py at level 3 (Nt = 2^3 + 10
     # steps of RK4 over T = 1, u_deform_rot) with remapping every 5 steps
     verts = m.vertices

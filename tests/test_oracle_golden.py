@@ -189,6 +189,47 @@ def test_transport_flows_and_tracers():
                                        err_msg=name)
     for name in ("cosine_bell", "IC_SC", "static_vort_IC", "rotating_vort_IC"):
         np.testing.assert_allclose(TR.tracer(name, X, t=0.4), d[f"tr_{name}"], rtol=0, atol=1e-14, err_msg=name)
+    # the degree-32 random series: the same scipy function and draws, summed
+    # in the same order
+    np.testing.assert_allclose(TR.tracer("random_initial_condition", X), d["tr_random_initial_condition"],
+                               rtol=0, atol=1e-13)
+
+
+def test_random_tracer_series_form():
+    """The device form of random_initial_condition folds Re Y_l^-m =
+    (-1)^m Re Y_l^m into a cosine series over m >= 0 with the orthonormal
+    Pbar_lm recurrence; that rearrangement, restated in numpy, against the
+    reference's values."""
+    from oracle import transport as TR
+    d = load("transport_l3.npz")
+    X = d["X"]
+    c = np.random.RandomState(42).uniform(-1, 1, 33 ** 2)
+    x, y, z = X[:, 0], X[:, 1], X[:, 2]
+    rho = np.hypot(x, y)
+    ct, st = z / np.hypot(rho, z), rho / np.hypot(rho, z)
+    phi = np.arctan2(y, x)
+    f = np.zeros(len(X))
+    pmm = np.full(len(X), np.sqrt(1 / (4 * np.pi)))
+    for m in range(33):
+        if m:
+            pmm = -pmm * np.sqrt((2 * m + 1) / (2 * m)) * st
+        p1, p = np.zeros(len(X)), pmm
+        for l in range(m, 33):
+            if l > m:
+                a = np.sqrt((4 * l * l - 1) / (l * l - m * m))
+                b = 0.0 if l == m + 1 else 1 / np.sqrt((4 * (l - 1) ** 2 - 1) / ((l - 1) ** 2 - m * m))
+                p1, p = p, a * (ct * p - b * p1)
+            if l == 0:
+                continue
+            base = l * (l - 1) + l
+            if m == 0:
+                A = c[base]
+            elif m < l:
+                A = c[base + m] + (-1) ** m * c[base - m]
+            else:
+                A = (-1) ** l * c[base - l]
+            f += A * p * np.cos(m * phi)
+    np.testing.assert_allclose(f, d["tr_random_initial_condition"], rtol=0, atol=1e-11)
 
 
 def test_transport_run_with_remaps():
