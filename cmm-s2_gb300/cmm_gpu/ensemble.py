@@ -30,8 +30,8 @@ from .workloads import spectral_perturbation
 class SharedResources:
     """Read-only objects shared by the members: map meshes and stencil
     frames per level, velocity meshes per band-limit (and record
-    precision), the MWSS sample points and the split-BF16 table owner per
-    band-limit."""
+    precision), the MWSS sample points and the Legendre table owners
+    (split-BF16 and FP64) per band-limit."""
 
     def __init__(self, device):
         self.device = device
@@ -71,7 +71,8 @@ class SharedResources:
         return self._grid[L]
 
     def sht_tables(self, L):
-        """The plan holding the split-BF16 tables of band-limit L, or None."""
+        """The plan holding the split-BF16 tables of band-limit L (key L), or
+        the FP64 Pbar tables (key ("fp64", L)), or None."""
         return self._sht.get(L)
 
     def set_sht_tables(self, L, sht):

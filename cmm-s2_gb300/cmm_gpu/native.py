@@ -393,7 +393,9 @@ class Sht:
         return self
 
     def share_tables(self, src):
-        """Split-BF16 mode on src's Pbar tables (cmm_sht_share_tables)."""
+        """Share src's Legendre tables (cmm_sht_share_tables): split-BF16
+        mode on src's tables when src is in that mode, else src's FP64 Pbar
+        tables."""
         with torch.cuda.device(self.device):
             check(lib.cmm_sht_share_tables(self.h, src.h), "cmm_sht_share_tables")
         self._tables_from = src   # keep the owner alive

@@ -105,6 +105,13 @@ class BVESolver:
                     resources.set_sht_tables(L, self.sht)
         else:
             self.precision_mode = native.Sht.FP64
+            tabled = L <= 512 if fp64_tables is None else bool(fp64_tables)
+            if resources is not None and tabled:
+                src = resources.sht_tables(("fp64", L))
+                if src is not None:
+                    self.sht.share_tables(src)
+                else:
+                    resources.set_sht_tables(("fp64", L), self.sht)
         ns = [i for i in range(1, Nt) if i % n_maps == 0]
         ns.append(Nt)
         self.ns = ns

@@ -241,7 +241,7 @@ int sht_scalar_jets(cmm_sht* p, const cmm_mesh* vm, const double2* alm, double* 
 int sht_power(cmm_sht* p, const double2* alm, double* power, cudaStream_t s);
 int* sht_status_word(cmm_sht* p);
 int sht_set_tables(cmm_sht* p, int mode);
-int sht_share_tables(cmm_sht* p, const cmm_sht* src);
+int sht_share_tables(cmm_sht* p, cmm_sht* src);
 int sht_velocity_bwd(cmm_sht* p, const cmm_mesh* vm, const double* gjets, double* gomega, cudaStream_t s);
 int sht_trim(cmm_sht* p);
 int bve_create(const cmm_bve_desc* d, cmm_bve** out);

@@ -23,6 +23,7 @@
 #include <cufft.h>
 
 #include <cmath>
+#include <memory>
 #include <vector>
 
 #include "cmm_internal.h"
@@ -973,7 +974,12 @@ struct cmm_sht {
   cufftHandle torus_fwd_t = 0, pad_inv_t = 0;
   bool have_tplans[2] = {false, false};
   cmm::DeviceBuffer ct_rings, ct_fine, w_fine, pmm_rings, pmm_fine, ra, rb;
-  cmm::DeviceBuffer tab_a, tab_s;   // Pbar tables of the FP64 stages
+  // Pbar tables of the FP64 stages (analysis a, synthesis s); plans of one
+  // band-limit may hold the same tables (cmm_sht_share_tables)
+  struct PbarTables {
+    cmm::DeviceBuffer a, s;
+  };
+  std::shared_ptr<PbarTables> tab;
   int tab_mode = 0;                 // cmm_sht_set_tables: 0 auto, 1 always, -1 never
   cmm::DeviceBuffer spec, torus, pad, alm, fields, synth, samples, status;
   cmm::TcPlan* tc = nullptr;
@@ -1139,7 +1145,7 @@ static int ensure_tables(cmm_sht* p, cudaStream_t s, bool* ok) {
   *ok = false;
   const int L = p->L;
   if (p->tab_mode < 0 || (p->tab_mode == 0 && L > kTabMaxL) || L > kTabShared) return CMM_OK;
-  if (p->tab_a.p && p->tab_s.p) {
+  if (p->tab) {
     *ok = true;
     return CMM_OK;
   }
@@ -1152,21 +1158,19 @@ static int ensure_tables(cmm_sht* p, cudaStream_t s, bool* ok) {
   const int64_t tri = (int64_t)L * (L + 1) / 2;
   const int na = L + 1, ns = L / 2 + 1;
   int rc;
-  if ((rc = p->tab_a.alloc((size_t)tri * na * 8)) || (rc = p->tab_s.alloc((size_t)tri * ns * 8))) {
-    p->tab_a.release();
-    p->tab_s.release();
-    return rc;
-  }
+  auto tab = std::make_shared<cmm_sht::PbarTables>();
+  if ((rc = tab->a.alloc((size_t)tri * na * 8)) || (rc = tab->s.alloc((size_t)tri * ns * 8))) return rc;
   build_pbar_kernel<<<dim3((na + 127) / 128, L), 128, 0, s>>>(L, na, (const double*)p->ct_fine.p,
                                                               (const double*)p->pmm_fine.p, 2 * L + 1,
                                                               (const double*)p->ra.p, (const double*)p->rb.p,
-                                                              false, (double*)p->tab_a.p);
+                                                              false, (double*)tab->a.p);
   if ((rc = check_launch("build_pbar_kernel"))) return rc;
   build_pbar_kernel<<<dim3((ns + 127) / 128, L), 128, 0, s>>>(L, ns, (const double*)p->ct_rings.p,
                                                               (const double*)p->pmm_rings.p, L + 1,
                                                               (const double*)p->ra.p, (const double*)p->rb.p,
-                                                              true, (double*)p->tab_s.p);
+                                                              true, (double*)tab->s.p);
   if ((rc = check_launch("build_pbar_kernel"))) return rc;
+  p->tab = std::move(tab);
   *ok = true;
   return CMM_OK;
 }
@@ -1255,7 +1259,7 @@ int sht_forward(cmm_sht* p, const double* samples, double2* out, cudaStream_t s)
   if ((rc = ensure_tables(p, s, &tab))) return rc;
   if (tab) {
     analysis_tab_kernel<<<dim3(L, (L + kTabBlock - 1) / kTabBlock), kTabBlock, 0, s>>>(
-        (const double2*)p->pad.p, L, (const double*)p->w_fine.p, (const double*)p->tab_a.p, out);
+        (const double2*)p->pad.p, L, (const double*)p->w_fine.p, (const double*)p->tab->a.p, out);
     return check_launch("analysis_tab_kernel");
   }
   analysis_kernel<<<L, 256, 0, s>>>((const double2*)p->pad.p, L, (const double*)p->w_fine.p,
@@ -1296,9 +1300,9 @@ int sht_inverse(cmm_sht* p, const double2* alm, int nf, double* samples, cudaStr
     const int G = nf == kFields ? 3 : 1;
     dim3 gt(L, (npair + kTabBlock - 1) / kTabBlock, nf / G);
     if (G == 3)
-      synthesis_tab_kernel<3><<<gt, kTabBlock, 0, s>>>(alm, L, (const double*)p->tab_s.p, S);
+      synthesis_tab_kernel<3><<<gt, kTabBlock, 0, s>>>(alm, L, (const double*)p->tab->s.p, S);
     else
-      synthesis_tab_kernel<1><<<gt, kTabBlock, 0, s>>>(alm, L, (const double*)p->tab_s.p, S);
+      synthesis_tab_kernel<1><<<gt, kTabBlock, 0, s>>>(alm, L, (const double*)p->tab->s.p, S);
     if ((rc = check_launch("synthesis_tab_kernel"))) return rc;
   } else {
   dim3 g(L, (npair + kSynthBlock - 1) / kSynthBlock);
@@ -1412,7 +1416,7 @@ int sht_velocity_bwd(cmm_sht* p, const cmm_mesh* vm, const double* gjets, double
     if ((rc = ensure_tables(p, s, &tab))) return rc;
     if (tab) {
       const dim3 gt(L, (L + kTabBlock - 1) / kTabBlock, kFields / 2);
-      legendre_sum_tab_kernel<2><<<gt, kTabBlock, 0, s>>>(Sb, L + 1, L, 2.0, (const double*)p->tab_s.p, Fb, fin,
+      legendre_sum_tab_kernel<2><<<gt, kTabBlock, 0, s>>>(Sb, L + 1, L, 2.0, (const double*)p->tab->s.p, Fb, fin,
                                                           fout);
     } else if (npair <= 256)
       legendre_sum_kernel<1><<<gl, 256, 0, s>>>(Sb, L + 1, L, L, nullptr, 2.0, ct, pm, L + 1, ra, rb, Fb, fin, fout);
@@ -1508,15 +1512,34 @@ int sht_set_tables(cmm_sht* p, int mode) {
   if (mode < 0 || (mode == 0 && p->L > kTabMaxL)) {
     cudaError_t e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return cuda_fail(e, "cmm_sht_set_tables");
-    p->tab_a.release();
-    p->tab_s.release();
+    p->tab.reset();
   }
   return CMM_OK;
 }
 
-int sht_share_tables(cmm_sht* p, const cmm_sht* src) {
-  if (!src->tc || src->L != p->L) {
-    set_last_error("cmm_sht_share_tables: source plan of the same L in CMM_SHT_SPLIT_BF16 mode expected");
+int sht_share_tables(cmm_sht* p, cmm_sht* src) {
+  if (src->L != p->L || p == src) {
+    set_last_error("cmm_sht_share_tables: a different source plan of the same L expected");
+    return CMM_ERR_ARG;
+  }
+  if (src->precision == CMM_SHT_FP64) {
+    // the FP64 Pbar tables, built on the source first when its table mode
+    // gives it tables; p keeps its precision and takes src's table mode
+    bool ok = false;
+    int rc = ensure_tables(src, 0, &ok);
+    cudaError_t e = cudaDeviceSynchronize();
+    if (rc) return rc;
+    if (e != cudaSuccess) return cuda_fail(e, "cmm_sht_share_tables");
+    if (!ok) {
+      set_last_error("cmm_sht_share_tables: the source plan's FP64 stages run without Pbar tables");
+      return CMM_ERR_ARG;
+    }
+    p->tab = src->tab;
+    p->tab_mode = src->tab_mode;
+    return CMM_OK;
+  }
+  if (!src->tc) {
+    set_last_error("cmm_sht_share_tables: source plan without split-BF16 tables");
     return CMM_ERR_ARG;
   }
   if (p->tc) {
@@ -1536,8 +1559,7 @@ int sht_trim(cmm_sht* p) {
   if (e != cudaSuccess) return cuda_fail(e, "cmm_sht_trim");
   p->synth.release();
   p->samples.release();
-  p->tab_a.release();
-  p->tab_s.release();
+  p->tab.reset();
   return CMM_OK;
 }
 

@@ -310,10 +310,14 @@ int cmm_sht_destroy(cmm_sht* plan);
 #define CMM_SHT_FP64 0
 #define CMM_SHT_SPLIT_BF16 1
 int cmm_sht_set_precision(cmm_sht* plan, int mode);
-/* Put `plan` in CMM_SHT_SPLIT_BF16 mode using the Pbar tables of `src`
- * (same L, already in that mode) instead of building its own: plans of one
- * band-limit share the ~4.4 GB of tables at L = 1024 and still run
- * concurrently (each keeps its own data tiles and FFT scratch). */
+/* Share the Legendre tables of `src` (another plan of the same L) instead
+ * of building them again; plans of one band-limit then share one copy and
+ * still run concurrently (each keeps its own data tiles and FFT scratch).
+ * src in CMM_SHT_SPLIT_BF16 mode: `plan` is put in that mode on src's
+ * split-bf16 Pbar tables (~4.4 GB at L = 1024).  src in CMM_SHT_FP64 mode:
+ * `plan` keeps its precision and takes src's FP64 Pbar tables (built on
+ * src first; 0.8 GB at L = 512) and table mode; CMM_ERR_ARG when src's
+ * FP64 stages run without tables (cmm_sht_set_tables).  Synchronises. */
 int cmm_sht_share_tables(cmm_sht* plan, cmm_sht* src);
 /* Failure-path self-test: runs the tensor-core kernels' bounded mbarrier
  * wait on a barrier that nothing ever completes, with a limit of `polls`

@@ -17,23 +17,25 @@ def mods():
     return ensemble, spherical_simulations, autotune, workloads, meshgen
 
 
-def _alone(mods, spec, i, seed, Nt, T, lmax, rms, n_maps):
+def _alone(mods, spec, i, seed, Nt, T, lmax, rms, n_maps, precision="split_bf16"):
     ensemble, sims, _, workloads, meshgen = mods
     level, L = spec
     verts, tris = meshgen.icosahedral_mesh(level)
     pert = workloads.spectral_perturbation(lmax, seed=seed * 100003 + i, slope=-2.0, rms=rms)
     s = sims.BVESolver(verts, tris, level, L, Nt, T, sims.Vorticity(spline_sh=pert), n_maps=n_maps,
-                       precision="split_bf16")
+                       precision=precision)
     return s.run()
 
 
-@pytest.mark.parametrize("persistent", [False, True])
-def test_ensemble_graph_matches_members_alone(mods, persistent):
+@pytest.mark.parametrize("persistent,precision", [(False, "split_bf16"), (True, "split_bf16"),
+                                                  (True, "fp64")])
+def test_ensemble_graph_matches_members_alone(mods, persistent, precision):
     """One graph replay per step, or (persistent) the whole remaining run
-    captured as one graph and launched once."""
+    captured as one graph and launched once; FP64 members share one set of
+    Pbar tables per band-limit."""
     ensemble, sims, autotune, _, _ = mods
     kw = dict(levels=(2, 3), bandlimits=(16, 32), Nt=14, T=0.1, lmax=8, rms=3.0, n_maps=4)
-    ens = ensemble.Ensemble.from_seed(5, seed=7, **kw).bootstrap()
+    ens = ensemble.Ensemble.from_seed(5, seed=7, precision=precision, **kw).bootstrap()
     tuner = autotune.Autotuner(reps=1)
     tuner.tune_ensemble_kernels(ens)
     tuner.tune_schedule(ens, stream_counts=(1, 3), steps_each=1)
@@ -45,7 +47,7 @@ def test_ensemble_graph_matches_members_alone(mods, persistent):
     torch.cuda.synchronize()
     assert ens.count == ens.members[0].Nt - 2
     for i, (m, spec) in enumerate(zip(ens.members, ens.specs)):
-        ref = _alone(mods, spec, i, 7, kw["Nt"], kw["T"], kw["lmax"], kw["rms"], kw["n_maps"])
+        ref = _alone(mods, spec, i, 7, kw["Nt"], kw["T"], kw["lmax"], kw["rms"], kw["n_maps"], precision)
         assert m.Nc == ref.Nc and m.count == ref.count
         assert torch.equal(m.omega, ref.omega), i
         for k in range(m.Nc):

@@ -245,6 +245,33 @@ def test_fp64_table_and_recurrence_stages_agree(nat, L):
         np.testing.assert_allclose(j1 / s, j0 / s, rtol=0, atol=1e-13)
 
 
+def test_shared_fp64_tables_give_the_owners_bits(nat):
+    """A plan on another plan's FP64 Pbar tables (cmm_sht_share_tables with
+    an FP64 source) gives the bits of a plan with its own tables, also after
+    the owner is trimmed (the tables live while a holder does); sharing from
+    a plan that runs without tables, or from itself, is an argument error."""
+    L = 48
+    rng = np.random.default_rng(3)
+    f = rng.standard_normal((L + 1, 2 * L))
+    f[0], f[-1] = f[0, 0], f[-1, 0]
+    a = np.tril(rng.standard_normal((L, L)) + 1j * rng.standard_normal((L, L)))
+    a[:, 0] = a[:, 0].real
+    many = dev(np.stack([mhalf(a * (k + 1)) for k in range(12)]))
+    own = nat.Sht(L)
+    ref = (own.forward(dev(f)), own.inverse(many))
+    src = nat.Sht(L)
+    user = nat.Sht(L).share_tables(src)
+    src.trim()
+    got = (user.forward(dev(f)), user.inverse(many))
+    for x, y in zip(ref, got):
+        assert torch.equal(x, y)
+    assert user.status() == 0
+    with pytest.raises(RuntimeError):
+        nat.Sht(L).share_tables(nat.Sht(L).set_tables(nat.Sht.TABLES_NEVER))
+    with pytest.raises(RuntimeError):
+        user.share_tables(user)
+
+
 def test_bounded_wait_timeout_sets_status_and_context_survives(nat):
     """The tensor-core kernels' bounded mbarrier wait, run on a barrier that
     nothing completes (cmm_sht_timeout_selftest, 1000 polls), runs out, sets
