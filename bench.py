@@ -167,6 +167,39 @@ def cpu_rate(verts, tris, jets, nq, workers, steps=1, warmup=0):
     return steps * nq * len(jets) / dt, workers
 
 
+def parity_sample(verts, tris, jets, Q, n=2048):
+    """The oracle on a seeded subset of the timed queries of rank 0 (the
+    same generator and seed as bench_gpu): images, chained Jacobians and
+    the triangle containing each query, with its distance to the nearest
+    edge great circle (the location-parity rule accepts either triangle
+    within 1e-14 of an edge)."""
+    from oracle import geometry as OG, spline as OS
+    from cmm_gpu.meshgen import random_sphere_points
+    idx = np.sort(np.random.default_rng(11).choice(Q, n, replace=False))
+    qs = random_sphere_points(Q, seed=3)[idx]
+    if "_ORC" not in globals():
+        _oracle_init(verts, tris, jets)
+    X, J = OS.composite_jacobian(_ORC, qs)
+    tri = _ORC.loc.locate(qs)
+    return {"idx": idx, "X": X, "J": J, "tri": tri, "edge": OG.edge_distance(verts, tris, tri, qs)}
+
+
+def parity_report(ref, got):
+    """Location, image and Jacobian agreement of the GPU outputs with the
+    oracle on the parity sample."""
+    mism = got["tri"] != ref["tri"]
+    near = ref["edge"] <= 1e-14
+    Jo, Jg = ref["J"], got["jac"]
+    jrel = np.abs(Jg - Jo).max(axis=(1, 2)) / np.abs(Jo).max(axis=(1, 2))
+    return {"sample": int(len(ref["idx"])),
+            "queries": "seeded subset (numpy default_rng(11)) of rank 0's timed queries",
+            "tri_mismatch": int(mism.sum()), "tri_mismatch_away_from_edges": int((mism & ~near).sum()),
+            "queries_within_1e-14_of_an_edge": int(near.sum()),
+            "points_max_abs_err": float(np.abs(got["out"] - ref["X"]).max()),
+            "jac_max_rel_err": float(jrel.max()),
+            "oracle": "numpy restatement of the reference, pinned to its golden vectors"}
+
+
 def cpu_bve_rate(steps=8):
     """BVE steps/s of the oracle (the restated reference driver) on the
     barotropic configuration of bench_bve (level 4, L=128, dt=1/200, remap
@@ -225,7 +258,7 @@ def max_over_ranks(ms, device=None):
     return float(t.item())
 
 
-def bench_gpu(args, rank, world):
+def bench_gpu(args, rank, world, sample_idx=None):
     import torch
     from cmm_gpu import native
 
@@ -302,6 +335,10 @@ def bench_gpu(args, rank, world):
     ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, dev)
     # the composition kernel alone (the roofline's kernel)
     ms_compose = sum(a.elapsed_time(b) for a, b in marks) / args.steps
+    sample = None
+    if sample_idx is not None:   # outputs of the timed steps at the parity sample
+        ix = torch.from_numpy(sample_idx).to(dev)
+        sample = {"out": out[ix].cpu().numpy(), "tri": tri[ix].cpu().numpy(), "jac": jac[ix].cpu().numpy()}
     # the same step with the queries grouped by coarse cell first
     # (cmm_query_order + cmm_compose_ordered): a fifth of the DRAM traffic,
     # reported beside the headline
@@ -366,7 +403,7 @@ def bench_gpu(args, rank, world):
     del scratch
 
     res = dict(ms=ms, ms_compose=ms_compose, ordered=ordered, values_only=values, value=value, ms_e2e=ms_e2e, launches=launches, clocks=clk.summary(), numa_cores=numa_cores,
-               nv=len(verts), nt=len(tris), Q=Q, fp64_fma_per_s=fp64_fma_per_s)
+               nv=len(verts), nt=len(tris), Q=Q, fp64_fma_per_s=fp64_fma_per_s, sample=sample)
     if rank == 0 and not args.no_bve:
         try:
             res["bve"] = bench_bve(args, dev)
@@ -911,7 +948,7 @@ def main():
         return
     if world > 1:
         torch.distributed.init_process_group("nccl")
-    cpu = cpu_bve = None
+    cpu = cpu_bve = par = None
     if rank == 0 and not args.no_cpu:
         # timed before any CUDA work so the spawn pool starts cleanly
         verts, tris, jets, _ = workload()
@@ -919,9 +956,10 @@ def main():
         cpu = {"value": rate, "unit": "map evals/s", "cores": used, "kind": "port",
                "sample": f"{max(1024, args.cpu_queries // 8)} queries x {SUBMAPS} submaps with "
                          "Jacobians, numpy oracle (restated reference), 1 thread"}
+        par = parity_sample(verts, tris, jets, 1 << LOGQ)
         if not args.no_bve:
             cpu_bve = cpu_bve_rate()
-    r = bench_gpu(args, rank, world)
+    r = bench_gpu(args, rank, world, None if par is None else par["idx"])
     if rank != 0:
         torch.distributed.destroy_process_group()
         return
@@ -951,6 +989,8 @@ def main():
         "clocks": r["clocks"], "gpu_launches": r["launches"],
     }
     line["points_only"] = r["values_only"]
+    if par is not None and r.get("sample") is not None:
+        line["parity"] = parity_report(par, r["sample"])
     for key in ("bve", "rh_error", "bve_l7_L1024", "kernels", "ensemble", "adjoint", "transport"):
         if key in r:
             line[key] = r[key]
