@@ -9,8 +9,8 @@
 // lo = bf16(x - hi)), and the product is taken as three tensor-core
 // products hi*hi + hi*lo + lo*hi accumulated in FP32 in tensor memory; the
 // FP32 partial sums of every 64-l chunk are drained into compensated
-// (Kahan) FP32 register sums, converted to FP64 once at the end (FP64
-// issue per chunk would bind the kernel on GB300's FP64 pipe).
+// (Kahan) FP32 register sums, combined into the FP32 spectra at the end
+// (FP64 issue would bind the kernel on GB300's FP64 pipe).
 //
 // Data movement: the Pbar tables (per m, ring block of 128 pairs, l chunk)
 // are built once per plan directly in the shared-memory image the MMA
@@ -30,6 +30,7 @@
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <memory>
 #include <vector>
 
@@ -117,6 +118,7 @@ struct KahanF {
     s = t;
   }
   __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+  __device__ __forceinline__ float valuef() const { return s - c; }
 };
 
 // Shared-memory matrix descriptor: start, leading (k-group) and stride
@@ -248,31 +250,88 @@ __global__ void build_atab_kernel(TcGeometry g, const double2* __restrict__ fiel
 }
 
 // ------------------------------------------------------------ synthesis
-// Block (ring block, m); 128 threads.  Writes spectra S[f][t][m] for the
-// ring pair (t, L-t) of each row.
-__global__ void __launch_bounds__(kThreads) synth_tc_kernel(TcGeometry g,
-                                                            const unsigned char* __restrict__ ptab,
-                                                            const unsigned char* __restrict__ atab,
-                                                            float2* __restrict__ S,
-                                                            int* __restrict__ status) {
-  extern __shared__ __align__(1024) unsigned char smem[];
-  unsigned char* sP = smem;                    // kPRecord bytes
-  unsigned char* sA = smem + kPRecord;         // kARecord bytes
-  __shared__ __align__(8) uint64_t load_bar, mma_bar;
+// Persistent: CTA b takes the work items (m, ring block) b, b + G, ... in
+// order of increasing m (G = gridDim.x, one CTA per SM) and streams their
+// l chunks through a two-stage pipeline: once the products of chunk k are
+// in TMEM its stage is refilled with chunk k+2, chunk k+1 goes to the
+// tensor cores (the other TMEM buffer), and all four warps drain chunk k
+// into the compensated FP32 sums meanwhile.  Each work item
+// writes its spectra S[f][t][m] for the ring pairs (t, L-t) of its rows
+// after its last chunk.
+constexpr int kSynStage = kPRecord + kARecord;   // 80 KiB per stage
+constexpr uint32_t kTmemColsS = 128;             // 2 buffers x (even, odd) x 32 columns
+
+struct SynCursor {
+  int item, c, nch, m, blk;
+};
+
+// Cursor at work item `item`; false past the last one.
+__device__ __forceinline__ bool syn_set(SynCursor& u, int item, int nitems, const TcGeometry& g) {
+  u.item = item;
+  u.c = 0;
+  if (item >= nitems) return false;
+  u.m = item / g.nrb;
+  u.blk = item % g.nrb;
+  u.nch = nchunks(g.L, u.m);
+  return true;
+}
+
+// Next chunk of this CTA's stream; false at its end.
+__device__ __forceinline__ bool syn_next(SynCursor& u, int nitems, const TcGeometry& g) {
+  if (++u.c < u.nch) return true;
+  return syn_set(u, u.item + gridDim.x, nitems, g);
+}
+
+__device__ __forceinline__ void syn_load(const TcGeometry& g, const unsigned char* ptab,
+                                         const unsigned char* atab, const SynCursor& u, unsigned char* stage,
+                                         uint64_t* bar) {
+  const int64_t chunk = g.cbase[u.m] + u.c;
+  const unsigned char* srcP = ptab + (chunk * g.nrb + u.blk) * kPRecord;
+  const unsigned char* srcA = atab + chunk * kARecord;
+  mbar_expect_tx(bar, kSynStage);
+  for (int q = 0; q < 4; ++q) bulk_g2s(stage + q * kPTile, srcP + q * kPTile, kPTile, bar);
+  bulk_g2s(stage + kPRecord, srcA, kARecord, bar);
+}
+
+// The chunk's products: even and odd l into the accumulators d, d + kN.
+__device__ __forceinline__ void syn_mma(uint32_t stage, uint32_t d, uint32_t idesc) {
+  const uint32_t p0 = stage, a0 = stage + kPRecord;
+  for (int ks = 0; ks < kKc / 16; ++ks)
+    for (int par = 0; par < 2; ++par) {
+      const uint64_t ph = smem_desc(p0 + (2 * par) * kPTile + ks * 256);
+      const uint64_t pl = smem_desc(p0 + (2 * par + 1) * kPTile + ks * 256);
+      const uint64_t ah = smem_desc(a0 + (2 * par) * kATile + ks * 256);
+      const uint64_t al = smem_desc(a0 + (2 * par + 1) * kATile + ks * 256);
+      const uint32_t dd = d + par * kN;
+      mma_bf16(dd, ph, ah, idesc, ks > 0 ? 1u : 0u);
+      mma_bf16(dd, ph, al, idesc, 1u);
+      mma_bf16(dd, pl, ah, idesc, 1u);
+    }
+}
+
+__global__ void __launch_bounds__(kThreads, 1) synth_tc_kernel(TcGeometry g, int nitems,
+                                                               const unsigned char* __restrict__ ptab,
+                                                               const unsigned char* __restrict__ atab,
+                                                               float2* __restrict__ S,
+                                                               int* __restrict__ status) {
+  extern __shared__ __align__(1024) unsigned char smem[];   // 2 stages of kSynStage bytes
+  __shared__ __align__(8) uint64_t load_bar[2], mma_bar[2];
   __shared__ uint32_t tmem_base_s;
   __shared__ int abort_s;
-  const int blk = blockIdx.x, m = blockIdx.y, L = g.L;
+  const int L = g.L;
   const int tid = threadIdx.x, warp = tid >> 5;
   if (tid == 0) {
-    mbar_init(&load_bar, 1);
-    mbar_init(&mma_bar, 1);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&load_bar[b], 1);
+      mbar_init(&mma_bar[b], 1);
+    }
     abort_s = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(&tmem_base_s)),
-                 "r"(kTmemCols)
+                 "r"(kTmemColsS)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -281,81 +340,108 @@ __global__ void __launch_bounds__(kThreads) synth_tc_kernel(TcGeometry g,
   tc_fence_after();
   const uint32_t tmem = tmem_base_s;
   const uint32_t idesc = mma_idesc();
+  const uint32_t s0 = smem_u32(smem);
+  SynCursor dr;   // next chunk to drain (all threads)
+  bool have = syn_set(dr, blockIdx.x, nitems, g);
+  // tid 0 only: next chunk to load / to multiply, and the chunk counts of
+  // this CTA's stream issued and completed (chunk j uses stage and
+  // barriers j & 1, in barrier phase (j >> 1) & 1)
+  SynCursor ld = dr, mm = dr;
+  bool ld_ok = have, mm_ok = have;
+  long long n_ld = 0, n_ldw = 0, n_mm = 0, n_mmw = 0;
+  if (tid == 0 && have) {
+    for (int q = 0; q < 2 && ld_ok; ++q) {
+      syn_load(g, ptab, atab, ld, smem + (n_ld & 1) * kSynStage, &load_bar[n_ld & 1]);
+      ++n_ld;
+      ld_ok = syn_next(ld, nitems, g);
+    }
+    if (!mbar_wait(&load_bar[0], 0)) {
+      abort_s = 1;
+    } else {
+      n_ldw = 1;
+      tc_fence_after();
+      syn_mma(s0, tmem, idesc);
+      mma_commit(&mma_bar[0]);
+      n_mm = 1;
+      mm_ok = syn_next(mm, nitems, g);
+    }
+  }
   KahanF accE[kNUsed], accO[kNUsed];
-  const int nch = nchunks(L, m);
-  uint32_t ph_load = 0, ph_mma = 0;
-  for (int c = 0; c < nch; ++c) {
-    if (tid == 0) {
-      const unsigned char* srcP = ptab + ((int64_t)(g.cbase[m] + c) * g.nrb + blk) * kPRecord;
-      const unsigned char* srcA = atab + (int64_t)(g.cbase[m] + c) * kARecord;
-      mbar_expect_tx(&load_bar, kPRecord + kARecord);
-      for (int q = 0; q < 4; ++q) bulk_g2s(sP + q * kPTile, srcP + q * kPTile, kPTile, &load_bar);
-      bulk_g2s(sA, srcA, kARecord, &load_bar);
-      if (!mbar_wait(&load_bar, ph_load)) {
+  __syncthreads();
+  for (long long k = 0; have; ++k) {
+    if (tid == 0 && !abort_s) {
+      // chunk k's products (issued one iteration ago); its stage then takes
+      // chunk k+2, so two copies are in flight while chunk k+1 arrives
+      if (!mbar_wait(&mma_bar[k & 1], (uint32_t)((k >> 1) & 1))) {
         abort_s = 1;
-        mbar_wait(&load_bar, ph_load);   // bounded drain of the copies in flight
+      } else {
+        n_mmw = k + 1;
+        if (ld_ok) {
+          syn_load(g, ptab, atab, ld, smem + (n_ld & 1) * kSynStage, &load_bar[n_ld & 1]);
+          ++n_ld;
+          ld_ok = syn_next(ld, nitems, g);
+        }
       }
-      if (!abort_s) {
-        tc_fence_after();
-        const uint32_t p0 = smem_u32(sP), a0 = smem_u32(sA);
-        for (int ks = 0; ks < kKc / 16; ++ks)
-          for (int par = 0; par < 2; ++par) {
-            const uint64_t ph = smem_desc(p0 + (2 * par) * kPTile + ks * 256);
-            const uint64_t pl = smem_desc(p0 + (2 * par + 1) * kPTile + ks * 256);
-            const uint64_t ah = smem_desc(a0 + (2 * par) * kATile + ks * 256);
-            const uint64_t al = smem_desc(a0 + (2 * par + 1) * kATile + ks * 256);
-            const uint32_t d = tmem + par * kN;
-            mma_bf16(d, ph, ah, idesc, ks > 0 ? 1u : 0u);
-            mma_bf16(d, ph, al, idesc, 1u);
-            mma_bf16(d, pl, ah, idesc, 1u);
-          }
-        mma_commit(&mma_bar);
-        if (!mbar_wait(&mma_bar, ph_mma)) {
+      if (!abort_s && mm_ok) {   // chunk k+1 (= n_mm) into the other TMEM buffer
+        const int b1 = (int)(n_mm & 1);
+        if (!mbar_wait(&load_bar[b1], (uint32_t)((n_mm >> 1) & 1))) {
           abort_s = 1;
-          mbar_wait(&mma_bar, ph_mma);   // bounded drain of the MMAs in flight
+        } else {
+          n_ldw = n_mm + 1;
+          tc_fence_after();
+          syn_mma(s0 + b1 * kSynStage, tmem + b1 * 2 * kN, idesc);
+          mma_commit(&mma_bar[b1]);
+          ++n_mm;
+          mm_ok = syn_next(mm, nitems, g);
         }
       }
     }
-    ph_load ^= 1u;
-    ph_mma ^= 1u;
     __syncthreads();
     if (abort_s) break;
     tc_fence_after();
     float vE[32], vO[32];
-    const uint32_t lane_base = (uint32_t)(32 * warp) << 16;
-    tmem_ld32(tmem + lane_base, vE);
-    tmem_ld32(tmem + lane_base + kN, vO);
+    const uint32_t lanes = (uint32_t)(32 * warp) << 16;
+    const uint32_t buf = tmem + (uint32_t)(k & 1) * 2 * kN;
+    tmem_ld32(buf + lanes, vE);
+    tmem_ld32(buf + lanes + kN, vO);
 #pragma unroll
     for (int n = 0; n < kNUsed; ++n) {
       accE[n].add(vE[n]);
       accO[n].add(vO[n]);
     }
+    if (dr.c == dr.nch - 1) {   // the work item's last chunk: its spectra
+      const int t = dr.blk * kM + tid;   // TMEM lane = thread index
+      if (t < g.npair) {
+        // the spectra are FP32: the even/odd combination stays in FP32 (a
+        // few ulp; FP64 here took 240 FP64-pipe operations per thread and
+        // work item, the kernel's largest cost on GB300)
+        const int64_t row_len = L + 1;
+#pragma unroll
+        for (int f = 0; f < kNUsed / 2; ++f) {
+          const int64_t base = (int64_t)f * (L + 1) * row_len;
+          const float eR = accE[2 * f].valuef(), eI = accE[2 * f + 1].valuef();
+          const float oR = accO[2 * f].valuef(), oI = accO[2 * f + 1].valuef();
+          S[base + (int64_t)t * row_len + dr.m] = make_float2(eR + oR, eI + oI);
+          if (L - t != t) S[base + (int64_t)(L - t) * row_len + dr.m] = make_float2(eR - oR, eI - oI);
+        }
+      }
+#pragma unroll
+      for (int n = 0; n < kNUsed; ++n) accE[n] = accO[n] = KahanF();
+    }
     tc_fence_before();
     __syncthreads();
+    have = syn_next(dr, nitems, g);
   }
-  if (abort_s) {
-    if (tid == 0) atomicOr(status, CMM_FLAG_TIMEOUT);
-  } else {
-    const int row = tid;   // TMEM lane = thread index
-    const int t = blk * kM + row;
-    if (t < g.npair) {
-      const int64_t row_len = L + 1;
-      for (int f = 0; f < kNUsed / 2; ++f) {
-        const int64_t base = (int64_t)f * (L + 1) * row_len;
-        S[base + (int64_t)t * row_len + m] =
-            make_float2((float)(accE[2 * f].value() + accO[2 * f].value()),
-                        (float)(accE[2 * f + 1].value() + accO[2 * f + 1].value()));
-        if (L - t != t)
-          S[base + (int64_t)(L - t) * row_len + m] =
-              make_float2((float)(accE[2 * f].value() - accO[2 * f].value()),
-                          (float)(accE[2 * f + 1].value() - accO[2 * f + 1].value()));
-      }
-    }
+  if (tid == 0 && abort_s) {
+    // bounded drain of this CTA's copies and products in flight
+    for (long long j = n_ldw; j < n_ld; ++j) mbar_wait(&load_bar[j & 1], (uint32_t)((j >> 1) & 1));
+    for (long long j = n_mmw; j < n_mm; ++j) mbar_wait(&mma_bar[j & 1], (uint32_t)((j >> 1) & 1));
+    atomicOr(status, CMM_FLAG_TIMEOUT);
   }
   tc_fence_before();
   __syncthreads();
   if (warp == 0)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemColsS)
                  : "memory");
 }
 
@@ -586,6 +672,7 @@ struct TcTables {
 
 struct TcPlan {
   int L = 0, npair = 0, nrb = 0, total_chunks = 0;
+  int sms = 0;   // CTAs of the persistent synthesis (one per SM)
   // analysis: degree blocks of 128 per m (prefix sums), ring-pair chunks
   int nck = 0, total_lblocks = 0;
   std::shared_ptr<TcTables> tab;
@@ -628,7 +715,10 @@ int tc_plan_create(int L, const double* ct_rings, const double* pmm_rings, const
     return rc;
   }
   cudaError_t e = cudaFuncSetAttribute(synth_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       kPRecord + kARecord);
+                                       2 * kSynStage);
+  int dev = 0;
+  if (e == cudaSuccess) e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, dev);
   if (e != cudaSuccess) {
     delete p;
     return cuda_fail(e, "cudaFuncSetAttribute(synth_tc_kernel)");
@@ -679,6 +769,7 @@ int tc_plan_share(const TcPlan* src, TcPlan** out) {
   p->L = src->L;
   p->npair = src->npair;
   p->nrb = src->nrb;
+  p->sms = src->sms;
   p->total_chunks = src->total_chunks;
   p->nck = src->nck;
   p->total_lblocks = src->total_lblocks;
@@ -725,8 +816,9 @@ int tc_synthesis(TcPlan* p, const double2* fields, float2* S, int* status, cudaS
   build_atab_kernel<<<dim3(16, p->L), 256, 0, s>>>(g, fields, (unsigned char*)p->atab.p);
   int rc = check("build_atab_kernel");
   if (rc) return rc;
-  synth_tc_kernel<<<dim3(p->nrb, p->L), kThreads, kPRecord + kARecord, s>>>(
-      g, (const unsigned char*)p->tab->ptab.p, (const unsigned char*)p->atab.p, S, status);
+  const int nitems = p->L * p->nrb;
+  synth_tc_kernel<<<std::min(nitems, std::max(p->sms, 1)), kThreads, 2 * kSynStage, s>>>(
+      g, nitems, (const unsigned char*)p->tab->ptab.p, (const unsigned char*)p->atab.p, S, status);
   return check("synth_tc_kernel");
 }
 
