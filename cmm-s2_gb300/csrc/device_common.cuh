@@ -180,7 +180,8 @@ __device__ __forceinline__ BccF bcc_rel_f(const MeshView& m, int t, const float*
                                           double z) {
   const int v1 = __ldg(&m.tri_v[t].x);
   const double* v = m.verts + 4 * (int64_t)v1;
-  const float dx = (float)(x - __ldg(v)), dy = (float)(y - __ldg(v + 1)), dz = (float)(z - __ldg(v + 2));
+  const float dx = to_f32_trunc(x - __ldg(v)), dy = to_f32_trunc(y - __ldg(v + 1)),
+              dz = to_f32_trunc(z - __ldg(v + 2));
   BccF b = bcc_of_f(L, dx, dy, dz);
   b.b0 += 1.0f;
   return b;
@@ -368,7 +369,7 @@ static __device__ __noinline__ int latlon_locate_exact(const MeshView& m, double
 // Otherwise the exact FP64 path decides, so both give the same triangle.
 __device__ __forceinline__ int latlon_locate(const MeshView& m, double x, double y, double z) {
   const int N = 2 * m.L, M = m.L + 1;
-  const float xf = (float)x, yf = (float)y, zf = (float)z;
+  const float xf = to_f32_trunc(x), yf = to_f32_trunc(y), zf = to_f32_trunc(z);
   float phif = atan2f(yf, xf);
   if (phif < 0.f) phif += 6.28318530717958647692f;
   const float thef = atan2f(sqrtf(xf * xf + yf * yf), zf);
@@ -507,7 +508,7 @@ __device__ __forceinline__ double latlon_scalar_f(const MeshView& m, const doubl
   const double* rec = coeffs + (int64_t)t * kCoeffStride1;
   float o[6];
 #pragma unroll
-  for (int k = 0; k < 6; ++k) o[k] = (float)__ldg(rec + id[k]);
+  for (int k = 0; k < 6; ++k) o[k] = to_f32_trunc(__ldg(rec + id[k]));
   const float V = g[0], E = g[1], C = g[2];
   return (double)(V * V * o[0] + E * E * o[1] + C * C * o[2] + 2 * V * E * o[3] + 2 * E * C * o[4] +
                   2 * V * C * o[5]);

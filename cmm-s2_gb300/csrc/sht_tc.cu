@@ -35,6 +35,7 @@
 #include <vector>
 
 #include "cmm_internal.h"
+#include "device_common.cuh"
 
 namespace cmm {
 
@@ -49,7 +50,6 @@ constexpr int kATile = kN * kKc * 2;     // 4 KiB
 constexpr int kPRecord = 4 * kPTile;     // E_hi, E_lo, O_hi, O_lo
 constexpr int kARecord = 4 * kATile;
 constexpr int kThreads = 128;
-constexpr uint32_t kTmemCols = 64;       // 2 accumulators x 32 columns
 constexpr long long kSpinLimit = 1LL << 26;
 
 // Byte offset of element (row, k) in a K-major no-swizzle tile image with
@@ -235,13 +235,15 @@ __global__ void build_atab_kernel(TcGeometry g, const double2* __restrict__ fiel
     const int c = e / per_chunk, r = e % per_chunk;
     const int par = r / (kNUsed * kKc), n = (r / kKc) % kNUsed, k = r % kKc;
     const int l = m + par + 2 * (c * kKc + k);
-    double v = 0.0;
+    float v = 0.f;
     if (l < L) {
       const double2 a = fields[(int64_t)(n >> 1) * L * L + (int64_t)m * L + l];
-      v = (n & 1) ? a.y : a.x;
+      v = dev::to_f32_trunc((n & 1) ? a.y : a.x);
     }
-    const __nv_bfloat16 h = __double2bfloat16(v);
-    const __nv_bfloat16 lo = __double2bfloat16(v - (double)__bfloat162float(h));
+    // the split in FP32 from the coefficient truncated to FP32 (2^-23
+    // relative, far inside the split's 2^-17): no FP64 pipe work
+    const __nv_bfloat16 h = __float2bfloat16_rn(v);
+    const __nv_bfloat16 lo = __float2bfloat16_rn(v - __bfloat162float(h));
     unsigned char* rec = atab + (int64_t)(g.cbase[m] + c) * kARecord;
     const int off = tile_offset(n, k);
     *(__nv_bfloat16*)(rec + (2 * par) * kATile + off) = h;
@@ -533,22 +535,20 @@ __global__ void build_xtab_kernel(TcFwdGeometry g, const float2* __restrict__ fi
     const int c = e / (2 * 2 * kKc), r = e % (2 * 2 * kKc);
     const int par = r / (2 * kKc), n = (r / kKc) % 2, k = r % kKc;
     const int j = c * kKc + k;
-    double v = 0.0;
-    if (j <= L) {
-      const float2 af = fine[(int64_t)j * L + m];
-      const double2 a = make_double2(af.x, af.y);
-      double2 s;
+    float v = 0.f;
+    if (j <= L) {   // FP32 throughout: the samples are FP32, the split keeps 2^-17
+      const float2 a = fine[(int64_t)j * L + m];
+      float2 s;
       if (j < L) {
-        const float2 bf = fine[(int64_t)(2 * L - j) * L + m];
-        const double2 b = make_double2(bf.x, bf.y);
-        s = par == 0 ? make_double2(a.x + b.x, a.y + b.y) : make_double2(a.x - b.x, a.y - b.y);
+        const float2 b = fine[(int64_t)(2 * L - j) * L + m];
+        s = par == 0 ? make_float2(a.x + b.x, a.y + b.y) : make_float2(a.x - b.x, a.y - b.y);
       } else {
-        s = par == 0 ? a : make_double2(0.0, 0.0);
+        s = par == 0 ? a : make_float2(0.f, 0.f);
       }
-      v = w[j] * (n == 0 ? s.x : s.y);
+      v = dev::to_f32_trunc(w[j]) * (n == 0 ? s.x : s.y);
     }
-    const __nv_bfloat16 h = __double2bfloat16(v);
-    const __nv_bfloat16 lo = __double2bfloat16(v - (double)__bfloat162float(h));
+    const __nv_bfloat16 h = __float2bfloat16_rn(v);
+    const __nv_bfloat16 lo = __float2bfloat16_rn(v - __bfloat162float(h));
     unsigned char* rec = xtab + ((int64_t)m * g.nck + c) * kXRecord;
     const int off = tile_offset(n, k);
     *(__nv_bfloat16*)(rec + (2 * par) * kXTile + off) = h;

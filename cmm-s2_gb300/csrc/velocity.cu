@@ -59,7 +59,7 @@ __device__ __forceinline__ void velocity_at(const MeshView& m, const VelPtrs& vc
 #pragma unroll
     for (int l = 0; l < 3; ++l) {
       if (l >= nvs) break;
-      const float wl = (float)(l == 0 ? w.a : (l == 1 ? w.b : w.c));
+      const float wl = to_f32_trunc(l == 0 ? w.a : (l == 1 ? w.b : w.c));
       OrdsF<3> o;
       load_ords_f<3>((const float*)vc.p[l] + (int64_t)t * kCoeffStride3, sp, o);
       float P[3];

@@ -127,7 +127,7 @@ __global__ void __launch_bounds__(256) vorticity_kernel(VortParams vp, const dou
     const double x = X[3 * i], y = X[3 * i + 1], z = X[3 * i + 2];
     double w = 0.0, ct;
     if (vm.field32) {
-      const float xf = (float)x, yf = (float)y, zf = (float)z;
+      const float xf = to_f32_trunc(x), yf = to_f32_trunc(y), zf = to_f32_trunc(z);
       float phif = atan2f(yf, xf);
       if (phif < 0.f) phif += 6.28318530717958647692f;
       const float thf = atan2f(sqrtf(xf * xf + yf * yf), zf);
