@@ -448,8 +448,8 @@ __device__ __forceinline__ void proj_bwd(const double* y, const double* sb, doub
   yb[2] = (sb[2] - s2 * d) / r;
 }
 
-__device__ __forceinline__ void proj(const double* y, double* s) {
-  const double r = 1.0 / sqrt(y[0] * y[0] + y[1] * y[1] + y[2] * y[2]);
+__device__ __forceinline__ void proj(const double* y, double* s) {   // as sphere_proj
+  const double r = rsqrt(y[0] * y[0] + y[1] * y[1] + y[2] * y[2]);
   s[0] = y[0] * r;
   s[1] = y[1] * r;
   s[2] = y[2] * r;

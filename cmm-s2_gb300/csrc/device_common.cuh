@@ -430,15 +430,20 @@ struct ShPoint {
   double ct, st, cp, sp;
 };
 
+// (reciprocal norms from the FP64 rsqrt, within 1 ulp: square roots and
+// divisions would cost ~60 FP64-pipe instructions per point)
 __device__ __forceinline__ ShPoint sh_point(double x, double y, double z) {
-  const double rho = sqrt(x * x + y * y), r = sqrt(rho * rho + z * z);
+  const double rho2 = x * x + y * y;
+  const double ir = rsqrt(rho2 + z * z);
   ShPoint p;
-  p.ct = z / r;
-  p.st = rho / r;
-  if (rho > 0.0) {
-    p.cp = x / rho;
-    p.sp = y / rho;
+  p.ct = z * ir;
+  if (rho2 > 0.0) {
+    const double irho = rsqrt(rho2);
+    p.st = rho2 * irho * ir;
+    p.cp = x * irho;
+    p.sp = y * irho;
   } else {   // atan2(0, 0) = 0
+    p.st = 0.0;
     p.cp = 1.0;
     p.sp = 0.0;
   }

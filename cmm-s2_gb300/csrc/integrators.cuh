@@ -16,9 +16,12 @@
 namespace cmm {
 namespace dev {
 
-// div_norm (evolution_functions.py:82-85): x * (1 / |x|)
+// div_norm (evolution_functions.py:82-85): x * (1 / |x|), the reciprocal
+// norm from the FP64 rsqrt (within 1 ulp): an IEEE square root and division
+// cost ~25 FP64-pipe instructions, a fifth of the RK4 foot point's FP64
+// budget on GB300.
 __device__ __forceinline__ void sphere_proj(double* x) {
-  const double r = 1.0 / sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
+  const double r = rsqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
   x[0] *= r;
   x[1] *= r;
   x[2] *= r;

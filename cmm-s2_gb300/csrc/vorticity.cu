@@ -132,14 +132,14 @@ __global__ void __launch_bounds__(256) vorticity_kernel(VortParams vp, const dou
       if (phif < 0.f) phif += 6.28318530717958647692f;
       const float thf = atan2f(sqrtf(xf * xf + yf * yf), zf);
       if (vp.kind != CMM_VORT_NONE) w = (double)omega0_f(vp, phif, thf);
-      ct = z / sqrt(x * x + y * y + z * z);   // cos(theta), FP64
+      ct = z * rsqrt(x * x + y * y + z * z);   // cos(theta), FP64
     } else if (vp.kind != CMM_VORT_NONE) {
       double phi, theta;
       cart2sphere(x, y, z, &phi, &theta);
       w = omega0(vp, phi, theta);
       ct = cos(theta);
     } else {
-      ct = z / sqrt(x * x + y * y + z * z);
+      ct = z * rsqrt(x * x + y * y + z * z);
     }
     if (sh) {
       double v;
