@@ -173,8 +173,10 @@ __global__ void __launch_bounds__(kBlock) integrate_kernel(MeshView m, VelPtrs v
 // Foot points of the mesh vertices and of their stencil points
 // (advect, cmm_s2/core/evolution_functions.py:117-133).  Point i < nv is
 // vertex i, point nv + k*nv + v is stencil point k of vertex v.  work:
-// yn (3,nv) followed by the stencil foot points (3,4,nv).
-__global__ void __launch_bounds__(kMaxBlock) advect_points_kernel(MeshView mesh, MeshView vm, VelPtrs vc,
+// yn (3,nv) followed by the stencil foot points (3,4,nv).  Register cap
+// for 3 blocks of 256 (6 of 128) per SM: 80 registers and a few spills
+// beat 120 registers at 16 warps by 4-6 %.
+__global__ void __launch_bounds__(kMaxBlock, 3) advect_points_kernel(MeshView mesh, MeshView vm, VelPtrs vc,
                                                                int nvs, TimeWeights tw, int scheme,
                                                                double dt,
                                                                const double* __restrict__ s_pts,
