@@ -4,9 +4,9 @@ Linear maps (assembly, the SHT velocity pipeline, the SH-coefficient part of
 the vorticity) by the dot-product test <A x, y> = <x, A^T y> (relative
 agreement 1e-12); nonlinear ones (composition, the point part of the
 vorticity) by centred differences of the forward call along random
-directions (relative agreement 1e-6 at step 1e-6); the composition also
-against torch autograd through the oracle's pure-torch FP64 restatement
-(normwise 1e-13)."""
+directions (relative agreement 1e-6 at step 1e-6); the composition and the
+vorticity also against torch autograd through the oracle's pure-torch FP64
+restatements (normwise 1e-13)."""
 import numpy as np
 import pytest
 import torch
@@ -158,6 +158,44 @@ def test_vorticity_bwd(mods):
     wm = vm.vorticity(native.VORT_NONE, [], X - h * dX, rot, sh=sh)
     fd = dot(wp - wm, y) / (2 * h)
     assert abs(fd - dot(Xv.grad, dX)) < 1e-6 * abs(fd)
+
+
+def test_vorticity_bwd_matches_autograd_restatement(mods):
+    """The vorticity's hand-written backward (cmm_vorticity_bwd) against
+    torch autograd on the CPU through the oracle's pure-torch restatement of
+    the SH series and the planetary term (oracle/vorticity_torch.py, pinned
+    to oracle.fields.sh_series by tests/test_oracle_autograd.py): the
+    coefficient gradient on the used entries (|m| <= l) and the tangent part
+    of the point gradient, L = 16, l <= 6, normwise to 1e-13 (measured
+    9e-16 and 1.4e-16)."""
+    from oracle.vorticity_torch import sampled_vorticity
+    native, adj, meshgen, workloads = mods
+    L = 16
+    theta, phi, grid, verts = meshgen.latlon_mesh_arrays(L)
+    vm = native.VelMesh(L, theta, phi, grid, verts)
+    _, a = workloads.random_sh_vorticity(6, seed=1)
+    X = torch.from_numpy(meshgen.random_sphere_points((L + 1) * 2 * L, seed=2))
+    y = torch.randn((L + 1, 2 * L), dtype=torch.float64, generator=torch.Generator().manual_seed(3))
+    rot = 2 * np.pi
+    Xv, shv = X.cuda().requires_grad_(True), torch.from_numpy(a).cuda().requires_grad_(True)
+    (adj.Vorticity.apply(Xv, shv, vm, rot) * y.cuda()).sum().backward()
+    Xr, shr = X.clone().requires_grad_(True), torch.from_numpy(a.copy()).requires_grad_(True)
+    (sampled_vorticity(shr, Xr, rot, 0.0) * y.reshape(-1)).sum().backward()
+
+    def rel(u, v):
+        return float((u - v).norm() / v.norm())
+    used = torch.zeros(shr.shape, dtype=torch.bool)
+    for l in range(used.shape[0]):
+        used[l, :2 * l + 1] = True
+    e = rel(shv.grad.cpu()[used], shr.grad[used])
+    print(f"coefficient gradient rel err {e:.2e}")
+    assert e < 1e-13
+
+    def tangent(g):
+        return g - (g * X).sum(1, keepdim=True) * X
+    e = rel(tangent(Xv.grad.cpu()), tangent(Xr.grad))
+    print(f"point gradient (tangent) rel err {e:.2e}")
+    assert e < 1e-13
 
 
 @pytest.mark.parametrize("scheme,nvs,with_prev", [(0, 1, False), (1, 2, False), (2, 2, True), (2, 3, True),

@@ -57,3 +57,29 @@ def test_restatement_gradient_matches_oracle_differences():
     assert abs(fd - ad) < 1e-8 * abs(ad), (fd, ad)
     # the composition is invariant to scaling q, so its gradient is tangent
     assert np.abs((qt.grad.numpy() * q).sum(1)).max() < 1e-10 * np.abs(qt.grad.numpy()).max()
+
+
+def test_vorticity_restatement_matches_oracle_series():
+    """oracle.vorticity_torch against oracle.fields.sh_series: values, and
+    the autograd point gradient against centred differences of the numpy
+    series along tangent directions."""
+    from cmm_gpu import meshgen, workloads
+    from oracle import fields as F
+    from oracle.vorticity_torch import sh_series_at
+    _, a = workloads.random_sh_vorticity(6, seed=1)
+    X = meshgen.random_sphere_points(500, seed=2)
+
+    def series(P):
+        P = P / np.linalg.norm(P, axis=1, keepdims=True)
+        return F.sh_series(a)(np.arctan2(P[:, 1], P[:, 0]), np.arccos(np.clip(P[:, 2], -1, 1)))
+    Xt = torch.from_numpy(X.copy()).requires_grad_(True)
+    w = sh_series_at(torch.from_numpy(a), Xt)
+    assert np.abs(w.detach().numpy() - series(X)).max() < 1e-12 * np.abs(series(X)).max()
+    y = np.random.default_rng(3).standard_normal(len(X))
+    (w * torch.from_numpy(y)).sum().backward()
+    dX = np.random.default_rng(4).standard_normal(X.shape)
+    dX -= (dX * X).sum(1, keepdims=True) * X
+    h = 1e-6
+    fd = float(((series(X + h * dX) - series(X - h * dX)) * y).sum()) / (2 * h)
+    ad = float((Xt.grad.numpy() * dX).sum())
+    assert abs(fd - ad) < 1e-8 * abs(ad), (fd, ad)
