@@ -38,7 +38,6 @@ _SIGS = {
     "cmm_last_error": (ctypes.c_char_p, []),
     "cmm_version": (_i, []),
     "cmm_launch_count": (ctypes.c_longlong, []),
-    "cmm_fp64_probe": (_i, [_i, _i, _p, _p]),
     "cmm_mesh_create": (_i, [_p, _i, _p, _i, _i, ctypes.POINTER(_p)]),
     "cmm_mesh_destroy": (_i, [_p]),
     "cmm_mesh_check": (_i, [_p, _i, _p, _i, _i, _p]),
@@ -77,6 +76,7 @@ _SIGS = {
     "cmm_advect_project_bwd": (_i, [_p, _p, ctypes.POINTER(_p), _i, _d, _i, _d, _d, _p, _p, _p, _d, _p,
                                     ctypes.POINTER(_p), _p, _p, _p]),
     "cmm_mesh_set_block": (_i, [_p, _i, _i]),
+    "cmm_mesh_set_variant": (_i, [_p, _i, _i]),
     "cmm_bve_create": (_i, [ctypes.POINTER(BveDesc), ctypes.POINTER(_p)]),
     "cmm_bve_destroy": (_i, [_p]),
     "cmm_bve_step": (_i, [_p, _p]),
@@ -167,6 +167,14 @@ class Mesh:
     def set_block(self, kernel, threads):
         """Launch shape of a tunable kernel on this mesh (cmm_mesh_set_block)."""
         check(lib.cmm_mesh_set_block(self.h, kernel, threads), "cmm_mesh_set_block")
+        return self
+
+    VARIANT_COMPOSE_JAC, VARIANT_COMPOSE = 0, 1
+
+    def set_variant(self, knob, value):
+        """Compiled variant (register budget) of a tunable kernel on this
+        mesh (cmm_mesh_set_variant)."""
+        check(lib.cmm_mesh_set_variant(self.h, knob, value), "cmm_mesh_set_variant")
         return self
 
     # ------------------------------------------------------------------

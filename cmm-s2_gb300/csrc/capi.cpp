@@ -21,17 +21,15 @@ int cmm_version(void) { return 1; }
 
 long long cmm_launch_count(void) { return launch_count(); }
 
-int cmm_fp64_probe(int blocks, int iters, double* sink, void* stream) {
-  if (blocks < 1 || iters < 1 || !sink) return arg_error("cmm_fp64_probe: bad argument");
-  return launch_fp64_probe(blocks, iters, sink, (cudaStream_t)stream);
-}
-
 int cmm_mesh_create(const double* verts, int nv, const int32_t* tris, int nt, int level,
                     cmm_mesh** out) {
   if (!verts || !tris || !out) return arg_error("cmm_mesh_create: null pointer");
   *out = nullptr;
   cmm_mesh* m = new (std::nothrow) cmm_mesh();
-  if (!m) return arg_error("cmm_mesh_create: out of host memory");
+  if (!m) {
+    set_last_error("cmm_mesh_create: out of host memory");
+    return CMM_ERR_NOMEM;
+  }
   int rc = CMM_OK;
   HostMesh hm;
   if (!rc) rc = build_host(verts, nv, tris, nt, level, &hm);
@@ -91,7 +89,10 @@ int cmm_velmesh_create(int L, const double* theta, const double* phi, const doub
   if (!theta || !phi || !grid || !verts || !out) return arg_error("cmm_velmesh_create: null pointer");
   *out = nullptr;
   cmm_mesh* m = new (std::nothrow) cmm_mesh();
-  if (!m) return arg_error("cmm_velmesh_create: out of host memory");
+  if (!m) {
+    set_last_error("cmm_velmesh_create: out of host memory");
+    return CMM_ERR_NOMEM;
+  }
   int rc = build_latlon(L, theta, phi, grid, verts, m);
   if (rc) {
     delete m;
@@ -233,6 +234,14 @@ int cmm_mesh_set_block(cmm_mesh* mesh, int kernel, int threads) {
   if (!mesh || kernel < 0 || kernel > 3 || threads < 0 || threads > 256 || threads % 32 != 0)
     return arg_error("cmm_mesh_set_block: bad argument");
   mesh->view.block[kernel] = threads;
+  return CMM_OK;
+}
+
+int cmm_mesh_set_variant(cmm_mesh* mesh, int knob, int value) {
+  const bool ok = mesh && ((knob == CMM_VARIANT_COMPOSE_JAC && (value == 0 || (value >= 2 && value <= 4))) ||
+                           (knob == CMM_VARIANT_COMPOSE && (value == 0 || value == 4 || value == 6)));
+  if (!ok) return arg_error("cmm_mesh_set_variant: bad argument");
+  mesh->view.variant[knob] = value;
   return CMM_OK;
 }
 

@@ -23,6 +23,8 @@ constexpr int kAsmStride = 48;
 // On the device the 45 used factors are stored factor-major,
 // tri_asm[j * nt + t], so that a warp's loads of one factor coalesce.
 constexpr int kAsmFactors = 45;
+constexpr int kWalkStride = 16;     // per-row walk record: 3 x float4 + padding
+constexpr int kWalkMax = 64;        // walk steps before falling back to the descent
 constexpr int kCoeffStride3 = 64;   // 19 ordinates x 3 components, padded
 constexpr int kCoeffStride1 = 24;   // 19 ordinates, padded
 
@@ -39,6 +41,15 @@ struct MeshView {
   const double* node_n;     // hierarchy nodes x 9: normals n0,n1,n2 (levels 0..level-1)
   const float* node_nf;     // same, FP32, unit normals
   const int* leaf_row;      // (nt) hierarchical leaf -> reference row
+  // walk location (locate_row): per row kWalkStride floats -- for each edge
+  // (v0v1, v1v2, v2v0) its inward unit normal (FP32) and the row across it
+  // (bit pattern in the 4th float) -- the FP64 normals (kWalkStride
+  // doubles per row, 9 used) and a cube-map jump table of 6 jump_res^2
+  // starting rows (NULL until built: the hierarchy descent is used)
+  const float* walk_f;
+  const double* walk_d;
+  const int* jump;
+  int jump_res;
   int* status;              // device status word
   // MWSS lat-lon velocity mesh (kind == kLatLon)
   int kind;                 // kIcosahedral or kLatLon
@@ -62,6 +73,10 @@ struct MeshView {
   // launch shapes chosen by an autotuner (cmm_mesh_set_block), threads per
   // block of the tunable kernels on this mesh; 0 = the library default
   int block[4];
+  // compiled variants chosen by an autotuner (cmm_mesh_set_variant): the
+  // register budget of the composition kernels, as resident 256-thread
+  // blocks per SM; 0 = the library default
+  int variant[2];
 };
 
 // Tunable kernels (index into MeshView::block).
@@ -105,7 +120,7 @@ struct DeviceBuffer {
 struct cmm_mesh {
   cmm::MeshView view;
   cmm::DeviceBuffer verts, tri_v, tri_loc, tri_asm, root, root_f, root_adj, node_n, node_nf, leaf_row,
-      status, theta, phi, grid, cos_theta, tri_asm_f, tri_loc_f, sh_ab, sh_fm;
+      status, theta, phi, grid, cos_theta, tri_asm_f, tri_loc_f, sh_ab, sh_fm, walk_f, walk_d, jump;
 };
 
 namespace cmm {
@@ -133,11 +148,14 @@ int launch_stencil_eval(const MeshView& m, const double* coeffs, const double* y
 // Host-side tables of an icosahedral mesh (before upload).
 struct HostMesh {
   int level = 0, nv = 0, nt = 0;
-  std::vector<double> vpad, loc, asmf, root, node_n;
-  std::vector<float> node_nf;
+  std::vector<double> vpad, loc, asmf, root, node_n, walk_d;
+  std::vector<float> node_nf, walk_f;
   std::vector<int4> tv;
   std::vector<int> root_adj, leaf_row;
 };
+// Cube-map jump table of the walk location (maps.cu): every cell centre
+// located by the hierarchy descent.
+int build_jump_table(cmm_mesh* m);
 int build_host(const double* verts, int nv, const int32_t* tris, int nt, int level, HostMesh* hm);
 int upload_mesh(const HostMesh& h, cmm_mesh* m);
 const char* last_error();
@@ -211,7 +229,6 @@ int launch_vorticity(int kind, const double* params, int nparams, const double* 
                      const MeshView& vm, const double* spline, double rot, const double* X,
                      int64_t Q, int npr, const double* cos_ring, double* omega, cudaStream_t s);
 
-int launch_fp64_probe(int blocks, int iters, double* sink, cudaStream_t s);
 
 // adjoints (adjoint.cu)
 constexpr int kAdjMaxSubmaps = 256;

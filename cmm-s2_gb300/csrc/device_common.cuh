@@ -49,8 +49,10 @@ __device__ __forceinline__ float to_f32_trunc(double x) {
   return __uint_as_float((hi & 0x80000000u) | f);
 }
 
-// Reference row of the icosahedral triangle containing q.
-__device__ __forceinline__ int locate_row(const MeshView& m, double x, double y, double z) {
+// Reference row of the icosahedral triangle containing q, by descent of
+// the refinement hierarchy (20 root faces, then one of four children per
+// level).
+__device__ __forceinline__ int locate_descent(const MeshView& m, double x, double y, double z) {
   const float fx = to_f32_trunc(x), fy = to_f32_trunc(y), fz = to_f32_trunc(z);
   // root face: nearest face centre (FP32), then exact edge checks with a
   // bounded walk across a violated edge
@@ -109,6 +111,77 @@ __device__ __forceinline__ int locate_row(const MeshView& m, double x, double y,
   return __ldg(m.leaf_row + f);
 }
 
+// Cell of the cube-map jump table containing the direction (x, y, z): the
+// face of the dominant axis, then R x R cells over the two other
+// coordinates divided by the dominant one.  Approximate arithmetic is
+// enough (the walk starts from any row); every input, NaN included, maps to
+// a valid cell.
+__device__ __forceinline__ int jump_cell(int R, float x, float y, float z) {
+  const float ax = fabsf(x), ay = fabsf(y), az = fabsf(z);
+  int face;
+  float u, v, den;
+  if (ax >= ay && ax >= az) {
+    face = x >= 0.f ? 0 : 1;
+    u = y;
+    v = z;
+    den = ax;
+  } else if (ay >= az) {
+    face = y >= 0.f ? 2 : 3;
+    u = x;
+    v = z;
+    den = ay;
+  } else {
+    face = z >= 0.f ? 4 : 5;
+    u = x;
+    v = y;
+    den = az;
+  }
+  const float sc = __fdividef(0.5f * (float)R, den);
+  const int iu = min(max((int)((u + den) * sc), 0), R - 1);
+  const int iv = min(max((int)((v + den) * sc), 0), R - 1);
+  return (face * R + iv) * R + iu;
+}
+
+// q strictly outside edge k of row t: the FP32 side test against the unit
+// edge normal, redone in FP64 within the filter.  The row across the edge
+// holds the exactly negated normals, so two rows never both reject q.
+__device__ __forceinline__ bool edge_out(const MeshView& m, int t, int k, float4 e, float fx, float fy, float fz,
+                                         double x, double y, double z) {
+  const float d = fmaf(e.x, fx, fmaf(e.y, fy, e.z * fz));
+  if (fabsf(d) > kFilter) return d < 0.0f;
+  const double* n = m.walk_d + (int64_t)t * kWalkStride + 3 * k;
+  return n[0] * x + n[1] * y + n[2] * z < 0.0;
+}
+
+// Reference row of the icosahedral triangle containing q.  With the jump
+// table built: start at the row that contains the centre of q's cube-map
+// cell and walk across the first edge that q lies outside of until q is
+// inside all three (a handful of steps: the cells are smaller than the
+// triangles); a walk that has not ended after kWalkMax steps falls back
+// to the hierarchy descent.  Both are exact containment tests, so they
+// agree except for queries within rounding distance of an edge, where
+// either neighbour contains the query.
+__device__ __forceinline__ int locate_row(const MeshView& m, double x, double y, double z) {
+  if (!m.jump) return locate_descent(m, x, y, z);
+  const float fx = to_f32_trunc(x), fy = to_f32_trunc(y), fz = to_f32_trunc(z);
+  int t = __ldg(m.jump + jump_cell(m.jump_res, fx, fy, fz));
+  for (int it = 0; it < kWalkMax; ++it) {
+    const float4* r = reinterpret_cast<const float4*>(m.walk_f + (int64_t)t * kWalkStride);
+    const float4 e0 = __ldg(r), e1 = __ldg(r + 1), e2 = __ldg(r + 2);
+    int nb;
+    if (edge_out(m, t, 0, e0, fx, fy, fz, x, y, z))
+      nb = __float_as_int(e0.w);
+    else if (edge_out(m, t, 1, e1, fx, fy, fz, x, y, z))
+      nb = __float_as_int(e1.w);
+    else if (edge_out(m, t, 2, e2, fx, fy, fz, x, y, z))
+      nb = __float_as_int(e2.w);
+    else
+      return t;
+    t = nb;
+  }
+  return locate_descent(m, x, y, z);
+}
+
 struct Bcc {
   double b0, b1, b2;
 };
@@ -127,13 +200,25 @@ struct Split {
   int lo, mid, hi;
 };
 
+// A signed integer with the order of the double x (-0 and +0 equal):
+// +|bits| or -|bits| of its magnitude.  Comparisons of these keys run on
+// the integer pipe and give exactly the FP64 comparisons of finite values,
+// which would occupy the FP64 pipe (a NaN orders as a large magnitude; the
+// split it selects is still one of the six).
+__device__ __forceinline__ long long ord_key(double x) {
+  const long long b = __double_as_longlong(x);
+  const long long mag = b & 0x7fffffffffffffffLL;
+  return b < 0 ? -mag : mag;
+}
+
 __device__ __forceinline__ Split split_of(const Bcc& b) {
+  const long long k0 = ord_key(b.b0), k1 = ord_key(b.b1), k2 = ord_key(b.b2);
   int lo = 0, hi = 0;
-  double vlo = b.b0, vhi = b.b0;
-  if (b.b1 < vlo) { vlo = b.b1; lo = 1; }
-  if (b.b2 < vlo) { vlo = b.b2; lo = 2; }
-  if (b.b1 > vhi) { vhi = b.b1; hi = 1; }
-  if (b.b2 > vhi) { vhi = b.b2; hi = 2; }
+  long long vlo = k0, vhi = k0;
+  if (k1 < vlo) { vlo = k1; lo = 1; }
+  if (k2 < vlo) { vlo = k2; lo = 2; }
+  if (k1 > vhi) { vhi = k1; hi = 1; }
+  if (k2 > vhi) { vhi = k2; hi = 2; }
   if (lo == hi) { lo = 1; hi = 0; }
   return Split{lo, 3 - lo - hi, hi};
 }

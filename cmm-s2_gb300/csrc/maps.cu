@@ -21,8 +21,11 @@
 // determinants (new_vpoints + bary_coords, :668-689).
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "cmm_internal.h"
 #include "device_common.cuh"
+#include "ff.cuh"
 
 namespace cmm {
 
@@ -31,6 +34,13 @@ using namespace dev;
 namespace {
 
 constexpr int kBlock = 256;
+// default register budgets of the compositions, as resident 256-thread
+// blocks per SM (measured at level 7, 2^24 queries, 8 submaps: Jacobians
+// 19.0 / 19.2 / 19.6 ms at 2 / 4 / 3 blocks in cell order; points only
+// 15.5 ms at 4 blocks against 19.6 ms at 6 in caller order, equal in cell
+// order)
+constexpr int kComposeJacBlocks = 2;
+constexpr int kComposeBlocks = 4;
 
 // Submap lists: by value in the kernel parameters (host calls), or a
 // device table whose length comes from a device-driven step's state.
@@ -48,20 +58,40 @@ struct DevSubmaps {
   __device__ __forceinline__ const double* at(int s, int S) const { return s < S - 1 ? tab[s] : last; }
 };
 
-// Orthonormal tangent basis (t1, t2) at the unit point p.
-__device__ __forceinline__ void tangent_basis(const double* p, double* t1, double* t2) {
-  const double ax = fabs(p[2]) < 0.9 ? 0.0 : 1.0, az = 1.0 - ax;
-  t1[0] = p[1] * az;
-  t1[1] = p[2] * ax - p[0] * az;
-  t1[2] = -p[1] * ax;
-  const double in = rsqrt(t1[0] * t1[0] + t1[1] * t1[1] + t1[2] * t1[2]);
-  t1[0] *= in;
-  t1[1] *= in;
-  t1[2] *= in;
-  t2[0] = p[1] * t1[2] - p[2] * t1[1];
-  t2[1] = p[2] * t1[0] - p[0] * t1[2];
-  t2[2] = p[0] * t1[1] - p[1] * t1[0];
+// Orthonormal tangent basis (t1, t2) at the unit point p, in float-float
+// from the FP64 point (the Jacobian's tangent pushes run in float-float on
+// the FP32 pipe).
+__device__ __forceinline__ void tangent_basis_ff(const double* p, ff* t1, ff* t2) {
+  const ff p0 = ff_of(p[0]), p1 = ff_of(p[1]), p2 = ff_of(p[2]);
+  const bool polar = !(fabsf(p2.h) < 0.9f);
+  // t1 = e x p normalised, e = z (or x near the poles): (p1, -p0, 0) or (0, p2, -p1)
+  const ff a = polar ? p2 : p1, b = polar ? ff_neg(p1) : ff_neg(p0);
+  const ff r = ff_rsqrt(ff_dot2(a, a, b, b));
+  const ff ua = ff_mul(a, r), ub = ff_mul(b, r);
+  const ff z{0.f, 0.f};
+  t1[0] = polar ? z : ua;
+  t1[1] = polar ? ua : ub;
+  t1[2] = polar ? ub : z;
+  // t2 = p x t1
+  t2[0] = ff_sub(ff_mul(p1, t1[2]), ff_mul(p2, t1[1]));
+  t2[1] = ff_sub(ff_mul(p2, t1[0]), ff_mul(p0, t1[2]));
+  t2[2] = ff_sub(ff_mul(p0, t1[1]), ff_mul(p1, t1[0]));
 }
+
+__device__ __forceinline__ ff pick_ff(const ff* b, int i) { return i == 0 ? b[0] : (i == 1 ? b[1] : b[2]); }
+
+// Twelve float-float values of one thread in shared memory, value-major
+// (value k at s[2k * stride], s[(2k + 1) * stride]: conflict-free): the two
+// tangent pushes (0..5) and their barycentric directions (6..11).
+struct Pushes {
+  float* s;
+  int stride;
+  __device__ __forceinline__ ff get(int k) const { return ff{s[2 * k * stride], s[(2 * k + 1) * stride]}; }
+  __device__ __forceinline__ void set(int k, ff v) {
+    s[2 * k * stride] = v.h;
+    s[(2 * k + 1) * stride] = v.l;
+  }
+};
 
 // 2^m as a double, from its bit pattern (0 <= m <= 4 here)
 __device__ __forceinline__ double pow2(int m) { return __longlong_as_double((long long)(1023 + m) << 52); }
@@ -228,23 +258,17 @@ __global__ void to_f32_kernel(const double* __restrict__ a, int64_t n, float* __
 // perm (nullable): process the queries in this order (grouped by coarse
 // cell, cmm_query_order) so that neighbouring threads gather neighbouring
 // records; every query's own arithmetic and output slot are unchanged.
-// Resident blocks per SM the register allocation must allow: the
-// Jacobian variant trades a few spills for 4 blocks (32 warps) to hide its
-// gather latency (8 % faster than 2 blocks at 102 registers); the
-// points-only variant fits 6 blocks in 40 registers.
-template <bool JAC>
-struct ComposeOccupancy {
-  static constexpr int kMinBlocks = JAC ? 4 : 6;
-};
-
-template <bool JAC, class Src>
-__global__ void __launch_bounds__(kBlock, ComposeOccupancy<JAC>::kMinBlocks) compose_kernel(MeshView m, Src cp,
+// MINB: resident 256-thread blocks per SM the register allocation must
+// allow (the register budget; cmm_mesh_set_variant).
+template <bool JAC, class Src, int MINB>
+__global__ void __launch_bounds__(kBlock, MINB) compose_kernel(MeshView m, Src cp,
                                                          const double* __restrict__ q, int64_t n,
                                                          double* __restrict__ out,
                                                          int32_t* __restrict__ tri,
                                                          int32_t* __restrict__ tri_all,
                                                          double* __restrict__ jac,
                                                          const int32_t* __restrict__ perm) {
+  __shared__ float push_smem[JAC ? 24 * kBlock : 1];
   const int S = cp.count();
   for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n;
        j += (int64_t)gridDim.x * blockDim.x) {
@@ -264,9 +288,24 @@ __global__ void __launch_bounds__(kBlock, ComposeOccupancy<JAC>::kMinBlocks) com
         for (int k = 0; k < 9; ++k) jac[9 * i + k] = nan("");
       continue;
     }
-    double w1[3], w2[3];
+    // Jacobian: two tangent vectors pushed through the chain in
+    // float-float on the FP32 pipe (the points, the location predicates,
+    // the barycentrics and the patch values stay FP64)
+    // The pushes live in shared memory, [value][thread], not in
+    // registers: with them the loop exceeds the register budget of four
+    // resident blocks and spills to local memory, whose traffic thrashes
+    // the L1 that the gathers need.
+    Pushes w{push_smem + threadIdx.x, (int)blockDim.x};
     int since = 0;   // submaps pushed since the last normalisation
-    if (JAC) tangent_basis(p, w1, w2);   // pushed from the tangent basis at q
+    if (JAC) {   // pushed from the tangent basis at q
+      ff t1[3], t2[3];
+      tangent_basis_ff(p, t1, t2);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        w.set(c, t1[c]);
+        w.set(3 + c, t2[c]);
+      }
+    }
     for (int s = S - 1; s >= 0; --s) {
       const int t = locate_row(m, p[0], p[1], p[2]);
       if (s == S - 1 && tri) tri[i] = t;
@@ -280,14 +319,35 @@ __global__ void __launch_bounds__(kBlock, ComposeOccupancy<JAC>::kMinBlocks) com
       double P[3];
       if (JAC) {
         // The patch is the quadratic form P_c = gamma^T M_c gamma of the
-        // symmetric ordinate matrix M_c; its half gradient M_c gamma serves
-        // the two tangent pushes (half derivatives along dgamma = T L w) and
-        // gives the value with three more operations per component.  The
-        // pushes' barycentric directions are formed first and the ordinates
-        // consumed one component at a time, which keeps the loop within 64
-        // registers.
-        const Gam e1 = gamma_of(Lr, bcc_of(Lr, w1[0], w1[1], w1[2]), sp);
-        const Gam e2 = gamma_of(Lr, bcc_of(Lr, w2[0], w2[1], w2[2]), sp);
+        // symmetric ordinate matrix M_c; its half gradient M_c gamma (FP64)
+        // gives the value with three more operations per component and
+        // serves the two tangent pushes: half derivatives along the
+        // barycentric directions dgamma = T Minv w, formed in float-float
+        // from the FP64 location record.
+        // the pushes' sub-triangle barycentric directions, ff values 6..11
+        // of the thread's shared-memory slots
+        {
+          ff d1[3], d2[3];
+          // the inverse vertex rows re-read (L1) rather than held in
+          // registers from the value path
+          const double* Lp = m.tri_loc + (int64_t)t * kLocStride;
+#pragma unroll
+          for (int r = 0; r < 3; ++r) {
+            const ff m0 = ff_of(__ldg(Lp + 3 * r)), m1 = ff_of(__ldg(Lp + 3 * r + 1)),
+                     m2 = ff_of(__ldg(Lp + 3 * r + 2));
+            d1[r] = ff_dot3(m0, w.get(0), m1, w.get(1), m2, w.get(2));
+            d2[r] = ff_dot3(m0, w.get(3), m1, w.get(4), m2, w.get(5));
+          }
+          const ff en = ff_of(edge_norm(Lr, sp.hi, sp.mid)), ec = ff_of(Lr[9]);
+          const ff l1 = pick_ff(d1, sp.lo), m1 = pick_ff(d1, sp.mid), h1 = pick_ff(d1, sp.hi);
+          const ff l2 = pick_ff(d2, sp.lo), m2 = pick_ff(d2, sp.mid), h2 = pick_ff(d2, sp.hi);
+          w.set(6, ff_sub(h1, m1));
+          w.set(7, ff_mul(en, ff_sub(m1, l1)));
+          w.set(8, ff_mul(ec, l1));
+          w.set(9, ff_sub(h2, m2));
+          w.set(10, ff_mul(en, ff_sub(m2, l2)));
+          w.set(11, ff_mul(ec, l2));
+        }
         const int* id = kSplitOrd[sp.lo][sp.hi];
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
@@ -298,8 +358,9 @@ __global__ void __launch_bounds__(kBlock, ComposeOccupancy<JAC>::kMinBlocks) com
           const double pE = g.E * o[1] + g.V * o[3] + g.C * o[4];
           const double pC = g.C * o[2] + g.E * o[4] + g.V * o[5];
           P[c] = g.V * pV + g.E * pE + g.C * pC;
-          w1[c] = pV * e1.V + pE * e1.E + pC * e1.C;
-          w2[c] = pV * e2.V + pE * e2.E + pC * e2.C;
+          const ff fV = ff_of(pV), fE = ff_of(pE), fC = ff_of(pC);
+          w.set(c, ff_dot3(fV, w.get(6), fE, w.get(7), fC, w.get(8)));
+          w.set(3 + c, ff_dot3(fV, w.get(9), fE, w.get(10), fC, w.get(11)));
         }
         ++since;
       } else {
@@ -327,14 +388,16 @@ __global__ void __launch_bounds__(kBlock, ComposeOccupancy<JAC>::kMinBlocks) com
       p[1] = P[1] * inv_n;
       p[2] = P[2] * inv_n;
       if (JAC) {
-        const double sc = inv_n * pow2(since);
+        const ff sc = ff_of(inv_n * pow2(since));
         since = 0;
-        const double d1 = p[0] * w1[0] + p[1] * w1[1] + p[2] * w1[2];
-        const double d2 = p[0] * w2[0] + p[1] * w2[1] + p[2] * w2[2];
+        const ff u0 = ff_of(p[0]), u1 = ff_of(p[1]), u2 = ff_of(p[2]);
+        const ff d1 = ff_dot3(u0, w.get(0), u1, w.get(1), u2, w.get(2));
+        const ff d2 = ff_dot3(u0, w.get(3), u1, w.get(4), u2, w.get(5));
+        const ff u[3] = {u0, u1, u2};
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-          w1[c] = (w1[c] - p[c] * d1) * sc;
-          w2[c] = (w2[c] - p[c] * d2) * sc;
+          w.set(c, ff_mul(ff_sub(w.get(c), ff_mul(u[c], d1)), sc));
+          w.set(3 + c, ff_mul(ff_sub(w.get(3 + c), ff_mul(u[c], d2)), sc));
         }
       }
     }
@@ -346,12 +409,13 @@ __global__ void __launch_bounds__(kBlock, ComposeOccupancy<JAC>::kMinBlocks) com
       // the basis again, from q re-read (cheaper than keeping it in
       // registers across the submap loop)
       const double q0[3] = {q[3 * i], q[3 * i + 1], q[3 * i + 2]};
-      double t1[3], t2[3];
-      tangent_basis(q0, t1, t2);
+      ff t1[3], t2[3];
+      tangent_basis_ff(q0, t1, t2);
 #pragma unroll
       for (int a = 0; a < 3; ++a)
 #pragma unroll
-        for (int b2 = 0; b2 < 3; ++b2) jac[9 * i + 3 * a + b2] = w1[a] * t1[b2] + w2[a] * t2[b2];
+        for (int b2 = 0; b2 < 3; ++b2)
+          jac[9 * i + 3 * a + b2] = ff_to_double(ff_dot2(w.get(a), t1[b2], w.get(3 + a), t2[b2]));
     }
   }
 }
@@ -509,6 +573,27 @@ __global__ void __launch_bounds__(kOrderBlock) order_scatter_kernel(const int32_
   }
 }
 
+// Cube-map jump table: the row containing every cell centre, by the
+// hierarchy descent (the view passed has no jump table yet).
+__global__ void __launch_bounds__(kBlock) jump_table_kernel(MeshView m, int R, int* __restrict__ table) {
+  const int64_t n = 6LL * R * R;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+    const int face = (int)(c / ((int64_t)R * R)), iv = (int)((c / R) % R), iu = (int)(c % R);
+    const double u = -1.0 + (iu + 0.5) * 2.0 / R, v = -1.0 + (iv + 0.5) * 2.0 / R;
+    const double sg = (face & 1) ? -1.0 : 1.0;
+    double d[3];
+    if (face < 2) {
+      d[0] = sg; d[1] = u; d[2] = v;
+    } else if (face < 4) {
+      d[0] = u; d[1] = sg; d[2] = v;
+    } else {
+      d[0] = u; d[1] = v; d[2] = sg;
+    }
+    const double in = 1.0 / sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    table[c] = locate_descent(m, d[0] * in, d[1] * in, d[2] * in);
+  }
+}
+
 int check_launch(const char* what) {
   note_launch();
   cudaError_t e = cudaGetLastError();
@@ -546,10 +631,19 @@ int launch_compose(const MeshView& m, const double* const* coeffs, int S, const 
   for (int k = 0; k < S; ++k) cp.p[k] = coeffs[k];
   const int b = block_for(m, kTuneCompose, kBlock, n);
   const int g = grid_for(n, b);
-  if (jac)
-    compose_kernel<true><<<g, b, 0, s>>>(m, cp, q, n, out, tri, tri_all, jac, perm);
-  else
-    compose_kernel<false><<<g, b, 0, s>>>(m, cp, q, n, out, tri, tri_all, jac, perm);
+  if (jac) {
+    const int v = m.variant[CMM_VARIANT_COMPOSE_JAC] ? m.variant[CMM_VARIANT_COMPOSE_JAC] : kComposeJacBlocks;
+    if (v == 2)
+      compose_kernel<true, SubmapPtrs, 2><<<g, b, 0, s>>>(m, cp, q, n, out, tri, tri_all, jac, perm);
+    else if (v == 3)
+      compose_kernel<true, SubmapPtrs, 3><<<g, b, 0, s>>>(m, cp, q, n, out, tri, tri_all, jac, perm);
+    else
+      compose_kernel<true, SubmapPtrs, 4><<<g, b, 0, s>>>(m, cp, q, n, out, tri, tri_all, jac, perm);
+  } else if ((m.variant[CMM_VARIANT_COMPOSE] ? m.variant[CMM_VARIANT_COMPOSE] : kComposeBlocks) == 4) {
+    compose_kernel<false, SubmapPtrs, 4><<<g, b, 0, s>>>(m, cp, q, n, out, tri, tri_all, jac, perm);
+  } else {
+    compose_kernel<false, SubmapPtrs, 6><<<g, b, 0, s>>>(m, cp, q, n, out, tri, tri_all, jac, perm);
+  }
   return check_launch("compose_kernel");
 }
 
@@ -566,6 +660,23 @@ int make_asm_f32(cmm_mesh* mesh) {
   if (e != cudaSuccess) return cuda_fail(e, "make_asm_f32");
   mesh->view.tri_asm_f = (const float*)mesh->tri_asm_f.p;
   mesh->view.tri_loc_f = (const float*)mesh->tri_loc_f.p;
+  return CMM_OK;
+}
+
+int build_jump_table(cmm_mesh* mesh) {
+  MeshView& v = mesh->view;
+  const int R = std::min(1024, std::max(16, 4 << v.level));
+  const int64_t n = 6LL * R * R;
+  int rc = mesh->jump.alloc(n * sizeof(int));
+  if (rc) return rc;
+  MeshView m = v;
+  m.jump = nullptr;
+  jump_table_kernel<<<grid_for(n, kBlock), kBlock>>>(m, R, (int*)mesh->jump.p);
+  if ((rc = check_launch("jump_table_kernel"))) return rc;
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return cuda_fail(e, "build_jump_table");
+  v.jump = (const int*)mesh->jump.p;
+  v.jump_res = R;
   return CMM_OK;
 }
 
@@ -597,8 +708,12 @@ int launch_compose_dev(const MeshView& m, const double* const* table, const BveS
   if (n == 0) return CMM_OK;
   DevSubmaps cp{table, st, last};
   const int b = block_for(m, kTuneCompose, kBlock, n);
-  compose_kernel<false><<<grid_for(n, b), b, 0, s>>>(m, cp, q, n, out, nullptr, nullptr,
-                                                                nullptr, nullptr);
+  if ((m.variant[CMM_VARIANT_COMPOSE] ? m.variant[CMM_VARIANT_COMPOSE] : kComposeBlocks) == 4)
+    compose_kernel<false, DevSubmaps, 4><<<grid_for(n, b), b, 0, s>>>(m, cp, q, n, out, nullptr, nullptr,
+                                                                      nullptr, nullptr);
+  else
+    compose_kernel<false, DevSubmaps, 6><<<grid_for(n, b), b, 0, s>>>(m, cp, q, n, out, nullptr, nullptr,
+                                                                      nullptr, nullptr);
   return check_launch("compose_kernel");
 }
 

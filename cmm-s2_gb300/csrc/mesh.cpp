@@ -281,6 +281,54 @@ int build_host(const double* verts, int nv, const int32_t* tris, int nt, int lev
     location_record(v1, v2, v3, &loc[(size_t)t * kLocStride]);
     assembly_factors(v1, v2, v3, &asmf[(size_t)t * kAsmStride]);
   }
+  // walk tables: inward edge normals and the row across each edge
+  std::vector<float> walk_f((size_t)nt * kWalkStride, 0.f);
+  std::vector<double> walk_d((size_t)nt * kWalkStride, 0.0);
+  {
+    // undirected edge -> the (at most two) rows that contain it
+    std::unordered_map<int64_t, std::pair<int, int>> edge_rows;
+    edge_rows.reserve((size_t)nt * 2);
+    for (int t = 0; t < nt; ++t)
+      for (int e = 0; e < 3; ++e) {
+        const int u = tris[3 * t + e], w = tris[3 * t + (e + 1) % 3];
+        auto ins = edge_rows.emplace((int64_t)std::min(u, w) * nv + std::max(u, w), std::make_pair(t, -1));
+        if (!ins.second) {
+          if (ins.first->second.second >= 0) {
+            set_last_error("cmm_mesh_create: an edge is shared by more than two triangles");
+            return CMM_ERR_MESH;
+          }
+          ins.first->second.second = t;
+        }
+      }
+    for (int t = 0; t < nt; ++t) {
+      const int a[3] = {tris[3 * t], tris[3 * t + 1], tris[3 * t + 2]};
+      const double sgn = det_cols(vtx(verts, a[0]), vtx(verts, a[1]), vtx(verts, a[2])) < 0 ? -1.0 : 1.0;
+      for (int e = 0; e < 3; ++e) {
+        const int u = a[e], w = a[(e + 1) % 3];
+        // the same plane seen from the row across the edge has exactly the
+        // negated normal (cross(w, u) = -cross(u, w) in FP64 without
+        // contraction), so the two rows' side decisions never conflict
+        const D3 n = sgn * unit(cross(vtx(verts, u), vtx(verts, w)));
+        const auto& pr = edge_rows[(int64_t)std::min(u, w) * nv + std::max(u, w)];
+        const int nb = pr.first == t ? pr.second : pr.first;
+        if (nb < 0) {
+          set_last_error("cmm_mesh_create: an edge has no second triangle (not a closed triangulation)");
+          return CMM_ERR_MESH;
+        }
+        float* f = &walk_f[(size_t)t * kWalkStride + 4 * e];
+        f[0] = (float)n.x;
+        f[1] = (float)n.y;
+        f[2] = (float)n.z;
+        std::memcpy(&f[3], &nb, sizeof(int));
+        double* d = &walk_d[(size_t)t * kWalkStride + 3 * e];
+        d[0] = n.x;
+        d[1] = n.y;
+        d[2] = n.z;
+      }
+    }
+  }
+  hm->walk_f.swap(walk_f);
+  hm->walk_d.swap(walk_d);
   hm->level = level;
   hm->nv = nv;
   hm->nt = nt;
@@ -319,6 +367,8 @@ int upload_mesh(const HostMesh& h, cmm_mesh* m) {
   if ((rc = m->node_n.upload(h.node_n.data(), h.node_n.size() * 8))) return rc;
   if ((rc = m->node_nf.upload(h.node_nf.data(), h.node_nf.size() * 4))) return rc;
   if ((rc = m->leaf_row.upload(h.leaf_row.data(), h.leaf_row.size() * 4))) return rc;
+  if ((rc = m->walk_f.upload(h.walk_f.data(), h.walk_f.size() * 4))) return rc;
+  if ((rc = m->walk_d.upload(h.walk_d.data(), h.walk_d.size() * 8))) return rc;
   int zero = 0;
   if ((rc = m->status.upload(&zero, sizeof(int)))) return rc;
   MeshView& v = m->view;
@@ -335,8 +385,11 @@ int upload_mesh(const HostMesh& h, cmm_mesh* m) {
   v.node_n = (const double*)m->node_n.p;
   v.node_nf = (const float*)m->node_nf.p;
   v.leaf_row = (const int*)m->leaf_row.p;
+  v.walk_f = (const float*)m->walk_f.p;
+  v.walk_d = (const double*)m->walk_d.p;
+  v.jump = nullptr;
   v.status = (int*)m->status.p;
-  return CMM_OK;
+  return build_jump_table(m);
 }
 
 }  // namespace cmm

@@ -1038,7 +1038,7 @@ int sht_create(int L, cmm_sht** out) {
   cmm_sht* p = new (std::nothrow) cmm_sht();
   if (!p) {
     set_last_error("cmm_sht_create: out of host memory");
-    return CMM_ERR_ARG;
+    return CMM_ERR_NOMEM;
   }
   p->L = L;
   std::vector<double> th(L + 1), thf(2 * L + 1), w(2 * L + 1);
@@ -1170,6 +1170,10 @@ static int ensure_tables(cmm_sht* p, cudaStream_t s, bool* ok) {
                                                               (const double*)p->ra.p, (const double*)p->rb.p,
                                                               true, (double*)tab->s.p);
   if ((rc = check_launch("build_pbar_kernel"))) return rc;
+  // published only once built: a later call of this plan on another
+  // stream, unordered with s, must not read a partly written table
+  cudaError_t e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(e, "build_pbar_kernel");
   p->tab = std::move(tab);
   *ok = true;
   return CMM_OK;

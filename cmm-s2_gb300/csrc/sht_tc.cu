@@ -436,9 +436,10 @@ __global__ void __launch_bounds__(kThreads, 1) synth_tc_kernel(TcGeometry g, int
   }
   if (tid == 0 && abort_s) {
     // bounded drain of this CTA's copies and products in flight
-    for (long long j = n_ldw; j < n_ld; ++j) mbar_wait(&load_bar[j & 1], (uint32_t)((j >> 1) & 1));
-    for (long long j = n_mmw; j < n_mm; ++j) mbar_wait(&mma_bar[j & 1], (uint32_t)((j >> 1) & 1));
-    atomicOr(status, CMM_FLAG_TIMEOUT);
+    bool drained = true;
+    for (long long j = n_ldw; j < n_ld; ++j) drained &= mbar_wait(&load_bar[j & 1], (uint32_t)((j >> 1) & 1));
+    for (long long j = n_mmw; j < n_mm; ++j) drained &= mbar_wait(&mma_bar[j & 1], (uint32_t)((j >> 1) & 1));
+    atomicOr(status, drained ? CMM_FLAG_TIMEOUT : CMM_FLAG_TIMEOUT | CMM_FLAG_DRAIN_TIMEOUT);
   }
   tc_fence_before();
   __syncthreads();
@@ -600,7 +601,7 @@ __global__ void __launch_bounds__(kThreads) analysis_tc_kernel(TcFwdGeometry g,
       bulk_g2s(sX, srcX, kXRecord, &load_bar);
       if (!mbar_wait(&load_bar, ph_load)) {
         abort_s = 1;
-        mbar_wait(&load_bar, ph_load);   // bounded drain of the copies in flight
+        if (!mbar_wait(&load_bar, ph_load)) abort_s = 2;   // bounded drain of the copies in flight
       }
       if (!abort_s) {
         tc_fence_after();
@@ -619,7 +620,7 @@ __global__ void __launch_bounds__(kThreads) analysis_tc_kernel(TcFwdGeometry g,
         mma_commit(&mma_bar);
         if (!mbar_wait(&mma_bar, ph_mma)) {
           abort_s = 1;
-          mbar_wait(&mma_bar, ph_mma);   // bounded drain of the MMAs in flight
+          if (!mbar_wait(&mma_bar, ph_mma)) abort_s = 2;   // bounded drain of the MMAs in flight
         }
       }
     }
@@ -640,7 +641,7 @@ __global__ void __launch_bounds__(kThreads) analysis_tc_kernel(TcFwdGeometry g,
     __syncthreads();
   }
   if (abort_s) {
-    if (tid == 0) atomicOr(status, CMM_FLAG_TIMEOUT);
+    if (tid == 0) atomicOr(status, abort_s == 2 ? CMM_FLAG_TIMEOUT | CMM_FLAG_DRAIN_TIMEOUT : CMM_FLAG_TIMEOUT);
   } else {
     const int i = lb * kM + tid;
     const int lE = m + 2 * i, lO = m + 1 + 2 * i;
@@ -689,7 +690,7 @@ int tc_plan_create(int L, const double* ct_rings, const double* pmm_rings, const
   TcPlan* p = new (std::nothrow) TcPlan();
   if (!p) {
     set_last_error("tc plan: out of host memory");
-    return CMM_ERR_ARG;
+    return CMM_ERR_NOMEM;
   }
   p->tab = std::make_shared<TcTables>();
   p->L = L;
@@ -764,7 +765,7 @@ int tc_plan_share(const TcPlan* src, TcPlan** out) {
   TcPlan* p = new (std::nothrow) TcPlan();
   if (!p) {
     set_last_error("tc plan: out of host memory");
-    return CMM_ERR_ARG;
+    return CMM_ERR_NOMEM;
   }
   p->L = src->L;
   p->npair = src->npair;

@@ -138,7 +138,7 @@ int bve_create(const cmm_bve_desc* d, cmm_bve** out) {
   cmm_bve* b = new (std::nothrow) cmm_bve();
   if (!b) {
     set_last_error("cmm_bve_create: out of host memory");
-    return CMM_ERR_ARG;
+    return CMM_ERR_NOMEM;
   }
   b->d = *d;
   b->d.stack = nullptr;

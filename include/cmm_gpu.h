@@ -40,7 +40,8 @@ typedef enum {
   CMM_ERR_NONFINITE = 4,    /* status bit: a non-finite value was met */
   CMM_ERR_LOCATE = 5,       /* status bit: a query fell outside its triangle */
   CMM_ERR_TIMEOUT = 6,      /* a bounded wait ran out */
-  CMM_ERR_UNSUPPORTED = 7
+  CMM_ERR_UNSUPPORTED = 7,
+  CMM_ERR_NOMEM = 8         /* a host allocation failed */
 } cmm_status;
 
 /* Bits of the device status word. */
@@ -48,17 +49,18 @@ typedef enum {
 #define CMM_FLAG_LOCATE 2
 #define CMM_FLAG_TIMEOUT 4   /* a bounded wait inside a kernel ran out */
 #define CMM_FLAG_INDEX 8     /* an index argument (a permutation entry) was out of range; skipped */
+/* After a timeout a tensor-core kernel waits (bounded) for its own copies
+ * and products still in flight before it releases its tensor memory and
+ * returns.  If that drain also runs out, operations of the kernel may still
+ * be in flight: this bit is set beside CMM_FLAG_TIMEOUT and the CUDA
+ * context must be treated as unusable (reset it before further work). */
+#define CMM_FLAG_DRAIN_TIMEOUT 16
 
 const char* cmm_last_error(void);
 int cmm_version(void);
 /* Number of kernels this library has launched so far in the process
  * (library-call kernels such as cuFFT's not included). */
 long long cmm_launch_count(void);
-/* FP64 issue-rate calibration (no counterpart in the reference): `blocks`
- * blocks of 256 threads each run 8 independent chains of `iters` FP64 FMAs
- * (16 * iters flops per thread); sink receives blocks*256 doubles.  Time it
- * on `stream` to obtain the FP64 peak of the GPU. */
-int cmm_fp64_probe(int blocks, int iters, double* sink, void* stream);
 
 /* ------------------------------------------------------------------ mesh */
 typedef struct cmm_mesh cmm_mesh;
@@ -249,7 +251,11 @@ int cmm_advect_project(const cmm_mesh* mesh, const cmm_mesh* velmesh,
  *    workspace).
  *  - The first call on each device looks up that device's copy of the
  *    scratch array (cudaGetSymbolAddress) with the device current; make
- *    that first call before any stream capture.
+ *    that first call before any stream capture.  The address is kept for
+ *    the life of the process: after cudaDeviceReset (or anything else
+ *    that destroys the device's primary context) the library's module is
+ *    loaded again and the kept address is stale, so do not call this entry
+ *    point on a device that has been reset.
  *  - All calls on a device share the one array and it keeps the last
  *    call's contents (every entry is rewritten before it is read, so
  *    nothing needs clearing): calls that overlap on the GPU, on different
@@ -329,7 +335,9 @@ int cmm_sht_timeout_selftest(cmm_sht* plan, long long polls, void* stream);
  * table contractions; 0.8 GB at L = 512, 6.5 GB at L = 1024) instead of
  * the on-the-fly recurrence: mode 0 (default) for L <= 512, 1 for any
  * L <= 1024, -1 never.  The tables are built at the next FP64 stage that
- * runs outside a stream capture.  No counterpart in the reference. */
+ * runs outside a stream capture, which then synchronises its stream once,
+ * so later calls of the plan on any stream find them complete.  No
+ * counterpart in the reference. */
 int cmm_sht_set_tables(cmm_sht* plan, int mode);
 /* Release the FP64 inverse scratch (about 400 MB at L = 1024) and, at
  * the FP64 Pbar tables (cmm_sht_set_tables); each is allocated
@@ -397,6 +405,18 @@ int cmm_velmesh_set_records(cmm_mesh* velmesh, int precision);
 #define CMM_TUNE_LOCATE 3
 int cmm_mesh_set_block(cmm_mesh* mesh, int kernel, int threads);
 
+/* Compiled variant of a tunable kernel launched on this mesh (set by an
+ * autotuner from measured timings; 0 restores the default).  The
+ * composition kernels are compiled for several register budgets, named by
+ * the resident 256-thread blocks per SM they allow: with Jacobians 2, 3 or
+ * 4 (128, 80 or 64 registers a thread; default 2), points only 4 or 6 (64
+ * or 40; default 4).  Fewer registers hide more gather latency, more avoid
+ * spills.  Results do not depend on the variant.  No counterpart in the
+ * reference. */
+#define CMM_VARIANT_COMPOSE_JAC 0
+#define CMM_VARIANT_COMPOSE 1
+int cmm_mesh_set_variant(cmm_mesh* mesh, int knob, int value);
+
 /* ---------------------------------------------- device-driven BVE steps */
 /* The main-loop body of euler_simulation_sphere_remapping
  * (cmm_s2/core/spherical_simulations.py:263-294) as one enqueue per step:
@@ -448,6 +468,10 @@ typedef struct {
   int count, nc, identity;
   double ts0;
 } cmm_bve_desc;
+/* Set-up call: uploads the state on the legacy default stream and
+ * synchronises the device, so it must not be called while a stream of
+ * the device is being captured.  A failed host allocation returns
+ * CMM_ERR_NOMEM. */
 int cmm_bve_create(const cmm_bve_desc* desc, cmm_bve** out);
 int cmm_bve_destroy(cmm_bve* bve);
 /* Enqueue one step on `stream` (no host synchronisation, capturable). */

@@ -104,6 +104,60 @@ class MWSS:
         return np.einsum("jm,lmj,j->lm", fine, self.Pf, self.w)
 
 
+# --------------------------------------------- single orders at large L
+def legendre_m(L, m, theta):
+    """Pbar_lm(theta) of one order m for m <= l < L: array (L, len(theta)),
+    rows l < m zero; the recurrence of legendre_table for that column only
+    (legendre_table(L) itself holds L^2 len(theta) values: 17 GB at L =
+    1024)."""
+    theta = np.asarray(theta, dtype=np.float64)
+    x, s = np.cos(theta), np.sin(theta)
+    P = np.zeros((L, len(theta)))
+    pmm = np.full(len(theta), np.sqrt(1 / (4 * np.pi)))
+    for k in range(1, m + 1):
+        pmm = -pmm * np.sqrt((2 * k + 1) / (2 * k)) * s
+    P[m] = pmm
+    if m + 1 < L:
+        P[m + 1] = np.sqrt(2 * m + 3) * x * pmm
+    for l in range(m + 2, L):
+        a = np.sqrt((4 * l * l - 1) / (l * l - m * m))
+        b = np.sqrt(((l - 1) ** 2 - m * m) / (4 * (l - 1) ** 2 - 1))
+        P[l] = a * (x * P[l - 1] - b * P[l - 2])
+    return P
+
+
+def inverse_orders(L, cols, ms):
+    """MWSS.inverse of coefficients that are zero outside the orders ms:
+    cols (len(ms), L) complex [k, l] holds a_{l, ms[k]}; real samples
+    (L+1, 2L)."""
+    theta = np.pi * np.arange(L + 1) / L
+    c = np.zeros((L + 1, L + 1), dtype=complex)
+    for k, m in enumerate(ms):
+        c[:, m] = cols[k] @ legendre_m(L, m, theta)
+    return np.fft.irfft(c, n=2 * L, axis=1) * (2 * L)
+
+
+def forward_orders(f, L, ms):
+    """MWSS.forward of the real samples f (L+1, 2L), the columns m in ms
+    only: (len(ms), L) complex [k, l] = a_{l, ms[k]}."""
+    ms = list(ms)
+    Fm = np.fft.rfft(f, axis=1)[:, ms] * (np.pi / L)
+    sign = (-1.0) ** np.asarray(ms)
+    G = np.empty((2 * L, len(ms)), dtype=complex)
+    G[:L + 1] = Fm
+    G[L + 1:] = sign * Fm[L - 1:0:-1]
+    Gh = np.fft.fft(G, axis=0) / (2 * L)
+    H = np.zeros((4 * L, len(ms)), dtype=complex)
+    H[:L] = Gh[:L]
+    H[3 * L + 1:] = Gh[L + 1:]
+    H[L] = Gh[L] / 2
+    H[3 * L] = Gh[L] / 2
+    fine = np.fft.ifft(H, axis=0)[:2 * L + 1] * (4 * L)
+    w = clenshaw_curtis(2 * L)
+    theta_fine = np.pi * np.arange(2 * L + 1) / (2 * L)
+    return np.stack([legendre_m(L, m, theta_fine) @ (fine[:, k] * w) for k, m in enumerate(ms)])
+
+
 # ------------------------------------------------------ coefficient layouts
 def full_from_half(alm):
     """(L,L) m>=0 -> pyssht 1-D vector (L*L,) using a_{l,-m} = (-1)^m conj(a_lm)."""

@@ -16,7 +16,13 @@ for packages that are absent here:
   the oracle's restated MWSS transform (pyssht itself is absent).
 
 Outputs: ``tests/golden/*.npz`` (small; committed).
-Usage: python tests/golden/make_golden.py
+Usage: python tests/golden/make_golden.py            (every fixture but the
+       large-level Qhull tables)
+       python tests/golden/make_golden.py qhull 5 6 (Qhull-order location
+       fixtures ``qhull_l5.npz``/``qhull_l6.npz``; the level-6 Delaunay build
+       takes ~13 min of one core)
+       python tests/golden/make_golden.py bve1      (the whole barotropic
+       configuration, level 4 / L = 128 / 200 steps: ``bve_l4_L128.npz``)
 """
 import os
 import sys
@@ -119,6 +125,59 @@ def save(name, **arrays):
     path = os.path.join(HERE, name)
     np.savez_compressed(path, **arrays)
     print("wrote", path, sum(a.nbytes for a in map(np.asarray, arrays.values())) // 1024, "KiB raw")
+
+
+def qhull_fixture(level, nq=16384):
+    """Qhull-order triangle table and ``find_simplex`` ids at a large level.
+
+    The reference's triangle index is the row of Qhull's Delaunay simplex
+    table (cmm_s2/core/mesh_functions.py:43-56, 82).  Stored: that table,
+    the ids and barycentrics of ``nq`` seeded random queries plus the exact
+    tie points; the vertices and the random queries are regenerated by the
+    test from ``icosahedral_mesh(level)`` and ``random_sphere_points(nq,
+    seed)``, with SHA-256 digests to prove they are the same bytes.
+    """
+    import hashlib
+    import time
+    t0 = time.time()
+    m = ref_mesh(level)
+    t1 = time.time()
+    tris = np.asarray(m.simplices)
+    seed = 50 + level
+    qr = random_sphere_points(nq, seed=seed)
+    qs = special_points(m.vertices, tris)
+    q = np.concatenate([qr, qs])
+    bcc, tri, _ = m.query(q)
+    print(f"level {level}: Delaunay {t1 - t0:.0f} s, query {time.time() - t1:.1f} s")
+    save(f"qhull_l{level}.npz", tris=tris.astype(np.int32), seed=seed, nq=nq, q_special=qs,
+         tri=tri.astype(np.int32), bcc=bcc,
+         verts_sha=hashlib.sha256(np.ascontiguousarray(m.vertices).tobytes()).hexdigest(),
+         q_sha=hashlib.sha256(np.ascontiguousarray(qr).tobytes()).hexdigest())
+
+
+def bve_config1(nq=2000):
+    """The barotropic configuration run in full by the reference driver
+    (euler_simulation_sphere_remapping, cmm_s2/core/spherical_simulations.py:
+    144-297): level-4 mesh, L = 128, T = 1 in 200 steps (dt = 1/200),
+    n_maps = 20 (remap every 20 steps, 10 submaps), rotation 2 pi; initial
+    vorticity the real SH series of degrees 1..16 with N(0,1) l^-1.5
+    coefficients from seed 0 (cmm_gpu.workloads.random_sh_vorticity).  The
+    restated MWSS transform stands in for pyssht.  Stored: the final
+    composite map at nq seeded random points and the vorticity there
+    (omega0(X) + 2 Omega cos theta(X) - 2 Omega cos theta)."""
+    import time
+    from cmm_gpu.workloads import random_sh_vorticity
+    omega0, a = random_sh_vorticity(16, seed=0)
+    m = ref_mesh(4)
+    t0 = time.time()
+    subs = rsim.euler_simulation_sphere_remapping(128, 200, 1.0, m, omega0, rot_rate=2 * np.pi, n_maps=20)
+    print(f"config-1 run {time.time() - t0:.0f} s")
+    q = random_sphere_points(nq, seed=123)
+    img = subs(q.copy())
+    phi, theta = rutils.cart2sphere(img.T)
+    _, theta_q = rutils.cart2sphere(q.T)
+    om = omega0(phi, theta) + 4 * np.pi * np.cos(theta) - 4 * np.pi * np.cos(theta_q)
+    save("bve_l4_L128.npz", q=q, img=img, omega=om, Nc=subs.Nc, ns=np.array(subs.ns), sh=a)
 
 
 def main():
@@ -291,4 +350,10 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    if len(sys.argv) > 1 and sys.argv[1] == "qhull":
+        for lv in sys.argv[2:]:
+            qhull_fixture(int(lv))
+    elif len(sys.argv) > 1 and sys.argv[1] == "bve1":
+        bve_config1()
+    else:
+        main()

@@ -36,7 +36,13 @@ def test_drop_in_calls(cmm):
     g, d, v = load("mesh_l3.npz"), load("map_l3.npz"), load("velocity_L8.npz")
     mesh = meshes.spherical_triangulation(g["verts"], g["tris"])
     bcc, tri, vs = mesh.query(g["q"][:3000])
-    assert (tri.cpu().numpy() == g["tri"][:3000]).mean() > 0.999
+    # triangle ids bit-exact except within 1e-14 of an edge of the
+    # reference's triangle, where the other container is accepted
+    tri = tri.cpu().numpy()
+    diff = tri != g["tri"][:3000]
+    near = OG.edge_distance(g["verts"], g["tris"], g["tri"][:3000], g["q"][:3000]) <= 1e-14
+    assert not (diff & ~near).any()
+    assert (OG.edge_distance(g["verts"], g["tris"], tri[diff], g["q"][:3000][diff]) <= 1e-14).all()
     mp = spl.sphere_diffeomorphism(mesh, d["jets"][0])
     img = mp(g["q"][:3000]).cpu().numpy()
     np.testing.assert_allclose(img, d["img"][:, :3000], rtol=0, atol=1e-12)

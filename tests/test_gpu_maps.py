@@ -62,6 +62,45 @@ def test_locate_matches_reference_qhull(nat, level):
     print(f"level {level}: {diff.sum()} of {len(tri)} near-edge queries resolved to the neighbour")
 
 
+def qhull_case(level):
+    """The Qhull-order fixture of a large level (tests/golden/make_golden.py
+    qhull_fixture): the reference's triangle table and find_simplex ids of
+    seeded random queries; vertices and queries regenerated here and
+    checked against the fixture's digests."""
+    import hashlib
+    from cmm_gpu.meshgen import icosahedral_mesh, random_sphere_points
+    d = golden(f"qhull_l{level}.npz")
+    verts, _ = icosahedral_mesh(level)
+    assert hashlib.sha256(np.ascontiguousarray(verts).tobytes()).hexdigest() == str(d["verts_sha"])
+    qr = random_sphere_points(int(d["nq"]), seed=int(d["seed"]))
+    assert hashlib.sha256(np.ascontiguousarray(qr).tobytes()).hexdigest() == str(d["q_sha"])
+    return verts, d["tris"], np.concatenate([qr, d["q_special"]]), d["tri"], d["bcc"]
+
+
+@pytest.mark.parametrize("level", [5, 6])
+def test_locate_matches_reference_qhull_large_levels(nat, level):
+    """Bit-exact triangle ids in the reference's own (Qhull) row order at
+    levels 5 and 6, except within 1e-14 of an edge (counted)."""
+    if not os.path.exists(os.path.join(GOLDEN, f"qhull_l{level}.npz")):
+        pytest.skip(f"qhull_l{level}.npz not generated")
+    verts, tris, q, ref_tri, ref_bcc = qhull_case(level)
+    m = nat.Mesh(verts, tris, level)
+    tri, bcc = m.locate(dev(q))
+    tri, bcc = host(tri), host(bcc)
+    diff = tri != ref_tri
+    near = OG.edge_distance(verts, tris, ref_tri, q) <= EDGE_TOL
+    assert not (diff & ~near).any(), int((diff & ~near).sum())
+    assert (OG.edge_distance(verts, tris, tri[diff], q[diff]) <= EDGE_TOL).all()
+    # barycentrics: the reference's determinant ratios carry a rounding
+    # error ~eps/h^2 (h the edge length), which grows 4x per level: 1e-13
+    # at level 4, scaled by 4 per level above it
+    same = ~diff
+    np.testing.assert_allclose(bcc[same], ref_bcc[same], rtol=0, atol=1e-13 * 4.0 ** (level - 4))
+    assert m.status() == 0
+    print(f"level {level}: {int(near.sum())} queries within 1e-14 of an edge, "
+          f"{int(diff.sum())} resolved to the neighbour, of {len(tri)}")
+
+
 @pytest.mark.parametrize("level", [5, 7])
 def test_locate_large_levels_against_cone_oracle(nat, level):
     from cmm_gpu.meshgen import icosahedral_mesh, random_sphere_points
@@ -236,9 +275,12 @@ def test_full_size_composition_properties(nat):
     queries, ids and Jacobians), through size-independent properties:
     images on the sphere; composing the stack in two launches (submaps 4-7,
     then 0-3) gives the same points bit for bit and the chain-rule product
-    of the two Jacobians; the ids of the first submap applied equal plain
-    location; and a 4096-query sample matches the oracle (1e-12 points,
-    1e-10 relative Jacobians)."""
+    of the two Jacobians (to 1e-10 relative: the tangent pushes run in
+    float-float, ~2^-47 per operation, and each push cancels terms ~1/h =
+    120 times larger than its result; measured 2.8e-11 over the 2^24
+    queries); the ids of the first submap applied equal plain location; and
+    a 4096-query sample matches the oracle (1e-12 points, 1e-10 relative
+    Jacobians)."""
     from cmm_gpu.meshgen import icosahedral_mesh, random_sphere_points, stencil_frames
     from cmm_gpu.workloads import submap_stack
     verts, tris = icosahedral_mesh(7)
@@ -256,7 +298,7 @@ def test_full_size_composition_properties(nat):
     JJ = torch.bmm(JA, JB)
     del JA, JB
     rel = float(((JJ - J).abs().amax(dim=(1, 2)) / J.abs().amax(dim=(1, 2))).max())
-    assert rel < 1e-12, rel
+    assert rel < 1e-10, rel
     del JJ
     t0, _ = m.locate(q)
     assert torch.equal(t0, tri)

@@ -143,12 +143,13 @@ def test_scalar_spline_route_matches_reference(nat):
     np.testing.assert_allclose(om, ref, rtol=0, atol=1e-12)
 
 
-@pytest.mark.parametrize("L", [32, 128, 256])
+@pytest.mark.parametrize("L", [32, 128, 256, 1024])
 def test_split_bf16_synthesis_against_fp64(nat, L):
     """The 12-field synthesis on the tensor cores (three bf16 products,
-    FP32 per 64-degree chunk, FP64 across chunks) against the FP64 path.
-    Stated error: max |split - fp64| <= 1e-4 of max |fp64| per field (each
-    split factor carries ~2^-17 relative error)."""
+    FP32 per 64-degree chunk, compensated FP32 across chunks) against the
+    FP64 path, up to the band-limit of the large configuration.  Measured
+    5.0e-6..5.8e-6 of max |fp64| per field; asserted below 2e-5 (each split
+    factor carries ~2^-17 relative error)."""
     rng = np.random.default_rng(L)
     a = np.zeros((12, L, L), dtype=complex)
     for f in range(12):
@@ -161,7 +162,7 @@ def test_split_bf16_synthesis_against_fp64(nat, L):
     assert tc.status() == 0
     err = np.abs(got - ref).max(axis=(1, 2)) / np.abs(ref).max(axis=(1, 2))
     print(f"L={L}: split-BF16 synthesis relative error per field max {err.max():.3e}")
-    assert err.max() < 1e-4
+    assert err.max() < 2e-5
     assert err.max() > 1e-9   # the tensor-core path really ran (not FP64)
 
 
@@ -169,8 +170,8 @@ def test_split_bf16_synthesis_against_fp64(nat, L):
 def test_split_bf16_analysis_against_fp64(nat, L):
     """The forward Legendre analysis on the tensor cores (M = 128 degrees,
     K = 64 fine ring pairs per chunk, weights folded into the data tiles)
-    against the FP64 path on generic samples.  Stated error:
-    max |split - fp64| <= 1e-4 of max |fp64|."""
+    against the FP64 path on generic samples.  Measured 3.4e-6..3.8e-6 of
+    max |fp64|; asserted below 1.5e-5."""
     rng = np.random.default_rng(1000 + L)
     f = rng.standard_normal((L + 1, 2 * L))
     f[0] = f[0, 0]
@@ -182,12 +183,16 @@ def test_split_bf16_analysis_against_fp64(nat, L):
     low = np.tril(np.ones((L, L), dtype=bool)).T   # [m, l] entries with l >= m
     err = np.abs(got - ref)[low].max() / np.abs(ref[low]).max()
     print(f"L={L}: split-BF16 analysis relative error {err:.3e}")
-    assert err < 1e-4
+    assert err < 1.5e-5
     assert err > 1e-9
 
 
-def test_split_bf16_velocity_jets(nat):
-    L = 128
+@pytest.mark.parametrize("L", [128, 1024])
+def test_split_bf16_velocity_jets(nat, L):
+    """The whole velocity pipeline (analysis, D^-1, ladders, 12-field
+    synthesis, jets) in the split-BF16 form against the FP64 form, up to
+    the band-limit of the large configuration.  Measured ~9e-6 of the
+    largest jet value; asserted below 3e-5."""
     theta, phi, g, verts, Phi, The = grid(L)
     vm = nat.VelMesh(L, theta, phi, g, verts)
     om = 30 * np.cos(The) * np.cos(4 * Phi) * np.sin(The) ** 4 + np.exp(-((np.cos(The) - 0.5) / 0.1) ** 2)
@@ -195,8 +200,9 @@ def test_split_bf16_velocity_jets(nat):
     tc = nat.Sht(L).set_precision(nat.Sht.SPLIT_BF16)
     got = tc.velocity(vm, dev(om)).cpu().numpy()
     err = np.abs(got - ref).max() / np.abs(ref).max()
-    print(f"split-BF16 velocity jets relative error {err:.3e}")
-    assert err < 1e-4
+    print(f"L={L}: split-BF16 velocity jets relative error {err:.3e}")
+    assert 1e-9 < err < 3e-5
+    assert tc.status() == 0
 
 
 def test_power_matches_energy_spectrum(nat):
@@ -296,7 +302,8 @@ def test_full_size_round_trip_and_split_error(nat):
     band-limited field synthesised and analysed again comes back to 1e-12 of
     its largest coefficient in FP64 (the MWSS transform is exact for
     band-limited samples); the split-BF16 analysis of the same samples stays
-    within 1e-4 and above 1e-9 (the tensor-core path ran)."""
+    within 2e-5 (measured ~5e-6) and above 1e-9 (the tensor-core path
+    ran)."""
     L = 1024
     rng = np.random.default_rng(11)
     a = np.tril(rng.standard_normal((L, L)) + 1j * rng.standard_normal((L, L)))
@@ -311,5 +318,44 @@ def test_full_size_round_trip_and_split_error(nat):
     tc = nat.Sht(L).set_precision(nat.Sht.SPLIT_BF16)
     b16 = tc.forward(f).cpu().numpy()
     err = np.abs(b16 - mhalf(a)).max() / scale
-    assert 1e-9 < err < 1e-4, err
+    assert 1e-9 < err < 2e-5, err
     assert tc.status() == 0 and sht.status() == 0
+
+
+ORDERS_1024 = [0, 1, 2, 17, 255, 511, 512, 777, 1000, 1022, 1023]
+
+
+def test_fp64_forward_matches_oracle_at_full_bandlimit(nat):
+    """FP64 analysis at L = 1024 of generic (not band-limited) samples
+    against the oracle's single-order restatement on a spread of orders m
+    (the full oracle table would hold 17 GB): 1e-12 of the largest
+    coefficient."""
+    L = 1024
+    rng = np.random.default_rng(1024)
+    f = rng.standard_normal((L + 1, 2 * L))
+    f[0], f[-1] = f[0, 0], f[-1, 0]
+    got = nat.Sht(L).forward(dev(f)).cpu().numpy()           # [m, l]
+    ref = S.forward_orders(f, L, ORDERS_1024)                # [k, l]
+    scale = np.abs(ref).max()
+    for k, m in enumerate(ORDERS_1024):
+        np.testing.assert_allclose(got[m, m:] / scale, ref[k, m:] / scale, rtol=0, atol=1e-12)
+
+
+def test_fp64_inverse_matches_oracle_at_full_bandlimit(nat):
+    """FP64 synthesis at L = 1024 of coefficients on a spread of orders
+    against the oracle's single-order restatement, every sample of the
+    (1025, 2048) grid: 1e-12 of the largest sample."""
+    L = 1024
+    rng = np.random.default_rng(1025)
+    cols = np.zeros((len(ORDERS_1024), L), dtype=complex)
+    a = np.zeros((L, L), dtype=complex)                      # [m, l]
+    for k, m in enumerate(ORDERS_1024):
+        c = (rng.standard_normal(L - m) + 1j * rng.standard_normal(L - m)) / np.sqrt(1.0 + np.arange(m, L))
+        if m == 0:
+            c = c.real
+        cols[k, m:] = c
+        a[m, m:] = c
+    ref = S.inverse_orders(L, cols, ORDERS_1024)
+    got = nat.Sht(L).inverse(dev(a)).cpu().numpy()
+    scale = np.abs(ref).max()
+    np.testing.assert_allclose(got / scale, ref / scale, rtol=0, atol=1e-12)

@@ -83,3 +83,45 @@ def test_vorticity_restatement_matches_oracle_series():
     fd = float(((series(X + h * dX) - series(X - h * dX)) * y).sum()) / (2 * h)
     ad = float((Xt.grad.numpy() * dX).sum())
     assert abs(fd - ad) < 1e-8 * abs(ad), (fd, ad)
+
+
+def _bve_case():
+    from cmm_gpu import meshgen, workloads
+    from oracle.bve_torch import BVETorch
+    verts, tris = meshgen.icosahedral_mesh(3)
+    _, a = workloads.random_sh_vorticity(6, seed=1)
+    return verts, tris, a, BVETorch(verts, tris, 8, 10, 0.05, n_maps=4)
+
+
+def test_whole_run_restatement_matches_oracle_run():
+    """The torch restatement of the whole barotropic run (oracle.bve_torch,
+    level 3, L = 8, 10 steps, remap every 4) against the numpy oracle's run
+    with the same closed-form choices.  The map update's stencil
+    differences over 4 eps = 4e-5 amplify rounding 2.5e4 times per step, so
+    two FP64 evaluations of the same run agree to ~1e-11, not 1e-16."""
+    from oracle.bve import BVEOracle
+    from oracle import fields as OF
+    verts, tris, a, bt = _bve_case()
+    om = bt.omega_T(torch.from_numpy(a)).numpy()
+    orc = BVEOracle(verts, tris, G.ConeLocator(verts, tris), 8, 10, 0.05, OF.sh_series(a), n_maps=4,
+                    closed=True, tie_fix=True).run()
+    assert np.abs(om - orc.last_omega).max() < 1e-10 * np.abs(orc.last_omega).max()
+
+
+def test_whole_run_restatement_gradient_against_differences():
+    """Its autograd gradient of J along a random direction against centred
+    differences of its own J (h = 1e-5)."""
+    verts, tris, a, bt = _bve_case()
+    target = 0.9 * bt.omega_T(torch.from_numpy(a)).detach()
+    J, g = bt.gradient(a, target)
+    d = np.random.default_rng(3).standard_normal(a.shape)
+    d[np.arange(7)[:, None] < np.abs(np.arange(13)[None, :] - np.arange(7)[:, None])] = 0   # |m| <= l only
+    h = 1e-5
+
+    def Jat(x):
+        with torch.no_grad():
+            return float((bt.W * (bt.omega_T(torch.from_numpy(x)) - target) ** 2).sum())
+
+    fd = (Jat(a + h * d) - Jat(a - h * d)) / (2 * h)
+    ad = float((g * d).sum())
+    assert abs(fd - ad) < 1e-6 * abs(ad), (fd, ad)

@@ -49,6 +49,29 @@ def test_cone_locator_matches_qhull(level):
     np.testing.assert_array_equal(bcc[same], d["bcc"][same])
 
 
+@pytest.mark.parametrize("level", [5, 6])
+def test_cone_locator_matches_qhull_large_levels(level):
+    """The oracle's locator against the reference's Qhull ids at levels 5
+    and 6 (vertices and queries regenerated, checked by digest)."""
+    import hashlib
+    from cmm_gpu.meshgen import icosahedral_mesh, random_sphere_points
+    if not os.path.exists(os.path.join(GOLDEN, f"qhull_l{level}.npz")):
+        pytest.skip(f"qhull_l{level}.npz not generated")
+    d = load(f"qhull_l{level}.npz")
+    verts, _ = icosahedral_mesh(level)
+    assert hashlib.sha256(np.ascontiguousarray(verts).tobytes()).hexdigest() == str(d["verts_sha"])
+    qr = random_sphere_points(int(d["nq"]), seed=int(d["seed"]))
+    assert hashlib.sha256(np.ascontiguousarray(qr).tobytes()).hexdigest() == str(d["q_sha"])
+    q, tris = np.concatenate([qr, d["q_special"]]), d["tris"]
+    tri = G.ConeLocator(verts, tris).locate(q)
+    diff = tri != d["tri"]
+    near = G.edge_distance(verts, tris, d["tri"], q) <= 1e-14
+    assert not (diff & ~near).any(), np.nonzero(diff & ~near)
+    assert (G.edge_distance(verts, tris, tri[diff], q[diff]) <= 1e-14).all()
+    bcc, _, _ = G.query(verts, tris, G.ConeLocator(verts, tris), q)
+    np.testing.assert_array_equal(bcc[~diff], d["bcc"][~diff])
+
+
 def test_qhull_locator_reproduces_reference_table():
     d = load("mesh_l3.npz")
     ql = G.QhullLocator(d["verts"])

@@ -56,3 +56,27 @@ def test_layout_round_trips():
     v = S.full_from_half(a)
     np.testing.assert_array_equal(S.half_from_full(v, L), a)
     np.testing.assert_array_equal(S.vec_from_shifted(S.shifted_from_vec(v, L), L), v)
+
+
+def test_single_order_transforms_match_full_tables():
+    """The per-order forms used at L = 1024 (where the full Legendre table
+    would hold 17 GB) against the full-table transforms at L = 64."""
+    L = 64
+    ms = [0, 1, 5, 31, 63]
+    rng = np.random.default_rng(8)
+    f = rng.standard_normal((L + 1, 2 * L))
+    f[0], f[-1] = f[0, 0], f[-1, 0]
+    sht = S.MWSS(L)
+    full = sht.forward(f)
+    part = S.forward_orders(f, L, ms)
+    for k, m in enumerate(ms):
+        np.testing.assert_allclose(part[k], full[:, m], rtol=0, atol=1e-14 * np.abs(full).max())
+    a = np.zeros((L, L), dtype=complex)
+    cols = np.zeros((len(ms), L), dtype=complex)
+    for k, m in enumerate(ms):
+        cols[k, m:] = rng.standard_normal(L - m) + 1j * rng.standard_normal(L - m)
+        if m == 0:
+            cols[k] = cols[k].real
+        a[:, m] = cols[k]
+    ref = sht.inverse(a)
+    np.testing.assert_allclose(S.inverse_orders(L, cols, ms), ref, rtol=0, atol=1e-13 * np.abs(ref).max())

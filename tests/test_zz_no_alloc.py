@@ -4,12 +4,14 @@ through the C ABI.
 It is meant for callers that cannot allocate device memory (an application
 that has given all GPU memory to its own pool, or a loop that must not call
 cudaMalloc, which can synchronise the device); its scratch is a fixed array
-compiled into the library.  Two calls in a row must reproduce the
-workspace-based cmm_advect_project on the same inputs, within the
-tolerances of the other map-update tests (jet values 1e-12, gradients
-5e-10), and meshes beyond its size limit must be refused.  This file is
-collected last so that a run stopping at its first failure has run every
-other test already; it also passes on its own in a fresh process."""
+compiled into the library.  It runs the same two kernels as the
+workspace-based cmm_advect_project on the same inputs, with only the
+scratch address changed, so two calls in a row must reproduce that entry
+point bit for bit -- on a small mesh and on a mesh of exactly the largest
+accepted size (level 5, 10242 vertices, the whole fixed array in use) --
+and meshes beyond the limit must be refused.  This file is collected last
+so that a run stopping at its first failure has run every other test
+already; it also passes on its own in a fresh process."""
 import ctypes
 import os
 
@@ -41,6 +43,16 @@ def call_noalloc(nat, mesh, vm, vc, ts0, scheme, t, dt, s_pts, tan, prev, jets):
         nat._ptr(prev), 1e-5, nat._ptr(jets), nat._stream())
 
 
+def check_against_workspace_version(nat, mesh, vm, vc, s_pts, tan, cases):
+    for scheme, nvs, t, pc in cases:       # calls in a row, different inputs
+        ref, _ = mesh.advect_project(vm, vc[:nvs], 0.0, scheme, t, 0.1, s_pts, tan, pc)
+        out = torch.full_like(ref, np.nan)
+        rc = call_noalloc(nat, mesh, vm, vc[:nvs], 0.0, scheme, t, 0.1, s_pts, tan, pc, out)
+        assert rc == 0, nat.lib.cmm_last_error()
+        assert torch.equal(out, ref)
+    assert mesh.status() == 0 and vm.status() == 0
+
+
 def test_noalloc_matches_workspace_version_twice(nat):
     from cmm_gpu.meshgen import latlon_mesh_arrays, stencil_frames
     g = np.load(os.path.join(GOLDEN, "mesh_l3.npz"))
@@ -53,16 +65,26 @@ def test_noalloc_matches_workspace_version_twice(nat):
     tan, s_pts = stencil_frames(g["verts"])
     tan, s_pts = dev(tan), dev(s_pts)
     prev = mesh.assemble(dev(a["jets_prev"]))
-    cases = [(nat.RK4, 3, 0.05, prev), (nat.EULER, 1, 0.0, None)]
-    for scheme, nvs, t, pc in cases:       # two calls in a row, different inputs
-        ref, _ = mesh.advect_project(vm, vc[:nvs], 0.0, scheme, t, 0.1, s_pts, tan, pc)
-        out = torch.full_like(ref, np.nan)
-        rc = call_noalloc(nat, mesh, vm, vc[:nvs], 0.0, scheme, t, 0.1, s_pts, tan, pc, out)
-        assert rc == 0, nat.lib.cmm_last_error()
-        out, ref = out.cpu().numpy(), ref.cpu().numpy()
-        np.testing.assert_allclose(out[:, 0], ref[:, 0], rtol=0, atol=1e-12)
-        np.testing.assert_allclose(out[:, 1:], ref[:, 1:], rtol=0, atol=5e-10)
-    assert mesh.status() == 0 and vm.status() == 0
+    check_against_workspace_version(nat, mesh, vm, vc, s_pts, tan,
+                                    [(nat.RK4, 3, 0.05, prev), (nat.EULER, 1, 0.0, None)])
+
+
+def test_noalloc_at_its_size_limit(nat):
+    """Level 5 has exactly the largest accepted vertex count, so the last
+    scratch entries (stencil foot points of the last vertices) are used."""
+    from cmm_gpu.meshgen import icosahedral_mesh, latlon_mesh_arrays, stencil_frames
+    from cmm_gpu.workloads import submap_stack
+    verts, tris = icosahedral_mesh(5)
+    assert len(verts) == 10242
+    mesh = nat.Mesh(verts, tris, 5)
+    v = np.load(os.path.join(GOLDEN, "velocity_L8.npz"))
+    theta, phi, grid, verts_u = latlon_mesh_arrays(8)
+    vm = nat.VelMesh(8, theta, phi, grid, verts_u)
+    vc = [vm.assemble(dev(v["vals"][n])) for n in range(3)]
+    tan, s_pts = stencil_frames(verts)
+    prev = mesh.assemble(dev(submap_stack(s_pts, tan, 1, seed=9)[0]))
+    check_against_workspace_version(nat, mesh, vm, vc, dev(s_pts), dev(tan),
+                                    [(nat.RK4, 3, 0.05, prev), (nat.IMPROVED_EULER, 2, 0.0, None)])
 
 
 def test_noalloc_refuses_meshes_beyond_its_limit(nat):
