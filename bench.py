@@ -5,8 +5,10 @@ level-7 icosahedral mesh (163,842 vertices, 327,680 triangles), a stack of
 8 composed Powell-Sabin submaps (seeded random rotations plus harmonic
 perturbations of amplitude 1e-2), 2^24 queries uniform on the sphere;
 outputs FP64 points, int32 triangle ids of the queries and FP64 3x3
-tangent Jacobians.  One step = one composition of all queries through all
-submaps.  metric = map evaluations per second = queries x submaps / time.
+tangent Jacobians.  One step = the queries sorted by coarse cell and
+composed through all submaps (as map forms: each Powell-Sabin patch stored
+as its quadratic form p^T Q p).  metric = map evaluations per second =
+queries x submaps / time.
 
   value      kernel-only, inputs resident in HBM (every buffer is larger
              than the 129 MB L2, so no flush is needed between steps)
@@ -42,17 +44,17 @@ sys.path.insert(0, os.path.join(ROOT, "cmm-s2_gb300"))
 
 LEVEL, SUBMAPS = 7, 8
 METRIC = "map evals/s"
-# DRAM bytes (read + write) of one compose launch per query, from the ncu
-# capture of 2^22 queries summarised in profiles/compose_level7.md
-# (18.671 GB + 1.118 GB); the gathers scale with the number of queries.
-COMPOSE_TRAFFIC_PER_QUERY = (18.671e9 + 1.118e9) / (1 << 22)
-# The same with the queries grouped by coarse cell (cmm_query_order), from
-# the same capture (3.101 GB read + 0.961 GB written: the output rows are
-# scattered).
-COMPOSE_TRAFFIC_PER_QUERY_ORDERED = (3.101e9 + 0.961e9) / (1 << 22)
-# FP64-pipe instructions per map evaluation (query x submap) with the
-# Jacobian, from the same capture (sm__thread_inst_executed_pipe_fp64).
-FP64_INSTR_PER_EVAL = 110.4
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one
+# Jacobian compose launch per query, from one ncu capture of compose_kernel
+# on 2^22 queries (level 7, 8 submaps), scaled to the headline's 2^24 by
+# the number of queries (the gathers and outputs grow with it): with the
+# queries grouped by coarse cell (the headline step) ...
+COMPOSE_TRAFFIC_PER_QUERY = (3.1035e9 + 1.0023e9) / (1 << 22)
+# ... and in the caller's order.
+COMPOSE_TRAFFIC_PER_QUERY_CALLER = (18.671e9 + 1.118e9) / (1 << 22)
+# FP64 instructions (DADD + DMUL + DFMA) per map evaluation (query x
+# submap) with the Jacobian, from the same capture.
+FP64_INSTR_PER_EVAL = 56.1
 
 
 def peaks():
@@ -345,6 +347,10 @@ def bench_gpu(args, rank, world, sample_idx=None):
     Q = 1 << args.logq
     mesh = native.Mesh(verts, tris, LEVEL)
     cs = [mesh.assemble(torch.from_numpy(j).to(dev)) for j in jets]
+    # every submap also as map-form records (quadratic forms), assembled
+    # once like the coefficient records
+    fs = [mesh.assemble_forms(c) for c in cs]
+    farr = (native.ctypes.c_void_p * SUBMAPS)(*[f.data_ptr() for f in fs])
     q = torch.from_numpy(rsp(Q, seed=3 + rank)).to(dev)
     out = torch.empty_like(q)
     tri = torch.empty(Q, dtype=torch.int32, device=dev)
@@ -355,23 +361,28 @@ def bench_gpu(args, rank, world, sample_idx=None):
     work = torch.empty(native.lib.cmm_query_order_workspace(Q), dtype=torch.int32, device=dev)
     st = native.ctypes.c_void_p(stream.cuda_stream)
 
-    def step(mark=None, ordered=False):
+    def step(mark=None, ordered=False, forms=True):
         # caller order, or (ordered) the queries grouped by coarse cell
-        # inside the step, then the composition in that order; `mark`
-        # records an event before the composition
-        if not ordered:
-            if mark is not None:
-                mark.record(stream)
-            native.check(native.lib.cmm_compose(mesh.h, arr, SUBMAPS, native._ptr(q), Q, native._ptr(out),
-                                                native._ptr(tri), None, native._ptr(jac), st), "cmm_compose")
-            return
-        native.check(native.lib.cmm_query_order(mesh.h, native._ptr(q), Q, native._ptr(perm),
-                                                native._ptr(work), st), "cmm_query_order")
+        # inside the step, then the composition in that order, through the
+        # map forms (or the coefficient records); `mark` records an event
+        # before the composition
+        if ordered:
+            native.check(native.lib.cmm_query_order(mesh.h, native._ptr(q), Q, native._ptr(perm),
+                                                    native._ptr(work), st), "cmm_query_order")
         if mark is not None:
             mark.record(stream)
-        native.check(native.lib.cmm_compose_ordered(mesh.h, arr, SUBMAPS, native._ptr(q), Q, native._ptr(perm),
-                                                    native._ptr(out), native._ptr(tri), None, native._ptr(jac),
-                                                    st), "cmm_compose_ordered")
+        pm = native._ptr(perm) if ordered else None
+        if forms:
+            native.check(native.lib.cmm_compose_forms(mesh.h, arr, farr, SUBMAPS, native._ptr(q), Q, pm,
+                                                      native._ptr(out), native._ptr(tri), None, native._ptr(jac),
+                                                      st), "cmm_compose_forms")
+        elif ordered:
+            native.check(native.lib.cmm_compose_ordered(mesh.h, arr, SUBMAPS, native._ptr(q), Q, pm,
+                                                        native._ptr(out), native._ptr(tri), None,
+                                                        native._ptr(jac), st), "cmm_compose_ordered")
+        else:
+            native.check(native.lib.cmm_compose(mesh.h, arr, SUBMAPS, native._ptr(q), Q, native._ptr(out),
+                                                native._ptr(tri), None, native._ptr(jac), st), "cmm_compose")
 
     def barrier():
         if world > 1:
@@ -393,7 +404,7 @@ def bench_gpu(args, rank, world, sample_idx=None):
     del sink
 
     for _ in range(args.warmup):
-        step()
+        step(ordered=True)
     torch.cuda.synchronize()
     assert mesh.status() == 0
     n0 = native.lib.cmm_launch_count()
@@ -405,7 +416,7 @@ def bench_gpu(args, rank, world, sample_idx=None):
         torch.cuda.synchronize()
         e0.record(stream)
         for k in range(args.steps):
-            step(marks[k][0])
+            step(marks[k][0], ordered=True)
             marks[k][1].record(stream)
         e1.record(stream)
         torch.cuda.synchronize()
@@ -418,21 +429,35 @@ def bench_gpu(args, rank, world, sample_idx=None):
     if sample_idx is not None:   # outputs of the timed steps at the parity sample
         ix = torch.from_numpy(sample_idx).to(dev)
         sample = {"out": out[ix].cpu().numpy(), "tri": tri[ix].cpu().numpy(), "jac": jac[ix].cpu().numpy()}
-    # the same step with the queries grouped by coarse cell first
-    # (cmm_query_order + cmm_compose_ordered): a fifth of the DRAM traffic,
-    # reported beside the headline
+    # the same composition in the caller's query order (no sort): about
+    # five times the DRAM traffic of the gathers, reported beside the
+    # headline
     for _ in range(2):
-        step(ordered=True)
+        step()
     torch.cuda.synchronize()
     e0.record(stream)
     for k in range(args.steps):
-        step(marks[k][0], ordered=True)
+        step(marks[k][0])
         marks[k][1].record(stream)
     e1.record(stream)
     torch.cuda.synchronize()
-    ordered = {"ms_per_step": e0.elapsed_time(e1) / args.steps,
-               "compose_ms": sum(a.elapsed_time(b) for a, b in marks) / args.steps,
-               "traffic_per_launch": COMPOSE_TRAFFIC_PER_QUERY_ORDERED * Q}
+    caller = {"ms_per_step": e0.elapsed_time(e1) / args.steps,
+              "compose_ms": sum(a.elapsed_time(b) for a, b in marks) / args.steps,
+              "traffic_per_launch": COMPOSE_TRAFFIC_PER_QUERY_CALLER * Q}
+    # the same step evaluated from the coefficient records (barycentrics +
+    # Bernstein sum) instead of the map forms
+    for _ in range(2):
+        step(ordered=True, forms=False)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for k in range(args.steps):
+        step(marks[k][0], ordered=True, forms=False)
+        marks[k][1].record(stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    caller["records_path"] = {"ms_per_step": e0.elapsed_time(e1) / args.steps,
+                              "compose_ms": sum(a.elapsed_time(b) for a, b in marks) / args.steps,
+                              "map_evals_per_s": Q * SUBMAPS / (e0.elapsed_time(e1) / args.steps / 1e3)}
     # points only (no ids, no Jacobians): gather-bound, where the
     # coarse-cell order pays
     values = {}
@@ -441,12 +466,9 @@ def bench_gpu(args, rank, world, sample_idx=None):
             if ordr:
                 native.check(native.lib.cmm_query_order(mesh.h, native._ptr(q), Q, native._ptr(perm),
                                                         native._ptr(work), st), "cmm_query_order")
-                native.check(native.lib.cmm_compose_ordered(mesh.h, arr, SUBMAPS, native._ptr(q), Q,
-                                                            native._ptr(perm), native._ptr(out), None, None,
-                                                            None, st), "cmm_compose_ordered")
-            else:
-                native.check(native.lib.cmm_compose(mesh.h, arr, SUBMAPS, native._ptr(q), Q, native._ptr(out),
-                                                    None, None, None, st), "cmm_compose")
+            native.check(native.lib.cmm_compose_forms(mesh.h, arr, farr, SUBMAPS, native._ptr(q), Q,
+                                                      native._ptr(perm) if ordr else None, native._ptr(out),
+                                                      None, None, None, st), "cmm_compose_forms")
         for _ in range(3):
             vstep()
         e0.record(stream)
@@ -466,14 +488,14 @@ def bench_gpu(args, rank, world, sample_idx=None):
     jh = torch.empty((Q, 3, 3), dtype=torch.float64).pin_memory()
     del out, jac, tri
     torch.cuda.empty_cache()
-    scratch, streams = native.compose_host(mesh, cs, qh, oh, th, jh, order=False)
+    scratch, streams = native.compose_host(mesh, cs, qh, oh, th, jh, order=True, forms=fs)
     torch.cuda.synchronize()
     barrier()
     t0 = time.perf_counter()
     e0.record(stream)
     for _ in range(args.steps):
         scratch, streams = native.compose_host(mesh, cs, qh, oh, th, jh, scratch=scratch, streams=streams,
-                                               order=False)
+                                               order=True, forms=fs)
     e1.record(stream)
     torch.cuda.synchronize()
     barrier()
@@ -481,7 +503,7 @@ def bench_gpu(args, rank, world, sample_idx=None):
     assert mesh.status() == 0
     del scratch
 
-    res = dict(ms=ms, ms_compose=ms_compose, ordered=ordered, values_only=values, value=value, ms_e2e=ms_e2e, launches=launches, clocks=clk.summary(), numa_cores=numa_cores,
+    res = dict(ms=ms, ms_compose=ms_compose, caller=caller, values_only=values, value=value, ms_e2e=ms_e2e, launches=launches, clocks=clk.summary(), numa_cores=numa_cores,
                nv=len(verts), nt=len(tris), Q=Q, fp64_fma_per_s=fp64_fma_per_s, sample=sample)
     if rank == 0 and not args.no_bve:
         try:
@@ -491,7 +513,7 @@ def bench_gpu(args, rank, world, sample_idx=None):
             res["bve"] = {"error": f"{type(exc).__name__}: {exc}"}
     if rank == 0 and not (args.no_bve3 and args.no_kernels and args.no_ensemble and args.no_adjoint and
                           args.no_transport):
-        del q, mesh, cs
+        del q, mesh, cs, fs
         torch.cuda.empty_cache()
     if rank == 0 and not args.no_kernels:
         try:
@@ -989,7 +1011,7 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint run")
     ap.add_argument("--no-transport", action="store_true", help="skip the linear-transport run")
     ap.add_argument("--transport-only", action="store_true", help="print only the linear-transport run")
-    ap.add_argument("--adjoint-fd", type=int, default=8,
+    ap.add_argument("--adjoint-fd", type=int, default=32,
                     help="coefficients checked by centred differences in the adjoint run")
     ap.add_argument("--adjoint-only", action="store_true", help="print only the adjoint run")
     ap.add_argument("--kernels-only", action="store_true",
@@ -1015,7 +1037,9 @@ def main():
            "level": LEVEL, "submaps": SUBMAPS, "queries_per_gpu": 1 << LOGQ,
            "l2": "inputs and outputs larger than L2 (queries 402 MB, Jacobians 1.2 GB), no flush",
            "parallelism": f"replicas x{args.gpus} (independent queries per GPU)",
-           "query_order": "caller order (the coarse-cell order is reported under roofline.ordered)"}
+           "query_order": "each step sorts the queries by coarse cell (cmm_query_order, inside the timed "
+                          "step) and composes in that order; caller order is reported under "
+                          "roofline.caller_order"}
 
     if args.impl == "reference":
         if rank != 0:
@@ -1075,7 +1099,7 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": how,
                      "traffic": COMPOSE_TRAFFIC_PER_QUERY * Q, "algorithmic_bytes": algo,
-                     "kernel": "compose_kernel", "kernel_ms": r["ms_compose"], "ordered": r["ordered"]},
+                     "kernel": "compose_kernel", "kernel_ms": r["ms_compose"], "caller_order": r["caller"]},
         "fp64": {"bound": "fp64 pipe (binding on GB300)",
                  "instr_per_eval": FP64_INSTR_PER_EVAL,
                  "achieved_tinstr_s": FP64_INSTR_PER_EVAL * kernel_rate / 1e12,

@@ -51,7 +51,8 @@ class Autotuner:
         t = float(s.tspan[s.step_index])
         prev = None if s.identity else s.coeffs_cur
         stages = {
-            native.Mesh.TUNE_COMPOSE: (s.mesh, lambda: s.mesh.compose(cs, s.sample_pts, out=X)),
+            native.Mesh.TUNE_COMPOSE: (s.mesh, lambda: s.mesh.compose(cs, s.sample_pts, out=X,
+                                                                      forms=s._forms(s.Nc, True))),
             native.Mesh.TUNE_ADVECT: (s.mesh, lambda: s.mesh.advect_project(
                 s.vm, s.vel_coeffs, s.ts0, native.RK4, t, s.dt, s.s_pts, s.tan, prev, jets=jets,
                 work=work)),

@@ -89,20 +89,27 @@ class Ensemble:
 
     @classmethod
     def from_seed(cls, n, seed, levels=(5, 6, 7), bandlimits=(256, 512, 1024), Nt=100, T=0.5,
-                  lmax=64, rms=5.0, n_maps=10, precision="split_bf16", device=None):
+                  lmax=64, rms=5.0, n_maps=10, precision="split_bf16", device=None, forms=None):
         """n members with mesh level and band-limit drawn from `seed`; each
         starts from seeded random vorticity over l <= lmax with a k^-3
         spectrum (coefficients N(0,1) l^-2, scaled to the given RMS),
-        evaluated through its scalar spline."""
+        evaluated through its scalar spline.  forms: the members' remapped
+        submaps with map-form records (BVESolver); None = when their
+        records (0.9 KB per triangle and slot) take at most half of the free
+        device memory."""
         device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
         rng = np.random.default_rng(seed)
         specs = [(int(rng.choice(levels)), int(rng.choice(bandlimits))) for _ in range(n)]
+        if forms is None:
+            slots = len([i for i in range(1, Nt) if i % n_maps == 0]) + 1
+            need = sum(slots * (20 << (2 * lv)) * native.Mesh.FORM_STRIDE * 8 for lv, _ in specs)
+            forms = need <= 0.5 * torch.cuda.mem_get_info(device)[0]
         res = SharedResources(device)
         members = []
         for i, (level, L) in enumerate(specs):
             pert = spectral_perturbation(lmax, seed=seed * 100003 + i, slope=-2.0, rms=rms)
             members.append(BVESolver(None, None, level, L, Nt, T, Vorticity(spline_sh=pert),
-                                     n_maps=n_maps, precision=precision, resources=res))
+                                     n_maps=n_maps, precision=precision, resources=res, forms=forms))
         ens = cls(members)
         ens.specs = specs
         ens.resources = res

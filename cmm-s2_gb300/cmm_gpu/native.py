@@ -31,7 +31,7 @@ class BveDesc(ctypes.Structure):
                 ("jets", _p), ("coeffs_cur", _p), ("work", _p), ("X", _p), ("omega", _p),
                 ("vel_jets", _p), ("vel", _p * 3), ("n_stack", _i), ("stack", _p),
                 ("stack_jets", _p), ("k", _i), ("count", _i), ("nc", _i), ("identity", _i),
-                ("ts0", _d)]
+                ("ts0", _d), ("stack_forms", _p)]
 
 
 _SIGS = {
@@ -53,6 +53,9 @@ _SIGS = {
     "cmm_query_order_workspace": (_i64, [_i64]),
     "cmm_query_order": (_i, [_p, _p, _i64, _p, _p, _p]),
     "cmm_compose_ordered": (_i, [_p, ctypes.POINTER(_p), _i, _p, _i64, _p, _p, _p, _p, _p, _p]),
+    "cmm_assemble_forms": (_i, [_p, _p, _p, _p]),
+    "cmm_compose_forms": (_i, [_p, ctypes.POINTER(_p), ctypes.POINTER(_p), _i, _p, _i64, _p, _p, _p, _p, _p,
+                               _p]),
     "cmm_stencil_eval": (_i, [_p, _p, _p, _p, _i64, _p, _p]),
     "cmm_velmesh_create": (_i, [_i, _p, _p, _p, _p, ctypes.POINTER(_p)]),
     "cmm_velocity_eval": (_i, [_p, ctypes.POINTER(_p), _i, _d, _d, _d, _p, _i64, _p, _p]),
@@ -62,6 +65,7 @@ _SIGS = {
     "cmm_sht_scalar_jets": (_i, [_p, _p, _p, _p, _p]),
     "cmm_sht_create": (_i, [_i, ctypes.POINTER(_p)]),
     "cmm_sht_set_precision": (_i, [_p, _i]),
+    "cmm_sht_set_schedule": (_i, [_p, _i]),
     "cmm_sht_status": (_i, [_p, _p, ctypes.POINTER(_i), _i]),
     "cmm_sht_power": (_i, [_p, _p, _p, _p]),
     "cmm_sht_share_tables": (_i, [_p, _p]),
@@ -208,6 +212,16 @@ class Mesh:
               "cmm_assemble")
         return out
 
+    FORM_STRIDE = 112
+
+    def assemble_forms(self, coeffs, out=None):
+        """Map-form records (Nt, 112) of coefficient records (cmm_assemble_forms)."""
+        if out is None:
+            out = torch.empty((self.nt, self.FORM_STRIDE), dtype=torch.float64, device=coeffs.device)
+        check(lib.cmm_assemble_forms(self.h, _ptr(coeffs), _ptr(out), _stream(coeffs.device)),
+              "cmm_assemble_forms")
+        return out
+
     def query_order(self, q, work=None):
         """Permutation grouping the queries by coarse hierarchy cell."""
         q = _dev(q)
@@ -221,9 +235,10 @@ class Mesh:
         return perm
 
     def compose(self, coeffs, q, want_tri=False, want_tri_all=False, want_jac=False, out=None,
-                perm=None):
+                perm=None, forms=None):
         """coeffs: list of coefficient tensors, submap 0 first (applied last).
-        perm: optional processing order (query_order), same results."""
+        perm: optional processing order (query_order), same results.
+        forms: optional list of map-form records (entries may be None)."""
         q = _dev(q)
         n = q.shape[0]
         S = len(coeffs)
@@ -232,7 +247,11 @@ class Mesh:
         tri = torch.empty(n, dtype=torch.int32, device=q.device) if want_tri else None
         tri_all = torch.empty((S, n), dtype=torch.int32, device=q.device) if want_tri_all else None
         jac = torch.empty((n, 3, 3), dtype=torch.float64, device=q.device) if want_jac else None
-        if perm is None:
+        if forms is not None:
+            farr = (ctypes.c_void_p * S)(*[None if f is None else f.data_ptr() for f in forms])
+            check(lib.cmm_compose_forms(self.h, arr, farr, S, _ptr(q), n, _ptr(perm), _ptr(out), _ptr(tri),
+                                        _ptr(tri_all), _ptr(jac), _stream(q.device)), "cmm_compose_forms")
+        elif perm is None:
             check(lib.cmm_compose(self.h, arr, S, _ptr(q), n, _ptr(out), _ptr(tri), _ptr(tri_all),
                                   _ptr(jac), _stream(q.device)), "cmm_compose")
         else:
@@ -400,6 +419,13 @@ class Sht:
             check(lib.cmm_sht_set_precision(self.h, mode), "cmm_sht_set_precision")
         return self
 
+    SCHEDULE_PER_CHUNK, SCHEDULE_WARP_SPECIALISED = 0, 1
+
+    def set_schedule(self, schedule):
+        """Split-BF16 synthesis schedule (cmm_sht_set_schedule)."""
+        check(lib.cmm_sht_set_schedule(self.h, schedule), "cmm_sht_set_schedule")
+        return self
+
     def share_tables(self, src):
         """Share src's Legendre tables (cmm_sht_share_tables): split-BF16
         mode on src's tables when src is in that mode, else src's FP64 Pbar
@@ -473,16 +499,15 @@ class Sht:
 
 
 def compose_host(mesh, coeffs, q_host, out_host, tri_host=None, jac_host=None, chunks=16,
-                 streams=None, scratch=None, order=None):
+                 streams=None, scratch=None, order=None, forms=None):
     """Composition of host-resident queries (pinned (n,3) float64) into
     host-resident outputs, pipelined in `chunks` pieces over two CUDA
     streams so the host<->device copies overlap the kernels.  order: each
     chunk is processed grouped by coarse cell (cmm_query_order, same
-    results); by default only without Jacobians, where the gathers rather
-    than the FP64 pipe bound the kernel.  Returns the scratch dict for
-    reuse."""
+    results; default), so that neighbouring threads gather neighbouring
+    records.  Returns the scratch dict for reuse."""
     if order is None:
-        order = jac_host is None
+        order = True
     n = q_host.shape[0]
     dev = mesh.device
     streams = streams or [torch.cuda.Stream(dev), torch.cuda.Stream(dev)]
@@ -498,6 +523,8 @@ def compose_host(mesh, coeffs, q_host, out_host, tri_host=None, jac_host=None, c
                 perm=torch.empty(step, dtype=torch.int32, device=dev),
                 work=torch.empty(lib.cmm_query_order_workspace(step), dtype=torch.int32, device=dev))
     arr = (ctypes.c_void_p * len(coeffs))(*[c.data_ptr() for c in coeffs])
+    farr = None if forms is None else (ctypes.c_void_p * len(coeffs))(
+        *[None if f is None else f.data_ptr() for f in forms])
     cur = torch.cuda.current_stream(dev)
     for s in streams:
         s.wait_stream(cur)
@@ -514,6 +541,11 @@ def compose_host(mesh, coeffs, q_host, out_host, tri_host=None, jac_host=None, c
             if order:
                 check(lib.cmm_query_order(mesh.h, _ptr(b["q"]), m, _ptr(b["perm"]), _ptr(b["work"]), st),
                       "cmm_query_order")
+            if farr is not None:
+                check(lib.cmm_compose_forms(mesh.h, arr, farr, len(coeffs), _ptr(b["q"]), m,
+                                            _ptr(b["perm"]) if order else None, _ptr(b["out"]), _ptr(b["tri"]),
+                                            None, _ptr(b["jac"]), st), "cmm_compose_forms")
+            elif order:
                 check(lib.cmm_compose_ordered(mesh.h, arr, len(coeffs), _ptr(b["q"]), m, _ptr(b["perm"]),
                                               _ptr(b["out"]), _ptr(b["tri"]), None, _ptr(b["jac"]), st),
                       "cmm_compose_ordered")

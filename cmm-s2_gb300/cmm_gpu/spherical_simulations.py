@@ -57,13 +57,17 @@ class Vorticity:
 
 class BVESolver:
     def __init__(self, verts, tris, level, L, Nt, T, vorticity, rot_rate=2 * np.pi, n_maps=10,
-                 device=None, precision="fp64", resources=None, fp64_tables=None):
+                 device=None, precision="fp64", resources=None, fp64_tables=None, forms=True):
         """verts, tris: the icosahedral mesh of `level` (reference row order);
         with `resources` (ensemble.SharedResources) they may be None and the
         mesh, stencil frames, velocity mesh, sample points and split-BF16
         tables are taken from (and shared through) it.  fp64_tables: the
         FP64 Legendre stages from Pbar tables (True), from the recurrence
-        (False) or by band-limit (None: tables for L <= 512)."""
+        (False) or by band-limit (None: tables for L <= 512).  forms: every
+        remapped submap also gets its map-form records (cmm_assemble_forms,
+        the patches as quadratic forms; 0.9 KB per triangle), through which
+        the sample points cross the stack at every step (the current map
+        stays on its coefficient records)."""
         self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
         dev = self.device
         if precision not in ("fp64", "split_bf16"):
@@ -122,6 +126,8 @@ class BVESolver:
         self.coeffs_cur = self.mesh.new_coeffs()
         self.stack = [self.mesh.new_coeffs() for _ in ns]
         self.stack_jets = [torch.empty_like(self.id_jets) for _ in ns]
+        self.stack_forms = ([torch.zeros((self.mesh.nt, native.Mesh.FORM_STRIDE), **f64) for _ in ns]
+                            if forms else None)
         self.vel_coeffs = [self.vm.new_coeffs() for _ in range(3)]
         self.vel_jets = torch.empty((3, 4, self.vm.nv), **f64)
         self.work = torch.empty(native.lib.cmm_advect_workspace(self.mesh.h), **f64)
@@ -165,10 +171,17 @@ class BVESolver:
         self.mesh.assemble(self.jets, out=self.coeffs_cur)
         self.launches += 3
 
+    def _forms(self, n, current):
+        """Form records of the first n stack slots (and None for the
+        current map when `current`), or None without forms."""
+        if self.stack_forms is None:
+            return None
+        return self.stack_forms[:n] + ([None] if current else [])
+
     def _sample(self):
         """submaps(curr_map(sample_pts)) (spherical_simulations.py:268)."""
         cs = self.stack[:self.Nc] + [self.coeffs_cur]
-        self.mesh.compose(cs, self.sample_pts, out=self.X)
+        self.mesh.compose(cs, self.sample_pts, out=self.X, forms=self._forms(self.Nc, True))
         self.launches += 1
         return self.X
 
@@ -220,6 +233,9 @@ class BVESolver:
             d.vel[k] = self.vel_coeffs[k].data_ptr()
         self._stack_arr = (ctypes.c_void_p * len(self.stack))(*[c.data_ptr() for c in self.stack])
         self._jets_arr = (ctypes.c_void_p * len(self.stack))(*[j.data_ptr() for j in self.stack_jets])
+        if self.stack_forms is not None:
+            self._forms_arr = (ctypes.c_void_p * len(self.stack))(*[f.data_ptr() for f in self.stack_forms])
+            d.stack_forms = ctypes.cast(self._forms_arr, ctypes.c_void_p)
         d.n_stack = len(self.stack)
         d.stack = ctypes.cast(self._stack_arr, ctypes.c_void_p)
         d.stack_jets = ctypes.cast(self._jets_arr, ctypes.c_void_p)
@@ -296,6 +312,8 @@ class BVESolver:
             idx = self.ns.index(self.count)
             self.Nc = idx + 1
             self.stack[idx].copy_(self.coeffs_cur)
+            if self.stack_forms is not None:
+                self.mesh.assemble_forms(self.stack[idx], out=self.stack_forms[idx])
             self.stack_jets[idx].copy_(self.jets)
             self.jets.copy_(self.id_jets)
             self.identity = True
@@ -374,7 +392,8 @@ class BVESolver:
         cs = self.stack[:self.Nc] + ([] if self.identity else [self.coeffs_cur])
         if not cs:
             return q.clone(), None
-        out, _, _, jac = self.mesh.compose(cs, q, want_jac=want_jac)
+        out, _, _, jac = self.mesh.compose(cs, q, want_jac=want_jac,
+                                           forms=self._forms(self.Nc, not self.identity))
         return out, jac
 
     def stack_coeffs(self):

@@ -71,6 +71,8 @@ def load_bve_state(solver, path):
     for i in range(Nc):
         s.stack_jets[i].copy_(torch.from_numpy(d["stack_jets"][i]).to(dev))
         s.mesh.assemble(s.stack_jets[i], out=s.stack[i])
+        if s.stack_forms is not None:
+            s.mesh.assemble_forms(s.stack[i], out=s.stack_forms[i])
     for k in range(3):
         s.vel_coeffs[k].copy_(torch.from_numpy(d["vel"][k]).to(dev))
     s.omega.copy_(torch.from_numpy(d["omega"]).to(dev))

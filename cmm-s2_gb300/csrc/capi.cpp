@@ -212,6 +212,11 @@ int cmm_sht_timeout_selftest(cmm_sht* plan, long long polls, void* stream) {
   return tc_wait_timeout_probe(polls, sht_status_word(plan), (cudaStream_t)stream);
 }
 
+int cmm_sht_set_schedule(cmm_sht* plan, int schedule) {
+  if (!plan) return arg_error("cmm_sht_set_schedule: null pointer");
+  return sht_set_schedule(plan, schedule);
+}
+
 int cmm_sht_set_tables(cmm_sht* plan, int mode) {
   if (!plan) return arg_error("cmm_sht_set_tables: null pointer");
   return sht_set_tables(plan, mode);
@@ -434,6 +439,24 @@ int cmm_query_order(const cmm_mesh* mesh, const double* q, int64_t n, int32_t* p
   if (!mesh || n < 0 || n > INT32_MAX || (n > 0 && (!q || !perm || !work)))
     return arg_error("cmm_query_order: bad argument");
   return launch_query_order(mesh->view, q, n, perm, work, (cudaStream_t)stream);
+}
+
+int cmm_assemble_forms(const cmm_mesh* mesh, const double* coeffs, double* forms, void* stream) {
+  if (!mesh || mesh->view.kind != kIcosahedral || !coeffs || !forms)
+    return arg_error("cmm_assemble_forms: bad argument");
+  return launch_assemble_forms(mesh->view, coeffs, forms, (cudaStream_t)stream);
+}
+
+int cmm_compose_forms(const cmm_mesh* mesh, const double* const* coeffs, const double* const* forms, int S,
+                      const double* q, int64_t n, const int32_t* perm, double* out, int32_t* tri,
+                      int32_t* tri_all, double* jac, void* stream) {
+  if (!mesh || mesh->view.kind != kIcosahedral || S < 1 || S > CMM_MAX_SUBMAPS || !coeffs || n < 0 ||
+      n > INT32_MAX || (n > 0 && (!q || !out)))
+    return arg_error("cmm_compose_forms: bad argument");
+  for (int k = 0; k < S; ++k)
+    if (!coeffs[k]) return arg_error("cmm_compose_forms: null coefficient pointer");
+  return launch_compose(mesh->view, coeffs, S, q, n, out, tri, tri_all, jac, (cudaStream_t)stream, perm,
+                        forms);
 }
 
 int cmm_compose_ordered(const cmm_mesh* mesh, const double* const* coeffs, int S, const double* q,

@@ -27,6 +27,10 @@ constexpr int kWalkStride = 16;     // per-row walk record: 3 x float4 + padding
 constexpr int kWalkMax = 64;        // walk steps before falling back to the descent
 constexpr int kCoeffStride3 = 64;   // 19 ordinates x 3 components, padded
 constexpr int kCoeffStride1 = 24;   // 19 ordinates, padded
+// Map-form record (doubles per triangle): for each of the 6 Powell-Sabin
+// sub-triangles (kSubIndex) and each component the homogeneous quadratic
+// form P(p) = p^T Q p as (Qxx, Qyy, Qzz, 2Qxy, 2Qxz, 2Qyz), 108 used.
+constexpr int kFormStride = 112;
 
 // Device view of an icosahedral mesh.
 struct MeshView {
@@ -43,7 +47,8 @@ struct MeshView {
   const int* leaf_row;      // (nt) hierarchical leaf -> reference row
   // walk location (locate_row): per row kWalkStride floats -- for each edge
   // (v0v1, v1v2, v2v0) its inward unit normal (FP32) and the row across it
-  // (bit pattern in the 4th float) -- the FP64 normals (kWalkStride
+  // (bit pattern in the 4th float), then the barycentric scales s_0..s_2
+  // (b_i = s_i n_(i+1,i+2) . q) -- the FP64 normals (kWalkStride
   // doubles per row, 9 used) and a cube-map jump table of 6 jump_res^2
   // starting rows (NULL until built: the hierarchy descent is used)
   const float* walk_f;
@@ -133,7 +138,14 @@ int launch_assemble(const MeshView& m, const double* jets, int ncomp, double* co
                     cudaStream_t s, const BveState* st = nullptr);
 int launch_compose(const MeshView& m, const double* const* coeffs, int S, const double* q,
                    int64_t n, double* out, int32_t* tri, int32_t* tri_all, double* jac,
-                   cudaStream_t s, const int32_t* perm = nullptr);
+                   cudaStream_t s, const int32_t* perm = nullptr, const double* const* forms = nullptr);
+// Map-form records (Nt, kFormStride) from coefficient records (Nt, 64).
+int launch_assemble_forms(const MeshView& m, const double* coeffs, double* forms, cudaStream_t s);
+// The forms of the stack slot a device-driven step remaps into (no-op on
+// the other steps).
+struct BveState;
+int launch_remap_forms(const MeshView& m, const BveState* st, int n_maps, int Nt, const double* const* table,
+                       double* const* ftable, cudaStream_t s);
 // Query order by coarse cell (cmm_query_order): perm (n) and work
 // (order_workspace(n) int32).
 int64_t order_workspace(int64_t n);
@@ -142,7 +154,8 @@ int launch_query_order(const MeshView& m, const double* q, int64_t n, int32_t* p
 // Composition through the st->nc submaps of the device table `table`
 // (submap 0 first) followed by `last` (applied first), no Jacobian.
 int launch_compose_dev(const MeshView& m, const double* const* table, const BveState* st,
-                       const double* last, const double* q, int64_t n, double* out, cudaStream_t s);
+                       const double* last, const double* q, int64_t n, double* out, cudaStream_t s,
+                       const double* const* ftable = nullptr);
 int launch_stencil_eval(const MeshView& m, const double* coeffs, const double* yn,
                         const double* st, int64_t nv, double* out, cudaStream_t s);
 // Host-side tables of an icosahedral mesh (before upload).
@@ -279,6 +292,8 @@ void tc_plan_destroy(TcPlan* p);
 int tc_plan_share(const TcPlan* src, TcPlan** out);
 size_t tc_plan_bytes(const TcPlan* p);
 int tc_synthesis(TcPlan* p, const double2* fields, float2* S, int* status, cudaStream_t s);
+void tc_set_schedule(TcPlan* p, int schedule);
+int sht_set_schedule(cmm_sht* p, int schedule);
 int tc_analysis(TcPlan* p, const float2* fine, const double* w, double2* alm, int* status,
                 cudaStream_t s);
 int tc_wait_timeout_probe(long long polls, int* status, cudaStream_t s);

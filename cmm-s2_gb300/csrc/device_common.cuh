@@ -142,44 +142,55 @@ __device__ __forceinline__ int jump_cell(int R, float x, float y, float z) {
   return (face * R + iv) * R + iu;
 }
 
-// q strictly outside edge k of row t: the FP32 side test against the unit
-// edge normal, redone in FP64 within the filter.  The row across the edge
-// holds the exactly negated normals, so two rows never both reject q.
-__device__ __forceinline__ bool edge_out(const MeshView& m, int t, int k, float4 e, float fx, float fy, float fz,
-                                         double x, double y, double z) {
-  const float d = fmaf(e.x, fx, fmaf(e.y, fy, e.z * fz));
+// FP32 side value of q against edge k's unit normal, and the decision
+// "q strictly outside edge k of row t": the FP32 sign, redone in FP64
+// within the filter.  The row across the edge holds the exactly negated
+// normals, so two rows never both reject q.
+__device__ __forceinline__ float edge_dot(float4 e, float fx, float fy, float fz) {
+  return fmaf(e.x, fx, fmaf(e.y, fy, e.z * fz));
+}
+
+__device__ __forceinline__ bool edge_out(const MeshView& m, int t, int k, float d, double x, double y, double z) {
   if (fabsf(d) > kFilter) return d < 0.0f;
   const double* n = m.walk_d + (int64_t)t * kWalkStride + 3 * k;
   return n[0] * x + n[1] * y + n[2] * z < 0.0;
 }
 
-// Reference row of the icosahedral triangle containing q.  With the jump
-// table built: start at the row that contains the centre of q's cube-map
-// cell and walk across the first edge that q lies outside of until q is
-// inside all three (a handful of steps: the cells are smaller than the
-// triangles); a walk that has not ended after kWalkMax steps falls back
-// to the hierarchy descent.  Both are exact containment tests, so they
-// agree except for queries within rounding distance of an edge, where
-// either neighbour contains the query.
-__device__ __forceinline__ int locate_row(const MeshView& m, double x, double y, double z) {
-  if (!m.jump) return locate_descent(m, x, y, z);
-  const float fx = to_f32_trunc(x), fy = to_f32_trunc(y), fz = to_f32_trunc(z);
+// Walk from the jump-table row of q's cube-map cell across the first edge
+// that q lies outside of until q is inside all three (a handful of steps:
+// the cells are smaller than the triangles).  Returns the row, with the
+// three FP32 edge values of the final row in d, or -1 after kWalkMax steps.
+__device__ __forceinline__ int walk_locate(const MeshView& m, double x, double y, double z, float fx, float fy,
+                                           float fz, float* d) {
   int t = __ldg(m.jump + jump_cell(m.jump_res, fx, fy, fz));
   for (int it = 0; it < kWalkMax; ++it) {
     const float4* r = reinterpret_cast<const float4*>(m.walk_f + (int64_t)t * kWalkStride);
     const float4 e0 = __ldg(r), e1 = __ldg(r + 1), e2 = __ldg(r + 2);
-    int nb;
-    if (edge_out(m, t, 0, e0, fx, fy, fz, x, y, z))
-      nb = __float_as_int(e0.w);
-    else if (edge_out(m, t, 1, e1, fx, fy, fz, x, y, z))
-      nb = __float_as_int(e1.w);
-    else if (edge_out(m, t, 2, e2, fx, fy, fz, x, y, z))
-      nb = __float_as_int(e2.w);
+    d[0] = edge_dot(e0, fx, fy, fz);
+    d[1] = edge_dot(e1, fx, fy, fz);
+    d[2] = edge_dot(e2, fx, fy, fz);
+    if (edge_out(m, t, 0, d[0], x, y, z))
+      t = __float_as_int(e0.w);
+    else if (edge_out(m, t, 1, d[1], x, y, z))
+      t = __float_as_int(e1.w);
+    else if (edge_out(m, t, 2, d[2], x, y, z))
+      t = __float_as_int(e2.w);
     else
       return t;
-    t = nb;
   }
-  return locate_descent(m, x, y, z);
+  return -1;
+}
+
+// Reference row of the icosahedral triangle containing q.  With the jump
+// table built: the walk, falling back to the hierarchy descent if it has
+// not ended after kWalkMax steps.  Both are exact containment tests, so
+// they agree except for queries within rounding distance of an edge,
+// where either neighbour contains the query.
+__device__ __forceinline__ int locate_row(const MeshView& m, double x, double y, double z) {
+  if (!m.jump) return locate_descent(m, x, y, z);
+  float d[3];
+  const int t = walk_locate(m, x, y, z, to_f32_trunc(x), to_f32_trunc(y), to_f32_trunc(z), d);
+  return t >= 0 ? t : locate_descent(m, x, y, z);
 }
 
 struct Bcc {
@@ -222,6 +233,44 @@ __device__ __forceinline__ Split split_of(const Bcc& b) {
   if (lo == hi) { lo = 1; hi = 0; }
   return Split{lo, 3 - lo - hi, hi};
 }
+
+// Row containing q and its Powell-Sabin sub-triangle.  The barycentrics
+// come in FP32 from the walk's final edge values (b_i = s_i d), and their
+// order decides the sub-triangle when every pair is farther apart than
+// the sum of their FP32 error bounds (s_i kFilter); otherwise -- and when
+// the walk fell back to the descent -- the FP64 barycentrics R q decide,
+// with split_of's rule.  Either way the choice is split_of(R q)'s.
+__device__ __forceinline__ int locate_split(const MeshView& m, double x, double y, double z, Split* sp) {
+  int t = -1;
+  if (m.jump) {
+    float d[3];
+    t = walk_locate(m, x, y, z, to_f32_trunc(x), to_f32_trunc(y), to_f32_trunc(z), d);
+    if (t >= 0) {
+      const float4 sc = __ldg(reinterpret_cast<const float4*>(m.walk_f + (int64_t)t * kWalkStride) + 3);
+      const float b0 = sc.x * d[1], b1 = sc.y * d[2], b2 = sc.z * d[0];
+      const float e0 = sc.x * kFilter, e1 = sc.y * kFilter, e2 = sc.z * kFilter;
+      if (fabsf(b0 - b1) > e0 + e1 && fabsf(b1 - b2) > e1 + e2 && fabsf(b0 - b2) > e0 + e2) {
+        const int lo = b0 < b1 ? (b0 < b2 ? 0 : 2) : (b1 < b2 ? 1 : 2);
+        const int hi = b0 > b1 ? (b0 > b2 ? 0 : 2) : (b1 > b2 ? 1 : 2);
+        *sp = Split{lo, 3 - lo - hi, hi};
+        return t;
+      }
+    }
+  }
+  if (t < 0) t = locate_descent(m, x, y, z);
+  const double* L = m.tri_loc + (int64_t)t * kLocStride;
+  double R[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) R[k] = __ldg(L + k);
+  *sp = split_of(bcc_of(R, x, y, z));
+  return t;
+}
+
+// Index of a sub-triangle (lo, hi), lo != hi, in a map-form record, and
+// the inverse tables.
+__constant__ const int kSubIndex[3][3] = {{0, 0, 1}, {2, 0, 3}, {4, 5, 0}};
+__constant__ const int kSubLo[6] = {0, 0, 1, 1, 2, 2};
+__constant__ const int kSubHi[6] = {1, 2, 0, 2, 0, 1};
 
 __device__ __forceinline__ double pick(const Bcc& b, int i) {
   return i == 0 ? b.b0 : (i == 1 ? b.b1 : b.b2);

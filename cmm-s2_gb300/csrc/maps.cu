@@ -24,6 +24,7 @@
 #include <algorithm>
 
 #include "cmm_internal.h"
+#include "dd.cuh"
 #include "device_common.cuh"
 #include "ff.cuh"
 
@@ -35,27 +36,34 @@ namespace {
 
 constexpr int kBlock = 256;
 // default register budgets of the compositions, as resident 256-thread
-// blocks per SM (measured at level 7, 2^24 queries, 8 submaps: Jacobians
-// 19.0 / 19.2 / 19.6 ms at 2 / 4 / 3 blocks in cell order; points only
-// 15.5 ms at 4 blocks against 19.6 ms at 6 in caller order, equal in cell
-// order)
-constexpr int kComposeJacBlocks = 2;
+// blocks per SM (measured at level 7, 2^24 queries, 8 submaps, map forms,
+// cell order: Jacobians 12.8 / 13.6 / 13.2 ms at 4 / 3 / 2 blocks; points
+// only 7.5 ms at 4 or 6 blocks, and 10.2 against 13.5 ms in caller order)
+constexpr int kComposeJacBlocks = 4;
 constexpr int kComposeBlocks = 4;
 
 // Submap lists: by value in the kernel parameters (host calls), or a
 // device table whose length comes from a device-driven step's state.
+// Each submap has its coefficient record and, optionally, its map-form
+// record (form(s) != NULL: evaluated as quadratic forms).
 struct SubmapPtrs {
   const double* p[CMM_MAX_SUBMAPS];
+  const double* f[CMM_MAX_SUBMAPS];
   int S;
   __device__ __forceinline__ int count() const { return S; }
   __device__ __forceinline__ const double* at(int s, int) const { return p[s]; }
+  __device__ __forceinline__ const double* form(int s, int) const { return f[s]; }
 };
 struct DevSubmaps {
   const double* const* tab;
+  const double* const* ftab;   // forms of the stack slots, or NULL
   const BveState* st;
   const double* last;
   __device__ __forceinline__ int count() const { return st->nc + 1; }
   __device__ __forceinline__ const double* at(int s, int S) const { return s < S - 1 ? tab[s] : last; }
+  __device__ __forceinline__ const double* form(int s, int S) const {
+    return ftab && s < S - 1 ? ftab[s] : nullptr;
+  }
 };
 
 // Orthonormal tangent basis (t1, t2) at the unit point p, in float-float
@@ -250,6 +258,79 @@ __global__ void __launch_bounds__(kAsmTri) assemble_f32_kernel(MeshView m, const
   for (int i = tl; i < nblk * kStride; i += kAsmTri) dst[i] = rec[(i / kStride) * kRow + i % kStride];
 }
 
+// Map forms: one thread per (triangle, sub-triangle).  The sub-triangle
+// barycentrics are gamma = T p with rows T_V = R_hi - R_mid,
+// T_E = |v_hi + v_mid| (R_mid - R_lo), T_C = |v1 + v2 + v3| R_lo (R the
+// inverse vertex rows of the location record), so the patch
+// P_c = gamma^T M_c gamma (M_c the symmetric matrix of the sub-triangle's
+// six ordinates) is the homogeneous quadratic form p^T Q_c p with
+// Q_c = T^T M_c T.  Q is O(1) while T is O(1/h), so its entries cancel
+// terms ~1/h^2 times larger: T, M_c T and Q_c are formed in double-double
+// and rounded once.  The result is the exact quadratic form of the patch
+// the record's rows R define, and p^T Q p then evaluates in FP64 without
+// cancellation (~2e-16 against the Bernstein sum's ~1e-14 from R p).
+__device__ __forceinline__ void assemble_form(const MeshView& m, const double* __restrict__ coeffs,
+                                              double* __restrict__ forms, int64_t idx) {
+  const int t = (int)(idx / 6), sub = (int)(idx % 6);
+  const int lo = kSubLo[sub], hi = kSubHi[sub], mid = 3 - lo - hi;
+  const double* L = m.tri_loc + (int64_t)t * kLocStride;
+  const double ne = edge_norm(L, hi, mid), n4 = __ldg(L + 9);
+  dd T[3][3];   // rows V, E, C
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    const double rh = __ldg(L + 3 * hi + j), rm = __ldg(L + 3 * mid + j), rl = __ldg(L + 3 * lo + j);
+    T[0][j] = dd_two_sum(rh, -rm);
+    T[1][j] = dd_mul_d(dd_two_sum(rm, -rl), ne);
+    T[2][j] = dd_two_prod(n4, rl);
+  }
+  const int* id = kSplitOrd[lo][hi];   // V^2, E^2, C^2, VE, EC, VC
+  const double* rec = coeffs + (int64_t)t * kCoeffStride3;
+  double* out = forms + (int64_t)t * kFormStride + 18 * sub;
+#pragma unroll 1
+  for (int c = 0; c < 3; ++c) {
+    double o[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) o[k] = __ldg(rec + 3 * id[k] + c);
+    const double M[3][3] = {{o[0], o[3], o[5]}, {o[3], o[1], o[4]}, {o[5], o[4], o[2]}};
+    dd U[3][3];   // U = M T
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+        U[a][j] = dd_add(dd_add(dd_mul_d(T[0][j], M[a][0]), dd_mul_d(T[1][j], M[a][1])), dd_mul_d(T[2][j], M[a][2]));
+    const int pi[6] = {0, 1, 2, 0, 0, 1}, pj[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+    for (int e = 0; e < 6; ++e) {
+      const int i = pi[e], j = pj[e];
+      dd q = dd_add(dd_add(dd_mul(T[0][i], U[0][j]), dd_mul(T[1][i], U[1][j])), dd_mul(T[2][i], U[2][j]));
+      if (i != j)   // the symmetric pair, 2 Q_ij
+        q = dd_add(q, dd_add(dd_add(dd_mul(T[0][j], U[0][i]), dd_mul(T[1][j], U[1][i])), dd_mul(T[2][j], U[2][i])));
+      out[6 * c + e] = dd_round(q);
+    }
+  }
+  if (sub == 0)
+    for (int k = 108; k < kFormStride; ++k) forms[(int64_t)t * kFormStride + k] = 0.0;
+}
+
+__global__ void __launch_bounds__(128) assemble_forms_kernel(MeshView m, const double* __restrict__ coeffs,
+                                                             double* __restrict__ forms) {
+  const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (idx < 6LL * m.nt) assemble_form(m, coeffs, forms, idx);
+}
+
+// The device-driven step's remap: the forms of the stack slot the current
+// map has just been copied to (st->count + 1 in the remap schedule), a
+// no-op on the other steps.
+__global__ void __launch_bounds__(128) remap_forms_kernel(MeshView m, const BveState* __restrict__ st, int n_maps,
+                                                          int Nt, const double* const* __restrict__ table,
+                                                          double* const* __restrict__ ftable) {
+  const int c = st->count + 1;
+  const int slot = c == Nt ? (Nt - 1) / n_maps : (c < Nt && c % n_maps == 0 ? c / n_maps - 1 : -1);
+  if (slot < 0) return;
+  const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (idx < 6LL * m.nt) assemble_form(m, table[slot], ftable[slot], idx);
+}
+
 __global__ void to_f32_kernel(const double* __restrict__ a, int64_t n, float* __restrict__ b) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i < n) b[i] = (float)a[i];
@@ -307,6 +388,45 @@ __global__ void __launch_bounds__(kBlock, MINB) compose_kernel(MeshView m, Src c
       }
     }
     for (int s = S - 1; s >= 0; --s) {
+      double P[3];
+      const double* fr = cp.form(s, S);
+      if (fr) {
+        // map-form record: P_c = p^T Q_c p of the sub-triangle's quadratic
+        // form (24 FP64 operations for the three components); the half
+        // derivative along w is (Q_c p) . w, formed in float-float
+        Split sp;
+        const int t = locate_split(m, p[0], p[1], p[2], &sp);
+        if (s == S - 1 && tri) tri[i] = t;
+        if (tri_all) tri_all[(int64_t)s * n + i] = t;
+        const double2* qf =
+            reinterpret_cast<const double2*>(fr + (int64_t)t * kFormStride + 18 * kSubIndex[sp.lo][sp.hi]);
+        const double xx = p[0] * p[0], yy = p[1] * p[1], zz = p[2] * p[2];
+        const double xy = p[0] * p[1], xz = p[0] * p[2], yz = p[1] * p[2];
+        if (JAC) {
+          const ff u0 = ff_of(p[0]), u1 = ff_of(p[1]), u2 = ff_of(p[2]);
+          const ff a0 = w.get(0), a1 = w.get(1), a2 = w.get(2), c0 = w.get(3), c1 = w.get(4), c2 = w.get(5);
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            const double2 q01 = __ldg(qf + 3 * c), q23 = __ldg(qf + 3 * c + 1), q45 = __ldg(qf + 3 * c + 2);
+            P[c] = q01.x * xx + q01.y * yy + q23.x * zz + q23.y * xy + q45.x * xz + q45.y * yz;
+            const ff Q00 = ff_of(q01.x), Q11 = ff_of(q01.y), Q22 = ff_of(q23.x);
+            const ff h01 = ff_of(q23.y), h02 = ff_of(q45.x), h12 = ff_of(q45.y);
+            const ff Q01{0.5f * h01.h, 0.5f * h01.l}, Q02{0.5f * h02.h, 0.5f * h02.l}, Q12{0.5f * h12.h, 0.5f * h12.l};
+            const ff g0 = ff_dot3(Q00, u0, Q01, u1, Q02, u2);
+            const ff g1 = ff_dot3(Q01, u0, Q11, u1, Q12, u2);
+            const ff g2 = ff_dot3(Q02, u0, Q12, u1, Q22, u2);
+            w.set(c, ff_dot3(g0, a0, g1, a1, g2, a2));
+            w.set(3 + c, ff_dot3(g0, c0, g1, c1, g2, c2));
+          }
+          ++since;
+        } else {
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            const double2 q01 = __ldg(qf + 3 * c), q23 = __ldg(qf + 3 * c + 1), q45 = __ldg(qf + 3 * c + 2);
+            P[c] = q01.x * xx + q01.y * yy + q23.x * zz + q23.y * xy + q45.x * xz + q45.y * yz;
+          }
+        }
+      } else {
       const int t = locate_row(m, p[0], p[1], p[2]);
       if (s == S - 1 && tri) tri[i] = t;
       if (tri_all) tri_all[(int64_t)s * n + i] = t;
@@ -316,7 +436,6 @@ __global__ void __launch_bounds__(kBlock, MINB) compose_kernel(MeshView m, Src c
       const Split sp = split_of(b);
       const Gam g = gamma_of(Lr, b, sp);
       const double* rec = cp.at(s, S) + (int64_t)t * kCoeffStride3;
-      double P[3];
       if (JAC) {
         // The patch is the quadratic form P_c = gamma^T M_c gamma of the
         // symmetric ordinate matrix M_c; its half gradient M_c gamma (FP64)
@@ -367,6 +486,7 @@ __global__ void __launch_bounds__(kBlock, MINB) compose_kernel(MeshView m, Src c
         Ords<3> o;
         load_ords<3>(rec, sp, o);
         sbb<3>(o, g, P);
+      }
       }
       // Location, barycentrics and sub-triangle choice are invariant under
       // p -> lambda p (lambda > 0) and the patch is homogeneous of degree 2,
@@ -624,11 +744,14 @@ int launch_assemble(const MeshView& m, const double* jets, int ncomp, double* co
 
 int launch_compose(const MeshView& m, const double* const* coeffs, int S, const double* q,
                    int64_t n, double* out, int32_t* tri, int32_t* tri_all, double* jac,
-                   cudaStream_t s, const int32_t* perm) {
+                   cudaStream_t s, const int32_t* perm, const double* const* forms) {
   if (n == 0) return CMM_OK;
   SubmapPtrs cp;
   cp.S = S;
-  for (int k = 0; k < S; ++k) cp.p[k] = coeffs[k];
+  for (int k = 0; k < S; ++k) {
+    cp.p[k] = coeffs[k];
+    cp.f[k] = forms ? forms[k] : nullptr;
+  }
   const int b = block_for(m, kTuneCompose, kBlock, n);
   const int g = grid_for(n, b);
   if (jac) {
@@ -645,6 +768,19 @@ int launch_compose(const MeshView& m, const double* const* coeffs, int S, const 
     compose_kernel<false, SubmapPtrs, 6><<<g, b, 0, s>>>(m, cp, q, n, out, tri, tri_all, jac, perm);
   }
   return check_launch("compose_kernel");
+}
+
+int launch_assemble_forms(const MeshView& m, const double* coeffs, double* forms, cudaStream_t s) {
+  const int64_t n = 6LL * m.nt;
+  assemble_forms_kernel<<<(int)((n + 127) / 128), 128, 0, s>>>(m, coeffs, forms);
+  return check_launch("assemble_forms_kernel");
+}
+
+int launch_remap_forms(const MeshView& m, const BveState* st, int n_maps, int Nt, const double* const* table,
+                       double* const* ftable, cudaStream_t s) {
+  const int64_t n = 6LL * m.nt;
+  remap_forms_kernel<<<(int)((n + 127) / 128), 128, 0, s>>>(m, st, n_maps, Nt, table, ftable);
+  return check_launch("remap_forms_kernel");
 }
 
 int make_asm_f32(cmm_mesh* mesh) {
@@ -704,9 +840,10 @@ int launch_query_order(const MeshView& m, const double* q, int64_t n, int32_t* p
 }
 
 int launch_compose_dev(const MeshView& m, const double* const* table, const BveState* st,
-                       const double* last, const double* q, int64_t n, double* out, cudaStream_t s) {
+                       const double* last, const double* q, int64_t n, double* out, cudaStream_t s,
+                       const double* const* ftable) {
   if (n == 0) return CMM_OK;
-  DevSubmaps cp{table, st, last};
+  DevSubmaps cp{table, ftable, st, last};
   const int b = block_for(m, kTuneCompose, kBlock, n);
   if ((m.variant[CMM_VARIANT_COMPOSE] ? m.variant[CMM_VARIANT_COMPOSE] : kComposeBlocks) == 4)
     compose_kernel<false, DevSubmaps, 4><<<grid_for(n, b), b, 0, s>>>(m, cp, q, n, out, nullptr, nullptr,

@@ -302,7 +302,14 @@ int build_host(const double* verts, int nv, const int32_t* tris, int nt, int lev
       }
     for (int t = 0; t < nt; ++t) {
       const int a[3] = {tris[3 * t], tris[3 * t + 1], tris[3 * t + 2]};
-      const double sgn = det_cols(vtx(verts, a[0]), vtx(verts, a[1]), vtx(verts, a[2])) < 0 ? -1.0 : 1.0;
+      const double det = det_cols(vtx(verts, a[0]), vtx(verts, a[1]), vtx(verts, a[2]));
+      const double sgn = det < 0 ? -1.0 : 1.0;
+      // barycentric b_i = R_i . q = s_i (n . q) with n the inward unit
+      // normal of the edge opposite vertex i (edge (i+1, i+2)) and
+      // s_i = |v_{i+1} x v_{i+2}| / |det| > 0, stored in floats 12..14
+      for (int i = 0; i < 3; ++i)
+        walk_f[(size_t)t * kWalkStride + 12 + i] =
+            (float)(norm(cross(vtx(verts, a[(i + 1) % 3]), vtx(verts, a[(i + 2) % 3]))) / std::fabs(det));
       for (int e = 0; e < 3; ++e) {
         const int u = a[e], w = a[(e + 1) % 3];
         // the same plane seen from the row across the edge has exactly the

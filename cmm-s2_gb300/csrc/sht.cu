@@ -983,6 +983,7 @@ struct cmm_sht {
   int tab_mode = 0;                 // cmm_sht_set_tables: 0 auto, 1 always, -1 never
   cmm::DeviceBuffer spec, torus, pad, alm, fields, synth, samples, status;
   cmm::TcPlan* tc = nullptr;
+  int tc_schedule = 1;   // split-BF16 synthesis schedule (cmm_sht_set_schedule)
   // split-BF16 form: FP32 ring FFTs and buffers, made with the tc plan
   cufftHandle f_ring_fwd = 0, f_torus_fwd = 0, f_pad_inv = 0, f_ring_inv = 0;
   bool have_fplans[4] = {false, false, false, false};
@@ -1485,6 +1486,16 @@ int sht_scalar_jets(cmm_sht* p, const cmm_mesh* vm, const double2* alm, double* 
   return check_launch("scalar_jets_kernel");
 }
 
+int sht_set_schedule(cmm_sht* p, int schedule) {
+  if (schedule != 0 && schedule != 1) {
+    set_last_error("cmm_sht_set_schedule: schedule 0 or 1 expected");
+    return CMM_ERR_ARG;
+  }
+  p->tc_schedule = schedule;
+  if (p->tc) tc_set_schedule(p->tc, schedule);
+  return CMM_OK;
+}
+
 int sht_set_precision(cmm_sht* p, int mode) {
   if (mode != CMM_SHT_FP64 && mode != CMM_SHT_SPLIT_BF16) {
     set_last_error("cmm_sht_set_precision: unknown mode");
@@ -1495,6 +1506,7 @@ int sht_set_precision(cmm_sht* p, int mode) {
                             (const double*)p->ct_fine.p, (const double*)p->pmm_fine.p,
                             (const double*)p->ra.p, (const double*)p->rb.p, &p->tc);
     if (rc) return rc;
+    tc_set_schedule(p->tc, p->tc_schedule);
     if (!p->have_fplans[0] && (rc = make_float_plans(p))) return rc;
     cudaError_t e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return cuda_fail(e, "cmm_sht_set_precision");
@@ -1551,6 +1563,7 @@ int sht_share_tables(cmm_sht* p, cmm_sht* src) {
     p->tc = nullptr;
   }
   int rc = tc_plan_share(src->tc, &p->tc);
+  if (!rc) tc_set_schedule(p->tc, p->tc_schedule);
   if (rc) return rc;
   if (!p->have_fplans[0] && (rc = make_float_plans(p))) return rc;
   p->precision = CMM_SHT_SPLIT_BF16;

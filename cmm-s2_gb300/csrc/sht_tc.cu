@@ -448,6 +448,170 @@ __global__ void __launch_bounds__(kThreads, 1) synth_tc_kernel(TcGeometry g, int
                  : "memory");
 }
 
+// ------------------------------------------ synthesis, warp-specialised
+// The same contraction with the work item's chunks accumulated in tensor
+// memory (FP32) and drained once per item, by three roles that run
+// concurrently: warp 4 streams the chunks' tiles into a two-stage ring of
+// shared memory (bulk copies), warp 5 issues each chunk's MMAs into the
+// item's accumulator pair as soon as its tiles have landed, and warps 0-3
+// (whose lanes are the 128 TMEM lanes, one ring pair each) drain an
+// item's accumulators and write its spectra while the next item's chunks
+// are multiplied into the other pair.  Stage and accumulator hand-offs go
+// through mbarriers (copies complete `full`, MMA commits complete `empty`
+// and `acc_full`, the four drain warps complete `acc_empty`); every wait
+// is bounded and a timeout in any role stops all three.
+constexpr int kSynWarps2 = 6;
+constexpr int kSynStages2 = 2;
+
+__device__ __forceinline__ bool wait_or_abort(uint64_t* bar, uint32_t parity, volatile int* abort) {
+  for (long long i = 0; i < kSpinLimit; ++i) {
+    if (mbar_test(bar, parity)) return true;
+    if ((i & 255) == 255 && *abort) return false;
+  }
+  *abort = 1;
+  return false;
+}
+
+__device__ __forceinline__ void syn_mma_acc(uint32_t stage, uint32_t d, uint32_t idesc, bool first) {
+  const uint32_t p0 = stage, a0 = stage + kPRecord;
+  for (int ks = 0; ks < kKc / 16; ++ks)
+    for (int par = 0; par < 2; ++par) {
+      const uint64_t ph = smem_desc(p0 + (2 * par) * kPTile + ks * 256);
+      const uint64_t pl = smem_desc(p0 + (2 * par + 1) * kPTile + ks * 256);
+      const uint64_t ah = smem_desc(a0 + (2 * par) * kATile + ks * 256);
+      const uint64_t al = smem_desc(a0 + (2 * par + 1) * kATile + ks * 256);
+      const uint32_t dd = d + par * kN;
+      mma_bf16(dd, ph, ah, idesc, (first && ks == 0) ? 0u : 1u);
+      mma_bf16(dd, ph, al, idesc, 1u);
+      mma_bf16(dd, pl, ah, idesc, 1u);
+    }
+}
+
+__global__ void __launch_bounds__(32 * kSynWarps2, 1) synth_tc2_kernel(TcGeometry g, int nitems,
+                                                                       const unsigned char* __restrict__ ptab,
+                                                                       const unsigned char* __restrict__ atab,
+                                                                       float2* __restrict__ S,
+                                                                       int* __restrict__ status) {
+  extern __shared__ __align__(1024) unsigned char smem[];   // kSynStages2 stages of kSynStage bytes
+  __shared__ __align__(8) uint64_t full[kSynStages2], empty[kSynStages2], acc_full[2], acc_empty[2];
+  __shared__ uint32_t tmem_base_s;
+  __shared__ volatile int abort_s;
+  __shared__ int drain_fail_s;
+  const int L = g.L;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (tid == 0) {
+    for (int b = 0; b < kSynStages2; ++b) {
+      mbar_init(&full[b], 1);
+      mbar_init(&empty[b], 1);
+    }
+    for (int a = 0; a < 2; ++a) {
+      mbar_init(&acc_full[a], 1);
+      mbar_init(&acc_empty[a], 4);
+    }
+    abort_s = 0;
+    drain_fail_s = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&tmem_base_s)),
+                 "r"(kTmemColsS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_base_s;
+  if (warp == 4 && lane == 0) {
+    // producer: the tiles of every chunk of this CTA's items, in order
+    long long j = 0;
+    SynCursor u;
+    bool ok = syn_set(u, blockIdx.x, nitems, g);
+    while (ok && !abort_s) {
+      const int st = (int)(j % kSynStages2);
+      if (j >= kSynStages2 && !wait_or_abort(&empty[st], (uint32_t)((j / kSynStages2 - 1) & 1), &abort_s)) break;
+      syn_load(g, ptab, atab, u, smem + st * kSynStage, &full[st]);
+      ++j;
+      ok = syn_next(u, nitems, g);
+    }
+    // copies still in flight land before the block exits: the stages'
+    // last uses complete `full` (bounded)
+    if (abort_s) {
+      bool drained = true;
+      for (long long k = (j > kSynStages2 ? j - kSynStages2 : 0); k < j; ++k)
+        drained &= mbar_wait(&full[k % kSynStages2], (uint32_t)((k / kSynStages2) & 1));
+      if (!drained) drain_fail_s = 1;
+    }
+  } else if (warp == 5 && lane == 0) {
+    // MMA issuer: each item's chunks into accumulator pair it & 1
+    const uint32_t idesc = mma_idesc();
+    const uint32_t s0 = smem_u32(smem);
+    long long j = 0, it = 0;
+    bool committed = false;
+    for (int item = blockIdx.x; item < nitems && !abort_s; item += gridDim.x, ++it) {
+      const int a = (int)(it & 1);
+      if (it >= 2 && !wait_or_abort(&acc_empty[a], (uint32_t)((it / 2 - 1) & 1), &abort_s)) break;
+      const int nch = nchunks(L, item / g.nrb);
+      bool ok = true;
+      for (int c = 0; c < nch; ++c, ++j) {
+        const int st = (int)(j % kSynStages2);
+        if (!wait_or_abort(&full[st], (uint32_t)((j / kSynStages2) & 1), &abort_s)) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        syn_mma_acc(s0 + st * kSynStage, tmem + a * 2 * kN, idesc, c == 0);
+        mma_commit(&empty[st]);
+        committed = true;
+      }
+      if (!ok) break;
+      mma_commit(&acc_full[a]);
+    }
+    // products still in flight complete before the tensor memory is
+    // released: the last commit's barrier (bounded)
+    if (abort_s && committed) {
+      const long long jl = j - 1;
+      if (!mbar_wait(&empty[jl % kSynStages2], (uint32_t)((jl / kSynStages2) & 1))) drain_fail_s = 1;
+    }
+  } else if (warp < 4) {
+    // drain: accumulators -> spectra of the item's ring pairs (TMEM lane =
+    // thread index = ring row of the block)
+    long long it = 0;
+    for (int item = blockIdx.x; item < nitems; item += gridDim.x, ++it) {
+      const int a = (int)(it & 1);
+      if (!wait_or_abort(&acc_full[a], (uint32_t)((it / 2) & 1), &abort_s)) break;
+      tc_fence_after();
+      float vE[32], vO[32];
+      const uint32_t lanes = (uint32_t)(32 * warp) << 16;
+      const uint32_t buf = tmem + (uint32_t)a * 2 * kN;
+      tmem_ld32(buf + lanes, vE);
+      tmem_ld32(buf + lanes + kN, vO);
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&acc_empty[a])) : "memory");
+      const int m = item / g.nrb, blk = item % g.nrb;
+      const int t = blk * kM + tid;
+      if (t < g.npair) {
+        const int64_t row_len = L + 1;
+#pragma unroll
+        for (int f = 0; f < kNUsed / 2; ++f) {
+          const int64_t base = (int64_t)f * (L + 1) * row_len;
+          const float eR = vE[2 * f], eI = vE[2 * f + 1], oR = vO[2 * f], oI = vO[2 * f + 1];
+          S[base + (int64_t)t * row_len + m] = make_float2(eR + oR, eI + oI);
+          if (L - t != t) S[base + (int64_t)(L - t) * row_len + m] = make_float2(eR - oR, eI - oI);
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (tid == 0 && abort_s) atomicOr(status, drain_fail_s ? CMM_FLAG_TIMEOUT | CMM_FLAG_DRAIN_TIMEOUT : CMM_FLAG_TIMEOUT);
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemColsS)
+                 : "memory");
+}
+
 // -------------------------------------------------------------- analysis
 // f_lm = sum_j Pbar_lm(theta'_j) X_par(l)[j] over the L+1 ring pairs j of
 // the 2L+1 fine rings, X_even = w_j (F_j + F_{2L-j}), X_odd = w_j (F_j -
@@ -674,6 +838,7 @@ struct TcTables {
 struct TcPlan {
   int L = 0, npair = 0, nrb = 0, total_chunks = 0;
   int sms = 0;   // CTAs of the persistent synthesis (one per SM)
+  int schedule = 1;   // synthesis: 1 warp-specialised (synth_tc2_kernel), 0 per-chunk drain
   // analysis: degree blocks of 128 per m (prefix sums), ring-pair chunks
   int nck = 0, total_lblocks = 0;
   std::shared_ptr<TcTables> tab;
@@ -717,6 +882,9 @@ int tc_plan_create(int L, const double* ct_rings, const double* pmm_rings, const
   }
   cudaError_t e = cudaFuncSetAttribute(synth_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        2 * kSynStage);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(synth_tc2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             kSynStages2 * kSynStage);
   int dev = 0;
   if (e == cudaSuccess) e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, dev);
@@ -812,13 +980,21 @@ int tc_wait_timeout_probe(long long polls, int* status, cudaStream_t s) {
   return check("wait_timeout_probe_kernel");
 }
 
+void tc_set_schedule(TcPlan* p, int schedule) { p->schedule = schedule; }
+
 int tc_synthesis(TcPlan* p, const double2* fields, float2* S, int* status, cudaStream_t s) {
   TcGeometry g{p->L, p->npair, p->nrb, (const int*)p->tab->cbase.p};
   build_atab_kernel<<<dim3(16, p->L), 256, 0, s>>>(g, fields, (unsigned char*)p->atab.p);
   int rc = check("build_atab_kernel");
   if (rc) return rc;
   const int nitems = p->L * p->nrb;
-  synth_tc_kernel<<<std::min(nitems, std::max(p->sms, 1)), kThreads, 2 * kSynStage, s>>>(
+  const int grid = std::min(nitems, std::max(p->sms, 1));
+  if (p->schedule == 1) {
+    synth_tc2_kernel<<<grid, 32 * kSynWarps2, kSynStages2 * kSynStage, s>>>(
+        g, nitems, (const unsigned char*)p->tab->ptab.p, (const unsigned char*)p->atab.p, S, status);
+    return check("synth_tc2_kernel");
+  }
+  synth_tc_kernel<<<grid, kThreads, 2 * kSynStage, s>>>(
       g, nitems, (const unsigned char*)p->tab->ptab.p, (const unsigned char*)p->atab.p, S, status);
   return check("synth_tc_kernel");
 }

@@ -108,7 +108,7 @@ int check(const char* what) {
 
 struct cmm_bve {
   cmm_bve_desc d;
-  cmm::DeviceBuffer state, table, jtable;
+  cmm::DeviceBuffer state, table, jtable, ftable;
   int64_t nrec = 0, njets = 0, nsample = 0;
 };
 
@@ -131,7 +131,7 @@ int bve_create(const cmm_bve_desc* d, cmm_bve** out) {
     return CMM_ERR_ARG;
   }
   for (int k = 0; k < d->n_stack; ++k)
-    if (!d->stack[k]) {
+    if (!d->stack[k] || (d->stack_forms && !d->stack_forms[k])) {
       set_last_error("cmm_bve_create: null stack slot");
       return CMM_ERR_ARG;
     }
@@ -143,6 +143,7 @@ int bve_create(const cmm_bve_desc* d, cmm_bve** out) {
   b->d = *d;
   b->d.stack = nullptr;
   b->d.stack_jets = nullptr;
+  b->d.stack_forms = nullptr;
   const int L = d->velmesh->view.L;
   b->nrec = (int64_t)d->mesh->view.nt * kCoeffStride3;
   b->njets = 12LL * d->mesh->view.nv;
@@ -158,7 +159,8 @@ int bve_create(const cmm_bve_desc* d, cmm_bve** out) {
   int rc;
   if ((rc = b->state.upload(&h, sizeof(h))) ||
       (rc = b->table.upload(d->stack, sizeof(double*) * d->n_stack)) ||
-      (d->stack_jets && (rc = b->jtable.upload(d->stack_jets, sizeof(double*) * d->n_stack)))) {
+      (d->stack_jets && (rc = b->jtable.upload(d->stack_jets, sizeof(double*) * d->n_stack))) ||
+      (d->stack_forms && (rc = b->ftable.upload(d->stack_forms, sizeof(double*) * d->n_stack)))) {
     delete b;
     return rc;
   }
@@ -197,7 +199,7 @@ int bve_step(cmm_bve* b, cudaStream_t s) {
   if ((rc = launch_assemble(mesh, d.jets, 3, d.coeffs_cur, s))) return rc;
   // sample points through stack and current map, vorticity, velocity
   if ((rc = launch_compose_dev(mesh, (const double* const*)b->table.p, st, d.coeffs_cur, d.sample_pts,
-                               b->nsample, d.X, s)))
+                               b->nsample, d.X, s, (const double* const*)b->ftable.p)))
     return rc;
   if ((rc = launch_vorticity(d.vort_kind, d.vort_params, d.nparams, d.sh, d.lmax, vm, d.spline,
                              d.rot_rate, d.X, b->nsample, 2 * vm.L,
@@ -211,6 +213,10 @@ int bve_step(cmm_bve* b, cudaStream_t s) {
                                                        (double* const*)b->table.p, b->nrec, d.jets,
                                                        (double* const*)b->jtable.p, d.id_jets, b->njets);
   if ((rc = check("bve_remap_kernel"))) return rc;
+  if (b->ftable.p &&
+      (rc = launch_remap_forms(mesh, st, d.n_maps, d.Nt, (const double* const*)b->table.p,
+                               (double* const*)b->ftable.p, s)))
+    return rc;
   bve_advance_kernel<<<1, 32, 0, s>>>((BveState*)b->state.p, d.n_maps, d.Nt);
   return check("bve_advance_kernel");
 }

@@ -180,6 +180,29 @@ int cmm_compose_ordered(const cmm_mesh* mesh, const double* const* coeffs, int S
                         int64_t n, const int32_t* perm, double* out, int32_t* tri,
                         int32_t* tri_all, double* jac, void* stream);
 
+/* Map forms: the same Powell-Sabin patches as a coefficient record,
+ * re-expressed per sub-triangle and component as the homogeneous quadratic
+ * form P(p) = p^T Q p in the ambient point (the sub-triangle barycentrics
+ * are linear in p, so each patch is exactly such a form; stored as Qxx,
+ * Qyy, Qzz, 2Qxy, 2Qxz, 2Qyz).  Q is assembled in double-double from the
+ * record's ordinates and the location record's inverse vertex rows, then
+ * rounded once; evaluating p^T Q p costs 24 FP64 operations against ~40
+ * for barycentrics plus the Bernstein sum, and with the Powell-Sabin
+ * sub-triangle chosen from FP32 barycentrics (FP64 when a pair is within
+ * the FP32 error bound) the composition needs no FP64 location at all.
+ * Same values to rounding (measured ~1e-16 per evaluation; the Bernstein
+ * sum carries ~1e-14 from the barycentric product).  No counterpart in the
+ * reference.  forms: (Nt, CMM_FORM_STRIDE) doubles. */
+#define CMM_FORM_STRIDE 112
+int cmm_assemble_forms(const cmm_mesh* mesh, const double* coeffs, double* forms, void* stream);
+/* cmm_compose / cmm_compose_ordered with map forms: forms is a HOST array
+ * of S device pointers to form records (an entry may be NULL: that submap
+ * is evaluated from its coefficient record) or NULL; perm may be NULL
+ * (caller order).  Outputs as cmm_compose's. */
+int cmm_compose_forms(const cmm_mesh* mesh, const double* const* coeffs, const double* const* forms, int S,
+                      const double* q, int64_t n, const int32_t* perm, double* out, int32_t* tri,
+                      int32_t* tri_all, double* jac, void* stream);
+
 /* Stencil evaluation: locate each vertex foot point yn[:,v] (3,nv), then
  * evaluate the 4 stencil foot points st (3,4,nv) in that same Powell-Sabin
  * sub-triangle, un-normalised -> out (3,4,nv).  Replaces
@@ -316,6 +339,14 @@ int cmm_sht_destroy(cmm_sht* plan);
 #define CMM_SHT_FP64 0
 #define CMM_SHT_SPLIT_BF16 1
 int cmm_sht_set_precision(cmm_sht* plan, int mode);
+/* Schedule of the split-BF16 synthesis kernel: 1 (default) warp-specialised
+ * -- a copy warp, an MMA warp and four drain warps run concurrently, each
+ * work item's 64-degree chunks accumulate in tensor memory (FP32) and are
+ * drained once; 0 -- one role per phase, every chunk drained into
+ * compensated FP32 register sums.  Both stay within the split form's
+ * stated error; results differ at FP32 rounding.  No counterpart in the
+ * reference. */
+int cmm_sht_set_schedule(cmm_sht* plan, int schedule);
 /* Share the Legendre tables of `src` (another plan of the same L) instead
  * of building them again; plans of one band-limit then share one copy and
  * still run concurrently (each keeps its own data tiles and FFT scratch).
@@ -409,7 +440,7 @@ int cmm_mesh_set_block(cmm_mesh* mesh, int kernel, int threads);
  * autotuner from measured timings; 0 restores the default).  The
  * composition kernels are compiled for several register budgets, named by
  * the resident 256-thread blocks per SM they allow: with Jacobians 2, 3 or
- * 4 (128, 80 or 64 registers a thread; default 2), points only 4 or 6 (64
+ * 4 (128, 80 or 64 registers a thread; default 4), points only 4 or 6 (64
  * or 40; default 4).  Fewer registers hide more gather latency, more avoid
  * spills.  Results do not depend on the variant.  No counterpart in the
  * reference. */
@@ -467,6 +498,11 @@ typedef struct {
   int k;                      /* tspan index of the next step's start */
   int count, nc, identity;
   double ts0;
+  /* map-form records of the stack slots (host array of n_stack device
+   * pointers to (Nt_map, CMM_FORM_STRIDE) records, copied at create), or
+   * NULL: each remap then also assembles the slot's forms and the
+   * composition evaluates the stack through them */
+  double* const* stack_forms;
 } cmm_bve_desc;
 /* Set-up call: uploads the state on the legacy default stream and
  * synchronises the device, so it must not be called while a stream of

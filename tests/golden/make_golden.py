@@ -164,7 +164,11 @@ def bve_config1(nq=2000):
     coefficients from seed 0 (cmm_gpu.workloads.random_sh_vorticity).  The
     restated MWSS transform stands in for pyssht.  Stored: the final
     composite map at nq seeded random points and the vorticity there
-    (omega0(X) + 2 Omega cos theta(X) - 2 Omega cos theta)."""
+    (omega0(X) + 2 Omega cos theta(X) - 2 Omega cos theta); and the same
+    from the oracle's run of the configuration with the closed-form
+    sub-triangle barycentrics (``img_closed``/``omega_closed``), whose
+    difference from the reference's run is the reference's own
+    finite-difference noise floor."""
     import time
     from cmm_gpu.workloads import random_sh_vorticity
     omega0, a = random_sh_vorticity(16, seed=0)
@@ -177,7 +181,18 @@ def bve_config1(nq=2000):
     phi, theta = rutils.cart2sphere(img.T)
     _, theta_q = rutils.cart2sphere(q.T)
     om = omega0(phi, theta) + 4 * np.pi * np.cos(theta) - 4 * np.pi * np.cos(theta_q)
-    save("bve_l4_L128.npz", q=q, img=img, omega=om, Nc=subs.Nc, ns=np.array(subs.ns), sh=a)
+    from oracle.bve import BVEOracle
+    from oracle import geometry as OG
+    tris = np.asarray(m.simplices)
+    t0 = time.time()
+    orc = BVEOracle(m.vertices, tris, OG.ConeLocator(m.vertices, tris), 128, 200, 1.0, omega0, n_maps=20,
+                    closed=True, tie_fix=True).run()
+    print(f"oracle closed-form run {time.time() - t0:.0f} s")
+    imgc = orc.composite()(q)
+    phc, thc = rutils.cart2sphere(imgc.T)
+    omc = omega0(phc, thc) + 4 * np.pi * np.cos(thc) - 4 * np.pi * np.cos(theta_q)
+    save("bve_l4_L128.npz", q=q, img=img, omega=om, img_closed=imgc, omega_closed=omc, Nc=subs.Nc,
+         ns=np.array(subs.ns), sh=a)
 
 
 def main():

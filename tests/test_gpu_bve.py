@@ -326,3 +326,39 @@ def test_reference_drivers(sims):
     assert s.Nc == 1
     q = dev(d["q"])
     assert torch.equal(one(q).T.contiguous(), s.composite(q)[0])
+
+
+def test_config1_whole_run_matches_reference(sims):
+    """The whole barotropic configuration (level 4, L = 128, 200 steps of
+    dt = 1/200, remap every 20: 10 submaps; random SH initial vorticity
+    l <= 16, seed 0) against the reference driver's own run of it and the
+    oracle's closed-form run (tests/golden/bve_l4_L128.npz).  Map points
+    within 1e-10 and vorticity within 1e-9 relative of the closed-form run;
+    within 5x the measured reference-vs-closed-form spread (the reference's
+    finite-difference noise floor) of the reference's run."""
+    from cmm_gpu.meshgen import icosahedral_mesh
+    d = np.load(os.path.join(GOLDEN, "bve_l4_L128.npz"))
+    if "img_closed" not in d:
+        pytest.skip("bve_l4_L128.npz without the closed-form run")
+    verts, _ = icosahedral_mesh(4)
+    tris = np.load(os.path.join(GOLDEN, "mesh_l4.npz"))["tris"]
+    s = sims.BVESolver(verts, tris, 4, 128, 200, 1.0, sims.Vorticity(sh=d["sh"]), n_maps=20).run()
+    assert s.Nc == int(d["Nc"]) and s.ns == list(d["ns"])
+    img = s.composite(dev(d["q"]))[0].cpu().numpy()
+    X = img.T
+    theta = np.arctan2(np.sqrt(X[0] ** 2 + X[1] ** 2), X[2])
+    phi = (np.arctan2(X[1], X[0]) + 2 * np.pi) % (2 * np.pi)
+    from oracle.fields import sh_series
+    _, theta_q = OG.cart2sphere(d["q"].T)
+    om = sh_series(d["sh"])(phi, theta) + 4 * np.pi * np.cos(theta) - 4 * np.pi * np.cos(theta_q)
+    spread = np.abs(d["img_closed"] - d["img"]).max()
+    e_closed = np.abs(img - d["img_closed"]).max()
+    e_ref = np.abs(img - d["img"]).max()
+    scale = np.abs(d["omega_closed"]).max()
+    e_om = np.abs(om - d["omega_closed"]).max() / scale
+    print(f"config 1: points vs closed-form run {e_closed:.2e}, vs reference run {e_ref:.2e} "
+          f"(reference's own spread {spread:.2e}); vorticity {e_om:.2e} relative")
+    assert e_closed < 1e-10
+    assert e_om < 1e-9
+    assert e_ref < 5 * spread + 1e-12
+    assert s.mesh.status() == 0 and s.vm.status() == 0

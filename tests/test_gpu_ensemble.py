@@ -17,13 +17,13 @@ def mods():
     return ensemble, spherical_simulations, autotune, workloads, meshgen
 
 
-def _alone(mods, spec, i, seed, Nt, T, lmax, rms, n_maps, precision="split_bf16"):
+def _alone(mods, spec, i, seed, Nt, T, lmax, rms, n_maps, precision="split_bf16", forms=True):
     ensemble, sims, _, workloads, meshgen = mods
     level, L = spec
     verts, tris = meshgen.icosahedral_mesh(level)
     pert = workloads.spectral_perturbation(lmax, seed=seed * 100003 + i, slope=-2.0, rms=rms)
     s = sims.BVESolver(verts, tris, level, L, Nt, T, sims.Vorticity(spline_sh=pert), n_maps=n_maps,
-                       precision=precision)
+                       precision=precision, forms=forms)
     return s.run()
 
 
@@ -47,7 +47,8 @@ def test_ensemble_graph_matches_members_alone(mods, persistent, precision):
     torch.cuda.synchronize()
     assert ens.count == ens.members[0].Nt - 2
     for i, (m, spec) in enumerate(zip(ens.members, ens.specs)):
-        ref = _alone(mods, spec, i, 7, kw["Nt"], kw["T"], kw["lmax"], kw["rms"], kw["n_maps"], precision)
+        ref = _alone(mods, spec, i, 7, kw["Nt"], kw["T"], kw["lmax"], kw["rms"], kw["n_maps"], precision,
+                     forms=m.stack_forms is not None)
         assert m.Nc == ref.Nc and m.count == ref.count
         assert torch.equal(m.omega, ref.omega), i
         for k in range(m.Nc):

@@ -312,6 +312,13 @@ def test_full_size_composition_properties(nat):
     Jg = host(J)[idx]
     scale = np.abs(Jo).max(axis=(1, 2))[:, None, None]
     np.testing.assert_allclose(Jg / scale, Jo / scale, rtol=0, atol=1e-10)
+    # the same workload through map forms: ids equal, points within 1e-13
+    fs = [m.assemble_forms(c) for c in cs]
+    Xf, tf, _, Jf = m.compose(cs, q, want_tri=True, want_jac=True, forms=fs)
+    assert torch.equal(tf, tri)
+    assert float((Xf - X).abs().max()) < 1e-13
+    assert float(((Jf - J).abs().amax(dim=(1, 2)) / J.abs().amax(dim=(1, 2))).max()) < 1e-10
+    assert m.status() == 0
 
 
 def test_ordered_compose_rejects_bad_permutation_entries(nat):
@@ -335,3 +342,47 @@ def test_ordered_compose_rejects_bad_permutation_entries(nat):
     keep[[3, 5]] = False
     assert torch.equal(out[keep], ref[keep])
     assert bool((out[~keep] == 7.0).all())
+
+
+def test_map_forms_match_coefficient_records(nat):
+    """Composition through map-form records (cmm_assemble_forms /
+    cmm_compose_forms: each Powell-Sabin patch as the quadratic form
+    p^T Q p, FP32-filtered sub-triangle choice) against the same submaps'
+    coefficient records and the oracle, level 5, 8 submaps, 2^16 queries:
+    same triangle ids; points within 1e-13 of the records' and 1e-12 of the
+    oracle's; Jacobians within 1e-11 (relative) of the records' and 1e-10
+    of the oracle's; a stack mixing forms and records; the coarse-cell
+    order bitwise equal to caller order."""
+    from cmm_gpu.meshgen import icosahedral_mesh, random_sphere_points, stencil_frames
+    from cmm_gpu.workloads import submap_stack
+    verts, tris = icosahedral_mesh(5)
+    tan, s_pts = stencil_frames(verts)
+    jets = submap_stack(s_pts, tan, 8, seed=4)
+    m = nat.Mesh(verts, tris, 5)
+    cs = [m.assemble(dev(j)) for j in jets]
+    fs = [m.assemble_forms(c) for c in cs]
+    q = dev(random_sphere_points(1 << 16, seed=6))
+    Xr, tr, tar, Jr = m.compose(cs, q, want_tri=True, want_tri_all=True, want_jac=True)
+    Xf, tf, taf, Jf = m.compose(cs, q, want_tri=True, want_tri_all=True, want_jac=True, forms=fs)
+    assert torch.equal(tr, tf) and torch.equal(tar, taf)
+    assert float((Xf - Xr).abs().max()) < 1e-13
+    scale = Jr.abs().amax(dim=(1, 2), keepdim=True)
+    assert float(((Jf - Jr).abs() / scale).max()) < 1e-11
+    Xm, _, _, Jm = m.compose(cs, q, want_jac=True, forms=[fs[0], None, fs[2], None, None, fs[5], fs[6], None])
+    assert float((Xm - Xr).abs().max()) < 1e-13
+    perm = m.query_order(q)
+    Xo, to, _, Jo = m.compose(cs, q, want_tri=True, want_jac=True, forms=fs, perm=perm)
+    assert torch.equal(Xo, Xf) and torch.equal(to, tf) and torch.equal(Jo, Jf)
+    comp = OS.CompositeOracle(verts, tris, OG.ConeLocator(verts, tris), jets, tie_fix=True)
+    qs = host(q)[:4096]
+    np.testing.assert_allclose(host(Xf)[:4096], comp(qs), rtol=0, atol=1e-12)
+    _, Jor = OS.composite_jacobian(comp, qs)
+    sc = np.abs(Jor).max(axis=(1, 2))[:, None, None]
+    np.testing.assert_allclose(host(Jf)[:4096] / sc, Jor / sc, rtol=0, atol=1e-10)
+    # non-finite queries through the forms path
+    qn = q[:64].clone()
+    qn[3, 1] = float("nan")
+    Xn, tn, _, Jn = m.compose(cs, qn, want_tri=True, want_jac=True, forms=fs)
+    assert torch.isnan(Xn[3]).all() and int(tn[3]) == -1 and torch.isfinite(Xn[4:]).all()
+    assert m.status(clear=True) == nat.FLAG_NONFINITE
+    assert m.status() == 0

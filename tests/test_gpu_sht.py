@@ -143,13 +143,16 @@ def test_scalar_spline_route_matches_reference(nat):
     np.testing.assert_allclose(om, ref, rtol=0, atol=1e-12)
 
 
+@pytest.mark.parametrize("schedule", [0, 1])
 @pytest.mark.parametrize("L", [32, 128, 256, 1024])
-def test_split_bf16_synthesis_against_fp64(nat, L):
+def test_split_bf16_synthesis_against_fp64(nat, L, schedule):
     """The 12-field synthesis on the tensor cores (three bf16 products,
     FP32 per 64-degree chunk, compensated FP32 across chunks) against the
     FP64 path, up to the band-limit of the large configuration.  Measured
     5.0e-6..5.8e-6 of max |fp64| per field; asserted below 2e-5 (each split
-    factor carries ~2^-17 relative error)."""
+    factor carries ~2^-17 relative error).  Both synthesis schedules: per
+    chunk drained into compensated sums (0), and warp-specialised with the
+    chunks accumulated in tensor memory (1)."""
     rng = np.random.default_rng(L)
     a = np.zeros((12, L, L), dtype=complex)
     for f in range(12):
@@ -157,11 +160,11 @@ def test_split_bf16_synthesis_against_fp64(nat, L):
         c[:, 0] = c[:, 0].real
         a[f] = mhalf(c / (1 + np.arange(L))[:, None])
     ref = nat.Sht(L).inverse(dev(a)).cpu().numpy()
-    tc = nat.Sht(L).set_precision(nat.Sht.SPLIT_BF16)
+    tc = nat.Sht(L).set_schedule(schedule).set_precision(nat.Sht.SPLIT_BF16)
     got = tc.inverse(dev(a)).cpu().numpy()
     assert tc.status() == 0
     err = np.abs(got - ref).max(axis=(1, 2)) / np.abs(ref).max(axis=(1, 2))
-    print(f"L={L}: split-BF16 synthesis relative error per field max {err.max():.3e}")
+    print(f"L={L} schedule {schedule}: split-BF16 synthesis relative error per field max {err.max():.3e}")
     assert err.max() < 2e-5
     assert err.max() > 1e-9   # the tensor-core path really ran (not FP64)
 
