@@ -797,6 +797,15 @@ def bench_adjoint(args, dev):
     rng = np.random.default_rng(13)
     rel, best = [], []
     ads, fd6, fdb = [], [], []
+    exceptions = []
+
+    def fd_at(l, c, h):
+        sp, sm = sh.clone(), sh.clone()
+        sp[l, c] += h
+        sm[l, c] -= h
+        with torch.no_grad():
+            return (float(run.misfit(sp, target)) - float(run.misfit(sm, target))) / (2 * h)
+
     for _ in range(args.adjoint_fd):
         l = int(rng.integers(1, lmax + 1))
         c = int(rng.integers(0, 2 * l + 1))
@@ -805,13 +814,18 @@ def bench_adjoint(args, dev):
         # h = 1e-6 (the configuration's step) for every sampled coefficient;
         # the comparison steps 1e-5 and 1e-4 for the first two only
         for h in ((1e-6, 1e-5, 1e-4) if len(ads) < 2 else (1e-6,)):
-            sp, sm = sh.clone(), sh.clone()
-            sp[l, c] += h
-            sm[l, c] -= h
-            with torch.no_grad():
-                fd = (float(run.misfit(sp, target)) - float(run.misfit(sm, target))) / (2 * h)
+            fd = fd_at(l, c, h)
             errs[h] = abs(fd - ad) / max(abs(ad), 1e-300)
             fds[h] = fd
+        if errs[1e-6] > 1e-6:
+            # an exception to the 1e-6 bar: the differences' own noise floor
+            # at this coefficient, |fd(h) - fd(2h)| (their truncation error at
+            # h = 2e-6 is ~1e-12 relative, so the spread is the rounding
+            # noise of J amplified by 1/h)
+            fd2 = fd_at(l, c, 2e-6)
+            noise = abs(fds[1e-6] - fd2) / max(abs(ad), 1e-300)
+            exceptions.append({"l": l, "m": c - l, "rel_err": errs[1e-6], "fd_noise_rel": noise,
+                               "explained": bool(errs[1e-6] <= 3 * noise)})
         ads.append(ad)
         fd6.append(fds[1e-6])
         fdb.append(fds[min(errs, key=errs.get)])
@@ -823,6 +837,9 @@ def bench_adjoint(args, dev):
             "J": J, "forward_s": t_fwd / 1e3, "forward_backward_s": t_grad / 1e3,
             "backward_over_forward": t_grad / t_fwd - 1.0,
             "fd_coefficients": args.adjoint_fd,
+            "within_1e-6": int(sum(r <= 1e-6 for r in rel)),
+            "exceptions": exceptions,
+            "exceptions_unexplained": int(sum(not e["explained"] for e in exceptions)),
             "rel_err_h1e-6_max": max(rel) if rel else None,
             "rel_err_h1e-6_median": float(np.median(rel)) if rel else None,
             "rel_err_best_h_max": max(best) if best else None,
@@ -835,7 +852,8 @@ def bench_adjoint(args, dev):
             "fd_note": "centred differences of J carry the map update's amplified rounding "
                        "(1/(4 eps) = 2.5e4 on every step) and curvature; h = 1e-6 for every sampled "
                        "coefficient; best_h = the smallest discrepancy over steps 1e-6, 1e-5, 1e-4, "
-                       "tried on the first two coefficients only"}
+                       "tried on the first two coefficients only; an exception (above 1e-6) is explained "
+                       "when it is within 3x the differences' measured noise |fd(1e-6) - fd(2e-6)|"}
 
 
 def bench_rh_error(dev):
@@ -986,7 +1004,8 @@ def north_star_summary(r):
         out["target_rh_error_ratio"] = 2.0
     adj = r.get("adjoint")
     if isinstance(adj, dict) and "rel_err_h1e-6_max" in adj:
-        out["adjoint"] = {k: adj.get(k) for k in ("fd_coefficients", "rel_err_h1e-6_max", "rel_err_h1e-6_median",
+        out["adjoint"] = {k: adj.get(k) for k in ("fd_coefficients", "within_1e-6", "exceptions_unexplained",
+                                                  "rel_err_h1e-6_max", "rel_err_h1e-6_median",
                                                   "vector_rel_err_h1e-6", "forward_backward_s")}
     return out
 

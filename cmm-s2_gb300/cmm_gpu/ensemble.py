@@ -95,15 +95,16 @@ class Ensemble:
         spectrum (coefficients N(0,1) l^-2, scaled to the given RMS),
         evaluated through its scalar spline.  forms: the members' remapped
         submaps with map-form records (BVESolver); None = when their
-        records (0.9 KB per triangle and slot) take at most half of the free
-        device memory."""
+        records (0.9 KB per triangle and slot) take at most a quarter of the
+        free device memory (the 64-member benchmark ensemble needs 84 GB of
+        them and runs without)."""
         device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
         rng = np.random.default_rng(seed)
         specs = [(int(rng.choice(levels)), int(rng.choice(bandlimits))) for _ in range(n)]
         if forms is None:
             slots = len([i for i in range(1, Nt) if i % n_maps == 0]) + 1
             need = sum(slots * (20 << (2 * lv)) * native.Mesh.FORM_STRIDE * 8 for lv, _ in specs)
-            forms = need <= 0.5 * torch.cuda.mem_get_info(device)[0]
+            forms = need <= 0.25 * torch.cuda.mem_get_info(device)[0]
         res = SharedResources(device)
         members = []
         for i, (level, L) in enumerate(specs):

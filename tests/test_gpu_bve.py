@@ -314,7 +314,10 @@ def test_nonfinite_initial_condition_is_reported(sims):
 def test_reference_drivers(sims):
     """euler_simulation_sphere_remapping with the reference's signature
     against the reference's own run (bve_l2_L8.npz, its 12-step run), and
-    euler_simulation_sphere (no remapping) equal to the solver's one-map run."""
+    euler_simulation_sphere (no remapping) equal to the solver's one-map run
+    (to rounding: the solver evaluates its remapped map through its map
+    forms, the returned sphere_diffeomorphism through its coefficient
+    record)."""
     d = np.load(os.path.join(GOLDEN, "bve_l2_L8.npz"))
     mesh = _ref_mesh_l2()
     comp = sims.euler_simulation_sphere_remapping(8, 12, 1.0, mesh, "rossby_wave", rot_rate=2 * np.pi, n_maps=5)
@@ -325,7 +328,7 @@ def test_reference_drivers(sims):
     s = sims.BVESolver(mesh.vertices, mesh.simplices, 2, 8, 12, 1.0, "rossby_wave", n_maps=12).run()
     assert s.Nc == 1
     q = dev(d["q"])
-    assert torch.equal(one(q).T.contiguous(), s.composite(q)[0])
+    assert float((one(q).T - s.composite(q)[0]).abs().max()) < 1e-13
 
 
 def test_config1_whole_run_matches_reference(sims):
