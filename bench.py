@@ -683,6 +683,7 @@ def bench_ensemble(args, dev):
     setup = time.perf_counter() - t0
     tuner = Autotuner(reps=2)
     tuner.tune_ensemble_kernels(ens)
+    tuner.tune_sht_schedule(ens.members)
     tuner.tune_schedule(ens, stream_counts=(1, 2, 4, 8), steps_each=2)
     n = ens.members[0].Nt - 2 - ens.count
     # the remaining run as ONE captured graph on the tuned schedule,
@@ -726,6 +727,8 @@ def bench_ensemble(args, dev):
             "graph_steps": n, "graph_capture_s": capture_s,
             "split_vs_fp64_omega_rel": {"member": i0, "level": lv0, "L": L0, "value": err0},
             "schedule": tuner.log["schedule"]["best"], "launch_shapes": tuner.log["kernels"],
+            "compose_variants": tuner.log.get("variants"), "sht_schedule": tuner.log.get("sht_schedule"),
+            "map_forms": ens.members[0].stack_forms is not None,
             "status_ok": ok}
 
 

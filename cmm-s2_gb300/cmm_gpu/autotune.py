@@ -1,7 +1,24 @@
-"""Project-written autotuner: launch shapes of the tunable kernels per
-size class, and the schedule (branch count, member order) of an
+"""Project-written autotuner: launch shapes and compiled variants of the
+tunable kernels per size class, the split-BF16 synthesis schedule per
+band-limit, and the schedule (branch count, member order) of an
 ensemble's captured graph, chosen from CUDA-event timings on the run's own
 data.
+
+What is tuned, and what is fixed by the data:
+* threads per block of the composition, the map update's foot points and
+  the vorticity kernel (cmm_mesh_set_block);
+* the composition's register budget (cmm_mesh_set_variant: resident
+  blocks 4 or 6 for points only) -- the same arithmetic compiled for
+  another register count, so results do not change;
+* the synthesis schedule (cmm_sht_set_schedule: per-chunk drain into
+  compensated sums, or warp-specialised with the chunks accumulated in
+  tensor memory) -- results differ at FP32 rounding, so it is tuned only
+  when asked (tune_sht_schedule), for all plans of a band-limit at once;
+* the graph's branch count and member order.
+The tensor-core tiles are fixed by the data: N = 32 columns holds the
+synthesis' 24 real columns (12 complex fields; N = 16 the analysis' 2),
+M = 128 the TMEM lanes, and K = 64 the chunk of the Pbar table images the
+MMAs read straight from shared memory (another K needs other tables).
 
 Launch shapes (cmm_mesh_set_block) are set per mesh, i.e. per mesh level
 (composition, foot points) or band-limit (vorticity); every member of a
@@ -32,6 +49,7 @@ def _time(fn, reps, stream):
 
 class Autotuner:
     BLOCKS = (64, 128, 192, 256)
+    COMPOSE_VARIANTS = (4, 6)
 
     def __init__(self, reps=3):
         self.reps = reps
@@ -68,6 +86,15 @@ class Autotuner:
             best = min(times, key=times.get)
             mesh.set_block(k, best)
             out[k] = (best, times)
+        # register budget of the grid composition (same results)
+        compose = stages[native.Mesh.TUNE_COMPOSE][1]
+        vt = {}
+        for v in self.COMPOSE_VARIANTS:
+            s.mesh.set_variant(native.Mesh.VARIANT_COMPOSE, v)
+            vt[v] = _time(compose, self.reps, stream)
+        vbest = min(vt, key=vt.get)
+        s.mesh.set_variant(native.Mesh.VARIANT_COMPOSE, vbest)
+        self.log.setdefault("variants", {})[f"level{s.level}_L{s.L}"] = {"compose_blocks": vbest, "ms": vt}
         self.log["kernels"][f"level{s.level}_L{s.L}"] = {
             name: {"best": out[k][0], "ms": out[k][1]}
             for name, k in (("compose", 0), ("advect", 1), ("vorticity", 2))}
@@ -83,6 +110,31 @@ class Autotuner:
             seen.add(key)
             self.tune_solver(m)
         return self.log["kernels"]
+
+    # ------------------------------------------------- synthesis schedule
+    def tune_sht_schedule(self, solvers, reps=3):
+        """Split-BF16 synthesis schedule per band-limit, timed on the first
+        solver of each L (its own velocity step) and applied to every
+        solver of that L."""
+        byL = {}
+        for s in solvers:
+            if s.precision_mode == native.Sht.SPLIT_BF16:
+                byL.setdefault(s.L, []).append(s)
+        res = {}
+        for L, group in byL.items():
+            s = group[0]
+            stream = torch.cuda.current_stream(s.device)
+            jets = torch.empty_like(s.vel_jets)
+            times = {}
+            for sched in (native.Sht.SCHEDULE_PER_CHUNK, native.Sht.SCHEDULE_WARP_SPECIALISED):
+                s.sht.set_schedule(sched)
+                times[sched] = _time(lambda: s.sht.velocity(s.vm, s.omega, jets=jets), reps, stream)
+            best = min(times, key=times.get)
+            for m in group:
+                m.sht.set_schedule(best)
+            res[f"L{L}"] = {"schedule": best, "ms": times}
+        self.log["sht_schedule"] = res
+        return res
 
     # ----------------------------------------------------------- schedule
     def tune_schedule(self, ens, stream_counts=(1, 2, 4, 8), steps_each=2):

@@ -58,5 +58,30 @@ __device__ __forceinline__ dd dd_mul(dd a, dd b) {
 
 __device__ __forceinline__ double dd_round(dd a) { return __dadd_rn(a.h, a.l); }
 
+// a + b with the low parts added in FP64 (Dekker's sum): error ~2^-105 of
+// |a| + |b|, enough where the cancellation is far below 2^52
+__device__ __forceinline__ dd dd_add_fast(dd a, dd b) {
+  const dd s = dd_two_sum(a.h, b.h);
+  return dd_fast_two_sum(s.h, __dadd_rn(s.l, __dadd_rn(a.l, b.l)));
+}
+
+// sum_k x_k m_k for six double-double x_k and doubles m_k, rounded once:
+// exact products of the high parts, their sum by a TwoSum cascade, every
+// error term and the low parts' products collected in one FP64
+// correction (relative error ~2^-104 of sum |x_k m_k|)
+__device__ __forceinline__ double dd_dot_d(const dd* x, const double* m) {
+  dd p = dd_two_prod(x[0].h, m[0]);
+  double err = __fma_rn(x[0].l, m[0], p.l);
+  double s = p.h;
+#pragma unroll
+  for (int k = 1; k < 6; ++k) {
+    const dd q = dd_two_prod(x[k].h, m[k]);
+    const dd t = dd_two_sum(s, q.h);
+    s = t.h;
+    err = __dadd_rn(err, __dadd_rn(t.l, __fma_rn(x[k].l, m[k], q.l)));
+  }
+  return __dadd_rn(s, err);
+}
+
 }  // namespace dev
 }  // namespace cmm

@@ -286,26 +286,30 @@ __device__ __forceinline__ void assemble_form(const MeshView& m, const double* _
   const int* id = kSplitOrd[lo][hi];   // V^2, E^2, C^2, VE, EC, VC
   const double* rec = coeffs + (int64_t)t * kCoeffStride3;
   double* out = forms + (int64_t)t * kFormStride + 18 * sub;
-#pragma unroll 1
-  for (int c = 0; c < 3; ++c) {
-    double o[6];
+  // M_c = [[V2, VE, VC], [VE, E2, EC], [VC, EC, C2]] of each component
+  double M[3][6];   // per component: the pairs (VV, EE, CC, VE, EC, VC)
 #pragma unroll
-    for (int k = 0; k < 6; ++k) o[k] = __ldg(rec + 3 * id[k] + c);
-    const double M[3][3] = {{o[0], o[3], o[5]}, {o[3], o[1], o[4]}, {o[5], o[4], o[2]}};
-    dd U[3][3];   // U = M T
+  for (int c = 0; c < 3; ++c)
 #pragma unroll
-    for (int a = 0; a < 3; ++a)
+    for (int k = 0; k < 6; ++k) M[c][k] = __ldg(rec + 3 * id[k] + c);
+  // Q_c[i][j] = sum over role pairs a <= b of M_c,ab P_ab[i][j] with
+  // P_aa = T_a,i T_a,j and P_ab = T_a,i T_b,j + T_b,i T_a,j (a < b):
+  // symmetric in (i, j) by construction, so the stored 2 Q_ij is exact
+  const int pa[6] = {0, 1, 2, 0, 1, 0}, pb[6] = {0, 1, 2, 1, 2, 2};   // VV, EE, CC, VE, EC, VC
+  const int ei[6] = {0, 1, 2, 0, 0, 1}, ej[6] = {0, 1, 2, 1, 2, 2};   // xx, yy, zz, xy, xz, yz
 #pragma unroll
-      for (int j = 0; j < 3; ++j)
-        U[a][j] = dd_add(dd_add(dd_mul_d(T[0][j], M[a][0]), dd_mul_d(T[1][j], M[a][1])), dd_mul_d(T[2][j], M[a][2]));
-    const int pi[6] = {0, 1, 2, 0, 0, 1}, pj[6] = {0, 1, 2, 1, 2, 2};
+  for (int e = 0; e < 6; ++e) {
+    const int i = ei[e], j = ej[e];
+    dd P[6];
 #pragma unroll
-    for (int e = 0; e < 6; ++e) {
-      const int i = pi[e], j = pj[e];
-      dd q = dd_add(dd_add(dd_mul(T[0][i], U[0][j]), dd_mul(T[1][i], U[1][j])), dd_mul(T[2][i], U[2][j]));
-      if (i != j)   // the symmetric pair, 2 Q_ij
-        q = dd_add(q, dd_add(dd_add(dd_mul(T[0][j], U[0][i]), dd_mul(T[1][j], U[1][i])), dd_mul(T[2][j], U[2][i])));
-      out[6 * c + e] = dd_round(q);
+    for (int k = 0; k < 6; ++k) {
+      const int a = pa[k], b = pb[k];
+      P[k] = a == b ? dd_mul(T[a][i], T[a][j]) : dd_add_fast(dd_mul(T[a][i], T[b][j]), dd_mul(T[b][i], T[a][j]));
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const double q = dd_dot_d(P, M[c]);
+      out[6 * c + e] = i == j ? q : 2.0 * q;
     }
   }
   if (sub == 0)
