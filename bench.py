@@ -45,16 +45,16 @@ sys.path.insert(0, os.path.join(ROOT, "cmm-s2_gb300"))
 LEVEL, SUBMAPS = 7, 8
 METRIC = "map evals/s"
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one
-# Jacobian compose launch per query, from one ncu capture of compose_kernel
-# on 2^22 queries (level 7, 8 submaps), scaled to the headline's 2^24 by
-# the number of queries (the gathers and outputs grow with it): with the
-# queries grouped by coarse cell (the headline step) ...
-COMPOSE_TRAFFIC_PER_QUERY = (3.1035e9 + 1.0023e9) / (1 << 22)
+# Jacobian compose launch through map forms per query, from one ncu capture
+# of compose_kernel on 2^22 queries (level 7, 8 submaps), scaled to the
+# headline's 2^24 by the number of queries (the gathers and outputs grow
+# with it): with the queries grouped by coarse cell (the headline step) ...
+COMPOSE_TRAFFIC_PER_QUERY = (4.1665e9 + 0.7657e9) / (1 << 22)
 # ... and in the caller's order.
 COMPOSE_TRAFFIC_PER_QUERY_CALLER = (18.671e9 + 1.118e9) / (1 << 22)
 # FP64 instructions (DADD + DMUL + DFMA) per map evaluation (query x
 # submap) with the Jacobian, from the same capture.
-FP64_INSTR_PER_EVAL = 56.1
+FP64_INSTR_PER_EVAL = 28.15
 
 
 def peaks():
@@ -821,14 +821,24 @@ def bench_adjoint(args, dev):
             errs[h] = abs(fd - ad) / max(abs(ad), 1e-300)
             fds[h] = fd
         if errs[1e-6] > 1e-6:
-            # an exception to the 1e-6 bar: the differences' own noise floor
-            # at this coefficient, |fd(h) - fd(2h)| (their truncation error at
-            # h = 2e-6 is ~1e-12 relative, so the spread is the rounding
-            # noise of J amplified by 1/h)
-            fd2 = fd_at(l, c, 2e-6)
-            noise = abs(fds[1e-6] - fd2) / max(abs(ad), 1e-300)
-            exceptions.append({"l": l, "m": c - l, "rel_err": errs[1e-6], "fd_noise_rel": noise,
-                               "explained": bool(errs[1e-6] <= 3 * noise)})
+            # an exception to the 1e-6 bar at h = 1e-6: the derivative again
+            # from the fourth-order five-point stencil at h = 5e-5, whose
+            # rounding noise is 50 times smaller and whose truncation error
+            # (~h^4) is negligible; the exception is the differences' own
+            # error when the adjoint agrees with that derivative to 1e-6
+            h4 = 5e-5
+            jv = {}
+            for k in (-2, -1, 1, 2):
+                x = sh.clone()
+                x[l, c] += k * h4
+                with torch.no_grad():
+                    jv[k] = float(run.misfit(x, target))
+            fd4 = (jv[-2] - 8 * jv[-1] + 8 * jv[1] - jv[2]) / (12 * h4)
+            den = max(abs(ad), 1e-300)
+            exceptions.append({"l": l, "m": c - l, "rel_err": errs[1e-6],
+                               "rel_err_vs_5point": abs(ad - fd4) / den,
+                               "fd_1e-6_error_rel": abs(fds[1e-6] - fd4) / den,
+                               "explained": bool(abs(ad - fd4) <= 1e-6 * den)})
         ads.append(ad)
         fd6.append(fds[1e-6])
         fdb.append(fds[min(errs, key=errs.get)])
@@ -855,8 +865,9 @@ def bench_adjoint(args, dev):
             "fd_note": "centred differences of J carry the map update's amplified rounding "
                        "(1/(4 eps) = 2.5e4 on every step) and curvature; h = 1e-6 for every sampled "
                        "coefficient; best_h = the smallest discrepancy over steps 1e-6, 1e-5, 1e-4, "
-                       "tried on the first two coefficients only; an exception (above 1e-6) is explained "
-                       "when it is within 3x the differences' measured noise |fd(1e-6) - fd(2e-6)|"}
+                       "tried on the first two coefficients only; an exception (above 1e-6 at h = 1e-6) is "
+                       "explained when the adjoint agrees to 1e-6 with the five-point fourth-order "
+                       "difference at h = 5e-5, i.e. the discrepancy is the h = 1e-6 difference's own error"}
 
 
 def bench_rh_error(dev):

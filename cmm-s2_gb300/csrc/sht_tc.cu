@@ -451,10 +451,9 @@ __global__ void __launch_bounds__(kThreads, 1) synth_tc_kernel(TcGeometry g, int
 // ------------------------------------------ synthesis, warp-specialised
 // The same contraction with the work item's chunks accumulated in tensor
 // memory (FP32) and drained once per item, by three roles that run
-// concurrently: warp 4 streams the tiles into a five-stage ring of shared
-// memory (bulk copies; a stage holds one parity of one chunk, 40 KiB, so
-// up to 200 KiB per SM are in flight), warp 5 issues each stage's MMAs
-// into the item's accumulator pair as soon as its tiles have landed, and warps 0-3
+// concurrently: warp 4 streams the chunks' tiles into a two-stage ring of
+// shared memory (bulk copies), warp 5 issues each chunk's MMAs into the
+// item's accumulator pair as soon as its tiles have landed, and warps 0-3
 // (whose lanes are the 128 TMEM lanes, one ring pair each) drain an
 // item's accumulators and write its spectra while the next item's chunks
 // are multiplied into the other pair.  Stage and accumulator hand-offs go
@@ -462,34 +461,7 @@ __global__ void __launch_bounds__(kThreads, 1) synth_tc_kernel(TcGeometry g, int
 // and `acc_full`, the four drain warps complete `acc_empty`); every wait
 // is bounded and a timeout in any role stops all three.
 constexpr int kSynWarps2 = 6;
-constexpr int kSynStages2 = 5;
-constexpr int kSynHalf = 2 * kPTile + 2 * kATile;   // one parity of a chunk: P hi, lo, A hi, lo
-
-// Tiles of parity par of the cursor's chunk into a stage: the P record's
-// two tiles of that parity and the A record's, each contiguous.
-__device__ __forceinline__ void syn_load_half(const TcGeometry& g, const unsigned char* ptab,
-                                              const unsigned char* atab, const SynCursor& u, int par,
-                                              unsigned char* stage, uint64_t* bar) {
-  const int64_t chunk = g.cbase[u.m] + u.c;
-  const unsigned char* srcP = ptab + (chunk * g.nrb + u.blk) * kPRecord + 2 * par * kPTile;
-  const unsigned char* srcA = atab + chunk * kARecord + 2 * par * kATile;
-  mbar_expect_tx(bar, kSynHalf);
-  bulk_g2s(stage, srcP, 2 * kPTile, bar);
-  bulk_g2s(stage + 2 * kPTile, srcA, 2 * kATile, bar);
-}
-
-// One parity's products into its accumulator d (first: the item's first chunk).
-__device__ __forceinline__ void syn_mma_half(uint32_t stage, uint32_t d, uint32_t idesc, bool first) {
-  for (int ks = 0; ks < kKc / 16; ++ks) {
-    const uint64_t ph = smem_desc(stage + ks * 256);
-    const uint64_t pl = smem_desc(stage + kPTile + ks * 256);
-    const uint64_t ah = smem_desc(stage + 2 * kPTile + ks * 256);
-    const uint64_t al = smem_desc(stage + 2 * kPTile + kATile + ks * 256);
-    mma_bf16(d, ph, ah, idesc, (first && ks == 0) ? 0u : 1u);
-    mma_bf16(d, ph, al, idesc, 1u);
-    mma_bf16(d, pl, ah, idesc, 1u);
-  }
-}
+constexpr int kSynStages2 = 2;
 
 __device__ __forceinline__ bool wait_or_abort(uint64_t* bar, uint32_t parity, volatile int* abort) {
   for (long long i = 0; i < kSpinLimit; ++i) {
@@ -500,12 +472,27 @@ __device__ __forceinline__ bool wait_or_abort(uint64_t* bar, uint32_t parity, vo
   return false;
 }
 
+__device__ __forceinline__ void syn_mma_acc(uint32_t stage, uint32_t d, uint32_t idesc, bool first) {
+  const uint32_t p0 = stage, a0 = stage + kPRecord;
+  for (int ks = 0; ks < kKc / 16; ++ks)
+    for (int par = 0; par < 2; ++par) {
+      const uint64_t ph = smem_desc(p0 + (2 * par) * kPTile + ks * 256);
+      const uint64_t pl = smem_desc(p0 + (2 * par + 1) * kPTile + ks * 256);
+      const uint64_t ah = smem_desc(a0 + (2 * par) * kATile + ks * 256);
+      const uint64_t al = smem_desc(a0 + (2 * par + 1) * kATile + ks * 256);
+      const uint32_t dd = d + par * kN;
+      mma_bf16(dd, ph, ah, idesc, (first && ks == 0) ? 0u : 1u);
+      mma_bf16(dd, ph, al, idesc, 1u);
+      mma_bf16(dd, pl, ah, idesc, 1u);
+    }
+}
+
 __global__ void __launch_bounds__(32 * kSynWarps2, 1) synth_tc2_kernel(TcGeometry g, int nitems,
                                                                        const unsigned char* __restrict__ ptab,
                                                                        const unsigned char* __restrict__ atab,
                                                                        float2* __restrict__ S,
                                                                        int* __restrict__ status) {
-  extern __shared__ __align__(1024) unsigned char smem[];   // kSynStages2 stages of kSynHalf bytes
+  extern __shared__ __align__(1024) unsigned char smem[];   // kSynStages2 stages of kSynStage bytes
   __shared__ __align__(8) uint64_t full[kSynStages2], empty[kSynStages2], acc_full[2], acc_empty[2];
   __shared__ uint32_t tmem_base_s;
   __shared__ volatile int abort_s;
@@ -538,21 +525,14 @@ __global__ void __launch_bounds__(32 * kSynWarps2, 1) synth_tc2_kernel(TcGeometr
   const uint32_t tmem = tmem_base_s;
   if (warp == 4 && lane == 0) {
     // producer: the tiles of every chunk of this CTA's items, in order
-    long long j = 0;   // stages issued: two per chunk (even, odd parity)
+    long long j = 0;
     SynCursor u;
     bool ok = syn_set(u, blockIdx.x, nitems, g);
     while (ok && !abort_s) {
-      bool stop = false;
-      for (int par = 0; par < 2; ++par) {
-        const int st = (int)(j % kSynStages2);
-        if (j >= kSynStages2 && !wait_or_abort(&empty[st], (uint32_t)((j / kSynStages2 - 1) & 1), &abort_s)) {
-          stop = true;
-          break;
-        }
-        syn_load_half(g, ptab, atab, u, par, smem + st * kSynHalf, &full[st]);
-        ++j;
-      }
-      if (stop) break;
+      const int st = (int)(j % kSynStages2);
+      if (j >= kSynStages2 && !wait_or_abort(&empty[st], (uint32_t)((j / kSynStages2 - 1) & 1), &abort_s)) break;
+      syn_load(g, ptab, atab, u, smem + st * kSynStage, &full[st]);
+      ++j;
       ok = syn_next(u, nitems, g);
     }
     // copies still in flight land before the block exits: the stages'
@@ -574,14 +554,14 @@ __global__ void __launch_bounds__(32 * kSynWarps2, 1) synth_tc2_kernel(TcGeometr
       if (it >= 2 && !wait_or_abort(&acc_empty[a], (uint32_t)((it / 2 - 1) & 1), &abort_s)) break;
       const int nch = nchunks(L, item / g.nrb);
       bool ok = true;
-      for (int h = 0; h < 2 * nch && ok; ++h, ++j) {   // h = 2 c + parity
+      for (int c = 0; c < nch; ++c, ++j) {
         const int st = (int)(j % kSynStages2);
         if (!wait_or_abort(&full[st], (uint32_t)((j / kSynStages2) & 1), &abort_s)) {
           ok = false;
           break;
         }
         tc_fence_after();
-        syn_mma_half(s0 + st * kSynHalf, tmem + a * 2 * kN + (h & 1) * kN, idesc, h < 2);
+        syn_mma_acc(s0 + st * kSynStage, tmem + a * 2 * kN, idesc, c == 0);
         mma_commit(&empty[st]);
         committed = true;
       }
@@ -904,7 +884,7 @@ int tc_plan_create(int L, const double* ct_rings, const double* pmm_rings, const
                                        2 * kSynStage);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(synth_tc2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             kSynStages2 * kSynHalf);
+                             kSynStages2 * kSynStage);
   int dev = 0;
   if (e == cudaSuccess) e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, dev);
@@ -1010,7 +990,7 @@ int tc_synthesis(TcPlan* p, const double2* fields, float2* S, int* status, cudaS
   const int nitems = p->L * p->nrb;
   const int grid = std::min(nitems, std::max(p->sms, 1));
   if (p->schedule == 1) {
-    synth_tc2_kernel<<<grid, 32 * kSynWarps2, kSynStages2 * kSynHalf, s>>>(
+    synth_tc2_kernel<<<grid, 32 * kSynWarps2, kSynStages2 * kSynStage, s>>>(
         g, nitems, (const unsigned char*)p->tab->ptab.p, (const unsigned char*)p->atab.p, S, status);
     return check("synth_tc2_kernel");
   }
