@@ -49,12 +49,17 @@ METRIC = "map evals/s"
 # of compose_kernel on 2^22 queries (level 7, 8 submaps), scaled to the
 # headline's 2^24 by the number of queries (the gathers and outputs grow
 # with it): with the queries grouped by coarse cell (the headline step) ...
-COMPOSE_TRAFFIC_PER_QUERY = (4.1665e9 + 0.7657e9) / (1 << 22)
+COMPOSE_TRAFFIC_PER_QUERY = (4.1636e9 + 0.7654e9) / (1 << 22)
 # ... and in the caller's order.
-COMPOSE_TRAFFIC_PER_QUERY_CALLER = (18.671e9 + 1.118e9) / (1 << 22)
+COMPOSE_TRAFFIC_PER_QUERY_CALLER = (9.9927e9 + 0.5103e9) / (1 << 22)
 # FP64 instructions (DADD + DMUL + DFMA) per map evaluation (query x
-# submap) with the Jacobian, from the same capture.
+# submap) with the Jacobian, from the same capture, and all issued
+# instructions per evaluation (smsp__inst_executed.sum x 32 / evaluations):
+# at 2 FP64 lane-operations per SM per clock and 4 warp instructions issued
+# per SM per clock, both cost ~14 SM cycles per evaluation at their peaks,
+# so the two bind together.
 FP64_INSTR_PER_EVAL = 28.15
+INSTR_PER_EVAL = 1803
 
 
 def peaks():
@@ -1124,6 +1129,8 @@ def main():
     algo = algorithmic_bytes(r["Q"], SUBMAPS, r["nv"], r["nt"])
     achieved = algo / (r["ms_compose"] / 1e3) / 1e9
     kernel_rate = r["Q"] * SUBMAPS / (r["ms_compose"] / 1e3)   # one GPU, composition kernel alone
+    sm_mhz = (r["clocks"] or {}).get("sm_mhz")
+    issue_peak = 4 * 32 * 152 * sm_mhz * 1e6 if sm_mhz else None   # thread instructions per second
     Q = r["Q"]
     line = {
         "metric": METRIC, "value": r["value"], "unit": "map evals/s", "n_gpus": world,
@@ -1133,12 +1140,15 @@ def main():
                      "frac": achieved / peak, "peak_kind": how,
                      "traffic": COMPOSE_TRAFFIC_PER_QUERY * Q, "algorithmic_bytes": algo,
                      "kernel": "compose_kernel", "kernel_ms": r["ms_compose"], "caller_order": r["caller"]},
-        "fp64": {"bound": "fp64 pipe (binding on GB300)",
+        "fp64": {"bound": "fp64 pipe and instruction issue (equal cost per evaluation)",
                  "instr_per_eval": FP64_INSTR_PER_EVAL,
                  "achieved_tinstr_s": FP64_INSTR_PER_EVAL * kernel_rate / 1e12,
                  "peak_tinstr_s": r["fp64_fma_per_s"] / 1e12,
                  "frac": FP64_INSTR_PER_EVAL * kernel_rate / r["fp64_fma_per_s"],
-                 "peak_kind": "measured (FMA-chain probe in this run)"},
+                 "peak_kind": "measured (FMA-chain probe in this run)",
+                 "issue": {"instr_per_eval": INSTR_PER_EVAL,
+                           "frac": INSTR_PER_EVAL * kernel_rate / issue_peak if issue_peak else None,
+                           "peak": "4 warp instructions per SM per clock x 152 SMs at the sampled SM clock"}},
         "cpu_baseline": cpu,
         "e2e": {"value": world * Q * SUBMAPS / (r["ms_e2e"] / 1e3), "unit": "map evals/s",
                 "h2d_bytes_per_step": Q * 24, "d2h_bytes_per_step": Q * (24 + 4 + 72),
