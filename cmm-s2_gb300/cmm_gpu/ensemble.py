@@ -79,6 +79,28 @@ class SharedResources:
         self._sht.setdefault(L, sht)
 
 
+# Map forms pay when the evaluations through a remapped submap outnumber
+# the triangles by more than this factor: assembling a submap's forms costs
+# 6.1 ms per 327,680 triangles (18.6 ns per triangle, double-double on the
+# FP64 pipe), and each evaluation through a form instead of a coefficient
+# record saves ~20 FP64 instructions (26.8 against 46.5), 32 ps at the
+# measured 0.63 x 10^12 FP64 instructions/s.
+FORMS_EVALS_PER_TRIANGLE = 582
+
+
+def forms_pay(level, L, Nt, n_maps):
+    """Whether map forms pay for a run of Nt steps at mesh level `level` and
+    band-limit L remapping every n_maps steps: the (L+1) x 2L sample points
+    pass through each remapped submap on every later step (on average the
+    remaining half of the run)."""
+    points = (L + 1) * 2 * L
+    remaps = [i for i in range(1, Nt) if i % n_maps == 0]
+    if not remaps:
+        return False
+    later = sum(Nt - i for i in remaps) / len(remaps)
+    return points * later > FORMS_EVALS_PER_TRIANGLE * (20 << (2 * level))
+
+
 class Ensemble:
     def __init__(self, members):
         self.members = list(members)
@@ -94,23 +116,28 @@ class Ensemble:
         starts from seeded random vorticity over l <= lmax with a k^-3
         spectrum (coefficients N(0,1) l^-2, scaled to the given RMS),
         evaluated through its scalar spline.  forms: the members' remapped
-        submaps with map-form records (BVESolver); None = when their
+        submaps with map-form records (BVESolver), True / False for all, or
+        None: per member, when they pay (forms_pay) and the chosen members'
         records (0.9 KB per triangle and slot) take at most a quarter of the
-        free device memory (the 64-member benchmark ensemble needs 84 GB of
-        them and runs without)."""
+        free device memory."""
         device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
         rng = np.random.default_rng(seed)
         specs = [(int(rng.choice(levels)), int(rng.choice(bandlimits))) for _ in range(n)]
         if forms is None:
+            use = [forms_pay(lv, L, Nt, n_maps) for lv, L in specs]
             slots = len([i for i in range(1, Nt) if i % n_maps == 0]) + 1
-            need = sum(slots * (20 << (2 * lv)) * native.Mesh.FORM_STRIDE * 8 for lv, _ in specs)
-            forms = need <= 0.25 * torch.cuda.mem_get_info(device)[0]
+            need = sum(slots * (20 << (2 * lv)) * native.Mesh.FORM_STRIDE * 8
+                       for (lv, _), u in zip(specs, use) if u)
+            if need > 0.25 * torch.cuda.mem_get_info(device)[0]:
+                use = [False] * n
+        else:
+            use = [bool(forms)] * n
         res = SharedResources(device)
         members = []
         for i, (level, L) in enumerate(specs):
             pert = spectral_perturbation(lmax, seed=seed * 100003 + i, slope=-2.0, rms=rms)
             members.append(BVESolver(None, None, level, L, Nt, T, Vorticity(spline_sh=pert),
-                                     n_maps=n_maps, precision=precision, resources=res, forms=forms))
+                                     n_maps=n_maps, precision=precision, resources=res, forms=use[i]))
         ens = cls(members)
         ens.specs = specs
         ens.resources = res

@@ -54,8 +54,9 @@ _SIGS = {
     "cmm_query_order": (_i, [_p, _p, _i64, _p, _p, _p]),
     "cmm_compose_ordered": (_i, [_p, ctypes.POINTER(_p), _i, _p, _i64, _p, _p, _p, _p, _p, _p]),
     "cmm_assemble_forms": (_i, [_p, _p, _p, _p]),
-    "cmm_compose_forms": (_i, [_p, ctypes.POINTER(_p), ctypes.POINTER(_p), _i, _p, _i64, _p, _p, _p, _p, _p,
-                               _p]),
+    "cmm_forms_ff": (_i, [_p, _p, _p, _p]),
+    "cmm_compose_forms": (_i, [_p, ctypes.POINTER(_p), ctypes.POINTER(_p), ctypes.POINTER(_p), _i, _p, _i64,
+                               _p, _p, _p, _p, _p, _p]),
     "cmm_stencil_eval": (_i, [_p, _p, _p, _p, _i64, _p, _p]),
     "cmm_velmesh_create": (_i, [_i, _p, _p, _p, _p, ctypes.POINTER(_p)]),
     "cmm_velocity_eval": (_i, [_p, ctypes.POINTER(_p), _i, _d, _d, _d, _p, _i64, _p, _p]),
@@ -222,6 +223,16 @@ class Mesh:
               "cmm_assemble_forms")
         return out
 
+    FORM_FF_STRIDE = 112
+
+    def forms_ff(self, forms, out=None):
+        """Low floats (Nt, 112) float32 of the float-float split of map-form
+        records (cmm_forms_ff), read by the Jacobian compositions."""
+        if out is None:
+            out = torch.empty((self.nt, self.FORM_FF_STRIDE), dtype=torch.float32, device=forms.device)
+        check(lib.cmm_forms_ff(self.h, _ptr(forms), _ptr(out), _stream(forms.device)), "cmm_forms_ff")
+        return out
+
     def query_order(self, q, work=None):
         """Permutation grouping the queries by coarse hierarchy cell."""
         q = _dev(q)
@@ -235,10 +246,11 @@ class Mesh:
         return perm
 
     def compose(self, coeffs, q, want_tri=False, want_tri_all=False, want_jac=False, out=None,
-                perm=None, forms=None):
+                perm=None, forms=None, forms_ff=None):
         """coeffs: list of coefficient tensors, submap 0 first (applied last).
         perm: optional processing order (query_order), same results.
-        forms: optional list of map-form records (entries may be None)."""
+        forms: optional list of map-form records (entries may be None);
+        forms_ff: optional list of their float-float copies (forms_ff())."""
         q = _dev(q)
         n = q.shape[0]
         S = len(coeffs)
@@ -249,8 +261,11 @@ class Mesh:
         jac = torch.empty((n, 3, 3), dtype=torch.float64, device=q.device) if want_jac else None
         if forms is not None:
             farr = (ctypes.c_void_p * S)(*[None if f is None else f.data_ptr() for f in forms])
-            check(lib.cmm_compose_forms(self.h, arr, farr, S, _ptr(q), n, _ptr(perm), _ptr(out), _ptr(tri),
-                                        _ptr(tri_all), _ptr(jac), _stream(q.device)), "cmm_compose_forms")
+            garr = None if forms_ff is None else \
+                (ctypes.c_void_p * S)(*[None if g is None else g.data_ptr() for g in forms_ff])
+            check(lib.cmm_compose_forms(self.h, arr, farr, garr, S, _ptr(q), n, _ptr(perm), _ptr(out),
+                                        _ptr(tri), _ptr(tri_all), _ptr(jac), _stream(q.device)),
+                  "cmm_compose_forms")
         elif perm is None:
             check(lib.cmm_compose(self.h, arr, S, _ptr(q), n, _ptr(out), _ptr(tri), _ptr(tri_all),
                                   _ptr(jac), _stream(q.device)), "cmm_compose")
@@ -499,13 +514,14 @@ class Sht:
 
 
 def compose_host(mesh, coeffs, q_host, out_host, tri_host=None, jac_host=None, chunks=16,
-                 streams=None, scratch=None, order=None, forms=None):
+                 streams=None, scratch=None, order=None, forms=None, forms_ff=None):
     """Composition of host-resident queries (pinned (n,3) float64) into
     host-resident outputs, pipelined in `chunks` pieces over two CUDA
     streams so the host<->device copies overlap the kernels.  order: each
     chunk is processed grouped by coarse cell (cmm_query_order, same
     results; default), so that neighbouring threads gather neighbouring
-    records.  Returns the scratch dict for reuse."""
+    records.  forms / forms_ff: map-form records and their float-float
+    copies (Mesh.compose).  Returns the scratch dict for reuse."""
     if order is None:
         order = True
     n = q_host.shape[0]
@@ -525,6 +541,8 @@ def compose_host(mesh, coeffs, q_host, out_host, tri_host=None, jac_host=None, c
     arr = (ctypes.c_void_p * len(coeffs))(*[c.data_ptr() for c in coeffs])
     farr = None if forms is None else (ctypes.c_void_p * len(coeffs))(
         *[None if f is None else f.data_ptr() for f in forms])
+    garr = None if forms_ff is None else (ctypes.c_void_p * len(coeffs))(
+        *[None if g is None else g.data_ptr() for g in forms_ff])
     cur = torch.cuda.current_stream(dev)
     for s in streams:
         s.wait_stream(cur)
@@ -542,7 +560,7 @@ def compose_host(mesh, coeffs, q_host, out_host, tri_host=None, jac_host=None, c
                 check(lib.cmm_query_order(mesh.h, _ptr(b["q"]), m, _ptr(b["perm"]), _ptr(b["work"]), st),
                       "cmm_query_order")
             if farr is not None:
-                check(lib.cmm_compose_forms(mesh.h, arr, farr, len(coeffs), _ptr(b["q"]), m,
+                check(lib.cmm_compose_forms(mesh.h, arr, farr, garr, len(coeffs), _ptr(b["q"]), m,
                                             _ptr(b["perm"]) if order else None, _ptr(b["out"]), _ptr(b["tri"]),
                                             None, _ptr(b["jac"]), st), "cmm_compose_forms")
             elif order:

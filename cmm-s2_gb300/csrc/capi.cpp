@@ -447,16 +447,22 @@ int cmm_assemble_forms(const cmm_mesh* mesh, const double* coeffs, double* forms
   return launch_assemble_forms(mesh->view, coeffs, forms, (cudaStream_t)stream);
 }
 
-int cmm_compose_forms(const cmm_mesh* mesh, const double* const* coeffs, const double* const* forms, int S,
-                      const double* q, int64_t n, const int32_t* perm, double* out, int32_t* tri,
-                      int32_t* tri_all, double* jac, void* stream) {
+int cmm_forms_ff(const cmm_mesh* mesh, const double* forms, float* forms_ff, void* stream) {
+  if (!mesh || mesh->view.kind != kIcosahedral || !forms || !forms_ff)
+    return arg_error("cmm_forms_ff: bad argument");
+  return launch_forms_ff(mesh->view, forms, forms_ff, (cudaStream_t)stream);
+}
+
+int cmm_compose_forms(const cmm_mesh* mesh, const double* const* coeffs, const double* const* forms,
+                      const float* const* forms_ff, int S, const double* q, int64_t n, const int32_t* perm,
+                      double* out, int32_t* tri, int32_t* tri_all, double* jac, void* stream) {
   if (!mesh || mesh->view.kind != kIcosahedral || S < 1 || S > CMM_MAX_SUBMAPS || !coeffs || n < 0 ||
       n > INT32_MAX || (n > 0 && (!q || !out)))
     return arg_error("cmm_compose_forms: bad argument");
   for (int k = 0; k < S; ++k)
     if (!coeffs[k]) return arg_error("cmm_compose_forms: null coefficient pointer");
   return launch_compose(mesh->view, coeffs, S, q, n, out, tri, tri_all, jac, (cudaStream_t)stream, perm,
-                        forms);
+                        forms, forms_ff);
 }
 
 int cmm_compose_ordered(const cmm_mesh* mesh, const double* const* coeffs, int S, const double* q,

@@ -31,6 +31,12 @@ constexpr int kCoeffStride1 = 24;   // 19 ordinates, padded
 // sub-triangles (kSubIndex) and each component the homogeneous quadratic
 // form P(p) = p^T Q p as (Qxx, Qyy, Qzz, 2Qxy, 2Qxz, 2Qyz), 108 used.
 constexpr int kFormStride = 112;
+// Low floats of a map-form record's float-float split (floats per
+// triangle), for the Jacobian pushes: per sub-triangle (18 floats) and
+// component (6) the symmetric matrix entries Qxx, Qyy, Qzz, Qxy, Qxz, Qyz
+// as the low float of ff_of (the cross terms halved, exact); the high
+// float is re-derived from the double's bits (ff_hi).  108 used.
+constexpr int kFormFFStride = 112;
 
 // Device view of an icosahedral mesh.
 struct MeshView {
@@ -138,9 +144,12 @@ int launch_assemble(const MeshView& m, const double* jets, int ncomp, double* co
                     cudaStream_t s, const BveState* st = nullptr);
 int launch_compose(const MeshView& m, const double* const* coeffs, int S, const double* q,
                    int64_t n, double* out, int32_t* tri, int32_t* tri_all, double* jac,
-                   cudaStream_t s, const int32_t* perm = nullptr, const double* const* forms = nullptr);
+                   cudaStream_t s, const int32_t* perm = nullptr, const double* const* forms = nullptr,
+                   const float* const* forms_ff = nullptr);
 // Map-form records (Nt, kFormStride) from coefficient records (Nt, 64).
 int launch_assemble_forms(const MeshView& m, const double* coeffs, double* forms, cudaStream_t s);
+// Float-float form records (Nt, kFormFFStride) of form records.
+int launch_forms_ff(const MeshView& m, const double* forms, float* forms_ff, cudaStream_t s);
 // The forms of the stack slot a device-driven step remaps into (no-op on
 // the other steps).
 struct BveState;

@@ -56,6 +56,18 @@ __device__ __forceinline__ ff ff_of(double x) {
   return ff{__uint_as_float(sgn | fh), sgn ? -lo : lo};
 }
 
+// The high float of ff_of(x) alone (the same bits): x truncated to 24
+// significand bits, from its bit pattern.
+__device__ __forceinline__ float ff_hi(double x) {
+  const long long b = __double_as_longlong(x);
+  const unsigned hw = (unsigned)(b >> 32), lw = (unsigned)b;
+  const unsigned mag = hw & 0x7fffffffu, sgn = hw & 0x80000000u;
+  const unsigned e = mag >> 20;
+  unsigned fh = e < 897u ? 0u : (((mag - (896u << 20)) << 3) | (lw >> 29));
+  if (e > 1150u) fh = (e == 2047u && ((mag & 0xfffffu) | lw) != 0u) ? 0x7fc00000u : 0x7f800000u;
+  return __uint_as_float(sgn | fh);
+}
+
 // h + l rounded to a double (one FP64 addition; the conversions are exact)
 __device__ __forceinline__ double ff_to_double(ff a) { return (double)a.h + (double)a.l; }
 

@@ -46,13 +46,18 @@ constexpr int kComposeBlocks = 4;
 // device table whose length comes from a device-driven step's state.
 // Each submap has its coefficient record and, optionally, its map-form
 // record (form(s) != NULL: evaluated as quadratic forms).
+// A submap with a form record may also have the low floats of its
+// float-float split (the Jacobian pushes then load them instead of
+// extracting them from the doubles on the integer pipe).
 struct SubmapPtrs {
   const double* p[CMM_MAX_SUBMAPS];
   const double* f[CMM_MAX_SUBMAPS];
+  const float* g[CMM_MAX_SUBMAPS];
   int S;
   __device__ __forceinline__ int count() const { return S; }
   __device__ __forceinline__ const double* at(int s, int) const { return p[s]; }
   __device__ __forceinline__ const double* form(int s, int) const { return f[s]; }
+  __device__ __forceinline__ const float* form_ff(int s, int) const { return g[s]; }
 };
 struct DevSubmaps {
   const double* const* tab;
@@ -64,6 +69,7 @@ struct DevSubmaps {
   __device__ __forceinline__ const double* form(int s, int S) const {
     return ftab && s < S - 1 ? ftab[s] : nullptr;
   }
+  __device__ __forceinline__ const float* form_ff(int, int) const { return nullptr; }
 };
 
 // Orthonormal tangent basis (t1, t2) at the unit point p, in float-float
@@ -335,6 +341,24 @@ __global__ void __launch_bounds__(128) remap_forms_kernel(MeshView m, const BveS
   if (idx < 6LL * m.nt) assemble_form(m, table[slot], ftable[slot], idx);
 }
 
+// Low floats of the form records' float-float split: one thread per
+// (triangle, sub-triangle, component), the low floats of ff_of of the six
+// entries of Q, the cross terms halved (exact), written as three float2
+// (padding floats zeroed).
+__global__ void __launch_bounds__(128) forms_ff_kernel(int nt, const double* __restrict__ forms,
+                                                       float* __restrict__ out) {
+  const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (idx >= 18LL * nt) return;
+  const int t = (int)(idx / 18), sc = (int)(idx % 18);   // sc = 3 sub + c
+  const double* q = forms + (int64_t)t * kFormStride + 6 * sc;
+  float2* o = reinterpret_cast<float2*>(out + (int64_t)t * kFormFFStride + 6 * sc);
+  o[0] = make_float2(ff_of(q[0]).l, ff_of(q[1]).l);
+  o[1] = make_float2(ff_of(q[2]).l, 0.5f * ff_of(q[3]).l);
+  o[2] = make_float2(0.5f * ff_of(q[4]).l, 0.5f * ff_of(q[5]).l);
+  if (sc == 0)
+    for (int k = 108; k < kFormFFStride; ++k) out[(int64_t)t * kFormFFStride + k] = 0.f;
+}
+
 __global__ void to_f32_kernel(const double* __restrict__ a, int64_t n, float* __restrict__ b) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i < n) b[i] = (float)a[i];
@@ -344,8 +368,9 @@ __global__ void to_f32_kernel(const double* __restrict__ a, int64_t n, float* __
 // cell, cmm_query_order) so that neighbouring threads gather neighbouring
 // records; every query's own arithmetic and output slot are unchanged.
 // MINB: resident 256-thread blocks per SM the register allocation must
-// allow (the register budget; cmm_mesh_set_variant).
-template <bool JAC, class Src, int MINB>
+// allow (the register budget; cmm_mesh_set_variant).  FF: every submap
+// with a form record also has the low floats of its float-float split.
+template <bool JAC, class Src, int MINB, bool FF = false>
 __global__ void __launch_bounds__(kBlock, MINB) compose_kernel(MeshView m, Src cp,
                                                          const double* __restrict__ q, int64_t n,
                                                          double* __restrict__ out,
@@ -409,13 +434,32 @@ __global__ void __launch_bounds__(kBlock, MINB) compose_kernel(MeshView m, Src c
         if (JAC) {
           const ff u0 = ff_of(p[0]), u1 = ff_of(p[1]), u2 = ff_of(p[2]);
           const ff a0 = w.get(0), a1 = w.get(1), a2 = w.get(2), c0 = w.get(3), c1 = w.get(4), c2 = w.get(5);
+          const float2* qg =
+              FF ? reinterpret_cast<const float2*>(cp.form_ff(s, S) + (int64_t)t * kFormFFStride +
+                                                   18 * kSubIndex[sp.lo][sp.hi])
+                 : nullptr;
 #pragma unroll
           for (int c = 0; c < 3; ++c) {
             const double2 q01 = __ldg(qf + 3 * c), q23 = __ldg(qf + 3 * c + 1), q45 = __ldg(qf + 3 * c + 2);
             P[c] = q01.x * xx + q01.y * yy + q23.x * zz + q23.y * xy + q45.x * xz + q45.y * yz;
-            const ff Q00 = ff_of(q01.x), Q11 = ff_of(q01.y), Q22 = ff_of(q23.x);
-            const ff h01 = ff_of(q23.y), h02 = ff_of(q45.x), h12 = ff_of(q45.y);
-            const ff Q01{0.5f * h01.h, 0.5f * h01.l}, Q02{0.5f * h02.h, 0.5f * h02.l}, Q12{0.5f * h12.h, 0.5f * h12.l};
+            ff Q00, Q11, Q22, Q01, Q02, Q12;
+            if (FF) {   // the stored low floats; the high floats from the doubles' bits
+              const float2 ga = __ldg(qg + 3 * c), gb = __ldg(qg + 3 * c + 1), gc = __ldg(qg + 3 * c + 2);
+              Q00 = ff{ff_hi(q01.x), ga.x};
+              Q11 = ff{ff_hi(q01.y), ga.y};
+              Q22 = ff{ff_hi(q23.x), gb.x};
+              Q01 = ff{0.5f * ff_hi(q23.y), gb.y};
+              Q02 = ff{0.5f * ff_hi(q45.x), gc.x};
+              Q12 = ff{0.5f * ff_hi(q45.y), gc.y};
+            } else {   // the same pairs converted here
+              Q00 = ff_of(q01.x);
+              Q11 = ff_of(q01.y);
+              Q22 = ff_of(q23.x);
+              const ff h01 = ff_of(q23.y), h02 = ff_of(q45.x), h12 = ff_of(q45.y);
+              Q01 = ff{0.5f * h01.h, 0.5f * h01.l};
+              Q02 = ff{0.5f * h02.h, 0.5f * h02.l};
+              Q12 = ff{0.5f * h12.h, 0.5f * h12.l};
+            }
             const ff g0 = ff_dot3(Q00, u0, Q01, u1, Q02, u2);
             const ff g1 = ff_dot3(Q01, u0, Q11, u1, Q12, u2);
             const ff g2 = ff_dot3(Q02, u0, Q12, u1, Q22, u2);
@@ -748,22 +792,34 @@ int launch_assemble(const MeshView& m, const double* jets, int ncomp, double* co
 
 int launch_compose(const MeshView& m, const double* const* coeffs, int S, const double* q,
                    int64_t n, double* out, int32_t* tri, int32_t* tri_all, double* jac,
-                   cudaStream_t s, const int32_t* perm, const double* const* forms) {
+                   cudaStream_t s, const int32_t* perm, const double* const* forms,
+                   const float* const* forms_ff) {
   if (n == 0) return CMM_OK;
   SubmapPtrs cp;
   cp.S = S;
+  // the float-float copies are used when every submap with a form record
+  // has one
+  bool ff = forms_ff != nullptr;
   for (int k = 0; k < S; ++k) {
     cp.p[k] = coeffs[k];
     cp.f[k] = forms ? forms[k] : nullptr;
+    cp.g[k] = forms && forms[k] && forms_ff ? forms_ff[k] : nullptr;
+    if (cp.f[k] && !cp.g[k]) ff = false;
   }
   const int b = block_for(m, kTuneCompose, kBlock, n);
   const int g = grid_for(n, b);
   if (jac) {
     const int v = m.variant[CMM_VARIANT_COMPOSE_JAC] ? m.variant[CMM_VARIANT_COMPOSE_JAC] : kComposeJacBlocks;
-    if (v == 2)
+    if (v == 2 && ff)
+      compose_kernel<true, SubmapPtrs, 2, true><<<g, b, 0, s>>>(m, cp, q, n, out, tri, tri_all, jac, perm);
+    else if (v == 2)
       compose_kernel<true, SubmapPtrs, 2><<<g, b, 0, s>>>(m, cp, q, n, out, tri, tri_all, jac, perm);
+    else if (v == 3 && ff)
+      compose_kernel<true, SubmapPtrs, 3, true><<<g, b, 0, s>>>(m, cp, q, n, out, tri, tri_all, jac, perm);
     else if (v == 3)
       compose_kernel<true, SubmapPtrs, 3><<<g, b, 0, s>>>(m, cp, q, n, out, tri, tri_all, jac, perm);
+    else if (ff)
+      compose_kernel<true, SubmapPtrs, 4, true><<<g, b, 0, s>>>(m, cp, q, n, out, tri, tri_all, jac, perm);
     else
       compose_kernel<true, SubmapPtrs, 4><<<g, b, 0, s>>>(m, cp, q, n, out, tri, tri_all, jac, perm);
   } else if ((m.variant[CMM_VARIANT_COMPOSE] ? m.variant[CMM_VARIANT_COMPOSE] : kComposeBlocks) == 4) {
@@ -778,6 +834,12 @@ int launch_assemble_forms(const MeshView& m, const double* coeffs, double* forms
   const int64_t n = 6LL * m.nt;
   assemble_forms_kernel<<<(int)((n + 127) / 128), 128, 0, s>>>(m, coeffs, forms);
   return check_launch("assemble_forms_kernel");
+}
+
+int launch_forms_ff(const MeshView& m, const double* forms, float* forms_ff, cudaStream_t s) {
+  const int64_t n = 18LL * m.nt;
+  forms_ff_kernel<<<(int)((n + 127) / 128), 128, 0, s>>>(m.nt, forms, forms_ff);
+  return check_launch("forms_ff_kernel");
 }
 
 int launch_remap_forms(const MeshView& m, const BveState* st, int n_maps, int Nt, const double* const* table,

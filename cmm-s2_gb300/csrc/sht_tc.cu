@@ -449,17 +449,20 @@ __global__ void __launch_bounds__(kThreads, 1) synth_tc_kernel(TcGeometry g, int
 }
 
 // ------------------------------------------ synthesis, warp-specialised
-// The same contraction with the work item's chunks accumulated in tensor
-// memory (FP32) and drained once per item, by three roles that run
-// concurrently: warp 4 streams the chunks' tiles into a two-stage ring of
-// shared memory (bulk copies), warp 5 issues each chunk's MMAs into the
-// item's accumulator pair as soon as its tiles have landed, and warps 0-3
-// (whose lanes are the 128 TMEM lanes, one ring pair each) drain an
-// item's accumulators and write its spectra while the next item's chunks
-// are multiplied into the other pair.  Stage and accumulator hand-offs go
+// The same contraction and the same arithmetic as synth_tc_kernel (each
+// 64-degree chunk's products accumulated in FP32 in tensor memory, the
+// chunk partials summed in compensated FP32 registers), by three roles
+// that run concurrently: warp 4 streams the chunks' tiles into a
+// two-stage ring of shared memory (bulk copies), warp 5 issues each
+// chunk's MMAs into one of two accumulator pairs as soon as its tiles have
+// landed, and warps 0-3 (whose lanes are the 128 TMEM lanes, one ring pair
+// each) add each chunk's partials into their compensated sums while the
+// next chunk is multiplied into the other pair, writing a work item's
+// spectra after its last chunk.  Stage and accumulator hand-offs go
 // through mbarriers (copies complete `full`, MMA commits complete `empty`
 // and `acc_full`, the four drain warps complete `acc_empty`); every wait
-// is bounded and a timeout in any role stops all three.
+// is bounded and a timeout in any role stops all three.  The results are
+// bitwise those of synth_tc_kernel.
 constexpr int kSynWarps2 = 6;
 constexpr int kSynStages2 = 2;
 
@@ -470,21 +473,6 @@ __device__ __forceinline__ bool wait_or_abort(uint64_t* bar, uint32_t parity, vo
   }
   *abort = 1;
   return false;
-}
-
-__device__ __forceinline__ void syn_mma_acc(uint32_t stage, uint32_t d, uint32_t idesc, bool first) {
-  const uint32_t p0 = stage, a0 = stage + kPRecord;
-  for (int ks = 0; ks < kKc / 16; ++ks)
-    for (int par = 0; par < 2; ++par) {
-      const uint64_t ph = smem_desc(p0 + (2 * par) * kPTile + ks * 256);
-      const uint64_t pl = smem_desc(p0 + (2 * par + 1) * kPTile + ks * 256);
-      const uint64_t ah = smem_desc(a0 + (2 * par) * kATile + ks * 256);
-      const uint64_t al = smem_desc(a0 + (2 * par + 1) * kATile + ks * 256);
-      const uint32_t dd = d + par * kN;
-      mma_bf16(dd, ph, ah, idesc, (first && ks == 0) ? 0u : 1u);
-      mma_bf16(dd, ph, al, idesc, 1u);
-      mma_bf16(dd, pl, ah, idesc, 1u);
-    }
 }
 
 __global__ void __launch_bounds__(32 * kSynWarps2, 1) synth_tc2_kernel(TcGeometry g, int nitems,
@@ -544,29 +532,24 @@ __global__ void __launch_bounds__(32 * kSynWarps2, 1) synth_tc2_kernel(TcGeometr
       if (!drained) drain_fail_s = 1;
     }
   } else if (warp == 5 && lane == 0) {
-    // MMA issuer: each item's chunks into accumulator pair it & 1
+    // MMA issuer: chunk j of this CTA's stream into accumulator pair j & 1
     const uint32_t idesc = mma_idesc();
     const uint32_t s0 = smem_u32(smem);
-    long long j = 0, it = 0;
+    long long j = 0;
     bool committed = false;
-    for (int item = blockIdx.x; item < nitems && !abort_s; item += gridDim.x, ++it) {
-      const int a = (int)(it & 1);
-      if (it >= 2 && !wait_or_abort(&acc_empty[a], (uint32_t)((it / 2 - 1) & 1), &abort_s)) break;
-      const int nch = nchunks(L, item / g.nrb);
-      bool ok = true;
-      for (int c = 0; c < nch; ++c, ++j) {
-        const int st = (int)(j % kSynStages2);
-        if (!wait_or_abort(&full[st], (uint32_t)((j / kSynStages2) & 1), &abort_s)) {
-          ok = false;
-          break;
-        }
-        tc_fence_after();
-        syn_mma_acc(s0 + st * kSynStage, tmem + a * 2 * kN, idesc, c == 0);
-        mma_commit(&empty[st]);
-        committed = true;
-      }
-      if (!ok) break;
+    SynCursor u;
+    bool ok = syn_set(u, blockIdx.x, nitems, g);
+    while (ok && !abort_s) {
+      const int a = (int)(j & 1), st = (int)(j % kSynStages2);
+      if (j >= 2 && !wait_or_abort(&acc_empty[a], (uint32_t)(((j >> 1) - 1) & 1), &abort_s)) break;
+      if (!wait_or_abort(&full[st], (uint32_t)((j / kSynStages2) & 1), &abort_s)) break;
+      tc_fence_after();
+      syn_mma(s0 + st * kSynStage, tmem + a * 2 * kN, idesc);
+      mma_commit(&empty[st]);
       mma_commit(&acc_full[a]);
+      committed = true;
+      ++j;
+      ok = syn_next(u, nitems, g);
     }
     // products still in flight complete before the tensor memory is
     // released: the last commit's barrier (bounded)
@@ -575,12 +558,16 @@ __global__ void __launch_bounds__(32 * kSynWarps2, 1) synth_tc2_kernel(TcGeometr
       if (!mbar_wait(&empty[jl % kSynStages2], (uint32_t)((jl / kSynStages2) & 1))) drain_fail_s = 1;
     }
   } else if (warp < 4) {
-    // drain: accumulators -> spectra of the item's ring pairs (TMEM lane =
-    // thread index = ring row of the block)
-    long long it = 0;
-    for (int item = blockIdx.x; item < nitems; item += gridDim.x, ++it) {
-      const int a = (int)(it & 1);
-      if (!wait_or_abort(&acc_full[a], (uint32_t)((it / 2) & 1), &abort_s)) break;
+    // drain: each chunk's partials into the compensated sums of the ring
+    // pair (TMEM lane = thread index = ring row of the block), the spectra
+    // after the item's last chunk
+    KahanF accE[kNUsed], accO[kNUsed];
+    long long j = 0;
+    SynCursor dr;
+    bool have = syn_set(dr, blockIdx.x, nitems, g);
+    while (have) {
+      const int a = (int)(j & 1);
+      if (!wait_or_abort(&acc_full[a], (uint32_t)((j >> 1) & 1), &abort_s)) break;
       tc_fence_after();
       float vE[32], vO[32];
       const uint32_t lanes = (uint32_t)(32 * warp) << 16;
@@ -590,18 +577,29 @@ __global__ void __launch_bounds__(32 * kSynWarps2, 1) synth_tc2_kernel(TcGeometr
       tc_fence_before();
       __syncwarp();
       if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&acc_empty[a])) : "memory");
-      const int m = item / g.nrb, blk = item % g.nrb;
-      const int t = blk * kM + tid;
-      if (t < g.npair) {
-        const int64_t row_len = L + 1;
 #pragma unroll
-        for (int f = 0; f < kNUsed / 2; ++f) {
-          const int64_t base = (int64_t)f * (L + 1) * row_len;
-          const float eR = vE[2 * f], eI = vE[2 * f + 1], oR = vO[2 * f], oI = vO[2 * f + 1];
-          S[base + (int64_t)t * row_len + m] = make_float2(eR + oR, eI + oI);
-          if (L - t != t) S[base + (int64_t)(L - t) * row_len + m] = make_float2(eR - oR, eI - oI);
-        }
+      for (int n = 0; n < kNUsed; ++n) {
+        accE[n].add(vE[n]);
+        accO[n].add(vO[n]);
       }
+      if (dr.c == dr.nch - 1) {   // the work item's last chunk: its spectra
+        const int t = dr.blk * kM + tid;
+        if (t < g.npair) {
+          const int64_t row_len = L + 1;
+#pragma unroll
+          for (int f = 0; f < kNUsed / 2; ++f) {
+            const int64_t base = (int64_t)f * (L + 1) * row_len;
+            const float eR = accE[2 * f].valuef(), eI = accE[2 * f + 1].valuef();
+            const float oR = accO[2 * f].valuef(), oI = accO[2 * f + 1].valuef();
+            S[base + (int64_t)t * row_len + dr.m] = make_float2(eR + oR, eI + oI);
+            if (L - t != t) S[base + (int64_t)(L - t) * row_len + dr.m] = make_float2(eR - oR, eI - oI);
+          }
+        }
+#pragma unroll
+        for (int n = 0; n < kNUsed; ++n) accE[n] = accO[n] = KahanF();
+      }
+      ++j;
+      have = syn_next(dr, nitems, g);
     }
   }
   tc_fence_before();

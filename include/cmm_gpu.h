@@ -195,13 +195,27 @@ int cmm_compose_ordered(const cmm_mesh* mesh, const double* const* coeffs, int S
  * reference.  forms: (Nt, CMM_FORM_STRIDE) doubles. */
 #define CMM_FORM_STRIDE 112
 int cmm_assemble_forms(const cmm_mesh* mesh, const double* coeffs, double* forms, void* stream);
+/* Low floats of the float-float split of form records, for the Jacobian
+ * pushes (which run in float-float): per sub-triangle and component the
+ * entries Qxx, Qyy, Qzz, Qxy, Qxz, Qyz of the symmetric matrix, each split
+ * as hi = the double truncated to 24 significand bits, lo = the next 24
+ * bits truncated (the cross terms halved, exact); lo is stored, hi is
+ * re-derived from the double.  The composition then skips most of the
+ * split's integer work; the results are bitwise the same.  Pays with the
+ * queries grouped by coarse cell (cmm_query_order); in random order the
+ * 72 more bytes gathered per evaluation cost more than they save.
+ * forms_ff: (Nt, CMM_FORM_FF_STRIDE) floats. */
+#define CMM_FORM_FF_STRIDE 112
+int cmm_forms_ff(const cmm_mesh* mesh, const double* forms, float* forms_ff, void* stream);
 /* cmm_compose / cmm_compose_ordered with map forms: forms is a HOST array
  * of S device pointers to form records (an entry may be NULL: that submap
- * is evaluated from its coefficient record) or NULL; perm may be NULL
- * (caller order).  Outputs as cmm_compose's. */
-int cmm_compose_forms(const cmm_mesh* mesh, const double* const* coeffs, const double* const* forms, int S,
-                      const double* q, int64_t n, const int32_t* perm, double* out, int32_t* tri,
-                      int32_t* tri_all, double* jac, void* stream);
+ * is evaluated from its coefficient record) or NULL; forms_ff a HOST array
+ * of S device pointers to their low floats (cmm_forms_ff; used when every
+ * submap with a form record has them) or NULL; perm may be NULL (caller
+ * order).  Outputs as cmm_compose's. */
+int cmm_compose_forms(const cmm_mesh* mesh, const double* const* coeffs, const double* const* forms,
+                      const float* const* forms_ff, int S, const double* q, int64_t n, const int32_t* perm,
+                      double* out, int32_t* tri, int32_t* tri_all, double* jac, void* stream);
 
 /* Stencil evaluation: locate each vertex foot point yn[:,v] (3,nv), then
  * evaluate the 4 stencil foot points st (3,4,nv) in that same Powell-Sabin
@@ -330,7 +344,8 @@ int cmm_sht_destroy(cmm_sht* plan);
  * cmm_sht_inverse: CMM_SHT_FP64 (default; FP64 recurrence and sums) or
  * CMM_SHT_SPLIT_BF16: each factor split into bf16 hi + lo, products
  * hi*hi + hi*lo + lo*hi on the tensor cores (tcgen05) accumulated in FP32
- * per 64-term chunk and in FP64 across chunks, for both the forward
+ * per 64-term chunk and in compensated (Kahan) FP32 sums across chunks,
+ * for both the forward
  * analysis (cmm_sht_forward, the analysis inside cmm_sht_velocity) and the
  * 12-field synthesis, whose ring FFTs then run in FP32; Pbar tables
  * (about 4.4 GB at L = 1024) are built when the mode is first selected.
@@ -340,12 +355,11 @@ int cmm_sht_destroy(cmm_sht* plan);
 #define CMM_SHT_SPLIT_BF16 1
 int cmm_sht_set_precision(cmm_sht* plan, int mode);
 /* Schedule of the split-BF16 synthesis kernel: 1 (default) warp-specialised
- * -- a copy warp, an MMA warp and four drain warps run concurrently, each
- * work item's 64-degree chunks accumulate in tensor memory (FP32) and are
- * drained once; 0 -- one role per phase, every chunk drained into
- * compensated FP32 register sums.  Both stay within the split form's
- * stated error; results differ at FP32 rounding.  No counterpart in the
- * reference. */
+ * -- a copy warp, an MMA warp and four drain warps run concurrently; 0 --
+ * the same warps take each role in turn.  Both accumulate each 64-degree
+ * chunk in FP32 in tensor memory and add the chunk partials into
+ * compensated FP32 register sums in the same order: bitwise the same
+ * results.  No counterpart in the reference. */
 int cmm_sht_set_schedule(cmm_sht* plan, int schedule);
 /* Share the Legendre tables of `src` (another plan of the same L) instead
  * of building them again; plans of one band-limit then share one copy and

@@ -379,6 +379,21 @@ def test_map_forms_match_coefficient_records(nat):
     _, Jor = OS.composite_jacobian(comp, qs)
     sc = np.abs(Jor).max(axis=(1, 2))[:, None, None]
     np.testing.assert_allclose(host(Jf)[:4096] / sc, Jor / sc, rtol=0, atol=1e-10)
+    # the low floats of the forms' float-float split (cmm_forms_ff): the
+    # Jacobian pushes load the same floats they would extract, so every
+    # output is bitwise the one without them, in both orders and in a
+    # mixed stack
+    gs = [m.forms_ff(f) for f in fs]
+    assert gs[0].shape == (m.nt, nat.Mesh.FORM_FF_STRIDE) and gs[0].dtype == torch.float32
+    assert bool((gs[0][:, 108:] == 0).all())
+    Xg, tg, tag, Jg = m.compose(cs, q, want_tri=True, want_tri_all=True, want_jac=True, forms=fs, forms_ff=gs)
+    assert torch.equal(Xg, Xf) and torch.equal(tg, tf) and torch.equal(tag, taf) and torch.equal(Jg, Jf)
+    Xgo, _, _, Jgo = m.compose(cs, q, want_jac=True, forms=fs, forms_ff=gs, perm=perm)
+    assert torch.equal(Xgo, Xf) and torch.equal(Jgo, Jf)
+    mixed = [fs[0], None, fs[2], None, None, fs[5], fs[6], None]
+    Xgm, _, _, Jgm = m.compose(cs, q, want_jac=True, forms=mixed,
+                               forms_ff=[gs[0], None, gs[2], None, None, None, gs[6], None])
+    assert torch.equal(Xgm, Xm) and torch.equal(Jgm, Jm)
     # non-finite queries through the forms path
     qn = q[:64].clone()
     qn[3, 1] = float("nan")

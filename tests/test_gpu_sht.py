@@ -151,8 +151,8 @@ def test_split_bf16_synthesis_against_fp64(nat, L, schedule):
     FP64 path, up to the band-limit of the large configuration.  Measured
     5.0e-6..5.8e-6 of max |fp64| per field; asserted below 2e-5 (each split
     factor carries ~2^-17 relative error).  Both synthesis schedules: per
-    chunk drained into compensated sums (0), and warp-specialised with the
-    chunks accumulated in tensor memory (1)."""
+    chunk drained into compensated sums by the same warps (0), and
+    warp-specialised (1), where copy, MMA and drain warps run concurrently."""
     rng = np.random.default_rng(L)
     a = np.zeros((12, L, L), dtype=complex)
     for f in range(12):
@@ -167,6 +167,26 @@ def test_split_bf16_synthesis_against_fp64(nat, L, schedule):
     print(f"L={L} schedule {schedule}: split-BF16 synthesis relative error per field max {err.max():.3e}")
     assert err.max() < 2e-5
     assert err.max() > 1e-9   # the tensor-core path really ran (not FP64)
+
+
+@pytest.mark.parametrize("L", [128, 1024])
+def test_split_bf16_synthesis_schedules_bitwise_equal(nat, L):
+    """Both synthesis schedules issue the same products per 64-degree chunk
+    and add the chunk partials into the same compensated FP32 sums in the
+    same order: their spectra, and so the synthesised fields, are bitwise
+    equal."""
+    rng = np.random.default_rng(7 + L)
+    a = np.zeros((12, L, L), dtype=complex)
+    for f in range(12):
+        c = np.tril(rng.standard_normal((L, L)) + 1j * rng.standard_normal((L, L)))
+        c[:, 0] = c[:, 0].real
+        a[f] = mhalf(c / (1 + np.arange(L))[:, None])
+    outs = []
+    for schedule in (0, 1):
+        tc = nat.Sht(L).set_schedule(schedule).set_precision(nat.Sht.SPLIT_BF16)
+        outs.append(tc.inverse(dev(a)))
+        assert tc.status() == 0
+    assert torch.equal(outs[0], outs[1])
 
 
 @pytest.mark.parametrize("L", [33, 128, 256])
