@@ -11,9 +11,11 @@
 //   * Dekker's exact product (Dekker 1971, "A floating-point technique for
 //     extending the available precision") in its FMA form:
 //     p = fl(a b), e = fma(a, b, -p), a b = p + e exactly.
-// Every rounding step of a transformation is written with the _rn
-// intrinsics, which the compiler neither contracts into FMAs nor
-// reassociates; the error terms themselves are plain float expressions.
+// Every operation is written as an _rn intrinsic or an explicit fmaf, which
+// the compiler neither contracts nor reassociates: each kernel that
+// inlines these functions computes bitwise the same values, whatever code
+// surrounds them (a plain a * b + c may or may not become an FMA,
+// depending on the instruction schedule of each instantiation).
 #pragma once
 #include <cuda_runtime.h>
 
@@ -51,7 +53,7 @@ __device__ __forceinline__ ff ff_of(double x) {
     const bool nan_x = e == 2047u && ((mag & 0xfffffu) | lw) != 0u;
     fh = nan_x ? 0x7fc00000u : 0x7f800000u;
   } else if (r != 0u && e >= 950u) {
-    lo = __uint2float_rz(r) * __uint_as_float((e - 948u) << 23);
+    lo = __fmul_rn(__uint2float_rz(r), __uint_as_float((e - 948u) << 23));
   }
   return ff{__uint_as_float(sgn | fh), sgn ? -lo : lo};
 }
@@ -76,35 +78,45 @@ __device__ __forceinline__ ff ff_neg(ff a) { return ff{-a.h, -a.l}; }
 __device__ __forceinline__ ff ff_add(ff a, ff b) {
   const ff s = two_sum(a.h, b.h);
   const ff t = two_sum(a.l, b.l);
-  return two_sum(s.h, s.l + t.h + t.l);
+  return two_sum(s.h, __fadd_rn(__fadd_rn(s.l, t.h), t.l));
 }
 
 __device__ __forceinline__ ff ff_sub(ff a, ff b) { return ff_add(a, ff_neg(b)); }
 
 __device__ __forceinline__ ff ff_mul(ff a, ff b) {
   const float p = __fmul_rn(a.h, b.h);
-  const float e = fmaf(a.h, b.h, -p) + (a.h * b.l + a.l * b.h);
+  // the exact error of the leading product, then the cross terms by FMA
+  const float e = fmaf(a.h, b.l, fmaf(a.l, b.h, fmaf(a.h, b.h, -p)));
   return two_sum(p, e);
 }
 
 // a0 b0 + a1 b1 + a2 b2: the three leading products summed by TwoSum, every
-// rounding error and cross term collected in one float correction.
+// rounding error and cross term collected in one float correction (the
+// products' exact errors summed, then the cross terms by FMA).
 __device__ __forceinline__ ff ff_dot3(ff a0, ff b0, ff a1, ff b1, ff a2, ff b2) {
   const float p0 = __fmul_rn(a0.h, b0.h), p1 = __fmul_rn(a1.h, b1.h), p2 = __fmul_rn(a2.h, b2.h);
-  float e = fmaf(a0.h, b0.h, -p0) + fmaf(a1.h, b1.h, -p1) + fmaf(a2.h, b2.h, -p2);
-  e += a0.h * b0.l + a0.l * b0.h + a1.h * b1.l + a1.l * b1.h + a2.h * b2.l + a2.l * b2.h;
+  float e = __fadd_rn(__fadd_rn(fmaf(a0.h, b0.h, -p0), fmaf(a1.h, b1.h, -p1)), fmaf(a2.h, b2.h, -p2));
+  e = fmaf(a0.h, b0.l, e);
+  e = fmaf(a0.l, b0.h, e);
+  e = fmaf(a1.h, b1.l, e);
+  e = fmaf(a1.l, b1.h, e);
+  e = fmaf(a2.h, b2.l, e);
+  e = fmaf(a2.l, b2.h, e);
   const ff s = two_sum(p0, p1);
   const ff t = two_sum(s.h, p2);
-  return two_sum(t.h, e + s.l + t.l);
+  return two_sum(t.h, __fadd_rn(__fadd_rn(e, s.l), t.l));
 }
 
 // a0 b0 + a1 b1, as ff_dot3
 __device__ __forceinline__ ff ff_dot2(ff a0, ff b0, ff a1, ff b1) {
   const float p0 = __fmul_rn(a0.h, b0.h), p1 = __fmul_rn(a1.h, b1.h);
-  float e = fmaf(a0.h, b0.h, -p0) + fmaf(a1.h, b1.h, -p1);
-  e += a0.h * b0.l + a0.l * b0.h + a1.h * b1.l + a1.l * b1.h;
+  float e = __fadd_rn(fmaf(a0.h, b0.h, -p0), fmaf(a1.h, b1.h, -p1));
+  e = fmaf(a0.h, b0.l, e);
+  e = fmaf(a0.l, b0.h, e);
+  e = fmaf(a1.h, b1.l, e);
+  e = fmaf(a1.l, b1.h, e);
   const ff s = two_sum(p0, p1);
-  return two_sum(s.h, e + s.l);
+  return two_sum(s.h, __fadd_rn(e, s.l));
 }
 
 // 1/sqrt(a) for a > 0: the FP32 value 1/sqrt(a.h) (relative error below
@@ -116,7 +128,7 @@ __device__ __forceinline__ ff ff_rsqrt(ff a) {
 #pragma unroll
   for (int k = 0; k < 2; ++k) {
     const ff res = ff_sub(ff{1.f, 0.f}, ff_mul(a, ff_mul(r, r)));
-    r = ff_add(r, ff{0.5f * r.h * (res.h + res.l), 0.f});
+    r = ff_add(r, ff{__fmul_rn(__fmul_rn(0.5f, r.h), __fadd_rn(res.h, res.l)), 0.f});
   }
   return r;
 }

@@ -353,8 +353,8 @@ __global__ void __launch_bounds__(128) forms_ff_kernel(int nt, const double* __r
   const double* q = forms + (int64_t)t * kFormStride + 6 * sc;
   float2* o = reinterpret_cast<float2*>(out + (int64_t)t * kFormFFStride + 6 * sc);
   o[0] = make_float2(ff_of(q[0]).l, ff_of(q[1]).l);
-  o[1] = make_float2(ff_of(q[2]).l, 0.5f * ff_of(q[3]).l);
-  o[2] = make_float2(0.5f * ff_of(q[4]).l, 0.5f * ff_of(q[5]).l);
+  o[1] = make_float2(ff_of(q[2]).l, __fmul_rn(0.5f, ff_of(q[3]).l));
+  o[2] = make_float2(__fmul_rn(0.5f, ff_of(q[4]).l), __fmul_rn(0.5f, ff_of(q[5]).l));
   if (sc == 0)
     for (int k = 108; k < kFormFFStride; ++k) out[(int64_t)t * kFormFFStride + k] = 0.f;
 }
@@ -448,17 +448,17 @@ __global__ void __launch_bounds__(kBlock, MINB) compose_kernel(MeshView m, Src c
               Q00 = ff{ff_hi(q01.x), ga.x};
               Q11 = ff{ff_hi(q01.y), ga.y};
               Q22 = ff{ff_hi(q23.x), gb.x};
-              Q01 = ff{0.5f * ff_hi(q23.y), gb.y};
-              Q02 = ff{0.5f * ff_hi(q45.x), gc.x};
-              Q12 = ff{0.5f * ff_hi(q45.y), gc.y};
+              Q01 = ff{__fmul_rn(0.5f, ff_hi(q23.y)), gb.y};
+              Q02 = ff{__fmul_rn(0.5f, ff_hi(q45.x)), gc.x};
+              Q12 = ff{__fmul_rn(0.5f, ff_hi(q45.y)), gc.y};
             } else {   // the same pairs converted here
               Q00 = ff_of(q01.x);
               Q11 = ff_of(q01.y);
               Q22 = ff_of(q23.x);
               const ff h01 = ff_of(q23.y), h02 = ff_of(q45.x), h12 = ff_of(q45.y);
-              Q01 = ff{0.5f * h01.h, 0.5f * h01.l};
-              Q02 = ff{0.5f * h02.h, 0.5f * h02.l};
-              Q12 = ff{0.5f * h12.h, 0.5f * h12.l};
+              Q01 = ff{__fmul_rn(0.5f, h01.h), __fmul_rn(0.5f, h01.l)};
+              Q02 = ff{__fmul_rn(0.5f, h02.h), __fmul_rn(0.5f, h02.l)};
+              Q12 = ff{__fmul_rn(0.5f, h12.h), __fmul_rn(0.5f, h12.l)};
             }
             const ff g0 = ff_dot3(Q00, u0, Q01, u1, Q02, u2);
             const ff g1 = ff_dot3(Q01, u0, Q11, u1, Q12, u2);
