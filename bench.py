@@ -913,7 +913,9 @@ def bench_kernels(dev, level=7, L=1024, reps=5, stack=8, warm=True, nvtx=False):
     Legendre FLOPs):
       locate        2^22 uniform queries: 24 B in, 4 B id + 24 B bcc out;
       compose_grid  the MWSS sample points through `stack` submaps (no
-                    Jacobian): 48 B per point + 96 B per vertex per submap;
+                    Jacobian) as map forms (compose_grid_records: as
+                    coefficient records): 48 B per point + 96 B per vertex
+                    per submap;
       assemble_map  jets -> coefficient records: 96 B per vertex + 384 B
                     factors + 512 B record per triangle;
       assemble_vel  the same on the velocity mesh;
@@ -989,11 +991,15 @@ def bench_kernels(dev, level=7, L=1024, reps=5, stack=8, warm=True, nvtx=False):
         put("locate", timed(lambda: s.mesh.locate(q)), nbytes=(1 << 22) * 52)
         del q
         cs = [s.coeffs_cur] * stack
-        put("compose_grid", timed(lambda: s.mesh.compose(cs, s.sample_pts, out=s.X)),
+        put("compose_grid_records", timed(lambda: s.mesh.compose(cs, s.sample_pts, out=s.X)),
+            nbytes=Qg * 48 + stack * 96 * nv)
+        # through map forms, as the step composes its stack
+        fs = [s.mesh.assemble_forms(s.coeffs_cur)] * stack
+        put("compose_grid", timed(lambda: s.mesh.compose(cs, s.sample_pts, out=s.X, forms=fs)),
             nbytes=Qg * 48 + stack * 96 * nv)
         put("assemble_map", timed(lambda: s.mesh.assemble(s.jets, out=s.stack[0])),
             nbytes=nv * 96 + nt * (384 + 512))
-        del s, cs, prev, jt
+        del s, cs, fs, prev, jt
         torch.cuda.empty_cache()
     return out
 

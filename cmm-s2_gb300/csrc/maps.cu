@@ -40,6 +40,9 @@ constexpr int kBlock = 256;
 // cell order: Jacobians 12.8 / 13.6 / 13.2 ms at 4 / 3 / 2 blocks; points
 // only 7.5 ms at 4 or 6 blocks, and 10.2 against 13.5 ms in caller order)
 constexpr int kComposeJacBlocks = 4;
+// with the low floats of the forms' split loaded (fewer live values):
+// 10.83 / 11.02 / 11.59 ms at 3 / 4 / 2 blocks, same workload
+constexpr int kComposeJacBlocksFF = 3;
 constexpr int kComposeBlocks = 4;
 
 // Submap lists: by value in the kernel parameters (host calls), or a
@@ -809,7 +812,8 @@ int launch_compose(const MeshView& m, const double* const* coeffs, int S, const 
   const int b = block_for(m, kTuneCompose, kBlock, n);
   const int g = grid_for(n, b);
   if (jac) {
-    const int v = m.variant[CMM_VARIANT_COMPOSE_JAC] ? m.variant[CMM_VARIANT_COMPOSE_JAC] : kComposeJacBlocks;
+    const int v = m.variant[CMM_VARIANT_COMPOSE_JAC] ? m.variant[CMM_VARIANT_COMPOSE_JAC]
+                                                    : (ff ? kComposeJacBlocksFF : kComposeJacBlocks);
     if (v == 2 && ff)
       compose_kernel<true, SubmapPtrs, 2, true><<<g, b, 0, s>>>(m, cp, q, n, out, tri, tri_all, jac, perm);
     else if (v == 2)
