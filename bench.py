@@ -701,7 +701,7 @@ def bench_ensemble(args, dev):
     # launched once
     t1 = time.perf_counter()
     sched = ens.schedule
-    ens.capture(streams=sched["streams"], order=sched["order"], steps=n)
+    ens.capture(streams=sched["streams"], order=sched["order"], steps=n, batch=sched.get("batch", False))
     torch.cuda.synchronize()
     capture_s = time.perf_counter() - t1
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -740,6 +740,9 @@ def bench_ensemble(args, dev):
             "schedule": tuner.log["schedule"]["best"], "launch_shapes": tuner.log["kernels"],
             "compose_variants": tuner.log.get("variants"), "sht_schedule": tuner.log.get("sht_schedule"),
             "map_forms_members": sum(m.stack_forms is not None for m in ens.members),
+            # (band-limit, members) of each batched analysis
+            "analysis_batches": ([[b.plans[0].L, len(b.plans)] for b in ens.batches()[1]]
+                                 if sched.get("batch") else None),
             "status_ok": ok}
 
 

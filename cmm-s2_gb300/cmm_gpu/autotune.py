@@ -10,13 +10,15 @@ What is tuned, and what is fixed by the data:
 * the composition's register budget (cmm_mesh_set_variant: resident
   blocks 4 or 6 for points only) -- the same arithmetic compiled for
   another register count, so results do not change;
-* the synthesis schedule (cmm_sht_set_schedule: per-chunk drain into
-  compensated sums, or warp-specialised with the chunks accumulated in
-  tensor memory) -- results differ at FP32 rounding, so it is tuned only
-  when asked (tune_sht_schedule), for all plans of a band-limit at once;
-* the graph's branch count and member order.
+* the synthesis schedule (cmm_sht_set_schedule: one role per phase, or
+  warp-specialised; bitwise the same results), for all plans of a
+  band-limit at once (tune_sht_schedule);
+* the graph's branch count and member order, and whether the
+  same-band-limit members' forward analyses run batched (one tensor-core
+  launch per batch of up to 8; bitwise the same results).
 The tensor-core tiles are fixed by the data: N = 32 columns holds the
-synthesis' 24 real columns (12 complex fields; N = 16 the analysis' 2),
+synthesis' 24 real columns (12 complex fields; N = 16 the analysis' 2 per
+field, up to 8 fields when batched),
 M = 128 the TMEM lanes, and K = 64 the chunk of the Pbar table images the
 MMAs read straight from shared memory (another K needs other tables).
 
@@ -137,10 +139,12 @@ class Autotuner:
         return res
 
     # ----------------------------------------------------------- schedule
-    def tune_schedule(self, ens, stream_counts=(1, 2, 4, 8), steps_each=2):
+    def tune_schedule(self, ens, stream_counts=(1, 2, 4, 8), steps_each=2, batch=True):
         """Capture the ensemble's graph for each branch count and member
         order (as given; largest work first) and time `steps_each` replays
-        of each; keep the fastest.  Returns the timings."""
+        of each; then (batch) the best of them with the same-band-limit
+        members' analyses batched (Ensemble.capture(batch=True)); keep the
+        fastest.  Returns the timings."""
         work = [m.sample_pts.shape[0] * (1 + m.n_maps) + m.mesh.nv * 20 for m in ens.members]
         orders = {"given": list(range(len(ens.members))),
                   "largest_first": sorted(range(len(ens.members)), key=lambda i: -work[i])}
@@ -158,7 +162,25 @@ class Autotuner:
                 torch.cuda.synchronize()
                 results.append({"order": name, "streams": ns, "ms_per_step": e0.elapsed_time(e1) / steps_each})
         best = min(results, key=lambda r: r["ms_per_step"])
-        ens.capture(streams=best["streams"], order=orders[best["order"]])
+        for r in results:
+            r["batch"] = False
+        # the same-band-limit members' analyses batched (one tensor-core
+        # launch per batch), on the best unbatched schedule
+        if batch and ens.batches()[1]:
+            ens.capture(streams=best["streams"], order=orders[best["order"]], batch=True)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(steps_each):
+                ens.step()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            rb = {"order": best["order"], "streams": best["streams"], "batch": True,
+                  "ms_per_step": e0.elapsed_time(e1) / steps_each}
+            results.append(rb)
+            if rb["ms_per_step"] < best["ms_per_step"]:
+                best = rb
+        ens.capture(streams=best["streams"], order=orders[best["order"]], batch=best["batch"])
         self.log["schedule"] = {"best": best, "candidates": results}
         return self.log["schedule"]
 

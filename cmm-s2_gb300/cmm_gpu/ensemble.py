@@ -108,6 +108,7 @@ class Ensemble:
         self.graph = None
         self.schedule = None
         self.count = 0
+        self._batch_groups = None
 
     @classmethod
     def from_seed(cls, n, seed, levels=(5, 6, 7), bandlimits=(256, 512, 1024), Nt=100, T=0.5,
@@ -152,31 +153,80 @@ class Ensemble:
         torch.cuda.synchronize(self.device)
         return self
 
-    def capture(self, streams=4, order=None, steps=1):
+    def batches(self):
+        """The split-BF16 members grouped by band-limit into batches of up
+        to 8 whose forward analyses run as one tensor-core launch
+        (native.ShtBatch; a band-limit with one such member stays alone):
+        ({member index: batch}, [batches]), made once."""
+        if self._batch_groups is None:
+            byL = {}
+            for i, m in enumerate(self.members):
+                if m.precision_mode == native.Sht.SPLIT_BF16:
+                    byL.setdefault(m.L, []).append(i)
+            of, groups = {}, []
+            for L in sorted(byL):
+                idx = byL[L]
+                for k in range(0, len(idx), native.ShtBatch.MAX):
+                    grp = idx[k:k + native.ShtBatch.MAX]
+                    if len(grp) < 2:
+                        continue
+                    b = native.ShtBatch([self.members[i].sht for i in grp])
+                    groups.append(b)
+                    for i in grp:
+                        of[i] = b
+            self._batch_groups = (of, groups)
+        return self._batch_groups
+
+    def capture(self, streams=4, order=None, steps=1, batch=False):
         """`steps` steps of every member into one CUDA graph: members
         assigned round-robin (in `order`, default as given) to `streams`
         parallel branches forked from and joined into the capture stream;
         each branch runs its members' steps in order (a member's step k+1
         after its step k on the same branch; members never wait on each
         other).  Every step's state lives on the device (cmm_bve_step), so
-        the whole remaining run can be one graph: one launch."""
+        the whole remaining run can be one graph: one launch.
+        batch: the members of each analysis batch (batches()) run each step
+        in two halves (cmm_bve_step_pre / _post) around one batched
+        analysis per batch; the branches join before the analyses and
+        again before the second halves.  Same results bitwise."""
         order = list(range(len(self.members))) if order is None else list(order)
+        of, groups = self.batches() if batch else ({}, [])
         g = torch.cuda.CUDAGraph()
         side = [torch.cuda.Stream(self.device) for _ in range(streams)]
         torch.cuda.synchronize(self.device)
+
+        def join_fork(cap):
+            for st in side:
+                cap.wait_stream(st)
+            for st in side:
+                st.wait_stream(cap)
+
         with torch.cuda.graph(g):
             cap = torch.cuda.current_stream(self.device)
             for st in side:
                 st.wait_stream(cap)
             for _ in range(steps):
                 for k, i in enumerate(order):
-                    st = side[k % streams]
-                    with torch.cuda.stream(st):
-                        native.check(native.lib.cmm_bve_step(self.members[i]._bve,
-                                                             native._stream(self.device)), "cmm_bve_step")
+                    with torch.cuda.stream(side[k % streams]):
+                        fn, name = ((native.lib.cmm_bve_step_pre, "cmm_bve_step_pre") if i in of else
+                                    (native.lib.cmm_bve_step, "cmm_bve_step"))
+                        native.check(fn(self.members[i]._bve, native._stream(self.device)), name)
+                if groups:
+                    join_fork(cap)
+                    for j, b in enumerate(groups):
+                        with torch.cuda.stream(side[j % streams]):
+                            b.analysis(native._stream(self.device))
+                    join_fork(cap)
+                    for k, i in enumerate(order):
+                        if i in of:
+                            with torch.cuda.stream(side[k % streams]):
+                                native.check(native.lib.cmm_bve_step_post(self.members[i]._bve,
+                                                                          native._stream(self.device)),
+                                             "cmm_bve_step_post")
             for st in side:
                 cap.wait_stream(st)
-        self.graph, self.schedule = g, {"streams": streams, "order": order, "steps": steps}
+        self.graph = g
+        self.schedule = {"streams": streams, "order": order, "steps": steps, "batch": bool(groups)}
         return self
 
     def step(self):
@@ -192,7 +242,7 @@ class Ensemble:
         current schedule, launched once."""
         n = self.members[0].Nt - 2 - self.count if nsteps is None else nsteps
         sched = self.schedule or {"streams": 4, "order": None}
-        self.capture(streams=sched["streams"], order=sched["order"], steps=n)
+        self.capture(streams=sched["streams"], order=sched["order"], steps=n, batch=sched.get("batch", False))
         self.step()
         return self
 

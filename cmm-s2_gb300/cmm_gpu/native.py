@@ -71,6 +71,10 @@ _SIGS = {
     "cmm_sht_power": (_i, [_p, _p, _p, _p]),
     "cmm_sht_share_tables": (_i, [_p, _p]),
     "cmm_sht_trim": (_i, [_p]),
+    "cmm_sht_batch_create": (_i, [ctypes.POINTER(_p), _i, ctypes.POINTER(_p)]),
+    "cmm_sht_batch_destroy": (_i, [_p]),
+    "cmm_sht_batch_analysis": (_i, [_p, _p]),
+    "cmm_sht_batch_forward": (_i, [_p, ctypes.POINTER(_p), ctypes.POINTER(_p), _p]),
     "cmm_sht_set_tables": (_i, [_p, _i]),
     "cmm_sht_timeout_selftest": (_i, [_p, _i64, _p]),
     "cmm_velmesh_set_records": (_i, [_p, _i]),
@@ -85,6 +89,8 @@ _SIGS = {
     "cmm_bve_create": (_i, [ctypes.POINTER(BveDesc), ctypes.POINTER(_p)]),
     "cmm_bve_destroy": (_i, [_p]),
     "cmm_bve_step": (_i, [_p, _p]),
+    "cmm_bve_step_pre": (_i, [_p, _p]),
+    "cmm_bve_step_post": (_i, [_p, _p]),
     "cmm_bve_state": (_i, [_p, _p, ctypes.POINTER(_i), ctypes.POINTER(_i), ctypes.POINTER(_i)]),
     "cmm_sht_destroy": (_i, [_p]),
     "cmm_sht_forward": (_i, [_p, _p, _p, _p]),
@@ -511,6 +517,43 @@ class Sht:
         check(lib.cmm_sht_velocity(self.h, velmesh.h, _ptr(omega), _ptr(psi), _ptr(jets),
                                    _stream(omega.device)), "cmm_sht_velocity")
         return jets
+
+
+class ShtBatch:
+    """Split-BF16 plans of one band-limit whose forward analyses run as one
+    tensor-core launch (cmm_sht_batch_create); holds its plans, so they
+    outlive it."""
+    MAX = 8
+
+    def __init__(self, plans):
+        self.plans = list(plans)
+        self.device = self.plans[0].device
+        arr = (ctypes.c_void_p * len(self.plans))(*[p.h.value for p in self.plans])
+        h = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            check(lib.cmm_sht_batch_create(arr, len(self.plans), ctypes.byref(h)), "cmm_sht_batch_create")
+        self.h = h
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h is not None and h.value:
+            lib.cmm_sht_batch_destroy(h)
+            self.h = None
+
+    def analysis(self, stream=None):
+        check(lib.cmm_sht_batch_analysis(self.h, stream if stream is not None else _stream(self.device)),
+              "cmm_sht_batch_analysis")
+
+    def forward(self, samples):
+        """Forward transforms of one field per member (cmm_sht_batch_forward):
+        samples[b] (L+1, 2L) -> alm[b] (L, L) complex128."""
+        samples = [_dev(x) for x in samples]
+        L = self.plans[0].L
+        alm = [torch.zeros((L, L), dtype=torch.complex128, device=self.device) for _ in samples]
+        sa = (ctypes.c_void_p * len(samples))(*[x.data_ptr() for x in samples])
+        aa = (ctypes.c_void_p * len(alm))(*[a.data_ptr() for a in alm])
+        check(lib.cmm_sht_batch_forward(self.h, sa, aa, _stream(self.device)), "cmm_sht_batch_forward")
+        return alm
 
 
 def compose_host(mesh, coeffs, q_host, out_host, tri_host=None, jac_host=None, chunks=16,

@@ -259,6 +259,16 @@ int cmm_bve_step(cmm_bve* bve, void* stream) {
   return bve_step(bve, (cudaStream_t)stream);
 }
 
+int cmm_bve_step_pre(cmm_bve* bve, void* stream) {
+  if (!bve) return arg_error("cmm_bve_step_pre: null handle");
+  return bve_step_pre(bve, (cudaStream_t)stream);
+}
+
+int cmm_bve_step_post(cmm_bve* bve, void* stream) {
+  if (!bve) return arg_error("cmm_bve_step_post: null handle");
+  return bve_step_post(bve, (cudaStream_t)stream);
+}
+
 int cmm_bve_state(cmm_bve* bve, void* stream, int* count, int* nc, int* identity) {
   if (!bve) return arg_error("cmm_bve_state: null handle");
   return bve_state(bve, (cudaStream_t)stream, count, nc, identity);
@@ -334,6 +344,25 @@ int cmm_sht_share_tables(cmm_sht* plan, cmm_sht* src) {
 int cmm_sht_trim(cmm_sht* plan) {
   if (!plan) return arg_error("cmm_sht_trim: null plan");
   return sht_trim(plan);
+}
+
+int cmm_sht_batch_create(cmm_sht* const* plans, int n, cmm_sht_batch** out) {
+  return sht_batch_create(plans, n, out);
+}
+
+int cmm_sht_batch_destroy(cmm_sht_batch* batch) { return sht_batch_destroy(batch); }
+
+int cmm_sht_batch_analysis(cmm_sht_batch* batch, void* stream) {
+  if (!batch) return arg_error("cmm_sht_batch_analysis: null batch");
+  return sht_batch_analysis(batch, nullptr, (cudaStream_t)stream);
+}
+
+int cmm_sht_batch_forward(cmm_sht_batch* batch, const double* const* samples, double* const* alm,
+                          void* stream) {
+  if (!batch || !samples || !alm) return arg_error("cmm_sht_batch_forward: null pointer");
+  for (int b = 0; b < sht_batch_size(batch); ++b)
+    if (!samples[b] || !alm[b]) return arg_error("cmm_sht_batch_forward: null member pointer");
+  return sht_batch_forward(batch, samples, (double2* const*)alm, (cudaStream_t)stream);
 }
 
 int cmm_sht_status(cmm_sht* plan, void* stream, int* flags, int clear) {

@@ -276,6 +276,14 @@ int sht_forward(cmm_sht* p, const double* samples, double2* out, cudaStream_t s)
 int sht_inverse(cmm_sht* p, const double2* alm, int nf, double* samples, cudaStream_t s);
 int sht_velocity(cmm_sht* p, const cmm_mesh* vm, const double* omega, double2* psi_out,
                  double* jets, cudaStream_t s);
+// sht_velocity(p, vm, omega, NULL, jets) around a batch's analysis
+int sht_velocity_pre(cmm_sht* p, const double* omega, cudaStream_t s);
+int sht_velocity_post(cmm_sht* p, const cmm_mesh* vm, double* jets, cudaStream_t s);
+int sht_batch_create(cmm_sht* const* plans, int n, cmm_sht_batch** out);
+int sht_batch_destroy(cmm_sht_batch* bt);
+int sht_batch_size(const cmm_sht_batch* bt);
+int sht_batch_analysis(cmm_sht_batch* bt, double2* const* out, cudaStream_t s);
+int sht_batch_forward(cmm_sht_batch* bt, const double* const* samples, double2* const* alm, cudaStream_t s);
 int sht_scalar_jets(cmm_sht* p, const cmm_mesh* vm, const double2* alm, double* jets, cudaStream_t s);
 int sht_power(cmm_sht* p, const double2* alm, double* power, cudaStream_t s);
 int* sht_status_word(cmm_sht* p);
@@ -285,6 +293,8 @@ int sht_velocity_bwd(cmm_sht* p, const cmm_mesh* vm, const double* gjets, double
 int sht_trim(cmm_sht* p);
 int bve_create(const cmm_bve_desc* d, cmm_bve** out);
 int bve_step(cmm_bve* b, cudaStream_t s);
+int bve_step_pre(cmm_bve* b, cudaStream_t s);
+int bve_step_post(cmm_bve* b, cudaStream_t s);
 int bve_destroy(cmm_bve* b);
 int bve_state(cmm_bve* b, cudaStream_t s, int* count, int* nc, int* identity);
 int sht_set_precision(cmm_sht* p, int mode);
@@ -305,5 +315,14 @@ void tc_set_schedule(TcPlan* p, int schedule);
 int sht_set_schedule(cmm_sht* p, int schedule);
 int tc_analysis(TcPlan* p, const float2* fine, const double* w, double2* alm, int* status,
                 cudaStream_t s);
+// The analysis in two parts, for several fields of one band-limit sharing
+// each streamed Pbar tile: the data tiles of one field into column pair
+// `slot` of the 16-column tiles xtab (tc_xtab_bytes, zeroed by the owner),
+// then the contraction of n <= 8 fields (slots 0..n-1) -> alm[b].
+size_t tc_xtab_bytes(const TcPlan* p);
+int tc_analysis_tiles(TcPlan* p, const float2* fine, const double* w, unsigned char* xtab, int slot,
+                      cudaStream_t s);
+int tc_analysis_batch(TcPlan* p, const unsigned char* xtab, double2* const* alm, int n, int* status,
+                      cudaStream_t s);
 int tc_wait_timeout_probe(long long polls, int* status, cudaStream_t s);
 }  // namespace cmm

@@ -991,7 +991,25 @@ struct cmm_sht {
   // adjoint: D2Z over the 12 fields' rings, C2R over one field's rings
   cufftHandle b_ring_fwd12 = 0, b_ring_inv1 = 0;
   bool have_bplans = false;
-  ~cmm_sht() {
+  // batch membership (cmm_sht_batch_create): the batch and this plan's slot
+  cmm_sht_batch* batch = nullptr;
+  int slot = -1;
+  ~cmm_sht();
+};
+
+// Up to 8 split-BF16 plans of one band-limit whose forward analyses run as
+// one tensor-core launch: each member writes its data tiles into column
+// pair `slot` of the shared 16-column tiles (cmm_sht_batch_tiles, inside
+// cmm_bve_step_pre), then one contraction streams every Pbar tile once for
+// all members (cmm_sht_batch_analysis).
+struct cmm_sht_batch {
+  int L = 0, n = 0;
+  cmm_sht* plans[8] = {};
+  cmm::DeviceBuffer xtab;
+};
+
+cmm_sht::~cmm_sht() {
+  {
     if (have_plans[0]) cufftDestroy(ring_fwd);
     if (have_plans[1]) cufftDestroy(torus_fwd);
     if (have_plans[2]) cufftDestroy(pad_inv);
@@ -1007,8 +1025,11 @@ struct cmm_sht {
       cufftDestroy(b_ring_inv1);
     }
     if (tc) cmm::tc_plan_destroy(tc);
+    // a plan destroyed before its batch leaves an empty slot, which the
+    // batch's analysis reports as an error
+    if (batch) batch->plans[slot] = nullptr;
   }
-};
+}
 
 namespace cmm {
 
@@ -1222,26 +1243,36 @@ static int make_float_plans(cmm_sht* p) {
 }
 
 // samples (L+1, 2L) -> alm (m-major half layout) in p->alm or `out`.
+// Split-BF16 forward transform up to the Legendre stage: the samples in
+// FP32, the ring FFTs, the torus extension and the padded inverse
+// transform -> p->f_pad (the analysis' input).
+static int forward_rings_f32(cmm_sht* p, const double* samples, cudaStream_t s) {
+  const int L = p->L;
+  int rc;
+  dim3 b(128), g1((L + 127) / 128, 2 * L), g2((L + 127) / 128, 4 * L);
+  const int64_t ns = (int64_t)(L + 1) * 2 * L;
+  to_float_kernel<<<(int)((ns + 255) / 256), 256, 0, s>>>(samples, ns, (float*)p->f_in.p);
+  if ((rc = check_launch("to_float_kernel"))) return rc;
+  cufftResult r = cufftExecR2C(p->f_ring_fwd, (cufftReal*)p->f_in.p, (cufftComplex*)p->f_spec.p);
+  if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExecR2C");
+  torus_kernel<float2><<<g1, b, 0, s>>>((const float2*)p->f_spec.p, L, (float2*)p->f_torus.p);
+  if ((rc = check_launch("torus_kernel"))) return rc;
+  r = cufftExecC2C(p->f_torus_fwd, (cufftComplex*)p->f_torus.p, (cufftComplex*)p->f_torus.p, CUFFT_FORWARD);
+  if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExecC2C(torus)");
+  pad_kernel<float2><<<g2, b, 0, s>>>((const float2*)p->f_torus.p, L, (float2*)p->f_pad.p);
+  if ((rc = check_launch("pad_kernel"))) return rc;
+  r = cufftExecC2C(p->f_pad_inv, (cufftComplex*)p->f_pad.p, (cufftComplex*)p->f_pad.p, CUFFT_INVERSE);
+  if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExecC2C(pad)");
+  return CMM_OK;
+}
+
 int sht_forward(cmm_sht* p, const double* samples, double2* out, cudaStream_t s) {
   const int L = p->L;
   int rc = set_streams(p, s);
   if (rc) return rc;
-  dim3 b(128), g1((L + 127) / 128, 2 * L), g2((L + 127) / 128, 4 * L);
+  dim3 b(128), g1((L + 127) / 128, 2 * L);
   if (p->precision == CMM_SHT_SPLIT_BF16) {
-    // ring FFTs in FP32, Legendre analysis on the tensor cores
-    const int64_t ns = (int64_t)(L + 1) * 2 * L;
-    to_float_kernel<<<(int)((ns + 255) / 256), 256, 0, s>>>(samples, ns, (float*)p->f_in.p);
-    if ((rc = check_launch("to_float_kernel"))) return rc;
-    cufftResult r = cufftExecR2C(p->f_ring_fwd, (cufftReal*)p->f_in.p, (cufftComplex*)p->f_spec.p);
-    if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExecR2C");
-    torus_kernel<float2><<<g1, b, 0, s>>>((const float2*)p->f_spec.p, L, (float2*)p->f_torus.p);
-    if ((rc = check_launch("torus_kernel"))) return rc;
-    r = cufftExecC2C(p->f_torus_fwd, (cufftComplex*)p->f_torus.p, (cufftComplex*)p->f_torus.p, CUFFT_FORWARD);
-    if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExecC2C(torus)");
-    pad_kernel<float2><<<g2, b, 0, s>>>((const float2*)p->f_torus.p, L, (float2*)p->f_pad.p);
-    if ((rc = check_launch("pad_kernel"))) return rc;
-    r = cufftExecC2C(p->f_pad_inv, (cufftComplex*)p->f_pad.p, (cufftComplex*)p->f_pad.p, CUFFT_INVERSE);
-    if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExecC2C(pad)");
+    if ((rc = forward_rings_f32(p, samples, s))) return rc;
     return tc_analysis(p->tc, (const float2*)p->f_pad.p, (const double*)p->w_fine.p, out,
                        (int*)p->status.p, s);
   }
@@ -1339,6 +1370,11 @@ int sht_inverse(cmm_sht* p, const double2* alm, int nf, double* samples, cudaStr
   return CMM_OK;
 }
 
+// The stream function's 12 velocity/jet fields, their synthesis and the
+// jets at the velocity mesh's vertices.
+static int velocity_from_psi(cmm_sht* p, const cmm_mesh* vm, const double2* psi, double* jets,
+                             cudaStream_t s);
+
 int sht_velocity(cmm_sht* p, const cmm_mesh* vm, const double* omega, double2* psi_out,
                  double* jets, cudaStream_t s) {
   const int L = p->L;
@@ -1356,6 +1392,129 @@ int sht_velocity(cmm_sht* p, const cmm_mesh* vm, const double* omega, double2* p
   } else {
     psi = psi_out;  // stream function given by the caller
   }
+  return velocity_from_psi(p, vm, psi, jets, s);
+}
+
+// Batched form of sht_velocity(p, vm, omega, NULL, jets): the forward
+// transform up to the member's data tiles in its batch slot ...
+int sht_velocity_pre(cmm_sht* p, const double* omega, cudaStream_t s) {
+  if (!p->batch || p->precision != CMM_SHT_SPLIT_BF16 || !p->tc) {
+    set_last_error("sht velocity (batched): a split-BF16 plan in a batch expected");
+    return CMM_ERR_ARG;
+  }
+  int rc = set_streams(p, s);
+  if (rc) return rc;
+  if ((rc = forward_rings_f32(p, omega, s))) return rc;
+  return tc_analysis_tiles(p->tc, (const float2*)p->f_pad.p, (const double*)p->w_fine.p,
+                           (unsigned char*)p->batch->xtab.p, p->slot, s);
+}
+
+// ... and after the batch's analysis (which wrote p->alm), the rest.
+int sht_velocity_post(cmm_sht* p, const cmm_mesh* vm, double* jets, cudaStream_t s) {
+  const int L = p->L;
+  int rc = set_streams(p, s);
+  if (rc) return rc;
+  double2* psi = (double2*)p->alm.p;
+  dinv_kernel<<<dim3((L + 127) / 128, L), 128, 0, s>>>(psi, L);
+  if ((rc = check_launch("dinv_kernel"))) return rc;
+  return velocity_from_psi(p, vm, psi, jets, s);
+}
+
+int sht_batch_create(cmm_sht* const* plans, int n, cmm_sht_batch** out) {
+  if (!plans || !out || n < 1 || n > 8) {
+    set_last_error("cmm_sht_batch_create: 1 to 8 plans expected");
+    return CMM_ERR_ARG;
+  }
+  for (int b = 0; b < n; ++b) {
+    cmm_sht* p = plans[b];
+    if (!p || p->L != plans[0]->L || p->precision != CMM_SHT_SPLIT_BF16 || !p->tc || p->batch) {
+      set_last_error("cmm_sht_batch_create: distinct split-BF16 plans of one band-limit, in no other batch, "
+                     "expected");
+      return CMM_ERR_ARG;
+    }
+    for (int c = 0; c < b; ++c)
+      if (plans[c] == p) {
+        set_last_error("cmm_sht_batch_create: a plan appears twice");
+        return CMM_ERR_ARG;
+      }
+  }
+  cmm_sht_batch* bt = new (std::nothrow) cmm_sht_batch();
+  if (!bt) {
+    set_last_error("cmm_sht_batch_create: out of host memory");
+    return CMM_ERR_NOMEM;
+  }
+  bt->L = plans[0]->L;
+  bt->n = n;
+  int rc = bt->xtab.alloc(tc_xtab_bytes(plans[0]->tc));
+  if (rc) {
+    delete bt;
+    return rc;
+  }
+  cudaError_t e = cudaMemset(bt->xtab.p, 0, bt->xtab.bytes);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) {
+    delete bt;
+    return cuda_fail(e, "cmm_sht_batch_create");
+  }
+  for (int b = 0; b < n; ++b) {
+    bt->plans[b] = plans[b];
+    plans[b]->batch = bt;
+    plans[b]->slot = b;
+  }
+  *out = bt;
+  return CMM_OK;
+}
+
+int sht_batch_size(const cmm_sht_batch* bt) { return bt->n; }
+
+int sht_batch_destroy(cmm_sht_batch* bt) {
+  if (!bt) return CMM_OK;
+  cudaError_t e = cudaDeviceSynchronize();
+  for (int b = 0; b < bt->n; ++b)
+    if (bt->plans[b]) {
+      bt->plans[b]->batch = nullptr;
+      bt->plans[b]->slot = -1;
+    }
+  delete bt;
+  return e == cudaSuccess ? CMM_OK : cuda_fail(e, "cmm_sht_batch_destroy");
+}
+
+// The batch's analysis into each member's own coefficients (out NULL) or
+// into out[b].
+int sht_batch_analysis(cmm_sht_batch* bt, double2* const* out, cudaStream_t s) {
+  double2* alm[8];
+  for (int b = 0; b < bt->n; ++b) {
+    cmm_sht* p = bt->plans[b];
+    if (!p || p->precision != CMM_SHT_SPLIT_BF16 || !p->tc || p->L != bt->L) {
+      set_last_error("cmm_sht_batch_analysis: a member plan was destroyed or is no longer split-BF16");
+      return CMM_ERR_ARG;
+    }
+    alm[b] = out ? out[b] : (double2*)p->alm.p;
+  }
+  return tc_analysis_batch(bt->plans[0]->tc, (const unsigned char*)bt->xtab.p, alm, bt->n,
+                           (int*)bt->plans[0]->status.p, s);
+}
+
+// Forward transforms of one field per member: each member's rings and data
+// tiles, then one batched analysis -> alm[b].
+int sht_batch_forward(cmm_sht_batch* bt, const double* const* samples, double2* const* alm, cudaStream_t s) {
+  for (int b = 0; b < bt->n; ++b) {
+    cmm_sht* p = bt->plans[b];
+    if (!p) {
+      set_last_error("cmm_sht_batch_forward: a member plan was destroyed");
+      return CMM_ERR_ARG;
+    }
+    int rc = sht_velocity_pre(p, samples[b], s);
+    if (rc) return rc;
+  }
+  return sht_batch_analysis(bt, alm, s);
+}
+
+static int velocity_from_psi(cmm_sht* p, const cmm_mesh* vm, const double2* psi, double* jets,
+                             cudaStream_t s) {
+  const int L = p->L;
+  int rc;
+  dim3 b(128), g((L + 127) / 128, L);
   double2* F = (double2*)p->fields.p;
   ladder1_kernel<<<g, b, 0, s>>>(psi, L, F);
   if ((rc = check_launch("ladder1_kernel"))) return rc;

@@ -687,12 +687,15 @@ __global__ void build_ftab_kernel(TcFwdGeometry g, const double* __restrict__ ct
 // Per transform: weighted, parity-folded fine-ring data -> X tile images
 // per (m, ring chunk).  fine: (4L, L) FP32 complex [j][m] from the FP32
 // ring FFTs, rows 0..2L used.
+// slot: the field's column pair (2 slot, 2 slot + 1) of the 16-column data
+// tiles (0 for a plan's own tiles; a batch's member index in shared tiles).
 __global__ void build_xtab_kernel(TcFwdGeometry g, const float2* __restrict__ fine,
-                                  const double* __restrict__ w, unsigned char* __restrict__ xtab) {
+                                  const double* __restrict__ w, unsigned char* __restrict__ xtab,
+                                  int slot) {
   const int m = blockIdx.y;
   const int L = g.L;
-  // only the 2 used columns (re, im); columns 2..15 are zeroed once when
-  // the plan is made and never written
+  // only the field's 2 columns (re, im); the other columns are zeroed once
+  // when the tiles are made and written only by the other slots' fields
   const int total = g.nck * 2 * 2 * kKc;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
     const int c = e / (2 * 2 * kKc), r = e % (2 * 2 * kKc);
@@ -713,17 +716,28 @@ __global__ void build_xtab_kernel(TcFwdGeometry g, const float2* __restrict__ fi
     const __nv_bfloat16 h = __float2bfloat16_rn(v);
     const __nv_bfloat16 lo = __float2bfloat16_rn(v - __bfloat162float(h));
     unsigned char* rec = xtab + ((int64_t)m * g.nck + c) * kXRecord;
-    const int off = tile_offset(n, k);
+    const int off = tile_offset(2 * slot + n, k);
     *(__nv_bfloat16*)(rec + (2 * par) * kXTile + off) = h;
     *(__nv_bfloat16*)(rec + (2 * par + 1) * kXTile + off) = lo;
   }
 }
 
-// Block (degree block, m); 128 threads; writes alm[m][l].
+// Outputs of the analysis: field b (columns 2b, 2b + 1 of the data tiles)
+// -> alm[b][m][l], b < n.
+constexpr int kBatchMax = kNA / 2;
+struct TcAlmOut {
+  double2* p[kBatchMax];
+  int n;
+};
+
+// Block (degree block, m); 128 threads; writes alm[b][m][l].  NB: column
+// pairs drained (1 for a plan's own field; kBatchMax for a batch, whose
+// fields share each Pbar tile the block streams).
+template <int NB>
 __global__ void __launch_bounds__(kThreads) analysis_tc_kernel(TcFwdGeometry g,
                                                                const unsigned char* __restrict__ ptab,
                                                                const unsigned char* __restrict__ xtab,
-                                                               double2* __restrict__ alm,
+                                                               TcAlmOut out,
                                                                int* __restrict__ status) {
   extern __shared__ __align__(1024) unsigned char smem[];
   unsigned char* sP = smem;                 // kPRecord
@@ -752,7 +766,7 @@ __global__ void __launch_bounds__(kThreads) analysis_tc_kernel(TcFwdGeometry g,
   tc_fence_after();
   const uint32_t tmem = tmem_base_s;
   const uint32_t idesc = mma_idesc_n16();
-  KahanF aE0, aE1, aO0, aO1;
+  KahanF aE[2 * NB], aO[2 * NB];
   uint32_t ph_load = 0, ph_mma = 0;
   for (int c = 0; c < g.nck; ++c) {
     if (tid == 0) {
@@ -795,10 +809,11 @@ __global__ void __launch_bounds__(kThreads) analysis_tc_kernel(TcFwdGeometry g,
     const uint32_t lane_base = (uint32_t)(32 * warp) << 16;
     tmem_ld16(tmem + lane_base, vE);
     tmem_ld16(tmem + lane_base + kNA, vO);
-    aE0.add(vE[0]);
-    aE1.add(vE[1]);
-    aO0.add(vO[0]);
-    aO1.add(vO[1]);
+#pragma unroll
+    for (int k = 0; k < 2 * NB; ++k) {
+      aE[k].add(vE[k]);
+      aO[k].add(vO[k]);
+    }
     tc_fence_before();
     __syncthreads();
   }
@@ -807,8 +822,13 @@ __global__ void __launch_bounds__(kThreads) analysis_tc_kernel(TcFwdGeometry g,
   } else {
     const int i = lb * kM + tid;
     const int lE = m + 2 * i, lO = m + 1 + 2 * i;
-    if (lE < L) alm[(int64_t)m * L + lE] = make_double2(aE0.value(), aE1.value());
-    if (lO < L) alm[(int64_t)m * L + lO] = make_double2(aO0.value(), aO1.value());
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+      if (b >= out.n) break;
+      double2* alm = out.p[b];
+      if (lE < L) alm[(int64_t)m * L + lE] = make_double2(aE[2 * b].value(), aE[2 * b + 1].value());
+      if (lO < L) alm[(int64_t)m * L + lO] = make_double2(aO[2 * b].value(), aO[2 * b + 1].value());
+    }
   }
   tc_fence_before();
   __syncthreads();
@@ -910,8 +930,11 @@ int tc_plan_create(int L, const double* ct_rings, const double* pmm_rings, const
     delete p;
     return rc;
   }
-  e = cudaFuncSetAttribute(analysis_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  e = cudaFuncSetAttribute(analysis_tc_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            kPRecord + kXRecord);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(analysis_tc_kernel<kBatchMax>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             kPRecord + kXRecord);
   if (e != cudaSuccess) {
     delete p;
     return cuda_fail(e, "cudaFuncSetAttribute(analysis_tc_kernel)");
@@ -1001,14 +1024,39 @@ int tc_synthesis(TcPlan* p, const double2* fields, float2* S, int* status, cudaS
 // w the 2L+1 Clenshaw-Curtis weights -> alm[m][l], l >= m.
 int tc_analysis(TcPlan* p, const float2* fine, const double* w, double2* alm, int* status,
                 cudaStream_t s) {
+  int rc = tc_analysis_tiles(p, fine, w, (unsigned char*)p->xtab.p, 0, s);
+  if (rc) return rc;
+  return tc_analysis_batch(p, (const unsigned char*)p->xtab.p, &alm, 1, status, s);
+}
+
+size_t tc_xtab_bytes(const TcPlan* p) { return p->xtab.bytes; }
+
+int tc_analysis_tiles(TcPlan* p, const float2* fine, const double* w, unsigned char* xtab, int slot,
+                      cudaStream_t s) {
   const int L = p->L;
   TcFwdGeometry g{L, p->nck, (const int*)p->tab->lbase.p};
-  build_xtab_kernel<<<dim3(8, L), 256, 0, s>>>(g, fine, w, (unsigned char*)p->xtab.p);
-  int rc = check("build_xtab_kernel");
-  if (rc) return rc;
+  build_xtab_kernel<<<dim3(8, L), 256, 0, s>>>(g, fine, w, xtab, slot);
+  return check("build_xtab_kernel");
+}
+
+int tc_analysis_batch(TcPlan* p, const unsigned char* xtab, double2* const* alm, int n, int* status,
+                      cudaStream_t s) {
+  if (n < 1 || n > kBatchMax) {
+    set_last_error("tc analysis: 1 to 8 fields per launch");
+    return CMM_ERR_ARG;
+  }
+  const int L = p->L;
+  TcFwdGeometry g{L, p->nck, (const int*)p->tab->lbase.p};
+  TcAlmOut out{};
+  for (int b = 0; b < n; ++b) out.p[b] = alm[b];
+  out.n = n;
   const int maxlb = ((L + 1) / 2 + kM - 1) / kM;
-  analysis_tc_kernel<<<dim3(maxlb, L), kThreads, kPRecord + kXRecord, s>>>(
-      g, (const unsigned char*)p->tab->ftab.p, (const unsigned char*)p->xtab.p, alm, status);
+  if (n == 1)
+    analysis_tc_kernel<1><<<dim3(maxlb, L), kThreads, kPRecord + kXRecord, s>>>(
+        g, (const unsigned char*)p->tab->ftab.p, xtab, out, status);
+  else
+    analysis_tc_kernel<kBatchMax><<<dim3(maxlb, L), kThreads, kPRecord + kXRecord, s>>>(
+        g, (const unsigned char*)p->tab->ftab.p, xtab, out, status);
   return check("analysis_tc_kernel");
 }
 

@@ -183,7 +183,11 @@ int bve_destroy(cmm_bve* b) {
   return CMM_OK;
 }
 
-int bve_step(cmm_bve* b, cudaStream_t s) {
+// The step's first half: map update and assembly, the sample points
+// through the stack, the vorticity there; then (batched) the forward
+// transform up to the member's data tiles, or (alone) the whole velocity
+// inversion.
+static int step_first(cmm_bve* b, cudaStream_t s, bool batched) {
   const cmm_bve_desc& d = b->d;
   const MeshView& mesh = d.mesh->view;
   const MeshView& vm = d.velmesh->view;
@@ -205,7 +209,17 @@ int bve_step(cmm_bve* b, cudaStream_t s) {
                              d.rot_rate, d.X, b->nsample, 2 * vm.L,
                              (const double*)d.velmesh->cos_theta.p, d.omega, s)))
     return rc;
-  if ((rc = sht_velocity(d.sht, d.velmesh, d.omega, nullptr, d.vel_jets, s))) return rc;
+  if (batched) return sht_velocity_pre(d.sht, d.omega, s);
+  return sht_velocity(d.sht, d.velmesh, d.omega, nullptr, d.vel_jets, s);
+}
+
+// The second half: the velocity levels, remap and bookkeeping.
+static int step_second(cmm_bve* b, cudaStream_t s) {
+  const cmm_bve_desc& d = b->d;
+  const MeshView& mesh = d.mesh->view;
+  const MeshView& vm = d.velmesh->view;
+  const BveState* st = (const BveState*)b->state.p;
+  int rc;
   if ((rc = launch_assemble(vm, d.vel_jets, 3, nullptr, s, st))) return rc;
   // bookkeeping
   const int64_t nmax = b->nrec > b->njets ? b->nrec : b->njets;
@@ -219,6 +233,19 @@ int bve_step(cmm_bve* b, cudaStream_t s) {
     return rc;
   bve_advance_kernel<<<1, 32, 0, s>>>((BveState*)b->state.p, d.n_maps, d.Nt);
   return check("bve_advance_kernel");
+}
+
+int bve_step(cmm_bve* b, cudaStream_t s) {
+  int rc = step_first(b, s, false);
+  return rc ? rc : step_second(b, s);
+}
+
+int bve_step_pre(cmm_bve* b, cudaStream_t s) { return step_first(b, s, true); }
+
+int bve_step_post(cmm_bve* b, cudaStream_t s) {
+  const cmm_bve_desc& d = b->d;
+  int rc = sht_velocity_post(d.sht, d.velmesh, d.vel_jets, s);
+  return rc ? rc : step_second(b, s);
 }
 
 int bve_state(cmm_bve* b, cudaStream_t s, int* count, int* nc, int* identity) {

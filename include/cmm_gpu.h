@@ -337,6 +337,7 @@ int cmm_vorticity_eval(const cmm_mesh* velmesh, int kind, const double* params, 
  * zero; negative orders follow from a_{l,-m} = (-1)^m conj(a_lm).
  * The plan owns its FFT plans and scratch buffers. */
 typedef struct cmm_sht cmm_sht;
+typedef struct cmm_sht_batch cmm_sht_batch;
 int cmm_sht_create(int L, cmm_sht** out);
 int cmm_sht_destroy(cmm_sht* plan);
 
@@ -393,6 +394,29 @@ int cmm_sht_trim(cmm_sht* plan);
 /* Read (and with clear != 0, reset) the plan's device status word
  * (CMM_FLAG_TIMEOUT); synchronises `stream`. */
 int cmm_sht_status(cmm_sht* plan, void* stream, int* flags, int clear);
+/* A batch of 1 to CMM_SHT_BATCH_MAX split-BF16 plans of one band-limit
+ * (distinct, in no other batch; best with shared tables,
+ * cmm_sht_share_tables) whose forward Legendre analyses run as one
+ * tensor-core launch: member b's field occupies columns 2b, 2b+1 of the
+ * N = 16 data tiles, so every Pbar tile streamed from HBM feeds all
+ * members.  Used by the split device-driven step (cmm_bve_step_pre /
+ * cmm_sht_batch_analysis / cmm_bve_step_post) of ensemble members of one
+ * band-limit; each member's coefficients are bitwise those of its own
+ * analysis.  Destroy the batch before its plans (a plan destroyed first
+ * makes the batch's analysis return CMM_ERR_ARG).  Create and destroy
+ * synchronise the device.  No counterpart in the reference. */
+#define CMM_SHT_BATCH_MAX 8
+int cmm_sht_batch_create(cmm_sht* const* plans, int n, cmm_sht_batch** out);
+int cmm_sht_batch_destroy(cmm_sht_batch* batch);
+/* The batch's analysis: after every member's cmm_bve_step_pre on this or
+ * an earlier-joined stream; timeouts are reported in the first member
+ * plan's status word. */
+int cmm_sht_batch_analysis(cmm_sht_batch* batch, void* stream);
+/* Forward transforms (as cmm_sht_forward) of one field per member through
+ * the batched analysis: samples[b] (L+1,2L) -> alm[b] (L,L) complex, HOST
+ * arrays of the batch's member count of device pointers. */
+int cmm_sht_batch_forward(cmm_sht_batch* batch, const double* const* samples, double* const* alm,
+                          void* stream);
 
 /* samples (L+1,2L) -> alm (L,L) complex.  Replaces pyssht.forward(...,
  * Method="MWSS", Reality=True) as called by inv_Laplacian
@@ -526,6 +550,14 @@ int cmm_bve_create(const cmm_bve_desc* desc, cmm_bve** out);
 int cmm_bve_destroy(cmm_bve* bve);
 /* Enqueue one step on `stream` (no host synchronisation, capturable). */
 int cmm_bve_step(cmm_bve* bve, void* stream);
+/* The same step in two halves around a batched analysis, for a run whose
+ * SHT plan is in a batch (cmm_sht_batch_create): _pre runs the step up to
+ * the forward transform's data tiles (written into the member's batch
+ * slot), cmm_sht_batch_analysis then contracts all members' tiles, and
+ * _post runs the rest (stream function, velocity jets, assembly, remap,
+ * bookkeeping).  Bitwise the same step as cmm_bve_step. */
+int cmm_bve_step_pre(cmm_bve* bve, void* stream);
+int cmm_bve_step_post(cmm_bve* bve, void* stream);
 /* Read the device state (synchronises `stream`). */
 int cmm_bve_state(cmm_bve* bve, void* stream, int* count, int* nc, int* identity);
 

@@ -27,18 +27,26 @@ def _alone(mods, spec, i, seed, Nt, T, lmax, rms, n_maps, precision="split_bf16"
     return s.run()
 
 
-@pytest.mark.parametrize("persistent,precision", [(False, "split_bf16"), (True, "split_bf16"),
-                                                  (True, "fp64")])
-def test_ensemble_graph_matches_members_alone(mods, persistent, precision):
+@pytest.mark.parametrize("persistent,precision,batch", [(False, "split_bf16", False),
+                                                        (True, "split_bf16", False),
+                                                        (False, "split_bf16", True),
+                                                        (True, "split_bf16", True),
+                                                        (True, "fp64", False)])
+def test_ensemble_graph_matches_members_alone(mods, persistent, precision, batch):
     """One graph replay per step, or (persistent) the whole remaining run
     captured as one graph and launched once; FP64 members share one set of
-    Pbar tables per band-limit."""
+    Pbar tables per band-limit; (batch) the same-band-limit members'
+    analyses batched into one tensor-core launch per batch."""
     ensemble, sims, autotune, _, _ = mods
     kw = dict(levels=(2, 3), bandlimits=(16, 32), Nt=14, T=0.1, lmax=8, rms=3.0, n_maps=4)
     ens = ensemble.Ensemble.from_seed(5, seed=7, precision=precision, **kw).bootstrap()
     tuner = autotune.Autotuner(reps=1)
     tuner.tune_ensemble_kernels(ens)
-    tuner.tune_schedule(ens, stream_counts=(1, 3), steps_each=1)
+    tuner.tune_schedule(ens, stream_counts=(1, 3), steps_each=1, batch=False)
+    if batch:
+        assert ens.batches()[1], "no band-limit with two split-BF16 members"
+        ens.capture(streams=ens.schedule["streams"], order=ens.schedule["order"], batch=True)
+        assert ens.schedule["batch"]
     if persistent:
         ens.run_persistent()
         assert ens.schedule["steps"] > 1

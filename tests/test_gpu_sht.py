@@ -189,6 +189,36 @@ def test_split_bf16_synthesis_schedules_bitwise_equal(nat, L):
     assert torch.equal(outs[0], outs[1])
 
 
+@pytest.mark.parametrize("L,n", [(33, 3), (128, 8), (1024, 4)])
+def test_batched_analysis_bitwise_equal(nat, L, n):
+    """Up to 8 split-BF16 plans of one band-limit (sharing the owner's
+    tables) whose analyses run as one tensor-core launch, member b in
+    columns 2b, 2b+1 of the N = 16 data tiles (cmm_sht_batch_forward):
+    each member's coefficients are bitwise its own plan's."""
+    rng = np.random.default_rng(50 + L)
+    owner = nat.Sht(L).set_precision(nat.Sht.SPLIT_BF16)
+    plans = [owner] + [nat.Sht(L).share_tables(owner) for _ in range(n - 1)]
+    fs = []
+    for _ in range(n):
+        f = rng.standard_normal((L + 1, 2 * L))
+        f[0], f[-1] = f[0, 0], f[-1, 0]
+        fs.append(dev(f))
+    batch = nat.ShtBatch(plans)
+    got = batch.forward(fs)
+    for b in range(n):
+        assert torch.equal(got[b], plans[b].forward(fs[b])), b
+    assert all(p.status() == 0 for p in plans)
+    # every member must be a distinct split-BF16 plan of the batch's
+    # band-limit, in no other batch
+    with pytest.raises(RuntimeError):
+        nat.ShtBatch([owner])
+    with pytest.raises(RuntimeError):
+        nat.ShtBatch([nat.Sht(L).share_tables(owner), nat.Sht(L)])
+    del batch
+    other = nat.ShtBatch(plans[:2])   # free again once the batch is gone
+    del other
+
+
 @pytest.mark.parametrize("L", [33, 128, 256])
 def test_split_bf16_analysis_against_fp64(nat, L):
     """The forward Legendre analysis on the tensor cores (M = 128 degrees,
