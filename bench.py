@@ -737,7 +737,8 @@ def bench_ensemble(args, dev):
             "device_memory_gb": torch.cuda.max_memory_allocated(dev) / 1e9, "setup_s": setup,
             "graph_steps": n, "graph_capture_s": capture_s,
             "split_vs_fp64_omega_rel": {"member": i0, "level": lv0, "L": L0, "value": err0},
-            "schedule": tuner.log["schedule"]["best"], "launch_shapes": tuner.log["kernels"],
+            "schedule": tuner.log["schedule"]["best"],
+            "schedule_candidates": tuner.log["schedule"]["candidates"], "launch_shapes": tuner.log["kernels"],
             "compose_variants": tuner.log.get("variants"), "sht_schedule": tuner.log.get("sht_schedule"),
             "map_forms_members": sum(m.stack_forms is not None for m in ens.members),
             # (band-limit, members) of each batched analysis
