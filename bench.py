@@ -45,21 +45,22 @@ sys.path.insert(0, os.path.join(ROOT, "cmm-s2_gb300"))
 LEVEL, SUBMAPS = 7, 8
 METRIC = "map evals/s"
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one
-# Jacobian compose launch through map forms per query, from one ncu capture
-# of compose_kernel on 2^22 queries (level 7, 8 submaps), scaled to the
-# headline's 2^24 by the number of queries (the gathers and outputs grow
-# with it): with the queries grouped by coarse cell (the headline step) ...
-COMPOSE_TRAFFIC_PER_QUERY = (4.1636e9 + 0.7654e9) / (1 << 22)
-# ... and in the caller's order.
+# Jacobian compose launch per query, from one ncu capture of compose_kernel
+# on 2^22 queries (level 7, 8 submaps), scaled to the headline's 2^24 by
+# the number of queries (the gathers and outputs grow with it): the
+# headline step (queries grouped by coarse cell, map forms and their low
+# floats) ...
+COMPOSE_TRAFFIC_PER_QUERY = (5.5332e9 + 0.8026e9) / (1 << 22)
+# ... and in the caller's order (map forms alone).
 COMPOSE_TRAFFIC_PER_QUERY_CALLER = (9.9927e9 + 0.5103e9) / (1 << 22)
 # FP64 instructions (DADD + DMUL + DFMA) per map evaluation (query x
-# submap) with the Jacobian, from the same capture, and all issued
-# instructions per evaluation (smsp__inst_executed.sum x 32 / evaluations):
-# at 2 FP64 lane-operations per SM per clock and 4 warp instructions issued
-# per SM per clock, both cost ~14 SM cycles per evaluation at their peaks,
-# so the two bind together.
+# submap) of the headline step's kernel, from the same capture, and all
+# issued instructions per evaluation (smsp__inst_executed.sum x 32 /
+# evaluations): at 2 FP64 lane-operations per SM per clock and 4 warp
+# instructions issued per SM per clock, they cost ~14 and ~12 SM cycles
+# per evaluation at their peaks, so the two bind together.
 FP64_INSTR_PER_EVAL = 28.15
-INSTR_PER_EVAL = 1803
+INSTR_PER_EVAL = 1574
 
 
 def peaks():
