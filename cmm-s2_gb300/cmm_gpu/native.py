@@ -557,10 +557,11 @@ class ShtBatch:
 
 
 def compose_host(mesh, coeffs, q_host, out_host, tri_host=None, jac_host=None, chunks=16,
-                 streams=None, scratch=None, order=None, forms=None, forms_ff=None):
+                 streams=None, scratch=None, order=None, forms=None, forms_ff=None, nstreams=2):
     """Composition of host-resident queries (pinned (n,3) float64) into
-    host-resident outputs, pipelined in `chunks` pieces over two CUDA
-    streams so the host<->device copies overlap the kernels.  order: each
+    host-resident outputs, pipelined in `chunks` pieces over `nstreams` CUDA
+    streams (each with its own device buffers) so the host<->device copies
+    overlap the kernels.  order: each
     chunk is processed grouped by coarse cell (cmm_query_order, same
     results; default), so that neighbouring threads gather neighbouring
     records.  forms / forms_ff: map-form records and their float-float
@@ -569,11 +570,11 @@ def compose_host(mesh, coeffs, q_host, out_host, tri_host=None, jac_host=None, c
         order = True
     n = q_host.shape[0]
     dev = mesh.device
-    streams = streams or [torch.cuda.Stream(dev), torch.cuda.Stream(dev)]
+    streams = streams or [torch.cuda.Stream(dev) for _ in range(nstreams)]
     step = (n + chunks - 1) // chunks
     if scratch is None:
         scratch = {}
-        for k in range(2):
+        for k in range(len(streams)):
             scratch[k] = dict(
                 q=torch.empty((step, 3), dtype=torch.float64, device=dev),
                 out=torch.empty((step, 3), dtype=torch.float64, device=dev),
@@ -593,7 +594,7 @@ def compose_host(mesh, coeffs, q_host, out_host, tri_host=None, jac_host=None, c
         lo, hi = c * step, min(n, (c + 1) * step)
         if lo >= hi:
             break
-        k = c % 2
+        k = c % len(streams)
         s, b = streams[k], scratch[k]
         m = hi - lo
         with torch.cuda.stream(s):
