@@ -556,12 +556,13 @@ class ShtBatch:
         return alm
 
 
-def compose_host(mesh, coeffs, q_host, out_host, tri_host=None, jac_host=None, chunks=16,
-                 streams=None, scratch=None, order=None, forms=None, forms_ff=None, nstreams=2):
+def compose_host(mesh, coeffs, q_host, out_host, tri_host=None, jac_host=None, chunks=8,
+                 streams=None, scratch=None, order=None, forms=None, forms_ff=None, nstreams=4):
     """Composition of host-resident queries (pinned (n,3) float64) into
     host-resident outputs, pipelined in `chunks` pieces over `nstreams` CUDA
     streams (each with its own device buffers) so the host<->device copies
-    overlap the kernels.  order: each
+    overlap the kernels (2^24 queries with Jacobians through 8 submaps:
+    12.8 ms with 8 chunks on 4 streams, 15.0 ms with 16 on 2).  order: each
     chunk is processed grouped by coarse cell (cmm_query_order, same
     results; default), so that neighbouring threads gather neighbouring
     records.  forms / forms_ff: map-form records and their float-float
