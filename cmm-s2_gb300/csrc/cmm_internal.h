@@ -68,6 +68,11 @@ struct MeshView {
   const double* theta;      // (L+1) ring colatitudes
   const double* phi;        // (2L) longitudes
   const double* grid;       // ((L+1)*2L, 4) ring points x,y,z,0
+  // lat-lon side-test normals, 4 doubles per (ring, sector p): ring_n =
+  // grid(ring, p) x grid(ring, p+1), diag_n = grid(ring, p) x
+  // grid(ring+1, p+1) (rings 0..L-1), each product rounded as numpy's cross
+  const double* ring_n;
+  const double* diag_n;
   double dphi, dthe;
   // velocity records (ncomp = 3) in FP32 (cmm_velmesh_set_records):
   // (nt, 64) floats, assembled from the FP32 copy of the factors
@@ -131,7 +136,8 @@ struct DeviceBuffer {
 struct cmm_mesh {
   cmm::MeshView view;
   cmm::DeviceBuffer verts, tri_v, tri_loc, tri_asm, root, root_f, root_adj, node_n, node_nf, leaf_row,
-      status, theta, phi, grid, cos_theta, tri_asm_f, tri_loc_f, sh_ab, sh_fm, walk_f, walk_d, jump;
+      status, theta, phi, grid, cos_theta, tri_asm_f, tri_loc_f, sh_ab, sh_fm, walk_f, walk_d, jump, ring_n,
+      diag_n;
 };
 
 namespace cmm {
@@ -142,6 +148,8 @@ struct BveState;
 // st != NULL: write into st->vel[0] instead of coeffs.
 int launch_assemble(const MeshView& m, const double* jets, int ncomp, double* coeffs,
                     cudaStream_t s, const BveState* st = nullptr);
+// FP32 velocity records (rec32) from FP32 jets into st->vel[0].
+int launch_assemble_f32_jets(const MeshView& m, const float* jets, cudaStream_t s, const BveState* st);
 int launch_compose(const MeshView& m, const double* const* coeffs, int S, const double* q,
                    int64_t n, double* out, int32_t* tri, int32_t* tri_all, double* jac,
                    cudaStream_t s, const int32_t* perm = nullptr, const double* const* forms = nullptr,
@@ -282,6 +290,8 @@ int sht_velocity_post(cmm_sht* p, const cmm_mesh* vm, double* jets, cudaStream_t
 int sht_batch_create(cmm_sht* const* plans, int n, cmm_sht_batch** out);
 int sht_batch_destroy(cmm_sht_batch* bt);
 int sht_batch_size(const cmm_sht_batch* bt);
+// The split form's last velocity jets as floats (12 x Nv_u), or NULL.
+const float* sht_jets_f32(const cmm_sht* p);
 int sht_batch_analysis(cmm_sht_batch* bt, double2* const* out, cudaStream_t s);
 int sht_batch_forward(cmm_sht_batch* bt, const double* const* samples, double2* const* alm, cudaStream_t s);
 int sht_scalar_jets(cmm_sht* p, const cmm_mesh* vm, const double2* alm, double* jets, cudaStream_t s);

@@ -445,9 +445,19 @@ __device__ __forceinline__ int py_mod(long long a, int n) {
   return (int)(r < 0 ? r + n : r);
 }
 
-__device__ __forceinline__ D3 gridpt(const MeshView& m, int ring, int p) {
-  const double* g = m.grid + 4 * ((int64_t)ring * 2 * m.L + p);
-  return D3{g[0], g[1], g[2]};
+// With g(ring, p) the ring points: g(ring, p) x g(ring, p+1) (ring edge)
+// and g(ring, p) x g(ring+1, p+1) (cell diagonal), from the mesh's tables
+// (numpy's rounding).
+__device__ __forceinline__ D3 table_normal(const double* tab, const MeshView& m, int ring, int p) {
+  const double2* e = reinterpret_cast<const double2*>(tab + 4 * ((int64_t)ring * 2 * m.L + p));
+  const double2 a = __ldg(e), b = __ldg(e + 1);
+  return D3{a.x, a.y, b.x};
+}
+__device__ __forceinline__ D3 ring_normal(const MeshView& m, int ring, int p) {
+  return table_normal(m.ring_n, m, ring, p);
+}
+__device__ __forceinline__ D3 diag_normal(const MeshView& m, int ring, int p) {
+  return table_normal(m.diag_n, m, ring, p);
 }
 
 // Triangle (row of the lat-lon table) containing q: ring and sector from
@@ -467,7 +477,6 @@ static __device__ __noinline__ int latlon_locate_exact(const MeshView& m, double
   if (theta_l < 0) theta_l = 0;
   if (theta_l > M - 2) theta_l = M - 2;
   const double theta_c = (theta - m.theta[theta_l]) / m.dthe;
-  const int phi_p1 = (phi_l + 1) % N;
   const D3 q = D3{x, y, z};
   const bool row_lo = theta_c <= 0.03 && theta_l != 0;
   const bool row_hi = !row_lo && theta_c > 0.85 && theta_l != M - 2;
@@ -479,16 +488,16 @@ static __device__ __noinline__ int latlon_locate_exact(const MeshView& m, double
     sincos(theta, &st, &cth);
     const D3 q0 = D3{st * cp, st * sp, cth};
     if (row_lo) {
-      const D3 n = cross(gridpt(m, theta_l, phi_l), gridpt(m, theta_l, phi_p1));
+      const D3 n = ring_normal(m, theta_l, phi_l);
       if (dot(n, q0) > 0.0) theta_l -= 1;
     } else {
-      const D3 n = cross(gridpt(m, theta_l + 1, phi_l), gridpt(m, theta_l + 1, phi_p1));
+      const D3 n = ring_normal(m, theta_l + 1, phi_l);
       if (-dot(n, q0) > 0.0) theta_l += 1;
     }
   }
   if (theta_l == 0) return phi_l;
   if (theta_l == M - 2) return 2 * N * (M - 2) - N + phi_l;
-  const D3 n = cross(gridpt(m, theta_l, phi_l), gridpt(m, theta_l + 1, phi_p1));
+  const D3 n = diag_normal(m, theta_l, phi_l);
   const int s = (-dot(n, q) > 0.0) ? 1 : 0;
   return N + 2 * (N * (theta_l - 1) + phi_l) + s;
 }
@@ -517,22 +526,21 @@ __device__ __forceinline__ int latlon_locate(const MeshView& m, double x, double
   if (!(fu > du && fu < 1.f - du && fv > dv && fv < 1.f - dv && fabsf(fv - 0.03f) > dv &&
         fabsf(fv - 0.85f) > dv && phi_l >= 0 && phi_l < N && theta_l >= 0 && theta_l <= M - 2))
     return latlon_locate_exact(m, x, y, z);
-  const int phi_p1 = (phi_l + 1) % N;
   const D3 q = D3{x, y, z};
   const bool row_lo = fv <= 0.03f && theta_l != 0;
   const bool row_hi = !row_lo && fv > 0.85f && theta_l != M - 2;
   if (row_lo) {
-    const double d = dot(cross(gridpt(m, theta_l, phi_l), gridpt(m, theta_l, phi_p1)), q);
+    const double d = dot(ring_normal(m, theta_l, phi_l), q);
     if (fabs(d) <= 1e-13) return latlon_locate_exact(m, x, y, z);
     if (d > 0.0) theta_l -= 1;
   } else if (row_hi) {
-    const double d = -dot(cross(gridpt(m, theta_l + 1, phi_l), gridpt(m, theta_l + 1, phi_p1)), q);
+    const double d = -dot(ring_normal(m, theta_l + 1, phi_l), q);
     if (fabs(d) <= 1e-13) return latlon_locate_exact(m, x, y, z);
     if (d > 0.0) theta_l += 1;
   }
   if (theta_l == 0) return phi_l;
   if (theta_l == M - 2) return 2 * N * (M - 2) - N + phi_l;
-  const D3 n = cross(gridpt(m, theta_l, phi_l), gridpt(m, theta_l + 1, phi_p1));
+  const D3 n = diag_normal(m, theta_l, phi_l);
   const int s = (-dot(n, q) > 0.0) ? 1 : 0;
   return N + 2 * (N * (theta_l - 1) + phi_l) + s;
 }

@@ -211,8 +211,11 @@ __global__ void __launch_bounds__(kAsmTri) assemble_kernel(MeshView m, const dou
 }
 
 // FP32 velocity records (velmesh with rec32, ncomp = 3): the same
-// ordinates from FP32 jets and the FP32 factor table, in FP32.
-__global__ void __launch_bounds__(kAsmTri) assemble_f32_kernel(MeshView m, const double* __restrict__ jets,
+// ordinates from FP32 jets and the FP32 factor table, in FP32.  J: the
+// jets' storage type (double jets are rounded to float here; float jets
+// are the split form's FP32 jets, the same values without conversions).
+template <typename J>
+__global__ void __launch_bounds__(kAsmTri) assemble_f32_kernel(MeshView m, const J* __restrict__ jets,
                                                                float* __restrict__ coeffs,
                                                                const BveState* __restrict__ st) {
   if (st) coeffs = (float*)st->vel[0];
@@ -785,12 +788,22 @@ int launch_assemble(const MeshView& m, const double* jets, int ncomp, double* co
                     cudaStream_t s, const BveState* st) {
   const int blocks = (m.nt + kAsmTri - 1) / kAsmTri;
   if (ncomp == 3 && m.rec32)
-    assemble_f32_kernel<<<blocks, kAsmTri, 0, s>>>(m, jets, (float*)coeffs, st);
+    assemble_f32_kernel<double><<<blocks, kAsmTri, 0, s>>>(m, jets, (float*)coeffs, st);
   else if (ncomp == 3)
     assemble_kernel<3><<<blocks, kAsmTri, 0, s>>>(m, jets, coeffs, st);
   else
     assemble_kernel<1><<<blocks, kAsmTri, 0, s>>>(m, jets, coeffs, st);
   return check_launch("assemble_kernel");
+}
+
+int launch_assemble_f32_jets(const MeshView& m, const float* jets, cudaStream_t s, const BveState* st) {
+  if (!m.rec32 || !st) {
+    set_last_error("assemble from FP32 jets: FP32 records and a device-driven state expected");
+    return CMM_ERR_ARG;
+  }
+  const int blocks = (m.nt + kAsmTri - 1) / kAsmTri;
+  assemble_f32_kernel<float><<<blocks, kAsmTri, 0, s>>>(m, jets, nullptr, st);
+  return check_launch("assemble_f32_kernel");
 }
 
 int launch_compose(const MeshView& m, const double* const* coeffs, int S, const double* q,

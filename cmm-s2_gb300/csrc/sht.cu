@@ -573,9 +573,10 @@ __global__ void __launch_bounds__(kTabBlock) synthesis_tab_kernel(const double2*
 // the 12 synthesised fields on the grid: vals[i][0] = u_i and, with
 // g = (iLx, iLy, iLz) u_i, vals[c][1+i] = (g x X - ((g x X).X/|X|) X)_c;
 // poles from sample 0 of the first and last rings.
+// jets_f (nullable): the same values as floats (exact for R = float).
 template <typename R>
 __global__ void jets_kernel(const R* __restrict__ fld, int L, const double* __restrict__ grid,
-                            double* __restrict__ jets) {
+                            double* __restrict__ jets, float* __restrict__ jets_f) {
   const int N = 2 * L;
   const int64_t nv = 2 + (int64_t)(L - 1) * N;
   const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -592,14 +593,17 @@ __global__ void jets_kernel(const R* __restrict__ fld, int L, const double* __re
   const R X0 = (R)grid[4 * node], X1 = (R)grid[4 * node + 1], X2 = (R)grid[4 * node + 2];
   const R nX = sqrt(X0 * X0 + X1 * X1 + X2 * X2);
   for (int i = 0; i < 3; ++i) {
-    jets[(int64_t)(i * 4) * nv + v] = (double)fld[i * fs + node];
     const R g0 = fld[(3 + 3 * i) * fs + node], g1 = fld[(4 + 3 * i) * fs + node],
             g2 = fld[(5 + 3 * i) * fs + node];
     const R c0 = g1 * X2 - g2 * X1, c1 = g2 * X0 - g0 * X2, c2 = g0 * X1 - g1 * X0;
     const R sc = (c0 * X0 + c1 * X1 + c2 * X2) / nX;
-    jets[(int64_t)(0 * 4 + 1 + i) * nv + v] = (double)(c0 - sc * X0);
-    jets[(int64_t)(1 * 4 + 1 + i) * nv + v] = (double)(c1 - sc * X1);
-    jets[(int64_t)(2 * 4 + 1 + i) * nv + v] = (double)(c2 - sc * X2);
+    const R val[4] = {fld[i * fs + node], c0 - sc * X0, c1 - sc * X1, c2 - sc * X2};
+    const int64_t slot[4] = {i * 4, 0 * 4 + 1 + i, 1 * 4 + 1 + i, 2 * 4 + 1 + i};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      jets[slot[k] * nv + v] = (double)val[k];
+      if (jets_f) jets_f[slot[k] * nv + v] = (float)val[k];
+    }
   }
 }
 
@@ -988,6 +992,9 @@ struct cmm_sht {
   cufftHandle f_ring_fwd = 0, f_torus_fwd = 0, f_pad_inv = 0, f_ring_inv = 0;
   bool have_fplans[4] = {false, false, false, false};
   cmm::DeviceBuffer f_in, f_spec, f_torus, f_pad, f_synth, f_samples;
+  // the velocity jets of the split form also as the FP32 values they are
+  // computed in (12 x Nv_u floats), which the FP32 velocity assembly reads
+  cmm::DeviceBuffer f_jets;
   // adjoint: D2Z over the 12 fields' rings, C2R over one field's rings
   cufftHandle b_ring_fwd12 = 0, b_ring_inv1 = 0;
   bool have_bplans = false;
@@ -1222,7 +1229,8 @@ static int make_float_plans(cmm_sht* p) {
       (rc = p->f_torus.alloc((size_t)2 * L * L * sizeof(float2))) ||
       (rc = p->f_pad.alloc((size_t)4 * L * L * sizeof(float2))) ||
       (rc = p->f_synth.alloc((size_t)kFields * (L + 1) * (L + 1) * sizeof(float2))) ||
-      (rc = p->f_samples.alloc((size_t)kFields * (L + 1) * 2 * L * sizeof(float))))
+      (rc = p->f_samples.alloc((size_t)kFields * (L + 1) * 2 * L * sizeof(float))) ||
+      (rc = p->f_jets.alloc((size_t)12 * (2 + (size_t)(L - 1) * 2 * L) * sizeof(float))))
     return rc;
   int n2[1] = {2 * L}, n4[1] = {4 * L};
   int inemb[1] = {2 * L}, onemb[1] = {L + 1}, tn[1] = {2 * L}, pn[1] = {4 * L};
@@ -1242,7 +1250,6 @@ static int make_float_plans(cmm_sht* p) {
   return CMM_OK;
 }
 
-// samples (L+1, 2L) -> alm (m-major half layout) in p->alm or `out`.
 // Split-BF16 forward transform up to the Legendre stage: the samples in
 // FP32, the ring FFTs, the torus extension and the padded inverse
 // transform -> p->f_pad (the analysis' input).
@@ -1266,6 +1273,7 @@ static int forward_rings_f32(cmm_sht* p, const double* samples, cudaStream_t s) 
   return CMM_OK;
 }
 
+// samples (L+1, 2L) -> alm (m-major half layout) in p->alm or `out`.
 int sht_forward(cmm_sht* p, const double* samples, double2* out, cudaStream_t s) {
   const int L = p->L;
   int rc = set_streams(p, s);
@@ -1524,10 +1532,10 @@ static int velocity_from_psi(cmm_sht* p, const cmm_mesh* vm, const double2* psi,
   const int64_t nv = 2 + (int64_t)(L - 1) * 2 * L;
   if (p->precision == CMM_SHT_SPLIT_BF16)
     jets_kernel<float><<<(int)((nv + 127) / 128), 128, 0, s>>>((const float*)p->f_samples.p, L,
-                                                                vm->view.grid, jets);
+                                                                vm->view.grid, jets, (float*)p->f_jets.p);
   else
     jets_kernel<double><<<(int)((nv + 127) / 128), 128, 0, s>>>((const double*)p->samples.p, L,
-                                                                 vm->view.grid, jets);
+                                                                 vm->view.grid, jets, nullptr);
   return check_launch("jets_kernel");
 }
 
@@ -1760,5 +1768,9 @@ int sht_destroy(cmm_sht* p) {
 }
 
 int sht_L(const cmm_sht* p) { return p->L; }
+
+const float* sht_jets_f32(const cmm_sht* p) {
+  return p->precision == CMM_SHT_SPLIT_BF16 && p->f_jets.p ? (const float*)p->f_jets.p : nullptr;
+}
 
 }  // namespace cmm

@@ -220,7 +220,11 @@ static int step_second(cmm_bve* b, cudaStream_t s) {
   const MeshView& vm = d.velmesh->view;
   const BveState* st = (const BveState*)b->state.p;
   int rc;
-  if ((rc = launch_assemble(vm, d.vel_jets, 3, nullptr, s, st))) return rc;
+  // FP32 records from the split form's FP32 jets (the same values as the
+  // double jets, without the conversions)
+  const float* jf = vm.rec32 ? sht_jets_f32(d.sht) : nullptr;
+  if ((rc = jf ? launch_assemble_f32_jets(vm, jf, s, st) : launch_assemble(vm, d.vel_jets, 3, nullptr, s, st)))
+    return rc;
   // bookkeeping
   const int64_t nmax = b->nrec > b->njets ? b->nrec : b->njets;
   bve_remap_kernel<<<dev::grid_for(nmax, 256), 256, 0, s>>>(st, d.n_maps, d.Nt, d.coeffs_cur,

@@ -67,6 +67,32 @@ int build_latlon(int L, const double* theta, const double* phi, const double* gr
   if ((rc = m->phi.upload(phi, (size_t)N * 8))) return rc;
   if ((rc = m->grid.upload(gpad.data(), gpad.size() * 8))) return rc;
   {
+    // side-test normals of the ring edges and the cell diagonals, each
+    // cross-product component a_i b_j - a_j b_i with both products rounded
+    // (host code without contraction), as numpy's cross
+    std::vector<double> rn(4 * (size_t)M * N, 0.0), dn(4 * (size_t)M * N, 0.0);
+    auto G = [&](int ring, int p) { return D3{gpad[4 * ((size_t)ring * N + p)], gpad[4 * ((size_t)ring * N + p) + 1],
+                                               gpad[4 * ((size_t)ring * N + p) + 2]}; };
+    for (int ring = 0; ring < M; ++ring)
+      for (int p = 0; p < N; ++p) {
+        const D3 a = G(ring, p), b = G(ring, (p + 1) % N);
+        const D3 r = cross(a, b);
+        double* o = &rn[4 * ((size_t)ring * N + p)];
+        o[0] = r.x;
+        o[1] = r.y;
+        o[2] = r.z;
+        if (ring + 1 < M) {
+          const D3 d = cross(a, G(ring + 1, (p + 1) % N));
+          double* e = &dn[4 * ((size_t)ring * N + p)];
+          e[0] = d.x;
+          e[1] = d.y;
+          e[2] = d.z;
+        }
+      }
+    if ((rc = m->ring_n.upload(rn.data(), rn.size() * 8))) return rc;
+    if ((rc = m->diag_n.upload(dn.data(), dn.size() * 8))) return rc;
+  }
+  {
     std::vector<double> ct(M);
     for (int t = 0; t < M; ++t) ct[t] = std::cos(theta[t]);
     if ((rc = m->cos_theta.upload(ct.data(), ct.size() * 8))) return rc;
@@ -108,6 +134,8 @@ int build_latlon(int L, const double* theta, const double* phi, const double* gr
   v.theta = (const double*)m->theta.p;
   v.phi = (const double*)m->phi.p;
   v.grid = (const double*)m->grid.p;
+  v.ring_n = (const double*)m->ring_n.p;
+  v.diag_n = (const double*)m->diag_n.p;
   v.status = (int*)m->status.p;
   v.sh_ab = (const double*)m->sh_ab.p;
   v.sh_fm = (const double*)m->sh_fm.p;
