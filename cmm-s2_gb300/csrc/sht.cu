@@ -1006,9 +1006,9 @@ struct cmm_sht {
 
 // Up to 8 split-BF16 plans of one band-limit whose forward analyses run as
 // one tensor-core launch: each member writes its data tiles into column
-// pair `slot` of the shared 16-column tiles (cmm_sht_batch_tiles, inside
-// cmm_bve_step_pre), then one contraction streams every Pbar tile once for
-// all members (cmm_sht_batch_analysis).
+// pair `slot` of the shared 16-column tiles (sht_velocity_pre, inside
+// cmm_bve_step_pre or cmm_sht_batch_forward), then one contraction streams
+// every Pbar tile once for all members (cmm_sht_batch_analysis).
 struct cmm_sht_batch {
   int L = 0, n = 0;
   cmm_sht* plans[8] = {};
