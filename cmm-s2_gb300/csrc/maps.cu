@@ -35,6 +35,10 @@ using namespace dev;
 namespace {
 
 constexpr int kBlock = 256;
+// The composition normalises the point every kNormEvery submaps (a power
+// of two); queries whose FP32 squared norm is outside [1/4, 4] are
+// normalised first, so the unnormalised chain stays far from overflow.
+constexpr int kNormEvery = 8;
 // default register budgets of the compositions, as resident 256-thread
 // blocks per SM (measured at level 7, 2^24 queries, 8 submaps, map forms,
 // cell order: Jacobians 12.8 / 13.6 / 13.2 ms at 4 / 3 / 2 blocks; points
@@ -110,7 +114,7 @@ struct Pushes {
   }
 };
 
-// 2^m as a double, from its bit pattern (0 <= m <= 4 here)
+// 2^m as a double, from its bit pattern (0 <= m <= kNormEvery here)
 __device__ __forceinline__ double pow2(int m) { return __longlong_as_double((long long)(1023 + m) << 52); }
 
 __global__ void __launch_bounds__(kBlock) locate_kernel(MeshView m, const double* __restrict__ q,
@@ -394,6 +398,16 @@ __global__ void __launch_bounds__(kBlock, MINB) compose_kernel(MeshView m, Src c
       continue;
     }
     double p[3] = {q[3 * i], q[3 * i + 1], q[3 * i + 2]};
+    {
+      const float f0 = to_f32_trunc(p[0]), f1 = to_f32_trunc(p[1]), f2 = to_f32_trunc(p[2]);
+      const float n2 = f0 * f0 + f1 * f1 + f2 * f2;
+      if (!(n2 > 0.25f && n2 < 4.f)) {   // also NaN / inf: then the check below flags it
+        const double inv = rsqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);
+        p[0] *= inv;
+        p[1] *= inv;
+        p[2] *= inv;
+      }
+    }
     if (!finite3(p[0], p[1], p[2])) {
       flag(m, CMM_FLAG_NONFINITE);
       out[3 * i] = out[3 * i + 1] = out[3 * i + 2] = nan("");
@@ -544,14 +558,15 @@ __global__ void __launch_bounds__(kBlock, MINB) compose_kernel(MeshView m, Src c
       }
       // Location, barycentrics and sub-triangle choice are invariant under
       // p -> lambda p (lambda > 0) and the patch is homogeneous of degree 2,
-      // so the projection onto the sphere can wait: normalising every fourth
-      // submap (and the result) keeps |p| within ~1e-4 of 1 (|P| = 1 +
-      // O(h^3) per submap) and saves the FP64 square root.  The tangent
-      // pushes then carry exactly the factor |p| / 2^(submaps since the last
-      // normalisation) against the normalised chain, and their components
-      // along p stay along p (DP(p)[p] = 2 P); both are removed where the
-      // point is normalised.
-      if ((s & 3) != 0) {
+      // so the projection onto the sphere can wait: normalising every
+      // kNormEvery-th submap (and the result) keeps |p| within ~1e-3 of 1
+      // for queries on the sphere (|P| = 1 + O(h^3) per submap, the
+      // deviation at most doubled per submap) and saves the FP64 square
+      // root and scaling.  The tangent pushes then carry exactly the factor
+      // |p| / 2^(submaps since the last normalisation) against the
+      // normalised chain, and their components along p stay along p
+      // (DP(p)[p] = 2 P); both are removed where the point is normalised.
+      if ((s & (kNormEvery - 1)) != 0) {
         p[0] = P[0];
         p[1] = P[1];
         p[2] = P[2];

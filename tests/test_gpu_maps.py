@@ -274,7 +274,9 @@ def test_full_size_composition_properties(nat):
     """The map-evaluation workload at full size (level 7, 8 submaps, 2^24
     queries, ids and Jacobians), through size-independent properties:
     images on the sphere; composing the stack in two launches (submaps 4-7,
-    then 0-3) gives the same points bit for bit and the chain-rule product
+    then 0-3) gives the same points to a few ulp (the second launch
+    normalises its input point, which the single launch carries
+    unnormalised through its deferred projection) and the chain-rule product
     of the two Jacobians (to 1e-10 relative: the tangent pushes run in
     float-float, ~2^-47 per operation, and each push cancels terms ~1/h =
     120 times larger than its result; measured 2.8e-11 over the 2^24
@@ -293,7 +295,7 @@ def test_full_size_composition_properties(nat):
     assert float((X.norm(dim=1) - 1).abs().max()) < 1e-15
     Y, _, _, JB = m.compose(cs[4:], q, want_jac=True)
     X2, _, _, JA = m.compose(cs[:4], Y, want_jac=True)
-    assert torch.equal(X, X2)
+    assert float((X - X2).abs().max()) < 2e-15
     del X2, Y
     JJ = torch.bmm(JA, JB)
     del JA, JB
