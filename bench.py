@@ -50,17 +50,17 @@ METRIC = "map evals/s"
 # the number of queries (the gathers and outputs grow with it): the
 # headline step (queries grouped by coarse cell, map forms and their low
 # floats) ...
-COMPOSE_TRAFFIC_PER_QUERY = (5.5332e9 + 0.8026e9) / (1 << 22)
+COMPOSE_TRAFFIC_PER_QUERY = (5.3716e9 + 0.7431e9) / (1 << 22)
 # ... and in the caller's order (map forms alone).
 COMPOSE_TRAFFIC_PER_QUERY_CALLER = (9.9927e9 + 0.5103e9) / (1 << 22)
 # FP64 instructions (DADD + DMUL + DFMA) per map evaluation (query x
 # submap) of the headline step's kernel, from the same capture, and all
 # issued instructions per evaluation (smsp__inst_executed.sum x 32 /
 # evaluations): at 2 FP64 lane-operations per SM per clock and 4 warp
-# instructions issued per SM per clock, they cost ~14 and ~12 SM cycles
+# instructions issued per SM per clock, they cost ~13 and ~12 SM cycles
 # per evaluation at their peaks, so the two bind together.
-FP64_INSTR_PER_EVAL = 28.15
-INSTR_PER_EVAL = 1574
+FP64_INSTR_PER_EVAL = 26.65
+INSTR_PER_EVAL = 1475
 
 
 def peaks():
