@@ -415,8 +415,13 @@ def bench_gpu(args, rank, world, sample_idx=None):
     fp64_fma_per_s = 152 * 8 * 256 * 8 * 20000 / (e0.elapsed_time(e1) / 1e3)
     del sink
 
+    # the Jacobian composition's register budget and the query order, by
+    # the autotuner on these queries (untimed; the same results either way)
+    from cmm_gpu.autotune import Autotuner
+    tuner = Autotuner(reps=2)
+    ordered = tuner.tune_composition(mesh, lambda o: step(ordered=o), stream)
     for _ in range(args.warmup):
-        step(ordered=True)
+        step(ordered=ordered)
     torch.cuda.synchronize()
     assert mesh.status() == 0
     n0 = native.lib.cmm_launch_count()
@@ -428,7 +433,7 @@ def bench_gpu(args, rank, world, sample_idx=None):
         torch.cuda.synchronize()
         e0.record(stream)
         for k in range(args.steps):
-            step(marks[k][0], ordered=True)
+            step(marks[k][0], ordered=ordered)
             marks[k][1].record(stream)
         e1.record(stream)
         torch.cuda.synchronize()
@@ -516,6 +521,7 @@ def bench_gpu(args, rank, world, sample_idx=None):
     del scratch
 
     res = dict(ms=ms, ms_compose=ms_compose, caller=caller, values_only=values, value=value, ms_e2e=ms_e2e, launches=launches, clocks=clk.summary(), numa_cores=numa_cores,
+               autotune=tuner.log.get("composition"),
                nv=len(verts), nt=len(tris), Q=Q, fp64_fma_per_s=fp64_fma_per_s, sample=sample)
     if rank == 0 and not args.no_bve:
         try:
@@ -1171,6 +1177,9 @@ def main():
         "clocks": r["clocks"], "gpu_launches": r["launches"],
     }
     line["points_only"] = r["values_only"]
+    line["autotune"] = r.get("autotune")
+    if r.get("autotune") and not r["autotune"]["ordered"]:
+        cfg["query_order"] = "caller order (the autotuner found it faster than sorting by coarse cell)"
     if par is not None and r.get("sample") is not None:
         line["parity"] = parity_report(par, r["sample"])
     for key in ("bve", "rh_error", "bve_l7_L1024", "kernels", "ensemble", "adjoint", "transport"):

@@ -8,8 +8,10 @@ What is tuned, and what is fixed by the data:
 * threads per block of the composition, the map update's foot points and
   the vorticity kernel (cmm_mesh_set_block);
 * the composition's register budget (cmm_mesh_set_variant: resident
-  blocks 4 or 6 for points only) -- the same arithmetic compiled for
-  another register count, so results do not change;
+  blocks 4 or 6 for points only, 2, 3 or 4 with Jacobians) -- the same
+  arithmetic compiled for another register count, so results do not
+  change -- and, for a query set, whether the queries are grouped by
+  coarse cell before the composition (tune_composition);
 * the synthesis schedule (cmm_sht_set_schedule: one role per phase, or
   warp-specialised; bitwise the same results), for all plans of a
   band-limit at once (tune_sht_schedule);
@@ -112,6 +114,27 @@ class Autotuner:
             seen.add(key)
             self.tune_solver(m)
         return self.log["kernels"]
+
+    # ------------------------------------------------------ composition
+    def tune_composition(self, mesh, step, stream, variants=(2, 3, 4), orders=(True, False), reps=3):
+        """Register budget of the Jacobian composition (cmm_mesh_set_variant,
+        resident blocks per SM: the same arithmetic compiled for another
+        register count, so results do not change) and whether the queries
+        are grouped by coarse cell first, from CUDA-event timings of
+        `step(ordered)` (one composition step on the caller's data, the
+        sort included when ordered).  Sets the best variant on the mesh and
+        returns the best order; the timings go to log["composition"]."""
+        times = {}
+        for v in variants:
+            mesh.set_variant(native.Mesh.VARIANT_COMPOSE_JAC, v)
+            for o in orders:
+                times[(v, o)] = _time(lambda: step(o), reps, stream)
+        (vb, ob) = min(times, key=times.get)
+        mesh.set_variant(native.Mesh.VARIANT_COMPOSE_JAC, vb)
+        self.log["composition"] = {"compose_jac_blocks": vb, "ordered": ob,
+                                   "ms": {f"blocks{v}_{'cell' if o else 'caller'}": t
+                                          for (v, o), t in times.items()}}
+        return ob
 
     # ------------------------------------------------- synthesis schedule
     def tune_sht_schedule(self, solvers, reps=3):
