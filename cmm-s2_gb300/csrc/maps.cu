@@ -41,11 +41,13 @@ constexpr int kBlock = 256;
 constexpr int kNormEvery = 8;
 // default register budgets of the compositions, as resident 256-thread
 // blocks per SM (measured at level 7, 2^24 queries, 8 submaps, map forms,
-// cell order: Jacobians 12.8 / 13.6 / 13.2 ms at 4 / 3 / 2 blocks; points
-// only 7.5 ms at 4 or 6 blocks, and 10.2 against 13.5 ms in caller order)
+// cell order, normalising every fourth submap: Jacobians 12.8 / 13.6 /
+// 13.2 ms at 4 / 3 / 2 blocks; points only 7.5 ms at 4 or 6 blocks, and
+// 10.2 against 13.5 ms in caller order); the autotuner may set others
 constexpr int kComposeJacBlocks = 4;
 // with the low floats of the forms' split loaded (fewer live values):
-// 10.83 / 11.02 / 11.59 ms at 3 / 4 / 2 blocks, same workload
+// 10.83 / 11.02 / 11.59 ms at 3 / 4 / 2 blocks, same workload; normalising
+// every eighth submap, 10.56 / 10.72 / 11.93 ms
 constexpr int kComposeJacBlocksFF = 3;
 constexpr int kComposeBlocks = 4;
 
