@@ -21,7 +21,7 @@ Usage: python tests/golden/make_golden.py            (every fixture but the
        python tests/golden/make_golden.py qhull 5 6 (Qhull-order location
        fixtures ``qhull_l5.npz``/``qhull_l6.npz``; the level-6 Delaunay build
        takes ~13 min of one core)
-       python tests/golden/make_golden.py bve1      (the whole barotropic
+       python tests/golden/make_golden.py bve_l4      (the whole barotropic
        configuration, level 4 / L = 128 / 200 steps: ``bve_l4_L128.npz``)
 """
 import os
@@ -155,7 +155,7 @@ def qhull_fixture(level, nq=16384):
          q_sha=hashlib.sha256(np.ascontiguousarray(qr).tobytes()).hexdigest())
 
 
-def bve_config1(nq=2000):
+def bve_level4_L128(nq=2000):
     """The barotropic configuration run in full by the reference driver
     (euler_simulation_sphere_remapping, cmm_s2/core/spherical_simulations.py:
     144-297): level-4 mesh, L = 128, T = 1 in 200 steps (dt = 1/200),
@@ -175,7 +175,7 @@ def bve_config1(nq=2000):
     m = ref_mesh(4)
     t0 = time.time()
     subs = rsim.euler_simulation_sphere_remapping(128, 200, 1.0, m, omega0, rot_rate=2 * np.pi, n_maps=20)
-    print(f"config-1 run {time.time() - t0:.0f} s")
+    print(f"level-4 / L=128 run {time.time() - t0:.0f} s")
     q = random_sphere_points(nq, seed=123)
     img = subs(q.copy())
     phi, theta = rutils.cart2sphere(img.T)
@@ -368,7 +368,7 @@ if __name__ == "__main__":
     if len(sys.argv) > 1 and sys.argv[1] == "qhull":
         for lv in sys.argv[2:]:
             qhull_fixture(int(lv))
-    elif len(sys.argv) > 1 and sys.argv[1] == "bve1":
-        bve_config1()
+    elif len(sys.argv) > 1 and sys.argv[1] == "bve_l4":
+        bve_level4_L128()
     else:
         main()

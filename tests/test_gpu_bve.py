@@ -331,7 +331,7 @@ def test_reference_drivers(sims):
     assert float((one(q).T - s.composite(q)[0]).abs().max()) < 1e-13
 
 
-def test_config1_whole_run_matches_reference(sims):
+def test_level4_L128_whole_run_matches_reference(sims):
     """The whole barotropic configuration (level 4, L = 128, 200 steps of
     dt = 1/200, remap every 20: 10 submaps; random SH initial vorticity
     l <= 16, seed 0) against the reference driver's own run of it and the
@@ -359,7 +359,7 @@ def test_config1_whole_run_matches_reference(sims):
     e_ref = np.abs(img - d["img"]).max()
     scale = np.abs(d["omega_closed"]).max()
     e_om = np.abs(om - d["omega_closed"]).max() / scale
-    print(f"config 1: points vs closed-form run {e_closed:.2e}, vs reference run {e_ref:.2e} "
+    print(f"level 4 / L = 128: points vs closed-form run {e_closed:.2e}, vs reference run {e_ref:.2e} "
           f"(reference's own spread {spread:.2e}); vorticity {e_om:.2e} relative")
     assert e_closed < 1e-10
     assert e_om < 1e-9
