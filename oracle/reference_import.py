@@ -3,7 +3,7 @@ arm of bench.py (and by the fixture generator).  Test infrastructure only:
 nothing in the library imports it.
 
 seth-tl/CMM-S2 is pure Python (numpy/scipy) whose modules import
-third-party packages that are absent here and on the GPU machine.  They are
+third-party packages that are not installed.  They are
 replaced by shims at import time, none of which is on the timed map path
 except through data it reads:
 
@@ -22,7 +22,7 @@ except through data it reads:
 Where the code comes from: ``copy_reference()`` copies the reference's
 ``cmm_s2`` package sources (``core`` and the package ``__init__``) into
 ``baseline/_ref/`` (git-ignored; it travels with the repository snapshot to
-the GPU box, where the reference checkout does not exist);
+machines where the reference checkout does not exist);
 ``import_core()`` imports from that copy.
 """
 import os
