@@ -104,3 +104,26 @@ def test_rejects_bad_meshes(native):
         native.mesh_check(moved, tris, 2)
     assert e.value.code == 2
     assert "midpoint" in str(e.value)
+
+
+def test_batch_and_form_entry_points_reject_bad_arguments(native):
+    """Argument checks of the batched-analysis, split-step and float-float
+    form entry points return CMM_ERR_ARG before any device work (null
+    handles and pointers, batch sizes outside 1..8), with a message."""
+    import ctypes
+    lib, P = native.lib, ctypes.c_void_p
+    ERR_ARG = 1
+    out = P()
+    assert lib.cmm_sht_batch_create(None, 2, ctypes.byref(out)) == ERR_ARG
+    plans = (P * 9)()
+    assert lib.cmm_sht_batch_create(plans, 0, ctypes.byref(out)) == ERR_ARG
+    assert lib.cmm_sht_batch_create(plans, 9, ctypes.byref(out)) == ERR_ARG
+    assert lib.cmm_sht_batch_create(plans, 2, ctypes.byref(out)) == ERR_ARG   # null plans
+    assert b"plans" in lib.cmm_last_error()
+    assert lib.cmm_sht_batch_analysis(None, None) == ERR_ARG
+    assert lib.cmm_sht_batch_forward(None, None, None, None) == ERR_ARG
+    assert lib.cmm_sht_batch_destroy(None) == 0
+    assert lib.cmm_bve_step_pre(None, None) == ERR_ARG
+    assert lib.cmm_bve_step_post(None, None) == ERR_ARG
+    assert lib.cmm_forms_ff(None, None, None, None) == ERR_ARG
+    assert native.Mesh.FORM_FF_STRIDE == 112 and native.ShtBatch.MAX == 8
